@@ -1,0 +1,144 @@
+/*
+ * self_gpu.h -- C ABI of the GB300 (sm_103a) spectral-element library (libselfgpu.so).
+ *
+ * It replaces the compute procedures of SELF's Fortran types (lileipku00/SELF) on the
+ * spectral-element hot path.  Every entry point is extern "C", takes plain pointers and sizes,
+ * and returns an int status (SELF_OK = 0, negative = error; self_last_error() gives the text).
+ * A Fortran ISO_C_BINDING interface to these functions is listed in INTEGRATION.md.
+ *
+ * Array conventions are the Fortran ones, so arrays pass without reordering:
+ *   matrices     D(i,j) at D[i + j*n], n = N+1 (column major, as DOUBLE D(0:N,0:N))
+ *   element data f(i,j,e) at f[i + n*(j + n*e)]            (Fortran f(0:N,0:N,1:nEl))
+ *   E-vectors    q(i,j,v,e) at q[i + n*(j + n*(v + nEq*e))] (Fortran G2D(0:N,0:N,1:nEq,1:nEl))
+ *   side data    b(i,side,e) at b[i + n*(side + 4*e)], side 0..3 = south, east, north, west
+ *   edge table   edges[6*k + 0..5] = e1, s1, e2, s2, start, inc with 1-based element and side
+ *                IDs (QuadMeshClass.f90 Edge: e2 < 0 is a boundary flag, s2 < 0 reversed)
+ * Handles are not thread safe; distinct handles may be used from distinct threads.  Host arrays
+ * are read or written synchronously.  The library owns all device memory it allocates.
+ */
+#ifndef SELF_GPU_H
+#define SELF_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define SELF_OK 0
+#define SELF_ERR_INVALID (-1)       /* bad argument or size */
+#define SELF_ERR_CUDA (-2)          /* a CUDA runtime call failed */
+#define SELF_ERR_ALLOC (-3)         /* device or host allocation failed */
+#define SELF_ERR_UNSUPPORTED (-4)   /* option outside the implemented path */
+#define SELF_ERR_TIMEOUT (-5)       /* a bounded device wait ran out */
+#define SELF_ERR_NOT_CONVERGED (-6) /* iterative solver hit maxIters (ioerr = -1) */
+#define SELF_ERR_NONFINITE (-7)     /* NaN or Inf met in a residual */
+
+/* ---------------------------------------------------------------- flags (ModelFlags.f90:80-137) */
+#define SELF_NO_NORMAL_FLOW (-100)
+#define SELF_INFLOW_ONE (-103)
+#define SELF_INFLOW_TWO (-104)
+#define SELF_DIRICHLET (-200)
+#define SELF_GAUSS 1
+#define SELF_GAUSS_LOBATTO (-1)
+#define SELF_DG 2000
+#define SELF_CG 2001
+
+#define SELF_MODEL_SW_CONSERVATIVE 1 /* ConservativeShallowWaterClass.f90 */
+#define SELF_MODEL_ADVECTION 2       /* AdvectionClass.f90 (kappa = 0) */
+
+#define SELF_PREC_FP64 0 /* plain FP64 drop-in */
+#define SELF_PREC_FP32 1 /* FP32 arithmetic; shallow water in perturbation form about the lake at rest */
+
+/* ---------------------------------------------------------------- context */
+typedef struct self_ctx self_ctx;
+
+/* One context per (process, device).  Replaces nothing in the reference (its drivers run on the
+ * host); it carries the CUDA device, stream and the last error text. */
+int self_ctx_create(int device, self_ctx** out);
+int self_ctx_destroy(self_ctx* ctx);
+int self_last_error(const self_ctx* ctx, char* buf, size_t len);
+const char* self_status_string(int status);
+int self_ctx_synchronize(self_ctx* ctx);
+/* number of kernels this context launched so far (for launch accounting) */
+long long self_ctx_kernel_launches(const self_ctx* ctx);
+/* CUDA-event timer on the context's stream: start records an event, stop records a second one,
+ * synchronises and returns the elapsed milliseconds between them. */
+int self_ctx_timer_start(self_ctx* ctx);
+int self_ctx_timer_stop(self_ctx* ctx, double* ms);
+/* Overwrite a scratch buffer of `bytes` on the context's stream (evicts L2 between timed steps). */
+int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
+/* Page-locked host memory for host<->device copies at full link speed. */
+int self_host_alloc(size_t bytes, void** ptr);
+int self_host_free(void* ptr);
+
+/* ---------------------------------------------------------------- host set-up (Build procedures)
+ * NodalStorage_2D%Build (NodalStorage_2D_Class.f90:101-230).  form = SELF_DG gives the weak
+ * derivative matrix -M^-1 D^T M in both directions; dmatS/dmatP/lag*: n*n and n doubles. */
+int self_nodal_build(int N, int quadrature, int form, double* nodes, double* qweights, double* dmatS,
+                     double* dmatP, double* lagW, double* lagE, double* lagS, double* lagN);
+
+/* QuadMesh%LoadDefaultMesh + ConstructEdges + ScaleTheMesh (QuadMeshClass.f90:1489-1627,1691-1859)
+ * on nx*ny elements of the unit square, with optional periodic connectivity, an optional warp
+ * x,y += warp*sin(2 pi x)sin(2 pi y) before scaling by (xscale, yscale), and boundary edges
+ * flagged boundary_flag.  Sizes: self_mesh_counts.  Outputs as in the conventions above:
+ * edges 6*nEdges; elemNodes 4*nEl; nodeType nNodes; node->element lists n2e_ptr (nNodes+1),
+ * n2e_elem/n2e_local (4*nEl); x,y,dxds,dxdp,dyds,dydp,J n*n*nEl; nhx,nhy,nlen,bx,by n*4*nEl. */
+int self_mesh_counts(int nx, int ny, int periodic_x, int periodic_y, int* nEl, int* nEdges, int* nNodes);
+int self_mesh_build(int nx, int ny, int periodic_x, int periodic_y, int N, int quadrature, double warp,
+                    double xscale, double yscale, int boundary_flag, int* edges, int* elemNodes, int* nodeType,
+                    int* n2e_ptr, int* n2e_elem, int* n2e_local, double* x, double* y, double* dxds,
+                    double* dxdp, double* dyds, double* dydp, double* J, double* nhx, double* nhy,
+                    double* nlen, double* bx, double* by);
+
+/* ---------------------------------------------------------------- DGSEM 2-D
+ * Replaces ShallowWater (ConservativeShallowWaterClass.f90:71-151) and Advection
+ * (AdvectionClass.f90:84-164) compute procedures:
+ *   self_dg2d_tendency == %GlobalTimeDerivative(t)        (:1222-1262)  [+ %GetTendency]
+ *   self_dg2d_rk3      == nsteps x %ForwardStepRK3(tn)    (:1173-1218)
+ *   self_dg2d_set_state/get_state == %SetSolution/%GetSolution for all elements
+ * All pointers in the descriptor are host arrays read once at create time. */
+typedef struct {
+  int N, nEl, nEdges, nEq;
+  int model;     /* SELF_MODEL_* */
+  int precision; /* SELF_PREC_* */
+  const double *dmatS, *dmatP, *qweight, *lagW, *lagE, *lagS, *lagN;
+  const int* edges;
+  const double *dxds, *dxdp, *dyds, *dydp, *J;
+  const double *nhx, *nhy, *nlen;
+  const double *h, *dhdx, *dhdy, *fcor; /* shallow water: bathymetry(:,:,1:3), planetary vorticity */
+  const double* relax;                  /* optional relaxation field (i,j,v,e) or NULL */
+  const double* rfac;                   /* optional: SW relaxation timescale (i,j,e); advection (i,j,v,e) */
+  const double *u, *v;                  /* advection velocity (i,j,e) */
+  double g, linear_drag, dt;
+} self_dg2d_desc;
+
+typedef struct self_dg2d self_dg2d;
+int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* desc, self_dg2d** out);
+int self_dg2d_destroy(self_dg2d* h);
+int self_dg2d_set_state(self_dg2d* h, const double* q);
+int self_dg2d_get_state(self_dg2d* h, double* q);
+int self_dg2d_tendency(self_dg2d* h, double t, double* dqdt);
+int self_dg2d_rk3(self_dg2d* h, double tn, int nsteps);
+/* Same as self_dg2d_rk3 but enqueued only (no host synchronisation); pair with self_ctx_synchronize. */
+int self_dg2d_rk3_async(self_dg2d* h, double tn, int nsteps);
+/* Device address of the resident state (FP64: double, FP32: float perturbation form). */
+int self_dg2d_state_device(self_dg2d* h, void** dptr, size_t* bytes);
+/* Measurement helper: average CUDA-event time (ms) of one launch of each kernel of an RK stage, each launch
+ * preceded by an L2 flush of flush_bytes; the resident state is restored afterwards.
+ * ms[0] = edge-flux kernel, ms[1] = volume + RK-update kernel. */
+int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* ms);
+
+/* Known answer helpers for the shallow-water set-up (host, FP64):
+ * CalculateBathymetryGradient (ConservativeShallowWaterClass.f90:1733-1868). */
+int self_sw_bathymetry_gradient(int N, int nEl, const double* dmatS, const double* dmatP, const double* qweight,
+                                const double* lagW, const double* lagE, const double* lagS, const double* lagN,
+                                const double* dxds, const double* dxdp, const double* dyds, const double* dydp,
+                                const double* J, const double* nhx, const double* nhy, const double* nlen,
+                                const double* h, double* dhdx, double* dhdy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SELF_GPU_H */

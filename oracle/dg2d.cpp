@@ -1,0 +1,387 @@
+// CPU oracle (test infrastructure): DGSEM 2-D tendency and low-storage RK3.
+// Restates src/highend/shallowwater/ConservativeShallowWaterClass.f90 (ForwardStepRK3 :1173-1218,
+// GlobalTimeDerivative :1222-1262, EdgeFlux :1266-1360, MappedTimeDerivative :1364-1522,
+// DGSystemDerivative :1526-1551, RiemannSolver :1555-1604, XFlux/YFlux :1608-1658, Source :1662-1694,
+// GetExternalState :1698-1729, CalculateBathymetryGradient :1733-1868), the matching routines of
+// src/highend/advection-diffusion2d/AdvectionClass.f90 (:1268-1886) and
+// src/dgsem/DGSEMSolutionStorageClass_2D.f90 CalculateSolutionAtBoundaries (:749-802).
+// Decision: the Riemann solver's undeclared "g" (:1589-1592) is the parameter g (locG).
+// OpenMP over elements and edges follows the reference's !$OMP DO placement.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "oracle.h"
+
+namespace {
+
+// ConstantsDictionary.f90:66-68
+const double rk3_a[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+const double rk3_b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
+const double rk3_g[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+
+struct Idx {
+  int n, nEq;
+  size_t q(int i, int j, int v, int e) const { return (size_t)i + n * (j + (size_t)n * (v + (size_t)nEq * e)); }
+  size_t f(int i, int j, int e) const { return (size_t)i + n * (j + (size_t)n * e); }
+  size_t b(int i, int v, int s, int e) const { return (size_t)i + n * (v + (size_t)nEq * (s + 4 * (size_t)e)); }
+  size_t nh(int i, int s, int e) const { return (size_t)i + n * (s + 4 * (size_t)e); }
+};
+
+// DGSystemDerivative: MATMUL(dMat, intFlux) + (rFlux*lagRight + lFlux*lagLeft)/qWei
+void dg_system_derivative(int n, const double* dMat, const double* qw, double lF, double rF, const double* f,
+                          const double* lL, const double* lR, double* out) {
+  for (int k = 0; k < n; ++k) {
+    double s = 0.0;
+    for (int m = 0; m < n; ++m) s = s + dMat[k + m * n] * f[m];
+    out[k] = s;
+  }
+  for (int k = 0; k < n; ++k) out[k] = out[k] + (rF * lR[k] + lF * lL[k]) / qw[k];
+}
+
+void sw_riemann(const double* in, const double* out, const double* nH, double g, double* flux) {
+  double jump[3] = {out[0] - in[0], out[1] - in[1], out[2] - in[2]};
+  double uL = in[0], vL = in[1], pL = in[2];
+  double uR = out[0], vR = out[1], pR = out[2];
+  double uOut = uR * nH[0] + vR * nH[1];
+  double uIn = uL * nH[0] + vL * nH[1];
+  double c1 = std::fabs(uOut / pR + std::sqrt(g * pR));
+  double c2 = std::fabs(uOut / pR - std::sqrt(g * pR));
+  double c3 = std::fabs(uIn / pL + std::sqrt(g * pL));
+  double c4 = std::fabs(uIn / pL - std::sqrt(g * pL));
+  double fac = std::fmax(std::fmax(std::fmax(c1, c2), c3), c4);
+  double aS[3];
+  aS[0] = (uOut / pR) * uR + 0.5 * g * pR * pR * nH[0] + (uIn / pL) * uL + 0.5 * g * pL * pL * nH[0];
+  aS[1] = (uOut / pR) * vR + 0.5 * g * pR * pR * nH[1] + (uIn / pL) * vL + 0.5 * g * pL * pL * nH[1];
+  aS[2] = uOut + uIn;
+  for (int k = 0; k < 3; ++k) flux[k] = 0.5 * (aS[k] - fac * jump[k]);
+}
+
+void sw_external(const double* nH, const double* in, double* ex) {  // NO_NORMAL_FLOW mirror
+  ex[0] = (nH[1] * nH[1] - nH[0] * nH[0]) * in[0] - 2.0 * nH[0] * nH[1] * in[1];
+  ex[1] = (nH[0] * nH[0] - nH[1] * nH[1]) * in[1] - 2.0 * nH[0] * nH[1] * in[0];
+  ex[2] = in[2];
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  extern void omp_set_num_threads(int);
+  omp_set_num_threads(n);
+#endif
+  return 0;
+}
+
+int orc_dg_traces(const orc_dg_problem* p, const double* q, double* bs) {
+  const int n = p->N + 1, nEq = p->nEq;
+  Idx I{n, nEq};
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < p->nEl; ++e) {
+    for (int j = 0; j < n; ++j)
+      for (int v = 0; v < nEq; ++v) {
+        double w = 0.0, ea = 0.0;
+        for (int i = 0; i < n; ++i) w = w + p->lW[i] * q[I.q(i, j, v, e)];
+        for (int i = 0; i < n; ++i) ea = ea + p->lE[i] * q[I.q(i, j, v, e)];
+        bs[I.b(j, v, 3, e)] = w;
+        bs[I.b(j, v, 1, e)] = ea;
+      }
+    for (int i = 0; i < n; ++i)
+      for (int v = 0; v < nEq; ++v) {
+        double s = 0.0, no = 0.0;
+        for (int j = 0; j < n; ++j) s = s + p->lS[j] * q[I.q(i, j, v, e)];
+        for (int j = 0; j < n; ++j) no = no + p->lN[j] * q[I.q(i, j, v, e)];
+        bs[I.b(i, v, 0, e)] = s;
+        bs[I.b(i, v, 2, e)] = no;
+      }
+  }
+  return 0;
+}
+
+int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double* bf) {
+  const int n = p->N + 1, nEq = p->nEq, N = p->N;
+  Idx I{n, nEq};
+  int err = 0;
+#pragma omp parallel for schedule(static) reduction(| : err)
+  for (int k = 0; k < p->nEdges; ++k) {
+    const int* E = p->edges + 6 * k;
+    int e1 = E[0] - 1, s1 = E[1] - 1, e2 = E[2], s2 = std::abs(E[3]) - 1, start = E[4], inc = E[5];
+    double in[16], ex[16], fl[16], nH[2];
+    if (nEq > 16) {
+      err |= 1;
+      continue;
+    }
+    if (e2 > 0) {
+      e2 -= 1;
+      int kk = start - inc;
+      for (int i = 0; i <= N; ++i) {
+        nH[0] = p->nhx[I.nh(i, s1, e1)];
+        nH[1] = p->nhy[I.nh(i, s1, e1)];
+        double len = p->nlen[I.nh(i, s1, e1)];
+        for (int v = 0; v < nEq; ++v) {
+          in[v] = bs[I.b(i, v, s1, e1)];
+          ex[v] = bs[I.b(kk, v, s2, e2)];
+        }
+        if (p->model == 1) {
+          sw_riemann(in, ex, nH, p->g, fl);
+        } else {
+          // advection (AdvectionClass.f90:1756-1787) with the primary element's boundary velocity
+          // (CalculateVelocityAtBoundaries: Lagrange traces of u and v)
+          double ub = 0.0, vb = 0.0;
+          const double* L = (s1 == 0) ? p->lS : (s1 == 1) ? p->lE : (s1 == 2) ? p->lN : p->lW;
+          for (int m = 0; m < n; ++m) {
+            size_t id = (s1 == 0 || s1 == 2) ? I.f(i, m, e1) : I.f(m, i, e1);
+            ub = ub + L[m] * p->u[id];
+            vb = vb + L[m] * p->v[id];
+          }
+          double un = ub * nH[0] + vb * nH[1];
+          for (int v = 0; v < nEq; ++v) {
+            double jump = ex[v] - in[v];
+            fl[v] = 0.5 * (un * (ex[v] + in[v]) - std::fabs(un) * jump);
+          }
+        }
+        for (int v = 0; v < nEq; ++v) {
+          double f = fl[v] * len;
+          bf[I.b(i, v, s1, e1)] = f;
+          bf[I.b(kk, v, s2, e2)] = -f;
+        }
+        kk = kk + inc;
+      }
+    } else {
+      for (int i = 0; i <= N; ++i) {
+        nH[0] = p->nhx[I.nh(i, s1, e1)];
+        nH[1] = p->nhy[I.nh(i, s1, e1)];
+        double len = p->nlen[I.nh(i, s1, e1)];
+        for (int v = 0; v < nEq; ++v) in[v] = bs[I.b(i, v, s1, e1)];
+        if (p->model == 1) {
+          if (e2 == ORC_NO_NORMAL_FLOW) {
+            sw_external(nH, in, ex);
+          } else {
+            ex[0] = ex[1] = ex[2] = 0.0;
+          }
+          sw_riemann(in, ex, nH, p->g, fl);
+        } else {
+          for (int v = 0; v < nEq; ++v) ex[v] = 0.0;
+          if (e2 == ORC_INFLOW_ONE) ex[0] = std::tanh(t);
+          if (e2 == ORC_INFLOW_TWO && nEq > 1) ex[1] = std::tanh(t);
+          double ub = 0.0, vb = 0.0;
+          const double* L = (s1 == 0) ? p->lS : (s1 == 1) ? p->lE : (s1 == 2) ? p->lN : p->lW;
+          for (int m = 0; m < n; ++m) {
+            size_t id = (s1 == 0 || s1 == 2) ? I.f(i, m, e1) : I.f(m, i, e1);
+            ub = ub + L[m] * p->u[id];
+            vb = vb + L[m] * p->v[id];
+          }
+          double un = ub * nH[0] + vb * nH[1];
+          for (int v = 0; v < nEq; ++v) {
+            double jump = ex[v] - in[v];
+            fl[v] = 0.5 * (un * (ex[v] + in[v]) - std::fabs(un) * jump);
+          }
+        }
+        for (int v = 0; v < nEq; ++v) bf[I.b(i, v, s1, e1)] = fl[v] * len;
+      }
+    }
+  }
+  return err ? -1 : 0;
+}
+
+// MappedTimeDerivative for one element
+static void mapped_time_derivative(const orc_dg_problem* p, double t, const double* q, const double* bf,
+                                   double* tend, int e) {
+  const int n = p->N + 1, nEq = p->nEq;
+  Idx I{n, nEq};
+  std::vector<double> cf(n * nEq), der(n), xF(nEq), yF(nEq), sol(nEq);
+  auto fluxes = [&](int i, int j) {
+    for (int v = 0; v < nEq; ++v) sol[v] = q[I.q(i, j, v, e)];
+    if (p->model == 1) {
+      // XFlux / YFlux (:1608-1658)
+      double g = p->g;
+      xF[0] = sol[0] * sol[0] / (sol[2]) + g * 0.5 * sol[2] * sol[2];
+      xF[1] = sol[0] * sol[1] / (sol[2]);
+      xF[2] = sol[0];
+      yF[0] = sol[1] * sol[0] / (sol[2]);
+      yF[1] = sol[1] * sol[1] / (sol[2]) + g * 0.5 * sol[2] * sol[2];
+      yF[2] = sol[1];
+    } else {
+      double u = p->u[I.f(i, j, e)], v = p->v[I.f(i, j, e)];
+      for (int k = 0; k < nEq; ++k) {
+        xF[k] = sol[k] * u;
+        yF[k] = sol[k] * v;
+      }
+    }
+  };
+  // s-direction (:1398-1445)
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < n; ++i) {
+      size_t id = I.f(i, j, e);
+      double dxdp = p->dxdp[id], dydp = p->dydp[id];
+      fluxes(i, j);
+      for (int v = 0; v < nEq; ++v) cf[i + n * v] = dydp * xF[v] - dxdp * yF[v];
+    }
+    for (int v = 0; v < nEq; ++v) {
+      double fL = bf[I.b(j, v, 3, e)], fR = bf[I.b(j, v, 1, e)];
+      dg_system_derivative(n, p->dmatS, p->qw, fL, fR, &cf[n * v], p->lW, p->lE, der.data());
+      for (int i = 0; i < n; ++i) tend[I.q(i, j, v, e)] = -der[i];
+    }
+  }
+  // p-direction (:1448-1494)
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) {
+      size_t id = I.f(i, j, e);
+      double dxds = p->dxds[id], dyds = p->dyds[id];
+      fluxes(i, j);
+      for (int v = 0; v < nEq; ++v) cf[j + n * v] = -dyds * xF[v] + dxds * yF[v];
+    }
+    for (int v = 0; v < nEq; ++v) {
+      double fL = bf[I.b(i, v, 0, e)], fR = bf[I.b(i, v, 2, e)];
+      dg_system_derivative(n, p->dmatP, p->qw, fL, fR, &cf[n * v], p->lS, p->lN, der.data());
+      for (int j = 0; j < n; ++j) {
+        double Jn = p->J[I.f(i, j, e)];
+        tend[I.q(i, j, v, e)] = (tend[I.q(i, j, v, e)] - der[j]) / Jn;
+      }
+    }
+  }
+  // sources (:1497-1519)
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      size_t id = I.f(i, j, e);
+      for (int v = 0; v < nEq; ++v) sol[v] = q[I.q(i, j, v, e)];
+      if (p->model == 1) {
+        double relax[3] = {0, 0, 0}, ts = 0.0;
+        if (p->relax) {
+          for (int v = 0; v < 3; ++v) relax[v] = p->relax[I.q(i, j, v, e)];
+        }
+        if (p->rfac) ts = p->rfac[id];
+        double plv = p->fcor[id], h = p->h[id], dhdx = p->dhdx[id], dhdy = p->dhdy[id];
+        double g = p->g, lD = p->drag;
+        double s0 = plv * sol[1] + g * sol[2] * dhdx - lD * sol[0] / h - (sol[0] - relax[0]) * ts;
+        double s1 = -plv * sol[0] + g * sol[2] * dhdy - lD * sol[1] / h - (sol[1] - relax[1]) * ts;
+        double s2 = -(sol[2] - relax[2]) * ts;
+        tend[I.q(i, j, 0, e)] = tend[I.q(i, j, 0, e)] + s0;
+        tend[I.q(i, j, 1, e)] = tend[I.q(i, j, 1, e)] + s1;
+        tend[I.q(i, j, 2, e)] = tend[I.q(i, j, 2, e)] + s2;
+      } else {
+        for (int v = 0; v < nEq; ++v) {
+          double r = p->relax ? p->relax[I.q(i, j, v, e)] : 0.0;
+          double rf = p->rfac ? p->rfac[I.q(i, j, v, e)] : 0.0;
+          tend[I.q(i, j, v, e)] = tend[I.q(i, j, v, e)] + (r - sol[v]) * rf;
+        }
+      }
+    }
+}
+
+int orc_dg_tendency(const orc_dg_problem* p, double t, const double* q, double* tend) {
+  if (p->kappa != 0.0) return -5;  // the BR1 diffusion passes are not restated
+  const int n = p->N + 1;
+  size_t nb = (size_t)n * p->nEq * 4 * p->nEl;
+  std::vector<double> bs(nb, 0.0), bf(nb, 0.0);
+  orc_dg_traces(p, q, bs.data());
+  if (orc_dg_edge_flux(p, t, bs.data(), bf.data()) != 0) return -1;
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < p->nEl; ++e) mapped_time_derivative(p, t, q, bf.data(), tend, e);
+  return 0;
+}
+
+int orc_dg_rk3(const orc_dg_problem* p, double tn, int nsteps, double* q) {
+  const int n = p->N + 1;
+  size_t nq = (size_t)n * n * p->nEq * p->nEl;
+  std::vector<double> G(nq), dS(nq);
+  double dt = p->dt;
+  for (int step = 0; step < nsteps; ++step) {
+    double t0 = tn + step * dt;
+    std::fill(G.begin(), G.end(), 0.0);
+    for (int m = 0; m < 3; ++m) {
+      double t = t0 + rk3_b[m] * dt;
+      int rc = orc_dg_tendency(p, t, q, dS.data());
+      if (rc) return rc;
+      double a = rk3_a[m], gdt = rk3_g[m] * dt;
+#pragma omp parallel for schedule(static)
+      for (long long k = 0; k < (long long)nq; ++k) {
+        G[k] = a * G[k] + dS[k];
+        q[k] = q[k] + gdt * G[k];
+      }
+    }
+  }
+  return 0;
+}
+
+// CalculateBathymetryGradient (:1733-1868): weak DG derivative of h with the boundary values of h.
+int orc_sw_bathymetry_gradient(const orc_dg_problem* p, double* dhdx, double* dhdy) {
+  const int n = p->N + 1;
+  Idx I{n, 1};
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < p->nEl; ++e) {
+    std::vector<double> hb(4 * n), cf(2 * n), der(n), tend(2 * n * n);
+    for (int j = 0; j < n; ++j) {
+      double w = 0, ea = 0;
+      for (int i = 0; i < n; ++i) w = w + p->lW[i] * p->h[I.f(i, j, e)];
+      for (int i = 0; i < n; ++i) ea = ea + p->lE[i] * p->h[I.f(i, j, e)];
+      hb[j + n * 3] = w;
+      hb[j + n * 1] = ea;
+    }
+    for (int i = 0; i < n; ++i) {
+      double s = 0, no = 0;
+      for (int j = 0; j < n; ++j) s = s + p->lS[j] * p->h[I.f(i, j, e)];
+      for (int j = 0; j < n; ++j) no = no + p->lN[j] * p->h[I.f(i, j, e)];
+      hb[i + n * 0] = s;
+      hb[i + n * 2] = no;
+    }
+    for (int j = 0; j < n; ++j) {
+      for (int i = 0; i < n; ++i) {
+        size_t id = I.f(i, j, e);
+        double h = p->h[id];
+        double xF[2] = {h, 0.0}, yF[2] = {0.0, h};
+        for (int v = 0; v < 2; ++v) cf[i + n * v] = p->dydp[id] * xF[v] - p->dxdp[id] * yF[v];
+      }
+      double nv[2], len, fR[2], fL[2];
+      nv[0] = p->nhx[I.nh(j, 1, e)];
+      nv[1] = p->nhy[I.nh(j, 1, e)];
+      len = p->nlen[I.nh(j, 1, e)];
+      fR[0] = (hb[j + n * 1] * nv[0]) * len;
+      fR[1] = (hb[j + n * 1] * nv[1]) * len;
+      nv[0] = p->nhx[I.nh(j, 3, e)];
+      nv[1] = p->nhy[I.nh(j, 3, e)];
+      len = p->nlen[I.nh(j, 3, e)];
+      fL[0] = (hb[j + n * 3] * nv[0]) * len;
+      fL[1] = (hb[j + n * 3] * nv[1]) * len;
+      for (int v = 0; v < 2; ++v) {
+        dg_system_derivative(n, p->dmatS, p->qw, fL[v], fR[v], &cf[n * v], p->lW, p->lE, der.data());
+        for (int i = 0; i < n; ++i) tend[i + n * (j + n * v)] = der[i];
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < n; ++j) {
+        size_t id = I.f(i, j, e);
+        double h = p->h[id];
+        double xF[2] = {h, 0.0}, yF[2] = {0.0, h};
+        for (int v = 0; v < 2; ++v) cf[j + n * v] = -p->dyds[id] * xF[v] + p->dxds[id] * yF[v];
+      }
+      double nv[2], len, fR[2], fL[2];
+      nv[0] = p->nhx[I.nh(i, 2, e)];
+      nv[1] = p->nhy[I.nh(i, 2, e)];
+      len = p->nlen[I.nh(i, 2, e)];
+      fR[0] = (hb[i + n * 2] * nv[0]) * len;
+      fR[1] = (hb[i + n * 2] * nv[1]) * len;
+      nv[0] = p->nhx[I.nh(i, 0, e)];
+      nv[1] = p->nhy[I.nh(i, 0, e)];
+      len = p->nlen[I.nh(i, 0, e)];
+      fL[0] = (hb[i + n * 0] * nv[0]) * len;
+      fL[1] = (hb[i + n * 0] * nv[1]) * len;
+      for (int v = 0; v < 2; ++v) {
+        dg_system_derivative(n, p->dmatP, p->qw, fL[v], fR[v], &cf[n * v], p->lS, p->lN, der.data());
+        for (int j = 0; j < n; ++j) {
+          double Jn = p->J[I.f(i, j, e)];
+          tend[i + n * (j + n * v)] = (tend[i + n * (j + n * v)] + der[j]) / Jn;
+        }
+      }
+    }
+    for (int k = 0; k < n * n; ++k) {
+      dhdx[(size_t)n * n * e + k] = tend[k];
+      dhdy[(size_t)n * n * e + k] = tend[n * n + k];
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

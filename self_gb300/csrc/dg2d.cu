@@ -1,0 +1,834 @@
+// DGSEM 2-D tendency and low-storage RK3 on sm_103a (plain FP64 form).
+//
+// Replaces, on the GPU, the per-stage work of ConservativeShallowWaterClass.f90 and
+// AdvectionClass.f90: CalculateSolutionAtBoundaries (DGSEMSolutionStorageClass_2D.f90:749-802),
+// EdgeFlux with the LLF / upwind Riemann solvers (:1266-1360, :1555-1604; Advection :1382-1478,
+// :1756-1787), MappedTimeDerivative with XFlux/YFlux, DGSystemDerivative and Source (:1364-1551,
+// :1608-1694) and the RK3 register update of ForwardStepRK3 (:1173-1218).
+//
+// One RK stage is two kernels:
+//   dg_edge_flux   one thread per (edge, edge node): both traces, Riemann flux x |n|, written to
+//                  the primary side and (negated, through start/inc) to the secondary side;
+//   dg_volume      one thread per element node, several elements per CTA: contravariant fluxes
+//                  into shared memory, the two 1-D weak-derivative contractions, lift, 1/J, source,
+//                  G <- a G + dq/dt, q <- q + g dt G, then the boundary traces of the new q for
+//                  the next stage's edge kernel (the trace pass is fused into this epilogue).
+// Layout in HBM: E-vectors q, G (element-contiguous, i fastest); per element a 5 n^2 metric block
+// (dxds, dxdp, dyds, dydp, 1/J); per element an aux block (dhdx, dhdy, f [, h] [, relaxation]);
+// traces and boundary fluxes (i, v, side, e); per edge a 4 n block (nx, ny, |n|, u.n).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "dg2d_fp32.cuh"
+#include "internal.hpp"
+
+using namespace selfgpu;
+
+namespace selfgpu {
+namespace dg {
+
+__constant__ double c_rk3_a[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+
+template <int N1>
+struct NodalConst {
+  double dS[N1 * N1];  // weak-derivative matrix, s direction, column major
+  double dP[N1 * N1];  // p direction
+  double lW[N1], lE[N1], lS[N1], lN[N1];
+  double qwinv[N1];  // 1 / quadrature weight
+};
+
+struct VolArgs {
+  const double* q;
+  double* qout;
+  double* G;
+  double* tend;  // tendency output (mode 0)
+  const double* bf;
+  double* bs;  // traces of the new state (write_traces)
+  const double* metrics;
+  const double* aux;
+  int nEl, naux, has_drag, has_relax;
+  double g, drag, a, gdt;
+  int mode;  // 0 tendency only, 1 RK stage with a = 0 (G not read), 2 RK stage reading G
+  int write_traces;
+};
+
+struct EdgeArgs {
+  const double* bs;
+  double* bf;
+  const int* edges;     // 6 per edge
+  const double* egeo;   // 4 n per edge: nx, ny, |n|, u.n (advection)
+  int nEdges;
+  double g, t;
+};
+
+// ------------------------------------------------------------------------------------ physics
+struct SWFlux {
+  template <int NEQ>
+  static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
+                                                 double un_adv, double g, double* f) {
+    (void)un_adv;
+    // RiemannSolver (ConservativeShallowWaterClass.f90:1555-1604), g taken from the parameters
+    const double uL = in[0], vL = in[1], pL = in[2];
+    const double uR = ex[0], vR = ex[1], pR = ex[2];
+    const double uOut = uR * nx + vR * ny;
+    const double uIn = uL * nx + vL * ny;
+    const double ipR = 1.0 / pR, ipL = 1.0 / pL;
+    const double cR = sqrt(g * pR), cL = sqrt(g * pL);
+    const double wR = uOut * ipR, wL = uIn * ipL;
+    const double fac = fmax(fmax(fabs(wR + cR), fabs(wR - cR)), fmax(fabs(wL + cL), fabs(wL - cL)));
+    const double a0 = wR * uR + 0.5 * g * pR * pR * nx + wL * uL + 0.5 * g * pL * pL * nx;
+    const double a1 = wR * vR + 0.5 * g * pR * pR * ny + wL * vL + 0.5 * g * pL * pL * ny;
+    const double a2 = uOut + uIn;
+    f[0] = 0.5 * (a0 - fac * (uR - uL));
+    f[1] = 0.5 * (a1 - fac * (vR - vL));
+    f[2] = 0.5 * (a2 - fac * (pR - pL));
+  }
+  template <int NEQ>
+  static __device__ __forceinline__ void external(int bc, double nx, double ny, double t, const double* in,
+                                                  double* ex) {
+    (void)t;
+    if (bc == SELF_NO_NORMAL_FLOW) {  // GetExternalState (:1698-1729)
+      ex[0] = (ny * ny - nx * nx) * in[0] - 2.0 * nx * ny * in[1];
+      ex[1] = (nx * nx - ny * ny) * in[1] - 2.0 * nx * ny * in[0];
+      ex[2] = in[2];
+    } else {
+      ex[0] = ex[1] = ex[2] = 0.0;
+    }
+  }
+};
+
+struct AdvFlux {
+  template <int NEQ>
+  static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
+                                                 double un, double g, double* f) {
+    (void)nx;
+    (void)ny;
+    (void)g;
+    // RiemannSolver (AdvectionClass.f90:1756-1787) with kappa = 0
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) f[v] = 0.5 * (un * (ex[v] + in[v]) - fabs(un) * (ex[v] - in[v]));
+  }
+  template <int NEQ>
+  static __device__ __forceinline__ void external(int bc, double nx, double ny, double t, const double* in,
+                                                  double* ex) {
+    (void)nx;
+    (void)ny;
+    (void)in;
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) ex[v] = 0.0;  // GetExternalState (:1851-1886)
+    if (bc == SELF_INFLOW_ONE) ex[0] = tanh(t);
+    if (NEQ > 1 && bc == SELF_INFLOW_TWO) ex[NEQ > 1 ? 1 : 0] = tanh(t);
+  }
+};
+
+// ------------------------------------------------------------------------------------ edge kernel
+template <int N1, int NEQ, class Phys>
+__global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = gid / N1;
+  const int i = gid - k * N1;
+  if (k >= A.nEdges) return;
+  const int* E = A.edges + 6 * k;
+  const int e1 = E[0] - 1, s1 = E[1] - 1, e2f = E[2];
+  const double* eg = A.egeo + (size_t)k * 4 * N1;
+  const double nx = eg[i], ny = eg[N1 + i], len = eg[2 * N1 + i], un = eg[3 * N1 + i];
+  double in[NEQ], ex[NEQ], f[NEQ];
+  const double* b1 = A.bs + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
+#pragma unroll
+  for (int v = 0; v < NEQ; ++v) in[v] = b1[i + N1 * v];
+  if (e2f > 0) {
+    const int e2 = e2f - 1, s2 = abs(E[3]) - 1, start = E[4], inc = E[5];
+    const int kk = start - inc + i * inc;
+    const double* b2 = A.bs + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
+    Phys::template riemann<NEQ>(in, ex, nx, ny, un, A.g, f);
+    double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
+    double* o2 = A.bf + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) {
+      const double fl = f[v] * len;
+      o1[i + N1 * v] = fl;
+      o2[kk + N1 * v] = -fl;
+    }
+  } else {
+    Phys::template external<NEQ>(e2f, nx, ny, A.t, in, ex);
+    Phys::template riemann<NEQ>(in, ex, nx, ny, un, A.g, f);
+    double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = f[v] * len;
+  }
+}
+
+// ------------------------------------------------------------------------------------ volume kernel
+template <int N1>
+constexpr int elems_per_block() {
+  return (N1 * N1 >= 256) ? 1 : (256 / (N1 * N1));
+}
+
+template <int N1, int NEQ>
+__device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const double* sq /*[EPB][NEQ][N1*N1]*/,
+                                             double* bs, int e, int tid) {
+  // 4 sides x NEQ x N1 values per element; side 0..3 = S,E,N,W (CalculateSolutionAtBoundaries)
+  constexpr int NV = 4 * NEQ * N1;
+  for (int t = tid; t < NV; t += N1 * N1) {
+    const int k = t % N1;
+    const int v = (t / N1) % NEQ;
+    const int side = t / (N1 * NEQ);
+    const double* Q = sq + v * N1 * N1;
+    double acc = 0.0;
+    if (side == 0 || side == 2) {
+      const double* L = (side == 0) ? C.lS : C.lN;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) acc += L[m] * Q[k + N1 * m];
+    } else {
+      const double* L = (side == 1) ? C.lE : C.lW;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) acc += L[m] * Q[m + N1 * k];
+    }
+    bs[(size_t)N1 * NEQ * (side + 4 * (size_t)e) + k + N1 * v] = acc;
+  }
+}
+
+template <int N1, int NEQ, bool SW>
+__global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
+  constexpr int NN = N1 * N1;
+  constexpr int EPB = elems_per_block<N1>();
+  __shared__ NodalConst<N1> C;
+  __shared__ double sF[EPB][NEQ][NN];
+  __shared__ double sG[EPB][NEQ][NN];
+  __shared__ double sB[EPB][4][NEQ][N1];
+
+  const int tid = threadIdx.x;           // node within element
+  const int le = threadIdx.y;            // element within block
+  const int e = blockIdx.x * EPB + le;
+  const bool active = e < A.nEl;
+  {
+    const int flat = tid + NN * le;
+    constexpr int NC = sizeof(NodalConst<N1>) / sizeof(double);
+    const double* src = reinterpret_cast<const double*>(&Cg);
+    double* dst = reinterpret_cast<double*>(&C);
+    for (int t = flat; t < NC; t += NN * EPB) dst[t] = src[t];
+  }
+  const int i = tid % N1, j = tid / N1;
+  double qv[NEQ];
+  double dxds = 0, dxdp = 0, dyds = 0, dydp = 0, invJ = 0;
+  if (active) {
+    const double* qe = A.q + (size_t)e * NEQ * NN;
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) qv[v] = qe[v * NN + tid];
+    const double* me = A.metrics + (size_t)e * 5 * NN;
+    dxds = me[tid];
+    dxdp = me[NN + tid];
+    dyds = me[2 * NN + tid];
+    dydp = me[3 * NN + tid];
+    invJ = me[4 * NN + tid];
+    // boundary fluxes of this element into shared memory
+    const double* be = A.bf + (size_t)e * 4 * NEQ * N1;
+    double* sb = &sB[le][0][0][0];
+    for (int t = tid; t < 4 * NEQ * N1; t += NN) sb[t] = be[t];
+    double xF[NEQ], yF[NEQ];
+    if (SW) {
+      // XFlux / YFlux (:1608-1658)
+      const double iH = 1.0 / qv[2];
+      const double p = A.g * 0.5 * qv[2] * qv[2];
+      xF[0] = qv[0] * qv[0] * iH + p;
+      xF[1] = qv[0] * qv[1] * iH;
+      xF[2] = qv[0];
+      yF[0] = qv[1] * qv[0] * iH;
+      yF[1] = qv[1] * qv[1] * iH + p;
+      yF[2] = qv[1];
+    } else {
+      const double* ae = A.aux + (size_t)e * A.naux * NN;
+      const double u = ae[tid], vv = ae[NN + tid];
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) {
+        xF[v] = qv[v] * u;
+        yF[v] = qv[v] * vv;
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) {
+      sF[le][v][tid] = dydp * xF[v] - dxdp * yF[v];
+      sG[le][v][tid] = -dyds * xF[v] + dxds * yF[v];
+    }
+  }
+  __syncthreads();
+  double tend[NEQ];
+  if (active) {
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) {
+      // s direction: MATMUL(dMatS, F(:,j)) + lift, along the row j
+      double ds = 0.0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) ds += C.dS[i + N1 * m] * sF[le][v][m + N1 * j];
+      ds += (sB[le][1][v][j] * C.lE[i] + sB[le][3][v][j] * C.lW[i]) * C.qwinv[i];
+      double dp = 0.0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) dp += C.dP[j + N1 * m] * sG[le][v][i + N1 * m];
+      dp += (sB[le][2][v][i] * C.lN[j] + sB[le][0][v][i] * C.lS[j]) * C.qwinv[j];
+      tend[v] = (-ds - dp) * invJ;
+    }
+    const double* ae = A.aux + (size_t)e * A.naux * NN;
+    if (SW) {
+      // Source (:1662-1694)
+      const double dhdx = ae[tid], dhdy = ae[NN + tid], f = ae[2 * NN + tid];
+      double s0 = f * qv[1] + A.g * qv[2] * dhdx;
+      double s1 = -f * qv[0] + A.g * qv[2] * dhdy;
+      double s2 = 0.0;
+      int o = 3;
+      if (A.has_drag) {
+        const double ih = 1.0 / ae[3 * NN + tid];
+        s0 -= A.drag * qv[0] * ih;
+        s1 -= A.drag * qv[1] * ih;
+        o = 4;
+      }
+      if (A.has_relax) {
+        const double ts = ae[(o + 3) * NN + tid];
+        s0 -= (qv[0] - ae[o * NN + tid]) * ts;
+        s1 -= (qv[1] - ae[(o + 1) * NN + tid]) * ts;
+        s2 -= (qv[2] - ae[(o + 2) * NN + tid]) * ts;
+      }
+      tend[0] += s0;
+      tend[1] += s1;
+      if (NEQ > 2) tend[NEQ > 2 ? 2 : 0] += s2;
+    } else if (A.has_relax) {
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) tend[v] += (ae[(2 + v) * NN + tid] - qv[v]) * ae[(2 + NEQ + v) * NN + tid];
+    }
+    if (A.mode == 0) {
+      double* te = A.tend + (size_t)e * NEQ * NN;
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) te[v * NN + tid] = tend[v];
+    } else {
+      double* Ge = A.G + (size_t)e * NEQ * NN;
+      double* qo = A.qout + (size_t)e * NEQ * NN;
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) {
+        double g = (A.mode == 2) ? (A.a * Ge[v * NN + tid] + tend[v]) : tend[v];
+        Ge[v * NN + tid] = g;
+        qv[v] = qv[v] + A.gdt * g;
+        qo[v * NN + tid] = qv[v];
+      }
+    }
+  }
+  if (A.write_traces) {
+    __syncthreads();  // sF is reused for the new state
+    if (active) {
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) sF[le][v][tid] = qv[v];
+    }
+    __syncthreads();
+    if (active) write_traces<N1, NEQ>(C, &sF[le][0][0], A.bs, e, tid);
+  }
+}
+
+// Boundary traces of q alone (start of a run, and the tendency entry point).
+template <int N1, int NEQ>
+__global__ void __launch_bounds__(256) dg_traces(const double* q, double* bs, int nEl, NodalConst<N1> Cg) {
+  constexpr int NN = N1 * N1;
+  constexpr int EPB = elems_per_block<N1>();
+  __shared__ NodalConst<N1> C;
+  __shared__ double sQ[EPB][NEQ][NN];
+  const int tid = threadIdx.x, le = threadIdx.y;
+  const int e = blockIdx.x * EPB + le;
+  {
+    const int flat = tid + NN * le;
+    constexpr int NC = sizeof(NodalConst<N1>) / sizeof(double);
+    const double* src = reinterpret_cast<const double*>(&Cg);
+    double* dst = reinterpret_cast<double*>(&C);
+    for (int t = flat; t < NC; t += NN * EPB) dst[t] = src[t];
+  }
+  if (e < nEl) {
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) sQ[le][v][tid] = q[(size_t)e * NEQ * NN + v * NN + tid];
+  }
+  __syncthreads();
+  if (e < nEl) write_traces<N1, NEQ>(C, &sQ[le][0][0], bs, e, tid);
+}
+
+}  // namespace dg
+}  // namespace selfgpu
+
+// ====================================================================================== handle
+struct self_dg2d {
+  self_ctx* ctx = nullptr;
+  int N = 0, n = 0, nEl = 0, nEdges = 0, nEq = 0, model = 0, precision = 0;
+  int naux = 0, has_drag = 0, has_relax = 0, has_inflow = 0;
+  double g = 9.81, drag = 0.0, dt = 0.0;
+  std::vector<double> dS, dP, lW, lE, lS, lN, qw;
+  DevBuf<double> q, G, bs, bf, metrics, aux, egeo, tend;
+  DevBuf<int> edges;
+  bool traces_valid = false;
+  cudaGraphExec_t step_graph = nullptr;
+  selfgpu::dg32::State* f32 = nullptr;  // FP32 form
+  ~self_dg2d() {
+    if (step_graph) cudaGraphExecDestroy(step_graph);
+    if (f32) selfgpu::dg32::destroy(f32);
+  }
+};
+
+namespace {
+
+using namespace selfgpu::dg;
+
+template <int N1>
+NodalConst<N1> make_const(const self_dg2d* h) {
+  NodalConst<N1> C;
+  for (int k = 0; k < N1 * N1; ++k) {
+    C.dS[k] = h->dS[k];
+    C.dP[k] = h->dP[k];
+  }
+  for (int k = 0; k < N1; ++k) {
+    C.lW[k] = h->lW[k];
+    C.lE[k] = h->lE[k];
+    C.lS[k] = h->lS[k];
+    C.lN[k] = h->lN[k];
+    C.qwinv[k] = 1.0 / h->qw[k];
+  }
+  return C;
+}
+
+template <int N1, int NEQ, bool SW>
+int launch_edge_t(self_dg2d* h, double t) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  EdgeArgs EA;
+  EA.bs = h->bs.p;
+  EA.bf = h->bf.p;
+  EA.edges = h->edges.p;
+  EA.egeo = h->egeo.p;
+  EA.nEdges = h->nEdges;
+  EA.g = h->g;
+  EA.t = t;
+  const int nthr = h->nEdges * N1;
+  if (SW)
+    dg_edge_flux<N1, NEQ, SWFlux><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
+  else
+    dg_edge_flux<N1, NEQ, AdvFlux><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
+template <int N1, int NEQ, bool SW>
+int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend,
+                    int write_traces) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  VolArgs VA;
+  VA.q = qin;
+  VA.qout = qout;
+  VA.G = h->G.p;
+  VA.tend = tend;
+  VA.bf = h->bf.p;
+  VA.bs = h->bs.p;
+  VA.metrics = h->metrics.p;
+  VA.aux = h->aux.p;
+  VA.nEl = h->nEl;
+  VA.naux = h->naux;
+  VA.has_drag = h->has_drag;
+  VA.has_relax = h->has_relax;
+  VA.g = h->g;
+  VA.drag = h->drag;
+  VA.a = a;
+  VA.gdt = gdt;
+  VA.mode = mode;
+  VA.write_traces = write_traces;
+  constexpr int EPB = elems_per_block<N1>();
+  dim3 blk(N1 * N1, EPB);
+  dg_volume<N1, NEQ, SW><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(VA, make_const<N1>(h));
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
+template <int N1, int NEQ, bool SW>
+int launch_stage_t(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout,
+                   double* tend, int write_traces) {
+  int rc = launch_edge_t<N1, NEQ, SW>(h, t);
+  if (rc) return rc;
+  return launch_volume_t<N1, NEQ, SW>(h, mode, a, gdt, qin, qout, tend, write_traces);
+}
+
+template <int N1, int NEQ>
+int launch_traces_t(self_dg2d* h, const double* q) {
+  constexpr int EPB = elems_per_block<N1>();
+  dim3 blk(N1 * N1, EPB);
+  dg_traces<N1, NEQ><<<(h->nEl + EPB - 1) / EPB, blk, 0, h->ctx->stream>>>(q, h->bs.p, h->nEl, make_const<N1>(h));
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+// dispatch over (N+1, nEq, model)
+template <int N1>
+int stage_n(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout, double* tend,
+            int wt) {
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_stage_t<N1, 3, true>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  switch (h->nEq) {
+    case 1: return launch_stage_t<N1, 1, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 2: return launch_stage_t<N1, 2, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 3: return launch_stage_t<N1, 3, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 4: return launch_stage_t<N1, 4, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  }
+  return SELF_ERR_UNSUPPORTED;
+}
+template <int N1>
+int edge_n(self_dg2d* h, double t) {
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_edge_t<N1, 3, true>(h, t);
+  switch (h->nEq) {
+    case 1: return launch_edge_t<N1, 1, false>(h, t);
+    case 2: return launch_edge_t<N1, 2, false>(h, t);
+    case 3: return launch_edge_t<N1, 3, false>(h, t);
+    case 4: return launch_edge_t<N1, 4, false>(h, t);
+  }
+  return SELF_ERR_UNSUPPORTED;
+}
+template <int N1>
+int volume_n(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend, int wt) {
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_volume_t<N1, 3, true>(h, mode, a, gdt, qin, qout, tend, wt);
+  switch (h->nEq) {
+    case 1: return launch_volume_t<N1, 1, false>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 2: return launch_volume_t<N1, 2, false>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 3: return launch_volume_t<N1, 3, false>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 4: return launch_volume_t<N1, 4, false>(h, mode, a, gdt, qin, qout, tend, wt);
+  }
+  return SELF_ERR_UNSUPPORTED;
+}
+template <int N1>
+int traces_n(self_dg2d* h, const double* q) {
+  switch (h->nEq) {
+    case 1: return launch_traces_t<N1, 1>(h, q);
+    case 2: return launch_traces_t<N1, 2>(h, q);
+    case 3: return launch_traces_t<N1, 3>(h, q);
+    case 4: return launch_traces_t<N1, 4>(h, q);
+  }
+  return SELF_ERR_UNSUPPORTED;
+}
+
+#define SELF_DISPATCH_N(FN, ...)                       \
+  switch (h->n) {                                      \
+    case 3: return FN<3>(__VA_ARGS__);                 \
+    case 4: return FN<4>(__VA_ARGS__);                 \
+    case 5: return FN<5>(__VA_ARGS__);                 \
+    case 6: return FN<6>(__VA_ARGS__);                 \
+    case 7: return FN<7>(__VA_ARGS__);                 \
+    case 8: return FN<8>(__VA_ARGS__);                 \
+    case 9: return FN<9>(__VA_ARGS__);                 \
+    case 10: return FN<10>(__VA_ARGS__);               \
+  }                                                    \
+  return SELF_ERR_UNSUPPORTED;
+
+int launch_stage(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout,
+                 double* tend, int wt) {
+  SELF_DISPATCH_N(stage_n, h, mode, a, gdt, t, qin, qout, tend, wt)
+}
+int launch_traces(self_dg2d* h, const double* q) { SELF_DISPATCH_N(traces_n, h, q) }
+int launch_edge_only(self_dg2d* h, double t) { SELF_DISPATCH_N(edge_n, h, t) }
+int launch_volume_only(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend,
+                       int wt) {
+  SELF_DISPATCH_N(volume_n, h, mode, a, gdt, qin, qout, tend, wt)
+}
+
+const double kRK3a[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+const double kRK3b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
+const double kRK3g[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+
+int enqueue_step(self_dg2d* h, double t0) {
+  for (int m = 0; m < 3; ++m) {
+    int rc = launch_stage(h, m == 0 ? 1 : 2, kRK3a[m], kRK3g[m] * h->dt, t0 + kRK3b[m] * h->dt, h->q.p, h->q.p,
+                          nullptr, 1);
+    if (rc) return rc;
+  }
+  return SELF_OK;
+}
+
+template <typename T>
+int upload(self_ctx* ctx, DevBuf<T>& b, const std::vector<T>& host) {
+  if (b.alloc(host.size()) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  SELF_CUDA_TRY(ctx, cudaMemcpy(b.p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return SELF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
+  if (!ctx || !d || !out) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const int n = d->N + 1;
+  if (n < 3 || n > 10) return set_error(ctx, SELF_ERR_UNSUPPORTED, "polynomial degree %d outside 2..9", d->N);
+  if (d->nEl < 1 || d->nEdges < 1) return set_error(ctx, SELF_ERR_INVALID, "empty mesh");
+  if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
+    if (d->nEq != 3) return set_error(ctx, SELF_ERR_INVALID, "shallow water needs nEq = 3");
+    if (!d->h || !d->dhdx || !d->dhdy || !d->fcor) return set_error(ctx, SELF_ERR_INVALID, "missing bathymetry");
+  } else if (d->model == SELF_MODEL_ADVECTION) {
+    if (d->nEq < 1 || d->nEq > 4) return set_error(ctx, SELF_ERR_UNSUPPORTED, "advection nEq must be 1..4");
+    if (!d->u || !d->v) return set_error(ctx, SELF_ERR_INVALID, "missing velocity");
+  } else {
+    return set_error(ctx, SELF_ERR_INVALID, "unknown model %d", d->model);
+  }
+  if (d->precision != SELF_PREC_FP64 && d->precision != SELF_PREC_FP32)
+    return set_error(ctx, SELF_ERR_INVALID, "unknown precision");
+  if (d->precision == SELF_PREC_FP32 && d->model != SELF_MODEL_SW_CONSERVATIVE && d->model != SELF_MODEL_ADVECTION)
+    return set_error(ctx, SELF_ERR_UNSUPPORTED, "FP32 form");
+  std::unique_ptr<self_dg2d> h(new self_dg2d());
+  h->ctx = ctx;
+  h->N = d->N;
+  h->n = n;
+  h->nEl = d->nEl;
+  h->nEdges = d->nEdges;
+  h->nEq = d->nEq;
+  h->model = d->model;
+  h->precision = d->precision;
+  h->g = d->g;
+  h->drag = d->linear_drag;
+  h->dt = d->dt;
+  const size_t NN = (size_t)n * n, nEl = d->nEl;
+  h->dS.assign(d->dmatS, d->dmatS + NN);
+  h->dP.assign(d->dmatP, d->dmatP + NN);
+  h->lW.assign(d->lagW, d->lagW + n);
+  h->lE.assign(d->lagE, d->lagE + n);
+  h->lS.assign(d->lagS, d->lagS + n);
+  h->lN.assign(d->lagN, d->lagN + n);
+  h->qw.assign(d->qweight, d->qweight + n);
+  // edge table validation (all indices are checked here so that the kernels need no bounds tests)
+  std::vector<int> ed(d->edges, d->edges + 6 * (size_t)d->nEdges);
+  for (int k = 0; k < d->nEdges; ++k) {
+    const int* E = &ed[6 * k];
+    if (E[0] < 1 || E[0] > d->nEl || E[1] < 1 || E[1] > 4)
+      return set_error(ctx, SELF_ERR_INVALID, "edge %d: bad primary element/side", k + 1);
+    if (E[2] > 0) {
+      if (E[2] > d->nEl || std::abs(E[3]) < 1 || std::abs(E[3]) > 4)
+        return set_error(ctx, SELF_ERR_INVALID, "edge %d: bad secondary element/side", k + 1);
+      int first = E[4] - E[5], last = first + d->N * E[5];
+      if ((E[5] != 1 && E[5] != -1) || first < 0 || first > d->N || last < 0 || last > d->N)
+        return set_error(ctx, SELF_ERR_INVALID, "edge %d: bad start/increment", k + 1);
+    } else if (E[2] == SELF_INFLOW_ONE || E[2] == SELF_INFLOW_TWO) {
+      h->has_inflow = 1;
+    }
+  }
+  // metric block (dxds, dxdp, dyds, dydp, 1/J) per element
+  std::vector<double> met(5 * NN * nEl);
+  for (size_t e = 0; e < nEl; ++e)
+    for (size_t k = 0; k < NN; ++k) {
+      size_t id = e * NN + k;
+      if (!(d->J[id] != 0.0)) return set_error(ctx, SELF_ERR_INVALID, "zero Jacobian in element %zu", e + 1);
+      met[(e * 5 + 0) * NN + k] = d->dxds[id];
+      met[(e * 5 + 1) * NN + k] = d->dxdp[id];
+      met[(e * 5 + 2) * NN + k] = d->dyds[id];
+      met[(e * 5 + 3) * NN + k] = d->dydp[id];
+      met[(e * 5 + 4) * NN + k] = 1.0 / d->J[id];
+    }
+  // aux block
+  std::vector<const double*> fields;
+  h->has_relax = (d->relax && d->rfac) ? 1 : 0;
+  if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
+    h->has_drag = d->linear_drag != 0.0 ? 1 : 0;
+    fields = {d->dhdx, d->dhdy, d->fcor};
+    if (h->has_drag) fields.push_back(d->h);
+  } else {
+    fields = {d->u, d->v};
+  }
+  h->naux = (int)fields.size();
+  int nrelax = 0;
+  if (h->has_relax) nrelax = (d->model == SELF_MODEL_SW_CONSERVATIVE) ? 4 : 2 * d->nEq;
+  h->naux += nrelax;
+  std::vector<double> aux((size_t)h->naux * NN * nEl);
+  for (size_t e = 0; e < nEl; ++e) {
+    int f = 0;
+    for (const double* src : fields) {
+      for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = src[e * NN + k];
+      ++f;
+    }
+    if (h->has_relax) {
+      for (int v = 0; v < d->nEq; ++v, ++f)
+        for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->relax[(e * d->nEq + v) * NN + k];
+      if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
+        for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->rfac[e * NN + k];
+      } else {
+        for (int v = 0; v < d->nEq; ++v, ++f)
+          for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->rfac[(e * d->nEq + v) * NN + k];
+      }
+    }
+  }
+  // per-edge geometry: primary side normals, lengths and (advection) normal velocity
+  std::vector<double> eg((size_t)4 * n * d->nEdges, 0.0);
+  for (int k = 0; k < d->nEdges; ++k) {
+    const int e1 = ed[6 * k] - 1, s1 = ed[6 * k + 1] - 1;
+    for (int i = 0; i < n; ++i) {
+      size_t ib = (size_t)i + n * (s1 + 4 * (size_t)e1);
+      double nx = d->nhx[ib], ny = d->nhy[ib];
+      eg[(size_t)k * 4 * n + i] = nx;
+      eg[(size_t)k * 4 * n + n + i] = ny;
+      eg[(size_t)k * 4 * n + 2 * n + i] = d->nlen[ib];
+      if (d->model == SELF_MODEL_ADVECTION) {
+        // CalculateVelocityAtBoundaries: Lagrange traces of the element velocity on side s1
+        const double* L = (s1 == 0) ? d->lagS : (s1 == 1) ? d->lagE : (s1 == 2) ? d->lagN : d->lagW;
+        double ub = 0.0, vb = 0.0;
+        for (int m = 0; m < n; ++m) {
+          size_t id = (s1 == 0 || s1 == 2) ? (size_t)e1 * NN + i + n * m : (size_t)e1 * NN + m + n * i;
+          ub += L[m] * d->u[id];
+          vb += L[m] * d->v[id];
+        }
+        eg[(size_t)k * 4 * n + 3 * n + i] = ub * nx + vb * ny;
+      }
+    }
+  }
+  int rc;
+  if ((rc = upload(ctx, h->edges, ed))) return rc;
+  if ((rc = upload(ctx, h->egeo, eg))) return rc;
+  if (d->precision == SELF_PREC_FP64) {
+    if ((rc = upload(ctx, h->metrics, met))) return rc;
+    if ((rc = upload(ctx, h->aux, aux))) return rc;
+    const size_t nq = NN * d->nEq * nEl, nb = (size_t)n * d->nEq * 4 * nEl;
+    if (h->q.alloc(nq) || h->G.alloc(nq) || h->bs.alloc(nb) || h->bf.alloc(nb))
+      return set_error(ctx, SELF_ERR_ALLOC, "device allocation of the state failed");
+    SELF_CUDA_TRY(ctx, cudaMemset(h->q.p, 0, h->q.bytes()));
+    SELF_CUDA_TRY(ctx, cudaMemset(h->G.p, 0, h->G.bytes()));
+    SELF_CUDA_TRY(ctx, cudaMemset(h->bf.p, 0, h->bf.bytes()));
+  } else {
+    h->f32 = selfgpu::dg32::make_state();
+    rc = selfgpu::dg32::create(h.get(), h->f32, d, met, aux, eg);
+    if (rc) return rc;
+  }
+  *out = h.release();
+  return SELF_OK;
+}
+
+int self_dg2d_destroy(self_dg2d* h) {
+  if (!h) return SELF_OK;
+  cudaSetDevice(h->ctx->device);
+  cudaStreamSynchronize(h->ctx->stream);
+  delete h;
+  return SELF_OK;
+}
+
+int self_dg2d_set_state(self_dg2d* h, const double* q) {
+  if (!h || !q) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::set_state(h, h->f32, q);
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->q.p, q, h->q.bytes(), cudaMemcpyHostToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  h->traces_valid = false;
+  return SELF_OK;
+}
+
+int self_dg2d_get_state(self_dg2d* h, double* q) {
+  if (!h || !q) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::get_state(h, h->f32, q);
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(q, h->q.p, h->q.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return SELF_OK;
+}
+
+int self_dg2d_state_device(self_dg2d* h, void** dptr, size_t* bytes) {
+  if (!h || !dptr) return SELF_ERR_INVALID;
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::state_device(h, h->f32, dptr, bytes);
+  *dptr = h->q.p;
+  if (bytes) *bytes = h->q.bytes();
+  return SELF_OK;
+}
+
+int self_dg2d_tendency(self_dg2d* h, double t, double* dqdt) {
+  if (!h) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::tendency(h, h->f32, t, dqdt);
+  if (h->tend.n == 0 && h->tend.alloc(h->q.n) != cudaSuccess)
+    return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  int rc = launch_traces(h, h->q.p);
+  if (rc) return rc;
+  rc = launch_stage(h, 0, 0.0, 0.0, t, h->q.p, nullptr, h->tend.p, 0);
+  if (rc) return rc;
+  if (dqdt) {
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(dqdt, h->tend.p, h->tend.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return SELF_OK;
+}
+
+int self_dg2d_rk3_async(self_dg2d* h, double tn, int nsteps) {
+  if (!h || nsteps < 0) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::rk3(h, h->f32, tn, nsteps);
+  int rc;
+  if (!h->traces_valid) {
+    if ((rc = launch_traces(h, h->q.p))) return rc;
+    h->traces_valid = true;
+  }
+  if (h->has_inflow) {  // time-dependent boundary data: plain launches
+    for (int s = 0; s < nsteps; ++s)
+      if ((rc = enqueue_step(h, tn + s * h->dt))) return rc;
+    return SELF_OK;
+  }
+  if (!h->step_graph) {  // capture one RK3 step (6 kernels) once, replay it nsteps times
+    cudaGraph_t g;
+    SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_step(h, tn);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&h->step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    ctx->launches.fetch_sub(6);  // captured, not launched
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    SELF_CUDA_TRY(ctx, cudaGraphLaunch(h->step_graph, ctx->stream));
+    ctx->launches.fetch_add(6);
+  }
+  return SELF_OK;
+}
+
+int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* ms) {
+  if (!h || !ms || reps < 1) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::time_kernels(h, h->f32, reps, flush_bytes, ms);
+  DevBuf<double> q0, G0;
+  if (q0.alloc(h->q.n) || G0.alloc(h->G.n)) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(q0.p, h->q.p, h->q.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(G0.p, h->G.p, h->G.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  int rc;
+  if (!h->traces_valid) {
+    if ((rc = launch_traces(h, h->q.p))) return rc;
+  }
+  double te = 0, tv = 0, t;
+  for (int r = 0; r < reps; ++r) {
+    // one full stage, each of its two kernels timed alone after an L2 flush
+    if ((rc = self_ctx_flush_l2(ctx, flush_bytes))) return rc;
+    if ((rc = self_ctx_timer_start(ctx))) return rc;
+    if ((rc = launch_edge_only(h, 0.0))) return rc;
+    if ((rc = self_ctx_timer_stop(ctx, &t))) return rc;
+    te += t;
+    if ((rc = self_ctx_flush_l2(ctx, flush_bytes))) return rc;
+    if ((rc = self_ctx_timer_start(ctx))) return rc;
+    if ((rc = launch_volume_only(h, 2, kRK3a[1], kRK3g[1] * h->dt, h->q.p, h->q.p, nullptr, 1))) return rc;
+    if ((rc = self_ctx_timer_stop(ctx, &t))) return rc;
+    tv += t;
+  }
+  ms[0] = te / reps;
+  ms[1] = tv / reps;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->q.p, q0.p, h->q.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->G.p, G0.p, h->G.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  h->traces_valid = false;
+  return SELF_OK;
+}
+
+int self_dg2d_rk3(self_dg2d* h, double tn, int nsteps) {
+  int rc = self_dg2d_rk3_async(h, tn, nsteps);
+  if (rc) return rc;
+  SELF_CUDA_TRY(h->ctx, cudaStreamSynchronize(h->ctx->stream));
+  return SELF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,29 @@
+"""Extract the golden vectors shipped with the reference's 1-D CGSEM example into tests/golden/.
+
+Source (reference output files, read as text, run in the build container where the reference is mounted):
+  examples/elliptic1d/parabola/run/residual.curve  -- CG residual history (N=5, 10 elements, tol 1e-8)
+  examples/elliptic1d/parabola/run/elliptic.curve  -- solution x, u at the GLL nodes
+  examples/elliptic1d/parabola/run/runtime.params  -- the namelist that produced them
+The fixtures keep the numbers verbatim (residual lines up to the first zero entry after convergence).
+"""
+import os
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.dirname(os.path.abspath(__file__))
+run = os.path.join(REF, "examples", "elliptic1d", "parabola", "run")
+
+res = open(os.path.join(run, "residual.curve")).read().splitlines()
+keep = []
+for line in res:
+    keep.append(line)
+    parts = line.split()
+    if len(parts) == 2 and float(parts[1]) == 0.0:
+        break
+open(os.path.join(OUT, "elliptic1d_residual.curve"), "w").write("\n".join(keep) + "\n")
+
+sol = open(os.path.join(run, "elliptic.curve")).read().split("#source")[0]
+open(os.path.join(OUT, "elliptic1d_solution.curve"), "w").write(sol)
+params = open(os.path.join(run, "runtime.params")).read()
+open(os.path.join(OUT, "elliptic1d_runtime.params"), "w").write(params)
+print("wrote", len(keep), "residual lines")

@@ -1,0 +1,138 @@
+"""GPU DGSEM 2-D (plain FP64 drop-in) against the CPU oracle on identical seeded inputs.
+
+Tolerance: per-variable relative error ||gpu - oracle||_inf / ||oracle||_inf <= 1e-12 for one tendency
+evaluation and short RK3 runs, <= 1e-11 after 1000 steps (FMA contraction and 1/J, 1/H multiplications
+on the GPU round differently from the Fortran-order oracle).
+"""
+import numpy as np
+import pytest
+
+from helpers import per_var_rel, rel_inf
+
+pytestmark = pytest.mark.gpu
+
+TOL1 = 1e-12
+TOLLONG = 1e-11
+
+
+def _sw_problem(oracle, N, nx, warp=0.05, seed=7, drag=0.0, relax=False, flow=True):
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, warp=warp, scale=(W.SW_L, W.SW_L))
+    q, h, fcor, dt = W.shallow_water(mesh, N, nx, seed=seed)
+    n2 = (N + 1) ** 2
+    if flow:  # give the state a velocity so every flux and source term is exercised
+        rng = np.random.default_rng(seed + 100)
+        qq = q.reshape(mesh.nEl, 3, n2)
+        qq[:, 0] = rng.normal(0, 50.0, (mesh.nEl, n2))
+        qq[:, 1] = rng.normal(0, 50.0, (mesh.nEl, n2))
+        q = qq.ravel()
+    dhdx, dhdy = sg.bathymetry_gradient(nod, mesh, h)
+    rl = ts = None
+    if relax:
+        rng = np.random.default_rng(seed + 200)
+        rl = (q + rng.normal(0, 1.0, q.size)).copy()
+        ts = np.full(h.size, 1e-4)
+    P = oracle.DGProblem(nod, mesh, 1, 3, dt, g=9.81, drag=drag, h=h, dhdx=dhdx, dhdy=dhdy, fcor=fcor, relax=rl,
+                         rfac=ts)
+    return nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, rl, ts
+
+
+@pytest.mark.parametrize("N,nx,warp,drag,relax", [(3, 4, 0.05, 0.0, False), (7, 16, 0.05, 0.0, False),
+                                                  (5, 6, 0.0, 1e-3, True), (9, 3, 0.05, 0.0, False)])
+def test_sw_tendency_parity(oracle, gpu_ctx, N, nx, warp, drag, relax):
+    import self_gb300 as sg
+    nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, rl, ts = _sw_problem(oracle, N, nx, warp, drag=drag, relax=relax)
+    sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, linear_drag=drag, dhdx=dhdx, dhdy=dhdy, relax=rl,
+                         timescale=ts)
+    sw.SetSolution(q)
+    got = sw.GlobalTimeDerivative(0.0)
+    ref = P.tendency(q)
+    errs = per_var_rel(got, ref, 3, (N + 1) ** 2)
+    assert max(errs) <= TOL1, errs
+    assert np.array_equal(sw.GetSolution(), q)
+
+
+def test_sw_rk3_parity_10_steps(oracle, gpu_ctx):
+    import self_gb300 as sg
+    N, nx = 7, 8
+    nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, _, _ = _sw_problem(oracle, N, nx)
+    sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy)
+    sw.SetSolution(q)
+    sw.ForwardStepRK3(0.0, 10)
+    got = sw.GetSolution()
+    ref = P.rk3(q, 10)
+    errs = per_var_rel(got, ref, 3, (N + 1) ** 2)
+    assert max(errs) <= TOL1, errs
+
+
+def test_sw_lake_at_rest_flat_bottom(gpu_ctx):
+    import self_gb300 as sg
+    N, nx = 5, 4
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, scale=(2e6, 2e6))
+    h = np.full(mesh.x.size, 1000.0)
+    sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, np.full_like(h, 1e-4), 1.0)
+    q = np.zeros((mesh.nEl, 3, (N + 1) ** 2))
+    q[:, 2] = 1000.0
+    sw.SetSolution(q.ravel())
+    td = sw.GlobalTimeDerivative().reshape(mesh.nEl, 3, -1)
+    assert np.abs(td[:, :2]).max() < 1e-9 * 9.81 * 1000.0 ** 2 / (2e6 / nx)
+    assert np.abs(td[:, 2]).max() == 0.0
+
+
+@pytest.mark.parametrize("nEq", [1, 3])
+def test_advection_tendency_parity(oracle, gpu_ctx, nEq):
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    N, nx = 7, 6
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, periodic=(True, True), warp=0.03)
+    c0, u, v, dt = W.advection_periodic(mesh, N, nx)
+    rng = np.random.default_rng(3)
+    u = u + 0.2 * np.sin(2 * np.pi * mesh.y)
+    q = np.concatenate([c0.reshape(mesh.nEl, 1, -1) * (k + 1) for k in range(nEq)], axis=1).ravel()
+    rl = rng.normal(size=q.size)
+    rf = np.abs(rng.normal(size=q.size))
+    P = oracle.DGProblem(nod, mesh, 2, nEq, dt, u=u, v=v, relax=rl, rfac=rf)
+    adv = sg.Advection(gpu_ctx, nod, mesh, u, v, dt, nTracers=nEq, relax=rl, rfac=rf)
+    adv.SetSolution(q)
+    got = adv.GlobalTimeDerivative(0.0)
+    errs = per_var_rel(got, P.tendency(q), nEq, (N + 1) ** 2)
+    assert max(errs) <= TOL1, errs
+
+
+def test_advection_inflow_boundaries(oracle, gpu_ctx):
+    """Non-periodic mesh with InflowOne edges: tanh(t) external state (AdvectionClass.f90:1851-1886)."""
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    N, nx = 4, 5
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, boundary_flag=sg._native.INFLOW_ONE)
+    c0, u, v, dt = W.advection_periodic(mesh, N, nx)
+    P = oracle.DGProblem(nod, mesh, 2, 1, dt, u=u, v=v)
+    adv = sg.Advection(gpu_ctx, nod, mesh, u, v, dt)
+    adv.SetSolution(c0)
+    assert max(per_var_rel(adv.GlobalTimeDerivative(0.7), P.tendency(c0, 0.7), 1, (N + 1) ** 2)) <= TOL1
+    adv.ForwardStepRK3(0.3, 5)
+    ref = P.rk3(c0, 5, tn=0.3)
+    assert rel_inf(adv.GetSolution(), ref) <= TOL1
+
+
+def test_advection_config1_1000_steps(oracle, gpu_ctx):
+    """16x16 periodic, N=7, velocity (1, 0.5), Gaussian, CFL 0.5, 1000 LSRK3 steps: oracle and analytic."""
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    N, nx, steps = 7, 16, 1000
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, periodic=(True, True))
+    c0, u, v, dt = W.advection_periodic(mesh, N, nx)
+    adv = sg.Advection(gpu_ctx, nod, mesh, u, v, dt)
+    adv.SetSolution(c0)
+    adv.ForwardStepRK3(0.0, steps)
+    got = adv.GetSolution()
+    ref = oracle.DGProblem(nod, mesh, 2, 1, dt, u=u, v=v).rk3(c0, steps)
+    assert rel_inf(got, ref) <= TOLLONG
+    ex = W.advection_exact(mesh.x, mesh.y, steps * dt)
+    assert np.abs(got - ex).max() < 1e-4
