@@ -138,6 +138,64 @@ int self_sw_bathymetry_gradient(int N, int nEl, const double* dmatS, const doubl
                                 const double* J, const double* nhx, const double* nhy, const double* nlen,
                                 const double* h, double* dhdx, double* dhdy);
 
+/* ---------------------------------------------------------------- CGSEM 2-D
+ * Replaces CGsemElliptic_2D (CGsemElliptic_2D_Class.f90:57-93) compute procedures on element-local
+ * ("L-vector") arrays u(0:N,0:N,1:nEl) with GLL nodes:
+ *   self_cg2d_matrix_action == %MatrixAction(u, Au)   (:930-976)  u is not modified
+ *   self_cg2d_residual      == %Residual(dirF, r)      (:980-1068) with source(:,:,:) given
+ *   self_cg2d_dot           == %DotProduct(u, v)       (:1072-1110)
+ *   self_cg2d_mask/unmask   == %Mask / %UnMask         (:350-542)
+ *   self_cg2d_solve         == %Solve (PCG, :1114-1207) and IterativeSolver GMRES (IterativeSolvers_Class.f90:493-652)
+ * Operator: op 0 = FluxDivergence - lambda*J*w_i*w_j (weak form of div(k grad u) - lambda u, the reference's
+ * sign); op 1 adds the advection term -J*w_i*w_j*(vx du/dx + vy du/dy) (nonsymmetric; use GMRES). */
+typedef struct {
+  int N, nEl, nEdges, nNodes;
+  const double *dmat, *qweight; /* GLL derivative matrix (CG form) and weights */
+  const int* edges;             /* e2 = SELF_DIRICHLET on Dirichlet edges */
+  const int* nodeType;          /* corner node types (SELF_DIRICHLET marks prescribed nodes) */
+  const int *n2e_ptr, *n2e_elem, *n2e_local; /* corner node -> (element, local corner 1..4), list order */
+  const double *dxds, *dxdp, *dyds, *dydp, *J;
+  const double* fluxCoeff; /* k(i,j,e) */
+  double lambda;
+  int op;
+  double vx, vy;
+} self_cg2d_desc;
+
+#define SELF_SOLVE_CG 0           /* conjugate gradient, no preconditioner */
+#define SELF_SOLVE_PCG_JACOBI 1   /* conjugate gradient, assembled-diagonal (Jacobi) preconditioner */
+#define SELF_SOLVE_GMRES 2        /* GMRES(m), modified Gram-Schmidt + Givens */
+
+typedef struct {
+  int method;             /* SELF_SOLVE_* */
+  int precision;          /* SELF_PREC_FP64: plain; SELF_PREC_FP32: FP32 inner CG under FP64 iterative refinement */
+  int maxIters;           /* iteration cap (total inner iterations for FP32 refinement) */
+  int m;                  /* GMRES restart length */
+  double tolerance;       /* stop at ||r|| / ||r0|| < tolerance (FP64 residual) */
+  double inner_tolerance; /* FP32 inner solve: relative reduction per refinement step (default 1e-4) */
+  int max_outer;          /* refinement steps cap (default 30) */
+} self_solve_opts;
+
+typedef struct {
+  int ioerr;            /* 0 converged, -1 not converged (reference meanings), -2 other */
+  int iterations;       /* CG iterations / GMRES Arnoldi steps (sum over refinement steps) */
+  int outer_iterations; /* refinement steps (1 for FP64) */
+  double r0;            /* ||r0|| (masked FP64 residual of the initial guess) */
+  double rel_residual;  /* final ||r|| / ||r0|| */
+} self_solve_report;
+
+typedef struct self_cg2d self_cg2d;
+int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* desc, self_cg2d** out);
+int self_cg2d_destroy(self_cg2d* h);
+int self_cg2d_matrix_action(self_cg2d* h, const double* u, double* Au);
+int self_cg2d_residual(self_cg2d* h, const double* source, const double* solution, double* r);
+int self_cg2d_dot(self_cg2d* h, const double* u, const double* v, double* out);
+int self_cg2d_mask(self_cg2d* h, double* u);
+int self_cg2d_unmask(self_cg2d* h, double* u);
+/* solution: initial guess in, solution out (unmasked, Dirichlet values from `dirichlet` or 0 when NULL).
+ * resi: NULL or maxIters+1 doubles (||r|| per iteration; per refinement step for the FP32 form). */
+int self_cg2d_solve(self_cg2d* h, const self_solve_opts* opts, const double* source, const double* dirichlet,
+                    double* solution, double* resi, self_solve_report* report);
+
 #ifdef __cplusplus
 }
 #endif

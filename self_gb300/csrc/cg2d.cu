@@ -1,0 +1,1127 @@
+// CGSEM 2-D matrix-free operator, direct-stiffness summation, masks and Krylov solvers on sm_103a.
+//
+// Replaces CGsemElliptic_2D's MatrixAction / Residual / DotProduct / Solve (CGsemElliptic_2D_Class.f90
+// :617-1207) and the GMRES(m) of IterativeSolvers_Class.f90 :493-652 (as used on element-local vectors
+// by Stommel_Class.f90 :1161-1322).
+//
+// Vectors are element-local "L-vectors" (Fortran u(0:N,0:N,1:nEl)), kept MASKED as in the reference:
+// a node shared by several elements holds its value in one primary copy, the other copies are zero, and
+// Dirichlet nodes are zero in every Krylov vector.  Shared-node topology is compiled once on the host into
+//   src[l]           local index of the primary copy of local node l (UnMask = gather x[src[l]]);
+//   groups (CSR)     one group per shared edge node (2 copies, primary first) and per mesh corner node
+//                    (its copies in node->element list order), plus single-copy groups for Dirichlet nodes.
+//                    GlobalSum followed by Mask = sum the group in list order, write the sum to the primary
+//                    copy and zero to the others (Dirichlet groups: zero to all) -- no atomics, the
+//                    summation order of the reference.
+// The element operator uses per-node factors folded on the host:
+//   G11 = k w_i w_j (dydp^2+dxdp^2)/J, G12 = -k w_i w_j (dyds dydp + dxds dxdp)/J, G22 = k w_i w_j (dxds^2+dyds^2)/J,
+//   M = lambda J w_i w_j, and for the advection-diffusion operator B1 = w_i w_j (vx dydp - vy dxdp),
+//   B2 = w_i w_j (vy dxds - vx dyds):
+//   Lu = -( D_s^T (G11 us + G12 up) + D_p^T (G12 us + G22 up) ) - M u - (B1 us + B2 up),  us = D_s u, up = D_p u,
+// which is FluxDivergence (:854-926) with CalculateGradient (:791-850) re-associated, plus the mass and
+// advection terms of the documented operators.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "internal.hpp"
+
+using namespace selfgpu;
+
+namespace selfgpu {
+namespace cg {
+
+// ---------------------------------------------------------------------------------- element operator
+template <int N1, typename R>
+struct CGConst {
+  R D[N1 * N1];  // collocation derivative matrix, column major
+};
+
+template <int N1>
+constexpr int cg_epb() {
+  return (N1 * N1 >= 256) ? 1 : (256 / (N1 * N1));
+}
+
+// out = [alpha*f*Jww] - Lu(x gathered through src), computed per element.  nf = 4 (Helmholtz) or 6 (adv-diff).
+template <int N1, typename R, int NF>
+__global__ void __launch_bounds__(256) cg_apply_local(const R* __restrict__ x, const int* __restrict__ src,
+                                                      const R* __restrict__ fac, const R* __restrict__ rhs,
+                                                      R* __restrict__ out, int nEl, CGConst<N1, R> Cg) {
+  constexpr int NN = N1 * N1;
+  constexpr int EPB = cg_epb<N1>();
+  __shared__ R D[N1 * N1];
+  __shared__ R su[EPB][NN];
+  __shared__ R s1[EPB][NN];
+  __shared__ R s2[EPB][NN];
+  const int tid = threadIdx.x, le = threadIdx.y;
+  const int e = blockIdx.x * EPB + le;
+  for (int t = tid + NN * le; t < N1 * N1; t += NN * EPB) D[t] = Cg.D[t];
+  const bool active = e < nEl;
+  const int i = tid % N1, j = tid / N1;
+  const size_t l = (size_t)e * NN + tid;
+  R u = 0;
+  if (active) {
+    u = x[src[l]];
+    su[le][tid] = u;
+  }
+  __syncthreads();
+  R us = 0, up = 0, G11 = 0, G12 = 0, G22 = 0, M = 0;
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      us += D[i + N1 * m] * su[le][m + N1 * j];
+      up += D[j + N1 * m] * su[le][i + N1 * m];
+    }
+    const R* fe = fac + (size_t)e * NF * NN;
+    G11 = fe[tid];
+    G12 = fe[NN + tid];
+    G22 = fe[2 * NN + tid];
+    M = fe[3 * NN + tid];
+    s1[le][tid] = G11 * us + G12 * up;
+    s2[le][tid] = G12 * us + G22 * up;
+  }
+  __syncthreads();
+  if (active) {
+    R a = 0, b = 0;
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      a += D[m + N1 * i] * s1[le][m + N1 * j];  // (D^T F1)(i, j)
+      b += D[m + N1 * j] * s2[le][i + N1 * m];  // (D^T F2)(i, j)
+    }
+    R Lu = -(a + b) - M * u;
+    if (NF == 6) {
+      const R* fe = fac + (size_t)e * NF * NN;
+      Lu -= fe[4 * NN + tid] * us + fe[5 * NN + tid] * up;
+    }
+    out[l] = rhs ? (rhs[l] - Lu) : Lu;
+  }
+}
+
+// GlobalSum + Mask over the shared-node groups (one thread per group).
+template <typename R>
+__global__ void cg_dss_mask(R* __restrict__ v, const int* __restrict__ gptr, const int* __restrict__ gidx,
+                            const unsigned char* __restrict__ gdir, int ngroups) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  const int a = gptr[g], b = gptr[g + 1];
+  if (gdir[g]) {
+    for (int k = a; k < b; ++k) v[gidx[k]] = 0;
+    return;
+  }
+  R s = 0;
+  for (int k = a; k < b; ++k) s += v[gidx[k]];
+  v[gidx[a]] = s;
+  for (int k = a + 1; k < b; ++k) v[gidx[k]] = 0;
+}
+
+// ---------------------------------------------------------------------------------- reductions
+constexpr int kRedThreads = 256;
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T sh[kRedThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) sh[w] = v;
+  __syncthreads();
+  T r = 0;
+  if (w == 0) {
+    r = (ln < kRedThreads / 32) ? sh[ln] : T(0);
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+// partial[k * nblk + blockIdx] = sum a_k * b_k (up to 2 dot products in one pass), FP64 accumulation
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) dot2_partials(const R* __restrict__ a0, const R* __restrict__ b0,
+                                                             const R* __restrict__ a1, const R* __restrict__ b1,
+                                                             size_t n, double* __restrict__ partial) {
+  double s0 = 0, s1 = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    s0 += (double)a0[k] * (double)b0[k];
+    if (a1) s1 += (double)a1[k] * (double)b1[k];
+  }
+  s0 = block_sum(s0);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
+  if (a1) {
+    s1 = block_sum(s1);
+    if (threadIdx.x == 0) partial[gridDim.x + blockIdx.x] = s1;
+  }
+}
+
+// deterministic final sum of nblk partials per slot, into out[slot]
+__global__ void __launch_bounds__(kRedThreads) reduce_partials(const double* __restrict__ partial, int nblk,
+                                                               int nslots, double* __restrict__ out) {
+  for (int s = 0; s < nslots; ++s) {
+    double v = 0;
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) v += partial[(size_t)s * nblk + k];
+    v = block_sum(v);
+    if (threadIdx.x == 0) out[s] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------------- CG scalar logic
+// Device scalar state of one GMRES cycle.
+struct GMScalars {
+  double r0, rc, tol;
+  int i, nr, done, breakdown;
+};
+
+// Device scalar state of one (P)CG solve.
+struct CGScalars {
+  double num, den, vz, rr, r0, tol;
+  int iter, done, ioerr, maxIters;
+};
+
+// w = r * dinv (dinv = 1 when no preconditioner) ; partial <r,w>  (also <r,r> in slot 1)
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) pcg_precond(const R* __restrict__ r, const R* __restrict__ dinv,
+                                                           R* __restrict__ w, size_t n, double* __restrict__ partial,
+                                                           const CGScalars* __restrict__ S) {
+  if (S->done) return;
+  double s0 = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    R wk = dinv ? r[k] * dinv[k] : r[k];
+    w[k] = wk;
+    s0 += (double)r[k] * (double)wk;
+  }
+  s0 = block_sum(s0);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
+}
+
+// v = w + beta v (beta = num/den, first iteration v = w), from the reduced <r,w>
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) pcg_update_v(const R* __restrict__ w, R* __restrict__ v, size_t n,
+                                                            const double* __restrict__ red, CGScalars* S) {
+  if (S->done) return;
+  const double num = red[0];
+  const bool first = (S->iter == 0);
+  const R beta = first ? R(0) : (R)(num / S->den);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    v[k] = first ? w[k] : w[k] + beta * v[k];
+  if (blockIdx.x == 0 && threadIdx.x == 0) S->num = num;
+}
+
+// u += a v ; r -= a z  with a = num / <v,z>; partial <r,r>
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) pcg_update_ur(R* __restrict__ u, R* __restrict__ r,
+                                                             const R* __restrict__ v, const R* __restrict__ z,
+                                                             size_t n, const double* __restrict__ red_vz,
+                                                             const CGScalars* __restrict__ S,
+                                                             double* __restrict__ partial) {
+  if (S->done) return;
+  const R a = (R)(S->num / red_vz[0]);
+  double s0 = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    u[k] += a * v[k];
+    R rk = r[k] - a * z[k];
+    r[k] = rk;
+    s0 += (double)rk * (double)rk;
+  }
+  s0 = block_sum(s0);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
+}
+
+// end of iteration: den = num, resi(iter) = ||r||, convergence test ||r||/||r0|| < tol
+__global__ void pcg_end_iter(const double* __restrict__ red_rr, CGScalars* S, double* __restrict__ resi) {
+  if (S->done) return;
+  const double rn = sqrt(red_rr[0]);
+  S->den = S->num;
+  S->iter += 1;
+  if (resi) resi[S->iter] = rn;
+  S->rr = rn;
+  if (!(rn == rn) || isinf(rn)) {  // non-finite residual
+    S->done = 1;
+    S->ioerr = -7;
+    return;
+  }
+  if (rn / S->r0 < S->tol) {
+    S->done = 1;
+    S->ioerr = 0;
+  } else if (S->iter >= S->maxIters) {
+    S->done = 1;
+    S->ioerr = -1;
+  }
+}
+
+// ---------------------------------------------------------------------------------- generic vector ops
+template <typename R>
+__global__ void axpby(R* __restrict__ y, const R* __restrict__ x, R a, R b, size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    y[k] = a * x[k] + b * y[k];
+}
+
+template <typename R>
+__global__ void scale_copy(R* __restrict__ y, const R* __restrict__ x, const double* __restrict__ s, int inv,
+                           size_t n) {
+  const double f = inv ? 1.0 / s[0] : s[0];
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    y[k] = (R)(f * (double)x[k]);
+}
+
+// y -= h * x where h = red[0]; and partial <x_next, y> when x_next != NULL (MGS fused step)
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) mgs_axpy_dot(R* __restrict__ y, const R* __restrict__ x,
+                                                            const double* __restrict__ red, const R* __restrict__ xn,
+                                                            size_t n, double* __restrict__ partial) {
+  const R h = (R)red[0];
+  double s0 = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    R yk = y[k] - h * x[k];
+    y[k] = yk;
+    if (xn) s0 += (double)xn[k] * (double)yk;
+    else s0 += (double)yk * (double)yk;
+  }
+  s0 = block_sum(s0);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
+}
+
+// x += sum_k V_k y_k
+template <typename R>
+__global__ void gmres_update(R* __restrict__ x, const R* __restrict__ V, const double* __restrict__ y, int nr,
+                             size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int j = 0; j < nr; ++j) s += (double)V[(size_t)j * n + k] * y[j];
+    x[k] += (R)s;
+  }
+}
+
+template <typename R, typename S>
+__global__ void convert(R* __restrict__ y, const S* __restrict__ x, size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    y[k] = (R)x[k];
+}
+
+}  // namespace cg
+}  // namespace selfgpu
+
+// ====================================================================================== handle
+using namespace selfgpu::cg;
+
+namespace {
+
+template <typename T>
+int upload(self_ctx* ctx, DevBuf<T>& b, const std::vector<T>& host) {
+  if (b.alloc(host.size()) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  if (!host.empty())
+    SELF_CUDA_TRY(ctx, cudaMemcpy(b.p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return SELF_OK;
+}
+
+inline int grid_for(const self_ctx* ctx, size_t n) {
+  size_t want = (n + kRedThreads - 1) / kRedThreads;
+  size_t cap = (size_t)std::max(1, ctx->num_sms) * 8;  // 8 CTAs of 256 threads per SM, grid-stride loops
+  return (int)std::max<size_t>(1, std::min(want, cap));
+}
+
+}  // namespace
+
+namespace selfgpu {
+namespace cg {
+
+// Operator data on the device in precision R.
+template <typename R>
+struct OpData {
+  DevBuf<R> fac;   // NF * n^2 per element
+  DevBuf<R> rhs_scale;  // J w_i w_j per node (load vector of the residual)
+  DevBuf<R> dinv;  // 1 / assembled diagonal (masked positions 1)
+  std::vector<R> D;
+};
+
+}  // namespace cg
+}  // namespace selfgpu
+
+struct self_cg2d {
+  self_ctx* ctx = nullptr;
+  int N = 0, n = 0, nEl = 0, nEdges = 0, nNodes = 0, op = 0, nf = 4;
+  size_t nl = 0;
+  double lambda = 0, vx = 0, vy = 0;
+  DevBuf<int> src, gptr, gidx;
+  DevBuf<unsigned char> gdir;
+  int ngroups = 0;
+  std::vector<int> h_src, h_gptr, h_gidx;
+  std::vector<unsigned char> h_gdir;
+  selfgpu::cg::OpData<double> op64;
+  selfgpu::cg::OpData<float> op32;
+  bool have32 = false;
+  // work vectors (FP64)
+  DevBuf<double> u, r, v, w, z, f, t, partial, red, resi;
+  DevBuf<selfgpu::cg::CGScalars> S;
+  // FP32 work vectors for the inner solves
+  DevBuf<float> u32, r32, v32, w32, z32;
+  DevBuf<double> gm_V, gm_y;  // GMRES basis (m+1) * nl, y
+  DevBuf<float> gm_V32;
+  DevBuf<double> gm_H, gm_rho, gm_c, gm_s, gm_bhat;
+  DevBuf<selfgpu::cg::GMScalars> GS;
+  std::vector<double> h_J, h_w;
+  int nblk = 0;
+};
+
+namespace {
+
+template <int N1, typename R, int NF>
+void launch_apply_t(self_cg2d* h, const R* x, const R* fac, const R* rhs, R* out, const std::vector<R>& D) {
+  CGConst<N1, R> C;
+  for (int k = 0; k < N1 * N1; ++k) C.D[k] = D[k];
+  constexpr int EPB = cg_epb<N1>();
+  dim3 blk(N1 * N1, EPB);
+  cg_apply_local<N1, R, NF><<<(h->nEl + EPB - 1) / EPB, blk, 0, h->ctx->stream>>>(x, h->src.p, fac, rhs, out,
+                                                                                 h->nEl, C);
+}
+
+template <typename R>
+int launch_apply(self_cg2d* h, const R* x, const R* rhs, R* out, const selfgpu::cg::OpData<R>& od) {
+  const R* fac = od.fac.p;
+  const bool adv = h->nf == 6;
+#define SELF_CG_CASE(NV)                                                       \
+  case NV:                                                                     \
+    if (adv)                                                                   \
+      launch_apply_t<NV, R, 6>(h, x, fac, rhs, out, od.D);                     \
+    else                                                                       \
+      launch_apply_t<NV, R, 4>(h, x, fac, rhs, out, od.D);                     \
+    break;
+  switch (h->n) {
+    SELF_CG_CASE(3)
+    SELF_CG_CASE(4)
+    SELF_CG_CASE(5)
+    SELF_CG_CASE(6)
+    SELF_CG_CASE(7)
+    SELF_CG_CASE(8)
+    SELF_CG_CASE(9)
+    SELF_CG_CASE(10)
+    default:
+      return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "CG degree %d", h->N);
+  }
+#undef SELF_CG_CASE
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+template <typename R>
+int launch_dss(self_cg2d* h, R* v) {
+  if (h->ngroups == 0) return SELF_OK;
+  cg_dss_mask<R><<<(h->ngroups + 255) / 256, 256, 0, h->ctx->stream>>>(v, h->gptr.p, h->gidx.p, h->gdir.p,
+                                                                       h->ngroups);
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+// MatrixAction: out = Mask(GlobalSum(L(UnMask(x))))
+template <typename R>
+int matrix_action(self_cg2d* h, const R* x, R* out, const selfgpu::cg::OpData<R>& od) {
+  int rc = launch_apply<R>(h, x, nullptr, out, od);
+  if (rc) return rc;
+  return launch_dss<R>(h, out);
+}
+
+// red[0..slots) = dot products (FP64 accumulation)
+template <typename R>
+int dots(self_cg2d* h, const R* a0, const R* b0, const R* a1, const R* b1, double* red) {
+  cudaStream_t st = h->ctx->stream;
+  dot2_partials<R><<<h->nblk, kRedThreads, 0, st>>>(a0, b0, a1, b1, h->nl, h->partial.p);
+  SELF_LAUNCHED(h->ctx);
+  reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, a1 ? 2 : 1, red);
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+int read_scalar(self_cg2d* h, const double* dptr, double* out) {
+  SELF_CUDA_TRY(h->ctx, cudaMemcpyAsync(out, dptr, sizeof(double), cudaMemcpyDeviceToHost, h->ctx->stream));
+  SELF_CUDA_TRY(h->ctx, cudaStreamSynchronize(h->ctx->stream));
+  return SELF_OK;
+}
+
+template <typename R>
+int residual(self_cg2d* h, const R* f, const R* sol, R* r, const selfgpu::cg::OpData<R>& od) {
+  int rc = launch_apply<R>(h, sol, f, r, od);  // r = f*Jww - L(unmask(sol))
+  if (rc) return rc;
+  return launch_dss<R>(h, r);
+}
+
+}  // namespace
+
+namespace selfgpu {
+namespace cg {
+
+
+// (P)CG iterations on the device from the current residual; returns ioerr and fills iters/resi.
+template <typename R>
+int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int maxIters, double tol, double r0,
+               double* resi_dev, int* iters, double* rel, const OpData<R>& od) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  CGScalars hs{};
+  hs.r0 = r0;
+  hs.tol = tol;
+  hs.maxIters = maxIters;
+  hs.iter = 0;
+  hs.done = (r0 < tol) || maxIters <= 0;
+  hs.ioerr = hs.done ? 0 : -2;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+  int rc;
+  const int check_every = 16;
+  for (int it = 0; it < maxIters; ++it) {
+    pcg_precond<R><<<h->nblk, kRedThreads, 0, st>>>(r, dinv, w, h->nl, h->partial.p, h->S.p);
+    SELF_LAUNCHED(ctx);
+    reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, 1, h->red.p);
+    SELF_LAUNCHED(ctx);
+    pcg_update_v<R><<<h->nblk, kRedThreads, 0, st>>>(w, v, h->nl, h->red.p, h->S.p);
+    SELF_LAUNCHED(ctx);
+    if ((rc = matrix_action<R>(h, v, z, od))) return rc;
+    if ((rc = dots<R>(h, v, z, nullptr, nullptr, h->red.p + 1))) return rc;
+    pcg_update_ur<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, v, z, h->nl, h->red.p + 1, h->S.p, h->partial.p);
+    SELF_LAUNCHED(ctx);
+    reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, 1, h->red.p + 2);
+    SELF_LAUNCHED(ctx);
+    pcg_end_iter<<<1, 1, 0, st>>>(h->red.p + 2, h->S.p, resi_dev);
+    SELF_LAUNCHED(ctx);
+    if ((it + 1) % check_every == 0 || it + 1 == maxIters) {
+      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (hs.done) break;
+    }
+  }
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  *iters = hs.iter;
+  *rel = hs.iter > 0 ? hs.rr / r0 : 0.0;
+  if (!hs.done) hs.ioerr = -1;
+  return hs.ioerr;
+}
+
+}  // namespace cg
+}  // namespace selfgpu
+
+
+// ---------------------------------------------------------------------------------- GMRES scalars
+namespace selfgpu {
+namespace cg {
+
+// After the Arnoldi step i (0-based): H(:, i) holds h(1..i+2, i+1) of the reference (hnext = h(i+2,i+1)).
+// Applies the previous Givens rotations to the new column, forms the new rotation, updates bhat and
+// the residual estimate (IterativeSolvers_Class.f90:560-600), all in FP64.
+__global__ void gmres_givens(const double* __restrict__ hcol, int i, int m, double* rho, double* c, double* s,
+                             double* bhat, GMScalars* G, double* resi, int l) {
+  // hcol[0..i] = h(1..i+1, i+1) ; hcol[i+1] = ||w||
+  const double hn = sqrt(hcol[i + 1]);
+  double* R = rho + (size_t)i * m;  // column i of rho (rho(k, i+1) at R[k])
+  G->nr = i + 1;
+  const double aeps = 2.220446049250313e-16;
+  if (fabs(hn) <= aeps) {  // AlmostEqual(h(i+1,i), 0): lucky breakdown
+    G->breakdown = 1;
+    G->done = 1;
+    return;
+  }
+  R[0] = hcol[0];
+  for (int k = 1; k <= i; ++k) {
+    const double g = c[k - 1] * R[k - 1] + s[k - 1] * hcol[k];
+    R[k] = -s[k - 1] * R[k - 1] + c[k - 1] * hcol[k];
+    R[k - 1] = g;
+  }
+  const double d = sqrt(R[i] * R[i] + hn * hn);
+  c[i] = R[i] / d;
+  s[i] = hn / d;
+  R[i] = c[i] * R[i] + s[i] * hn;
+  bhat[i + 1] = -s[i] * bhat[i];
+  bhat[i] = c[i] * bhat[i];
+  G->rc = fabs(bhat[i + 1]);
+  if (resi) resi[l] = G->rc;
+  if (G->rc / G->r0 <= G->tol) G->done = 1;
+}
+
+// back substitution of the triangular system (rho y = bhat) for nr columns
+__global__ void gmres_backsolve(const double* __restrict__ rho, const double* __restrict__ bhat, int m,
+                                const GMScalars* __restrict__ G, double* y) {
+  const int nr = G->nr;
+  auto RHO = [&](int k, int j) { return rho[(size_t)j * m + k]; };
+  y[nr - 1] = bhat[nr - 1] / RHO(nr - 1, nr - 1);
+  for (int k = nr - 2; k >= 0; --k) {
+    double t = bhat[k];
+    for (int j = k + 1; j < nr; ++j) t -= RHO(k, j) * y[j];
+    y[k] = t / RHO(k, k);
+  }
+}
+
+__global__ void sqrt_scalar(const double* __restrict__ a, double* __restrict__ b) { b[0] = sqrt(a[0]); }
+
+}  // namespace cg
+}  // namespace selfgpu
+
+namespace {
+
+using namespace selfgpu::cg;
+
+// Shared-node topology: groups and primary-copy gather indices (CGsemElliptic_2D_Class.f90 :350-787)
+int compile_topology(self_cg2d* h, const self_cg2d_desc* d) {
+  const int n = h->n, N = h->N;
+  const size_t NN = (size_t)n * n;
+  auto side_node = [&](int side, int k, int& i, int& j) {
+    switch (side) {
+      case 1: i = k; j = 0; break;
+      case 2: i = N; j = k; break;
+      case 3: i = k; j = N; break;
+      default: i = 0; j = k; break;
+    }
+  };
+  auto corner = [&](int c, int& i, int& j) {
+    static const int ci[4] = {0, 1, 1, 0}, cj[4] = {0, 0, 1, 1};
+    i = ci[c - 1] * N;
+    j = cj[c - 1] * N;
+  };
+  auto lid = [&](int e1based, int i, int j) { return (int)((size_t)(e1based - 1) * NN + i + (size_t)n * j); };
+  h->h_src.resize(h->nl);
+  for (size_t k = 0; k < h->nl; ++k) h->h_src[k] = (int)k;
+  h->h_gptr.assign(1, 0);
+  h->h_gidx.clear();
+  h->h_gdir.clear();
+  for (int k = 0; k < d->nEdges; ++k) {
+    const int* E = d->edges + 6 * k;
+    if (E[0] < 1 || E[0] > d->nEl || E[1] < 1 || E[1] > 4)
+      return set_error(h->ctx, SELF_ERR_INVALID, "edge %d: bad primary element/side", k + 1);
+    if (E[2] > 0) {
+      if (E[2] > d->nEl || std::abs(E[3]) < 1 || std::abs(E[3]) > 4 || (E[5] != 1 && E[5] != -1))
+        return set_error(h->ctx, SELF_ERR_INVALID, "edge %d: bad secondary element/side", k + 1);
+      int nn = E[4];
+      for (int m = 1; m <= N - 1; ++m, nn += E[5]) {
+        if (nn < 1 || nn > N - 1) return set_error(h->ctx, SELF_ERR_INVALID, "edge %d: bad start/inc", k + 1);
+        int i1, j1, i2, j2;
+        side_node(E[1], m, i1, j1);
+        side_node(std::abs(E[3]), nn, i2, j2);
+        int a = lid(E[0], i1, j1), b = lid(E[2], i2, j2);
+        h->h_gidx.push_back(a);
+        h->h_gidx.push_back(b);
+        h->h_gptr.push_back((int)h->h_gidx.size());
+        h->h_gdir.push_back(0);
+        h->h_src[b] = a;
+      }
+    } else if (E[2] == SELF_DIRICHLET) {
+      for (int m = 1; m <= N - 1; ++m) {
+        int i1, j1;
+        side_node(E[1], m, i1, j1);
+        h->h_gidx.push_back(lid(E[0], i1, j1));
+        h->h_gptr.push_back((int)h->h_gidx.size());
+        h->h_gdir.push_back(1);
+      }
+    }
+  }
+  for (int nd = 0; nd < d->nNodes; ++nd) {
+    const int a = d->n2e_ptr[nd], b = d->n2e_ptr[nd + 1];
+    if (b <= a) continue;
+    const bool dir = d->nodeType[nd] == SELF_DIRICHLET;
+    int first = -1;
+    for (int c = a; c < b; ++c) {
+      if (d->n2e_elem[c] < 1 || d->n2e_elem[c] > d->nEl || d->n2e_local[c] < 1 || d->n2e_local[c] > 4)
+        return set_error(h->ctx, SELF_ERR_INVALID, "node %d: bad element list", nd + 1);
+      int i, j;
+      corner(d->n2e_local[c], i, j);
+      int l = lid(d->n2e_elem[c], i, j);
+      h->h_gidx.push_back(l);
+      if (first < 0) first = l;
+      if (!dir) h->h_src[l] = first;
+    }
+    h->h_gptr.push_back((int)h->h_gidx.size());
+    h->h_gdir.push_back(dir ? 1 : 0);
+  }
+  h->ngroups = (int)h->h_gdir.size();
+  int rc;
+  if ((rc = upload(h->ctx, h->src, h->h_src))) return rc;
+  if ((rc = upload(h->ctx, h->gptr, h->h_gptr))) return rc;
+  if ((rc = upload(h->ctx, h->gidx, h->h_gidx))) return rc;
+  if ((rc = upload(h->ctx, h->gdir, h->h_gdir))) return rc;
+  return SELF_OK;
+}
+
+// Folded element factors, Jacobi diagonal; FP64 master copy, FP32 copy for the inner solves.
+int build_factors(self_cg2d* h, const self_cg2d_desc* d, std::vector<double>& Jww) {
+  const int n = h->n;
+  const size_t NN = (size_t)n * n;
+  const int nf = h->nf;
+  std::vector<double> fac((size_t)nf * NN * h->nEl), diag(h->nl);
+  Jww.resize(h->nl);
+  const double* D = d->dmat;
+  const double* w = d->qweight;
+  for (int e = 0; e < h->nEl; ++e)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const size_t id = (size_t)e * NN + i + (size_t)n * j;
+        const double J = d->J[id];
+        if (!(J != 0.0)) return set_error(h->ctx, SELF_ERR_INVALID, "zero Jacobian in element %d", e + 1);
+        const double k = d->fluxCoeff[id], ww = w[i] * w[j];
+        const double xs = d->dxds[id], xp = d->dxdp[id], ys = d->dyds[id], yp = d->dydp[id];
+        double* fe = &fac[(size_t)e * nf * NN];
+        const size_t t = i + (size_t)n * j;
+        fe[t] = k * ww * (yp * yp + xp * xp) / J;
+        fe[NN + t] = -k * ww * (ys * yp + xs * xp) / J;
+        fe[2 * NN + t] = k * ww * (xs * xs + ys * ys) / J;
+        fe[3 * NN + t] = h->lambda * J * ww;
+        if (nf == 6) {
+          fe[4 * NN + t] = ww * (h->vx * yp - h->vy * xp);
+          fe[5 * NN + t] = ww * (h->vy * xs - h->vx * ys);
+        }
+        Jww[id] = J * w[i] * w[j];
+      }
+  // local diagonal (operator applied to unit vectors, closed form)
+  for (int e = 0; e < h->nEl; ++e) {
+    const double* fe = &fac[(size_t)e * nf * NN];
+    for (int b = 0; b < n; ++b)
+      for (int a = 0; a < n; ++a) {
+        double s1 = 0, s2 = 0;
+        for (int m = 0; m < n; ++m) {
+          s1 += D[m + a * n] * D[m + a * n] * fe[m + (size_t)n * b];
+          s2 += D[m + b * n] * D[m + b * n] * fe[2 * NN + a + (size_t)n * m];
+        }
+        const size_t t = a + (size_t)n * b;
+        double v = -(s1 + s2 + 2.0 * D[a + a * n] * D[b + b * n] * fe[NN + t]) - fe[3 * NN + t];
+        if (nf == 6) v -= fe[4 * NN + t] * D[a + a * n] + fe[5 * NN + t] * D[b + b * n];
+        diag[(size_t)e * NN + t] = v;
+      }
+  }
+  // assemble over the groups: primary copy gets the sum, masked copies get 1
+  std::vector<double> dinv(h->nl);
+  for (size_t k = 0; k < h->nl; ++k) dinv[k] = 1.0 / diag[k];
+  for (int g = 0; g < h->ngroups; ++g) {
+    const int a = h->h_gptr[g], b = h->h_gptr[g + 1];
+    double s = 0;
+    for (int k = a; k < b; ++k) s += diag[h->h_gidx[k]];
+    for (int k = a; k < b; ++k) dinv[h->h_gidx[k]] = 1.0;
+    if (!h->h_gdir[g]) dinv[h->h_gidx[a]] = 1.0 / s;
+  }
+  int rc;
+  if ((rc = upload(h->ctx, h->op64.fac, fac))) return rc;
+  if ((rc = upload(h->ctx, h->op64.dinv, dinv))) return rc;
+  h->op64.D.assign(D, D + NN);
+  std::vector<float> f32(fac.begin(), fac.end()), di32(dinv.begin(), dinv.end());
+  if ((rc = upload(h->ctx, h->op32.fac, f32))) return rc;
+  if ((rc = upload(h->ctx, h->op32.dinv, di32))) return rc;
+  h->op32.D.assign(D, D + NN);
+  h->have32 = true;
+  return SELF_OK;
+}
+
+int ensure(self_ctx* ctx, DevBuf<double>& b, size_t n) {
+  if (b.n >= n) return SELF_OK;
+  if (b.alloc(n) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu doubles", n);
+  return SELF_OK;
+}
+int ensuref(self_ctx* ctx, DevBuf<float>& b, size_t n) {
+  if (b.n >= n) return SELF_OK;
+  if (b.alloc(n) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu floats", n);
+  return SELF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* d, self_cg2d** out) {
+  if (!ctx || !d || !out) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (d->N < 2 || d->N > 9) return set_error(ctx, SELF_ERR_UNSUPPORTED, "CG degree %d outside 2..9", d->N);
+  if (d->nEl < 1) return set_error(ctx, SELF_ERR_INVALID, "empty mesh");
+  if (d->op != 0 && d->op != 1) return set_error(ctx, SELF_ERR_INVALID, "operator %d", d->op);
+  std::unique_ptr<self_cg2d> h(new self_cg2d());
+  h->ctx = ctx;
+  h->N = d->N;
+  h->n = d->N + 1;
+  h->nEl = d->nEl;
+  h->nEdges = d->nEdges;
+  h->nNodes = d->nNodes;
+  h->op = d->op;
+  h->nf = d->op == 1 ? 6 : 4;
+  h->lambda = d->lambda;
+  h->vx = d->vx;
+  h->vy = d->vy;
+  h->nl = (size_t)h->n * h->n * h->nEl;
+  int rc = compile_topology(h.get(), d);
+  if (rc) return rc;
+  std::vector<double> Jww;
+  if ((rc = build_factors(h.get(), d, Jww))) return rc;
+  h->h_J.assign(d->J, d->J + h->nl);
+  h->h_w.assign(d->qweight, d->qweight + h->n);
+  h->nblk = grid_for(ctx, h->nl);
+  if ((rc = ensure(ctx, h->partial, (size_t)2 * h->nblk))) return rc;
+  if ((rc = ensure(ctx, h->red, 8))) return rc;
+  if (h->S.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  if ((rc = ensure(ctx, h->t, h->nl))) return rc;
+  *out = h.release();
+  return SELF_OK;
+}
+
+int self_cg2d_destroy(self_cg2d* h) {
+  if (!h) return SELF_OK;
+  cudaSetDevice(h->ctx->device);
+  cudaStreamSynchronize(h->ctx->stream);
+  delete h;
+  return SELF_OK;
+}
+
+// MatrixAction: Au = Mask(GlobalSum(L(UnMask(u)))).  u is read only (the reference leaves u masked).
+int self_cg2d_matrix_action(self_cg2d* h, const double* u, double* Au) {
+  if (!h || !u || !Au) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  int rc;
+  if ((rc = ensure(ctx, h->v, h->nl)) || (rc = ensure(ctx, h->z, h->nl))) return rc;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->v.p, u, h->nl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  if ((rc = matrix_action<double>(h, h->v.p, h->z.p, h->op64))) return rc;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(Au, h->z.p, h->nl * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return SELF_OK;
+}
+
+}  // extern "C"
+
+namespace selfgpu {
+namespace cg {
+
+// Mask: zero non-primary copies and Dirichlet nodes
+template <typename R>
+__global__ void cg_mask(R* __restrict__ v, const int* __restrict__ gptr, const int* __restrict__ gidx,
+                        const unsigned char* __restrict__ gdir, int ngroups) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  const int a = gptr[g], b = gptr[g + 1];
+  for (int k = gdir[g] ? a : a + 1; k < b; ++k) v[gidx[k]] = 0;
+}
+
+// UnMask: out[l] = in[src[l]]
+template <typename R>
+__global__ void cg_unmask(R* __restrict__ out, const R* __restrict__ in, const int* __restrict__ src, size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = in[src[k]];
+}
+
+}  // namespace cg
+}  // namespace selfgpu
+
+namespace {
+
+std::vector<double> make_load(const self_cg2d* h, const double* source) {
+  std::vector<double> f(h->nl);
+  const int n = h->n;
+  const size_t NN = (size_t)n * n;
+  for (size_t e = 0; e < (size_t)h->nEl; ++e)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const size_t id = e * NN + i + (size_t)n * j;
+        f[id] = source[id] * h->h_J[id] * h->h_w[i] * h->h_w[j];  // source*J*ws(iS)*wp(iP)
+      }
+  return f;
+}
+
+int upload_vec(self_cg2d* h, DevBuf<double>& b, const double* host) {
+  int rc = ensure(h->ctx, b, h->nl);
+  if (rc) return rc;
+  SELF_CUDA_TRY(h->ctx, cudaMemcpyAsync(b.p, host, h->nl * sizeof(double), cudaMemcpyHostToDevice, h->ctx->stream));
+  return SELF_OK;
+}
+
+int download_vec(self_cg2d* h, double* host, const double* dev) {
+  SELF_CUDA_TRY(h->ctx, cudaMemcpyAsync(host, dev, h->nl * sizeof(double), cudaMemcpyDeviceToHost, h->ctx->stream));
+  SELF_CUDA_TRY(h->ctx, cudaStreamSynchronize(h->ctx->stream));
+  return SELF_OK;
+}
+
+template <typename R>
+int mask_dev(self_cg2d* h, R* v) {
+  if (!h->ngroups) return SELF_OK;
+  cg_mask<R><<<(h->ngroups + 255) / 256, 256, 0, h->ctx->stream>>>(v, h->gptr.p, h->gidx.p, h->gdir.p, h->ngroups);
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+template <typename R>
+int unmask_dev(self_cg2d* h, R* out, const R* in) {
+  cg_unmask<R><<<h->nblk, kRedThreads, 0, h->ctx->stream>>>(out, in, h->src.p, h->nl);
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+// Dirichlet values into the solution's Dirichlet nodes (SetDirichletBoundaryCondition :234-301)
+void set_dirichlet_host(const self_cg2d* h, double* sol, const double* dir) {
+  for (int g = 0; g < h->ngroups; ++g) {
+    if (!h->h_gdir[g]) continue;
+    for (int k = h->h_gptr[g]; k < h->h_gptr[g + 1]; ++k) {
+      const int l = h->h_gidx[k];
+      sol[l] = dir ? dir[l] : 0.0;
+    }
+  }
+}
+
+double read1(self_cg2d* h, const double* dptr, int* rc) {
+  double v = 0;
+  *rc = read_scalar(h, dptr, &v);
+  return v;
+}
+
+// GMRES(m) (IterativeSolvers_Class.f90:493-652) on the device, FP64.  x, r are device vectors; r holds the
+// initial residual.  Returns ioerr; iters = total Arnoldi steps (the reference's l).
+int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int maxIters, double tol,
+                 double* resi_host, int* iters, double* rel, double* r0_out) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  const size_t nl = h->nl;
+  int rc;
+  if ((rc = ensure(ctx, h->gm_V, nl * (size_t)(m + 1)))) return rc;
+  if ((rc = ensure(ctx, h->gm_H, (size_t)(m + 2)))) return rc;
+  if ((rc = ensure(ctx, h->gm_rho, (size_t)m * m))) return rc;
+  if ((rc = ensure(ctx, h->gm_c, m)) || (rc = ensure(ctx, h->gm_s, m)) || (rc = ensure(ctx, h->gm_bhat, m + 1)) ||
+      (rc = ensure(ctx, h->gm_y, m + 1)) || (rc = ensure(ctx, h->w, nl)))
+    return rc;
+  if (h->GS.n == 0 && h->GS.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "allocation failed");
+  std::vector<double> resi_dev_host;
+  DevBuf<double> resi_dev;
+  if (resi_host && (rc = ensure(ctx, resi_dev, (size_t)maxIters + 1))) return rc;
+  if (resi_host) SELF_CUDA_TRY(ctx, cudaMemsetAsync(resi_dev.p, 0, ((size_t)maxIters + 1) * sizeof(double), st));
+  // r0
+  if ((rc = dots<double>(h, r, r, nullptr, nullptr, h->red.p))) return rc;
+  const double rr0 = read1(h, h->red.p, &rc);
+  if (rc) return rc;
+  const double r0 = std::sqrt(rr0);
+  *r0_out = r0;
+  if (resi_host) resi_host[0] = r0;
+  int l = 0;
+  int ioerr = -2;
+  double rcur = r0;
+  *iters = 0;
+  if (r0 == 0.0) {
+    *rel = 0.0;
+    return 0;
+  }
+  GMScalars G{};
+  for (int cyc = 1; cyc <= maxIters; ++cyc) {
+    // b = ||r|| ; v1 = r / b ; bhat(1) = b
+    if ((rc = dots<double>(h, r, r, nullptr, nullptr, h->red.p))) return rc;
+    sqrt_scalar<<<1, 1, 0, st>>>(h->red.p, h->red.p + 4);
+    SELF_LAUNCHED(ctx);
+    scale_copy<double><<<h->nblk, kRedThreads, 0, st>>>(h->gm_V.p, r, h->red.p + 4, 1, nl);
+    SELF_LAUNCHED(ctx);
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->gm_bhat.p, 0, (m + 1) * sizeof(double), st));
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->gm_bhat.p, h->red.p + 4, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->gm_rho.p, 0, (size_t)m * m * sizeof(double), st));
+    G = GMScalars{};
+    G.r0 = r0;
+    G.tol = tol;
+    G.rc = rcur;
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
+    int nr = 0;
+    bool cycle_done = false;
+    for (int i = 0; i < m; ++i) {
+      l += 1;
+      nr = i + 1;
+      double* vi = h->gm_V.p + (size_t)i * nl;
+      if ((rc = matrix_action<double>(h, vi, h->w.p, h->op64))) return rc;
+      // MGS: h(k,i) = <v_k, w>; w -= h(k,i) v_k, the axpy of step k fused with the dot of step k+1
+      if ((rc = dots<double>(h, h->gm_V.p, h->w.p, nullptr, nullptr, h->gm_H.p))) return rc;
+      for (int k = 0; k <= i; ++k) {
+        const double* vk = h->gm_V.p + (size_t)k * nl;
+        const double* vn = (k < i) ? h->gm_V.p + (size_t)(k + 1) * nl : nullptr;
+        mgs_axpy_dot<double><<<h->nblk, kRedThreads, 0, st>>>(h->w.p, vk, h->gm_H.p + k, vn, nl, h->partial.p);
+        SELF_LAUNCHED(ctx);
+        reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, 1, h->gm_H.p + k + 1);
+        SELF_LAUNCHED(ctx);
+      }
+      // gm_H[i+1] = <w,w>; Givens on the device
+      gmres_givens<<<1, 1, 0, st>>>(h->gm_H.p, i, m, h->gm_rho.p, h->gm_c.p, h->gm_s.p, h->gm_bhat.p, h->GS.p,
+                                    resi_host ? resi_dev.p : nullptr, l <= maxIters ? l : 0);
+      SELF_LAUNCHED(ctx);
+      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&G, h->GS.p, sizeof(G), cudaMemcpyDeviceToHost, st));
+      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (G.breakdown) {
+        nr = i;  // exit before this column enters the solve
+        cycle_done = true;
+        break;
+      }
+      rcur = G.rc;
+      // v_{i+1} = w / h(i+1, i)
+      sqrt_scalar<<<1, 1, 0, st>>>(h->gm_H.p + i + 1, h->red.p + 5);
+      SELF_LAUNCHED(ctx);
+      scale_copy<double><<<h->nblk, kRedThreads, 0, st>>>(h->gm_V.p + (size_t)(i + 1) * nl, h->w.p, h->red.p + 5,
+                                                          1, nl);
+      SELF_LAUNCHED(ctx);
+      if (G.done) {
+        cycle_done = true;
+        break;
+      }
+    }
+    if (!cycle_done || rcur / r0 > tol) nr = (G.breakdown && nr > 0) ? nr : (rcur / r0 > tol ? m : nr);
+    if (nr < 1) break;
+    G.nr = nr;
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
+    gmres_backsolve<<<1, 1, 0, st>>>(h->gm_rho.p, h->gm_bhat.p, m, h->GS.p, h->gm_y.p);
+    SELF_LAUNCHED(ctx);
+    gmres_update<double><<<h->nblk, kRedThreads, 0, st>>>(x, h->gm_V.p, h->gm_y.p, nr, nl);
+    SELF_LAUNCHED(ctx);
+    *iters = l;
+    if (rcur / r0 <= tol) {
+      ioerr = 0;
+      break;
+    }
+    if (l >= maxIters) break;
+    if ((rc = residual<double>(h, f, x, r, h->op64))) return rc;
+  }
+  if (rcur / r0 > tol) ioerr = -1;
+  if (resi_host) {
+    std::vector<double> tmp((size_t)maxIters + 1);
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(tmp.data(), resi_dev.p, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    for (int k = 1; k <= std::min(l, maxIters); ++k) resi_host[k] = tmp[k];
+  }
+  *rel = rcur / r0;
+  return ioerr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int self_cg2d_residual(self_cg2d* h, const double* source, const double* solution, double* r) {
+  if (!h || !source || !solution || !r) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  std::vector<double> load = make_load(h, source);
+  int rc;
+  if ((rc = upload_vec(h, h->f, load.data())) || (rc = upload_vec(h, h->u, solution)) ||
+      (rc = ensure(ctx, h->r, h->nl)))
+    return rc;
+  if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
+  return download_vec(h, r, h->r.p);
+}
+
+int self_cg2d_dot(self_cg2d* h, const double* u, const double* v, double* out) {
+  if (!h || !u || !v || !out) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  int rc;
+  if ((rc = upload_vec(h, h->v, u)) || (rc = upload_vec(h, h->w, v))) return rc;
+  if ((rc = mask_dev<double>(h, h->v.p)) || (rc = mask_dev<double>(h, h->w.p))) return rc;
+  if ((rc = dots<double>(h, h->v.p, h->w.p, nullptr, nullptr, h->red.p))) return rc;
+  return read_scalar(h, h->red.p, out);
+}
+
+int self_cg2d_mask(self_cg2d* h, double* u) {
+  if (!h || !u) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(h->ctx, cudaSetDevice(h->ctx->device));
+  int rc;
+  if ((rc = upload_vec(h, h->v, u)) || (rc = mask_dev<double>(h, h->v.p))) return rc;
+  return download_vec(h, u, h->v.p);
+}
+
+int self_cg2d_unmask(self_cg2d* h, double* u) {
+  if (!h || !u) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(h->ctx, cudaSetDevice(h->ctx->device));
+  int rc;
+  if ((rc = upload_vec(h, h->v, u)) || (rc = ensure(h->ctx, h->w, h->nl)) || (rc = unmask_dev<double>(h, h->w.p, h->v.p)))
+    return rc;
+  return download_vec(h, u, h->w.p);
+}
+
+int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source, const double* dirichlet,
+                    double* solution, double* resi, self_solve_report* rep) {
+  if (!h || !o || !source || !solution) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (o->maxIters < 0 || !(o->tolerance > 0)) return set_error(ctx, SELF_ERR_INVALID, "bad solver options");
+  if (o->method == SELF_SOLVE_GMRES && (o->m < 1 || o->m > 512))
+    return set_error(ctx, SELF_ERR_INVALID, "GMRES restart length %d", o->m);
+  if (o->method == SELF_SOLVE_GMRES && o->precision != SELF_PREC_FP64)
+    return set_error(ctx, SELF_ERR_UNSUPPORTED, "GMRES runs in FP64");
+  const size_t nl = h->nl;
+  int rc;
+  std::vector<double> x0(solution, solution + nl);
+  set_dirichlet_host(h, x0.data(), dirichlet);
+  std::vector<double> load = make_load(h, source);
+  if ((rc = upload_vec(h, h->f, load.data())) || (rc = upload_vec(h, h->u, x0.data())) ||
+      (rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->v, nl)) || (rc = ensure(ctx, h->w, nl)) ||
+      (rc = ensure(ctx, h->z, nl)))
+    return rc;
+  if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
+  self_solve_report R{};
+  R.ioerr = -2;
+  int iters = 0;
+  double rel = 0, r0 = 0;
+  if (o->method == SELF_SOLVE_GMRES) {
+    R.ioerr = gmres_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, resi, &iters, &rel, &r0);
+    R.outer_iterations = 1;
+  } else {
+    const bool jac = o->method == SELF_SOLVE_PCG_JACOBI;
+    if ((rc = dots<double>(h, h->r.p, h->r.p, nullptr, nullptr, h->red.p))) return rc;
+    r0 = std::sqrt(read1(h, h->red.p, &rc));
+    if (rc) return rc;
+    if (o->precision == SELF_PREC_FP64) {
+      DevBuf<double> resi_dev;
+      if (resi) {
+        if ((rc = ensure(ctx, resi_dev, (size_t)o->maxIters + 1))) return rc;
+        SELF_CUDA_TRY(ctx, cudaMemsetAsync(resi_dev.p, 0, ((size_t)o->maxIters + 1) * sizeof(double), ctx->stream));
+      }
+      R.ioerr = pcg_device<double>(h, h->u.p, h->r.p, h->v.p, h->w.p, h->z.p, jac ? h->op64.dinv.p : nullptr,
+                                   o->maxIters, o->tolerance, r0, resi ? resi_dev.p : nullptr, &iters, &rel, h->op64);
+      if (resi) {
+        SELF_CUDA_TRY(ctx, cudaMemcpyAsync(resi, resi_dev.p, ((size_t)o->maxIters + 1) * sizeof(double),
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+        SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        resi[0] = r0;
+      }
+      R.outer_iterations = 1;
+    } else {
+      // FP32 inner (P)CG under FP64 iterative refinement: x += A32^-1 r64, r64 = b - A64 x
+      if ((rc = ensuref(ctx, h->u32, nl)) || (rc = ensuref(ctx, h->r32, nl)) || (rc = ensuref(ctx, h->v32, nl)) ||
+          (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)))
+        return rc;
+      const double inner_tol = o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4;
+      const int max_outer = o->max_outer > 0 ? o->max_outer : 30;
+      double rn = r0;
+      int outer = 0, total = 0;
+      R.ioerr = (r0 < o->tolerance) ? 0 : -1;
+      if (resi) resi[0] = r0;
+      while (outer < max_outer && rn / r0 >= o->tolerance && total < o->maxIters) {
+        outer++;
+        convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->r32.p, h->r.p, nl);
+        SELF_LAUNCHED(ctx);
+        SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->u32.p, 0, nl * sizeof(float), ctx->stream));
+        int it_in = 0;
+        double rel_in = 0;
+        pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p, jac ? h->op32.dinv.p : nullptr,
+                          o->maxIters - total, inner_tol, rn, nullptr, &it_in, &rel_in, h->op32);
+        total += it_in;
+        // x += d (FP64), r = b - A x in FP64
+        convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->u32.p, nl);
+        SELF_LAUNCHED(ctx);
+        axpby<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, h->z.p, 1.0, 1.0, nl);
+        SELF_LAUNCHED(ctx);
+        if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
+        if ((rc = dots<double>(h, h->r.p, h->r.p, nullptr, nullptr, h->red.p))) return rc;
+        rn = std::sqrt(read1(h, h->red.p, &rc));
+        if (rc) return rc;
+        if (resi && outer <= o->maxIters) resi[outer] = rn;
+        if (!(rn == rn)) {
+          R.ioerr = SELF_ERR_NONFINITE;
+          break;
+        }
+        if (it_in == 0) break;
+      }
+      iters = total;
+      rel = rn / r0;
+      R.outer_iterations = outer;
+      if (R.ioerr != SELF_ERR_NONFINITE) R.ioerr = (rel < o->tolerance) ? 0 : -1;
+    }
+  }
+  // UnMask the solution and restore the Dirichlet values
+  if ((rc = unmask_dev<double>(h, h->w.p, h->u.p))) return rc;
+  if ((rc = download_vec(h, solution, h->w.p))) return rc;
+  set_dirichlet_host(h, solution, dirichlet);
+  R.iterations = iters;
+  R.r0 = r0;
+  R.rel_residual = rel;
+  if (rep) *rep = R;
+  if (R.ioerr == SELF_ERR_NONFINITE) return set_error(ctx, SELF_ERR_NONFINITE, "non-finite residual");
+  return SELF_OK;
+}
+
+}  // extern "C"

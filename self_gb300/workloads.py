@@ -61,3 +61,21 @@ def shallow_water(mesh, N, nx, seed=2, cfl=0.5, L=SW_L, nbumps=16):
 def sw_ensemble_member(mesh, N, nx, seed, cfl=0.5, L=SW_L):
     """Shallow-water ensemble member: same set-up, initial heights perturbed by the member's seed."""
     return shallow_water(mesh, N, nx, seed=seed, cfl=cfl, L=L)
+
+
+def helmholtz(mesh, N, seed=3, nmodes=32, kmax=16):
+    """Variable-coefficient Helmholtz on [0,1]^2: k = 1 + 0.5 sin(4 pi x) cos(4 pi y), f = seeded sum of 32
+    Fourier modes (wavenumbers |k| <= 16 per direction, N(0,1) amplitudes, random sin/cos phase).  Returns
+    (k, f, source) with source = -f: the operator -(K + lam M) of the reference's sign convention solves
+    -div(k grad u) + lam u = f with load source*J*w*w."""
+    rng = np.random.default_rng(seed)
+    x, y = mesh.x, mesh.y
+    k = 1.0 + 0.5 * np.sin(4 * np.pi * x) * np.cos(4 * np.pi * y)
+    f = np.zeros_like(x)
+    kx = rng.integers(-kmax, kmax + 1, nmodes)
+    ky = rng.integers(-kmax, kmax + 1, nmodes)
+    amp = rng.normal(0.0, 1.0, nmodes)
+    ph = rng.uniform(0.0, 2 * np.pi, nmodes)
+    for m in range(nmodes):
+        f += amp[m] * np.cos(2 * np.pi * (kx[m] * x + ky[m] * y) + ph[m])
+    return k, f, -f
