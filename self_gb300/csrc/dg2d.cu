@@ -554,6 +554,30 @@ int upload(self_ctx* ctx, DevBuf<T>& b, const std::vector<T>& host) {
 
 }  // namespace
 
+namespace selfgpu {
+namespace dg32 {
+self_ctx* handle_ctx(self_dg2d* h) { return h->ctx; }
+const int* handle_edges(self_dg2d* h) { return h->edges.p; }
+// FP64 tendency of the lake at rest (U = V = 0, H = h): the reference part of the FP32 perturbation form.
+int fp64_lake_tendency(const self_dg2d_desc* d, self_ctx* ctx, std::vector<double>& R0) {
+  self_dg2d_desc d64 = *d;
+  d64.precision = SELF_PREC_FP64;
+  self_dg2d* h64 = nullptr;
+  int rc = self_dg2d_create(ctx, &d64, &h64);
+  if (rc) return rc;
+  const size_t NN = (size_t)(d->N + 1) * (d->N + 1);
+  std::vector<double> q0(NN * 3 * d->nEl, 0.0);
+  for (size_t e = 0; e < (size_t)d->nEl; ++e)
+    for (size_t k = 0; k < NN; ++k) q0[(e * 3 + 2) * NN + k] = d->h[e * NN + k];
+  R0.assign(q0.size(), 0.0);
+  rc = self_dg2d_set_state(h64, q0.data());
+  if (!rc) rc = self_dg2d_tendency(h64, 0.0, R0.data());
+  self_dg2d_destroy(h64);
+  return rc;
+}
+}  // namespace dg32
+}  // namespace selfgpu
+
 extern "C" {
 
 int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {

@@ -1,22 +1,654 @@
-// FP32 form of the DGSEM 2-D step: placeholder until the perturbation-form kernels land.
+// FP32 form of the DGSEM 2-D step (same discretisation as the FP64 drop-in, FP32 arithmetic and storage).
+//
+// Shallow water runs in perturbation form about the lake at rest q0 = (0, 0, h):
+//   state q' = (U, V, eta = H - h) in FP32, and dq/dt = R0 + T'(q') where
+//   R0 = T(q0) is the FP64 tendency of the lake at rest (computed once by the FP64 kernels, stored FP32) and
+//   T'(q') = T(q0 + q') - T(q0) is evaluated with every large term cancelled analytically:
+//     1/2 g (H^2 - h^2) = g eta (h + eta/2) in the volume and Riemann fluxes,
+//     fac*jump(H) - fac0*jump(h) = fac*jump(eta) + (fac - fac0)*jump(h) in the LLF dissipation,
+//     g H dh/dx - g h dh/dx = g eta dh/dx in the bathymetry source.
+// FP32 rounding is then relative to the perturbation (metres of eta, not 1000 m of H), which keeps the height
+// error against FP64 far below 1e-6 after 1000 steps.  Advection (linear) runs the plain form in FP32.
+// Kernels mirror dg2d.cu: an edge-flux kernel and a fused volume + RK-update + traces kernel per stage.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
 #include "dg2d_fp32.cuh"
 
 namespace selfgpu {
 namespace dg32 {
 
-struct State {};
+template <int N1>
+struct NodalF {
+  float dS[N1 * N1], dP[N1 * N1];
+  float lW[N1], lE[N1], lS[N1], lN[N1];
+  float qwinv[N1];
+};
+
+template <int N1>
+constexpr int epb() {
+  return (N1 * N1 >= 256) ? 1 : (256 / (N1 * N1));
+}
+
+struct EdgeArgs32 {
+  const float* bs;
+  float* bf;
+  const int* edges;
+  const float* egeo;  // 4 n per edge: nx, ny, |n|, u.n
+  const float* hb;    // bathymetry traces (i, side, e), shallow water only
+  int nEdges;
+  float g;
+  double t;
+};
+
+struct VolArgs32 {
+  const float* q;
+  float* qout;
+  float* G;
+  float* tend;
+  const float* bf;
+  float* bs;
+  const float* metrics;
+  const float* aux;
+  const float* R0;  // lake-at-rest tendency (shallow water)
+  int nEl, naux, has_drag, has_relax;
+  float g, drag, a, gdt;
+  int mode, write_traces;
+};
+
+// LLF flux difference F*(q0+q') - F*(q0) (ConservativeShallowWaterClass.f90:1555-1604 in perturbation form)
+__device__ __forceinline__ void sw_riemann_pert(const float* in, const float* ex, float hL, float hR, float nx,
+                                                float ny, float g, float* f) {
+  const float UL = in[0], VL = in[1], eL = in[2];
+  const float UR = ex[0], VR = ex[1], eR = ex[2];
+  const float pL = hL + eL, pR = hR + eR;
+  const float uOut = UR * nx + VR * ny, uIn = UL * nx + VL * ny;
+  const float wR = uOut / pR, wL = uIn / pL;
+  const float cR = sqrtf(g * pR), cL = sqrtf(g * pL);
+  const float fac = fmaxf(fmaxf(fabsf(wR + cR), fabsf(wR - cR)), fmaxf(fabsf(wL + cL), fabsf(wL - cL)));
+  const float fac0 = fmaxf(sqrtf(g * hR), sqrtf(g * hL));
+  const float pr = 0.5f * g * eR * (2.0f * hR + eR), pl = 0.5f * g * eL * (2.0f * hL + eL);
+  const float a0 = wR * UR + pr * nx + wL * UL + pl * nx;
+  const float a1 = wR * VR + pr * ny + wL * VL + pl * ny;
+  const float a2 = uOut + uIn;
+  f[0] = 0.5f * (a0 - fac * (UR - UL));
+  f[1] = 0.5f * (a1 - fac * (VR - VL));
+  f[2] = 0.5f * (a2 - fac * (eR - eL) - (fac - fac0) * (hR - hL));
+}
+
+template <int N1, int NEQ, bool SW>
+__global__ void __launch_bounds__(256) edge32(EdgeArgs32 A) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = gid / N1, i = gid - (gid / N1) * N1;
+  if (k >= A.nEdges) return;
+  const int* E = A.edges + 6 * k;
+  const int e1 = E[0] - 1, s1 = E[1] - 1, e2f = E[2];
+  const float* eg = A.egeo + (size_t)k * 4 * N1;
+  const float nx = eg[i], ny = eg[N1 + i], len = eg[2 * N1 + i], un = eg[3 * N1 + i];
+  float in[NEQ], ex[NEQ], f[NEQ];
+  const float* b1 = A.bs + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
+#pragma unroll
+  for (int v = 0; v < NEQ; ++v) in[v] = b1[i + N1 * v];
+  float* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
+  if (e2f > 0) {
+    const int e2 = e2f - 1, s2 = abs(E[3]) - 1, start = E[4], inc = E[5];
+    const int kk = start - inc + i * inc;
+    const float* b2 = A.bs + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
+    if (SW) {
+      const float hL = A.hb[i + N1 * (s1 + 4 * (size_t)e1)], hR = A.hb[kk + N1 * (s2 + 4 * (size_t)e2)];
+      sw_riemann_pert(in, ex, hL, hR, nx, ny, A.g, f);
+    } else {
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) f[v] = 0.5f * (un * (ex[v] + in[v]) - fabsf(un) * (ex[v] - in[v]));
+    }
+    float* o2 = A.bf + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) {
+      const float fl = f[v] * len;
+      o1[i + N1 * v] = fl;
+      o2[kk + N1 * v] = -fl;
+    }
+  } else {
+    if (SW) {
+      const float hL = A.hb[i + N1 * (s1 + 4 * (size_t)e1)];
+      if (e2f == SELF_NO_NORMAL_FLOW) {
+        ex[0] = (ny * ny - nx * nx) * in[0] - 2.0f * nx * ny * in[1];
+        ex[1] = (nx * nx - ny * ny) * in[1] - 2.0f * nx * ny * in[0];
+        ex[2] = in[2];
+        sw_riemann_pert(in, ex, hL, hL, nx, ny, A.g, f);
+      } else {
+        // zero external state: H_ex = 0, i.e. eta_ex = -h_ex with h_ex = 0 reference -> plain difference
+        // of the two fluxes is formed from the full states (rare boundary type, FP32 of the full state)
+        ex[0] = ex[1] = 0.f;
+        ex[2] = -hL;
+        sw_riemann_pert(in, ex, hL, hL, nx, ny, A.g, f);
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) ex[v] = 0.f;
+      if (e2f == SELF_INFLOW_ONE) ex[0] = (float)tanh(A.t);
+      if (NEQ > 1 && e2f == SELF_INFLOW_TWO) ex[NEQ > 1 ? 1 : 0] = (float)tanh(A.t);
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) f[v] = 0.5f * (un * (ex[v] + in[v]) - fabsf(un) * (ex[v] - in[v]));
+    }
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = f[v] * len;
+  }
+}
+
+template <int N1, int NEQ>
+__device__ __forceinline__ void traces32(const NodalF<N1>& C, const float* sq, float* bs, int e, int tid) {
+  constexpr int NV = 4 * NEQ * N1;
+  for (int t = tid; t < NV; t += N1 * N1) {
+    const int k = t % N1, v = (t / N1) % NEQ, side = t / (N1 * NEQ);
+    const float* Q = sq + v * N1 * N1;
+    float acc = 0.f;
+    if (side == 0 || side == 2) {
+      const float* L = (side == 0) ? C.lS : C.lN;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) acc += L[m] * Q[k + N1 * m];
+    } else {
+      const float* L = (side == 1) ? C.lE : C.lW;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) acc += L[m] * Q[m + N1 * k];
+    }
+    bs[(size_t)N1 * NEQ * (side + 4 * (size_t)e) + k + N1 * v] = acc;
+  }
+}
+
+template <int N1, int NEQ, bool SW>
+__global__ void __launch_bounds__(256) volume32(VolArgs32 A, NodalF<N1> Cg) {
+  constexpr int NN = N1 * N1, EPB = epb<N1>();
+  __shared__ NodalF<N1> C;
+  __shared__ float sF[EPB][NEQ][NN];
+  __shared__ float sG[EPB][NEQ][NN];
+  __shared__ float sB[EPB][4][NEQ][N1];
+  const int tid = threadIdx.x, le = threadIdx.y;
+  const int e = blockIdx.x * EPB + le;
+  const bool active = e < A.nEl;
+  {
+    constexpr int NC = sizeof(NodalF<N1>) / sizeof(float);
+    const float* src = reinterpret_cast<const float*>(&Cg);
+    float* dst = reinterpret_cast<float*>(&C);
+    for (int t = tid + NN * le; t < NC; t += NN * EPB) dst[t] = src[t];
+  }
+  const int i = tid % N1, j = tid / N1;
+  float qv[NEQ];
+  float dxds = 0, dxdp = 0, dyds = 0, dydp = 0, invJ = 0, hn = 0;
+  const float* ae = A.aux + (size_t)(active ? e : 0) * A.naux * NN;
+  if (active) {
+    const float* qe = A.q + (size_t)e * NEQ * NN;
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) qv[v] = qe[v * NN + tid];
+    const float* me = A.metrics + (size_t)e * 5 * NN;
+    dxds = me[tid];
+    dxdp = me[NN + tid];
+    dyds = me[2 * NN + tid];
+    dydp = me[3 * NN + tid];
+    invJ = me[4 * NN + tid];
+    const float* be = A.bf + (size_t)e * 4 * NEQ * N1;
+    float* sb = &sB[le][0][0][0];
+    for (int t = tid; t < 4 * NEQ * N1; t += NN) sb[t] = be[t];
+    float xF[NEQ], yF[NEQ];
+    if (SW) {
+      hn = ae[3 * NN + tid];
+      const float iH = 1.0f / (hn + qv[2]);
+      const float p = A.g * qv[2] * (hn + 0.5f * qv[2]);  // 1/2 g (H^2 - h^2)
+      xF[0] = qv[0] * qv[0] * iH + p;
+      xF[1] = qv[0] * qv[1] * iH;
+      xF[2] = qv[0];
+      yF[0] = qv[1] * qv[0] * iH;
+      yF[1] = qv[1] * qv[1] * iH + p;
+      yF[2] = qv[1];
+    } else {
+      const float u = ae[tid], vv = ae[NN + tid];
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) {
+        xF[v] = qv[v] * u;
+        yF[v] = qv[v] * vv;
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) {
+      sF[le][v][tid] = dydp * xF[v] - dxdp * yF[v];
+      sG[le][v][tid] = -dyds * xF[v] + dxds * yF[v];
+    }
+  }
+  __syncthreads();
+  float tend[NEQ];
+  if (active) {
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) {
+      float ds = 0.f, dp = 0.f;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) ds += C.dS[i + N1 * m] * sF[le][v][m + N1 * j];
+      ds += (sB[le][1][v][j] * C.lE[i] + sB[le][3][v][j] * C.lW[i]) * C.qwinv[i];
+#pragma unroll
+      for (int m = 0; m < N1; ++m) dp += C.dP[j + N1 * m] * sG[le][v][i + N1 * m];
+      dp += (sB[le][2][v][i] * C.lN[j] + sB[le][0][v][i] * C.lS[j]) * C.qwinv[j];
+      tend[v] = (-ds - dp) * invJ;
+    }
+    if (SW) {
+      const float dhdx = ae[tid], dhdy = ae[NN + tid], f = ae[2 * NN + tid];
+      float s0 = f * qv[1] + A.g * qv[2] * dhdx;
+      float s1 = -f * qv[0] + A.g * qv[2] * dhdy;
+      float s2 = 0.f;
+      if (A.has_drag) {
+        s0 -= A.drag * qv[0] / hn;
+        s1 -= A.drag * qv[1] / hn;
+      }
+      if (A.has_relax) {
+        const float ts = ae[4 * NN + tid];
+        s0 -= qv[0] * ts;
+        s1 -= qv[1] * ts;
+        s2 -= qv[2] * ts;
+      }
+      const float* r0 = A.R0 + (size_t)e * 3 * NN;
+      tend[0] += s0 + r0[tid];
+      tend[1] += s1 + r0[NN + tid];
+      if (NEQ > 2) tend[NEQ > 2 ? 2 : 0] += s2 + r0[2 * NN + tid];
+    } else if (A.has_relax) {
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) tend[v] += (ae[(2 + v) * NN + tid] - qv[v]) * ae[(2 + NEQ + v) * NN + tid];
+    }
+    if (A.mode == 0) {
+      float* te = A.tend + (size_t)e * NEQ * NN;
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) te[v * NN + tid] = tend[v];
+    } else {
+      float* Ge = A.G + (size_t)e * NEQ * NN;
+      float* qo = A.qout + (size_t)e * NEQ * NN;
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) {
+        const float g = (A.mode == 2) ? (A.a * Ge[v * NN + tid] + tend[v]) : tend[v];
+        Ge[v * NN + tid] = g;
+        qv[v] = qv[v] + A.gdt * g;
+        qo[v * NN + tid] = qv[v];
+      }
+    }
+  }
+  if (A.write_traces) {
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) sF[le][v][tid] = qv[v];
+    }
+    __syncthreads();
+    if (active) traces32<N1, NEQ>(C, &sF[le][0][0], A.bs, e, tid);
+  }
+}
+
+template <int N1, int NEQ>
+__global__ void __launch_bounds__(256) tr32(const float* q, float* bs, int nEl, NodalF<N1> Cg) {
+  constexpr int NN = N1 * N1, EPB = epb<N1>();
+  __shared__ NodalF<N1> C;
+  __shared__ float sQ[EPB][NEQ][NN];
+  const int tid = threadIdx.x, le = threadIdx.y, e = blockIdx.x * EPB + le;
+  {
+    constexpr int NC = sizeof(NodalF<N1>) / sizeof(float);
+    const float* src = reinterpret_cast<const float*>(&Cg);
+    float* dst = reinterpret_cast<float*>(&C);
+    for (int t = tid + NN * le; t < NC; t += NN * EPB) dst[t] = src[t];
+  }
+  if (e < nEl) {
+#pragma unroll
+    for (int v = 0; v < NEQ; ++v) sQ[le][v][tid] = q[(size_t)e * NEQ * NN + v * NN + tid];
+  }
+  __syncthreads();
+  if (e < nEl) traces32<N1, NEQ>(C, &sQ[le][0][0], bs, e, tid);
+}
+
+// ----------------------------------------------------------------------------------- state
+struct State {
+  int n = 0, nEq = 0, nEl = 0, nEdges = 0, sw = 0, naux = 0, has_drag = 0, has_relax = 0, has_inflow = 0;
+  float g = 9.81f, drag = 0.f;
+  double dt = 0;
+  std::vector<float> dS, dP, lW, lE, lS, lN, qwinv;
+  std::vector<double> h;  // bathymetry per node (host, FP64) for the state conversion
+  DevBuf<float> q, G, bs, bf, metrics, aux, egeo, R0, hb, tend;
+  const int* edges = nullptr;  // owned by the FP64 handle
+  cudaGraphExec_t graph = nullptr;
+  bool traces_valid = false;
+  ~State() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
 State* make_state() { return new State(); }
 void destroy(State* s) { delete s; }
-int create(self_dg2d*, State*, const self_dg2d_desc*, const std::vector<double>&, const std::vector<double>&,
-           const std::vector<double>&) {
-  return set_error(nullptr, SELF_ERR_UNSUPPORTED, "FP32 form not built");
+
+}  // namespace dg32
+}  // namespace selfgpu
+
+// The FP64 handle type is defined in dg2d.cu; only its context and edge table are needed here.
+struct self_dg2d;
+namespace selfgpu {
+namespace dg32 {
+self_ctx* handle_ctx(self_dg2d* h);
+const int* handle_edges(self_dg2d* h);
+int fp64_lake_tendency(const self_dg2d_desc* d, self_ctx* ctx, std::vector<double>& R0);
+}  // namespace dg32
+}  // namespace selfgpu
+
+namespace {
+
+using namespace selfgpu;
+using namespace selfgpu::dg32;
+
+template <int N1>
+NodalF<N1> mk(const State* s) {
+  NodalF<N1> C;
+  for (int k = 0; k < N1 * N1; ++k) {
+    C.dS[k] = s->dS[k];
+    C.dP[k] = s->dP[k];
+  }
+  for (int k = 0; k < N1; ++k) {
+    C.lW[k] = s->lW[k];
+    C.lE[k] = s->lE[k];
+    C.lS[k] = s->lS[k];
+    C.lN[k] = s->lN[k];
+    C.qwinv[k] = s->qwinv[k];
+  }
+  return C;
 }
-int set_state(self_dg2d*, State*, const double*) { return SELF_ERR_UNSUPPORTED; }
-int get_state(self_dg2d*, State*, double*) { return SELF_ERR_UNSUPPORTED; }
-int state_device(self_dg2d*, State*, void**, size_t*) { return SELF_ERR_UNSUPPORTED; }
-int tendency(self_dg2d*, State*, double, double*) { return SELF_ERR_UNSUPPORTED; }
-int rk3(self_dg2d*, State*, double, int) { return SELF_ERR_UNSUPPORTED; }
-int time_kernels(self_dg2d*, State*, int, size_t, double*) { return SELF_ERR_UNSUPPORTED; }
+
+template <int N1, int NEQ, bool SW>
+int edge_t(self_ctx* ctx, State* s, double t) {
+  EdgeArgs32 A{s->bs.p, s->bf.p, s->edges, s->egeo.p, s->hb.p, s->nEdges, s->g, t};
+  const int nthr = s->nEdges * N1;
+  edge32<N1, NEQ, SW><<<(nthr + 255) / 256, 256, 0, ctx->stream>>>(A);
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
+template <int N1, int NEQ, bool SW>
+int volume_t(self_ctx* ctx, State* s, int mode, float a, float gdt, float* tend, int wt) {
+  VolArgs32 A;
+  A.q = s->q.p;
+  A.qout = s->q.p;
+  A.G = s->G.p;
+  A.tend = tend;
+  A.bf = s->bf.p;
+  A.bs = s->bs.p;
+  A.metrics = s->metrics.p;
+  A.aux = s->aux.p;
+  A.R0 = s->R0.p;
+  A.nEl = s->nEl;
+  A.naux = s->naux;
+  A.has_drag = s->has_drag;
+  A.has_relax = s->has_relax;
+  A.g = s->g;
+  A.drag = s->drag;
+  A.a = a;
+  A.gdt = gdt;
+  A.mode = mode;
+  A.write_traces = wt;
+  constexpr int EPB = epb<N1>();
+  volume32<N1, NEQ, SW><<<(s->nEl + EPB - 1) / EPB, dim3(N1 * N1, EPB), 0, ctx->stream>>>(A, mk<N1>(s));
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
+template <int N1, int NEQ>
+int traces_t(self_ctx* ctx, State* s) {
+  constexpr int EPB = epb<N1>();
+  tr32<N1, NEQ><<<(s->nEl + EPB - 1) / EPB, dim3(N1 * N1, EPB), 0, ctx->stream>>>(s->q.p, s->bs.p, s->nEl, mk<N1>(s));
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
+// op: 0 edge, 1 volume, 2 traces
+template <int N1>
+int run_n(self_ctx* ctx, State* s, int op, double t, int mode, float a, float gdt, float* tend, int wt) {
+#define SELF_F32_OPS(NEQ, SW)                                   \
+  if (op == 0) return edge_t<N1, NEQ, SW>(ctx, s, t);           \
+  if (op == 1) return volume_t<N1, NEQ, SW>(ctx, s, mode, a, gdt, tend, wt); \
+  return traces_t<N1, NEQ>(ctx, s);
+  if (s->sw) {
+    SELF_F32_OPS(3, true)
+  }
+  switch (s->nEq) {
+    case 1: { SELF_F32_OPS(1, false) }
+    case 2: { SELF_F32_OPS(2, false) }
+    case 3: { SELF_F32_OPS(3, false) }
+    case 4: { SELF_F32_OPS(4, false) }
+  }
+#undef SELF_F32_OPS
+  return SELF_ERR_UNSUPPORTED;
+}
+
+int run(self_ctx* ctx, State* s, int op, double t, int mode, float a, float gdt, float* tend, int wt) {
+  switch (s->n) {
+    case 3: return run_n<3>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 4: return run_n<4>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 5: return run_n<5>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 6: return run_n<6>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 7: return run_n<7>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 8: return run_n<8>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 9: return run_n<9>(ctx, s, op, t, mode, a, gdt, tend, wt);
+    case 10: return run_n<10>(ctx, s, op, t, mode, a, gdt, tend, wt);
+  }
+  return SELF_ERR_UNSUPPORTED;
+}
+
+const double kA[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+const double kB[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
+const double kG[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+
+int step(self_ctx* ctx, State* s, double t0) {
+  int rc;
+  for (int m = 0; m < 3; ++m) {
+    if ((rc = run(ctx, s, 0, t0 + kB[m] * s->dt, 0, 0.f, 0.f, nullptr, 0))) return rc;
+    if ((rc = run(ctx, s, 1, 0.0, m == 0 ? 1 : 2, (float)kA[m], (float)(kG[m] * s->dt), nullptr, 1))) return rc;
+  }
+  return SELF_OK;
+}
+
+template <typename T>
+int up(self_ctx* ctx, DevBuf<T>& b, const std::vector<T>& v) {
+  if (b.alloc(v.size()) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  SELF_CUDA_TRY(ctx, cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return SELF_OK;
+}
+
+std::vector<float> tof(const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); }
+
+}  // namespace
+
+namespace selfgpu {
+namespace dg32 {
+
+int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<double>& met,
+           const std::vector<double>& aux64, const std::vector<double>& egeo) {
+  self_ctx* ctx = handle_ctx(hd);
+  const int n = d->N + 1;
+  const size_t NN = (size_t)n * n, nEl = d->nEl;
+  s->n = n;
+  s->nEq = d->nEq;
+  s->nEl = d->nEl;
+  s->nEdges = d->nEdges;
+  s->sw = d->model == SELF_MODEL_SW_CONSERVATIVE;
+  s->g = (float)d->g;
+  s->drag = (float)d->linear_drag;
+  s->dt = d->dt;
+  s->edges = handle_edges(hd);
+  s->dS.assign(d->dmatS, d->dmatS + NN);
+  s->dP.assign(d->dmatP, d->dmatP + NN);
+  s->lW.assign(d->lagW, d->lagW + n);
+  s->lE.assign(d->lagE, d->lagE + n);
+  s->lS.assign(d->lagS, d->lagS + n);
+  s->lN.assign(d->lagN, d->lagN + n);
+  for (int k = 0; k < n; ++k) s->qwinv.push_back((float)(1.0 / d->qweight[k]));
+  int rc;
+  if ((rc = up(ctx, s->metrics, tof(met)))) return rc;
+  if ((rc = up(ctx, s->egeo, tof(egeo)))) return rc;
+  if (s->sw) {
+    s->has_drag = d->linear_drag != 0.0;
+    s->has_relax = (d->relax && d->rfac) ? 1 : 0;
+    s->naux = 4 + s->has_relax;
+    std::vector<double> aux((size_t)s->naux * NN * nEl);
+    const double* fld[4] = {d->dhdx, d->dhdy, d->fcor, d->h};
+    for (size_t e = 0; e < nEl; ++e) {
+      for (int f = 0; f < 4; ++f)
+        for (size_t k = 0; k < NN; ++k) aux[(e * s->naux + f) * NN + k] = fld[f][e * NN + k];
+      if (s->has_relax)
+        for (size_t k = 0; k < NN; ++k) aux[(e * s->naux + 4) * NN + k] = d->rfac[e * NN + k];
+    }
+    if ((rc = up(ctx, s->aux, tof(aux)))) return rc;
+    s->h.assign(d->h, d->h + NN * nEl);
+    // bathymetry traces on the four sides (CalculateBathymetryAtBoundaries)
+    std::vector<double> hb((size_t)4 * n * nEl);
+    for (size_t e = 0; e < nEl; ++e)
+      for (int k = 0; k < n; ++k) {
+        double sS = 0, sE = 0, sN = 0, sW = 0;
+        for (int m = 0; m < n; ++m) {
+          sS += d->lagS[m] * d->h[e * NN + k + (size_t)n * m];
+          sN += d->lagN[m] * d->h[e * NN + k + (size_t)n * m];
+          sW += d->lagW[m] * d->h[e * NN + m + (size_t)n * k];
+          sE += d->lagE[m] * d->h[e * NN + m + (size_t)n * k];
+        }
+        hb[k + n * (0 + 4 * e)] = sS;
+        hb[k + n * (1 + 4 * e)] = sE;
+        hb[k + n * (2 + 4 * e)] = sN;
+        hb[k + n * (3 + 4 * e)] = sW;
+      }
+    if ((rc = up(ctx, s->hb, tof(hb)))) return rc;
+    std::vector<double> R0;
+    if ((rc = fp64_lake_tendency(d, ctx, R0))) return rc;
+    if ((rc = up(ctx, s->R0, tof(R0)))) return rc;
+  } else {
+    s->has_relax = (d->relax && d->rfac) ? 1 : 0;
+    s->naux = (int)(aux64.size() / (NN * nEl));
+    if ((rc = up(ctx, s->aux, tof(aux64)))) return rc;
+    for (int k = 0; k < d->nEdges; ++k)
+      if (d->edges[6 * k + 2] == SELF_INFLOW_ONE || d->edges[6 * k + 2] == SELF_INFLOW_TWO) s->has_inflow = 1;
+  }
+  const size_t nq = NN * d->nEq * nEl, nb = (size_t)n * d->nEq * 4 * nEl;
+  if (s->q.alloc(nq) || s->G.alloc(nq) || s->bs.alloc(nb) || s->bf.alloc(nb))
+    return set_error(ctx, SELF_ERR_ALLOC, "device allocation of the FP32 state failed");
+  SELF_CUDA_TRY(ctx, cudaMemset(s->q.p, 0, s->q.bytes()));
+  SELF_CUDA_TRY(ctx, cudaMemset(s->G.p, 0, s->G.bytes()));
+  SELF_CUDA_TRY(ctx, cudaMemset(s->bf.p, 0, s->bf.bytes()));
+  return SELF_OK;
+}
+
+int set_state(self_dg2d* hd, State* s, const double* q) {
+  self_ctx* ctx = handle_ctx(hd);
+  const size_t NN = (size_t)s->n * s->n;
+  std::vector<float> f(s->q.n);
+  for (size_t e = 0; e < (size_t)s->nEl; ++e)
+    for (int v = 0; v < s->nEq; ++v)
+      for (size_t k = 0; k < NN; ++k) {
+        const size_t id = (e * s->nEq + v) * NN + k;
+        f[id] = (float)(s->sw && v == 2 ? q[id] - s->h[e * NN + k] : q[id]);
+      }
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->q.p, f.data(), s->q.bytes(), cudaMemcpyHostToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->traces_valid = false;
+  return SELF_OK;
+}
+
+int get_state(self_dg2d* hd, State* s, double* q) {
+  self_ctx* ctx = handle_ctx(hd);
+  const size_t NN = (size_t)s->n * s->n;
+  std::vector<float> f(s->q.n);
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(f.data(), s->q.p, s->q.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (size_t e = 0; e < (size_t)s->nEl; ++e)
+    for (int v = 0; v < s->nEq; ++v)
+      for (size_t k = 0; k < NN; ++k) {
+        const size_t id = (e * s->nEq + v) * NN + k;
+        q[id] = (s->sw && v == 2) ? s->h[e * NN + k] + (double)f[id] : (double)f[id];
+      }
+  return SELF_OK;
+}
+
+int state_device(self_dg2d*, State* s, void** dptr, size_t* bytes) {
+  *dptr = s->q.p;
+  if (bytes) *bytes = s->q.bytes();
+  return SELF_OK;
+}
+
+int tendency(self_dg2d* hd, State* s, double t, double* dqdt) {
+  self_ctx* ctx = handle_ctx(hd);
+  if (s->tend.n == 0 && s->tend.alloc(s->q.n) != cudaSuccess)
+    return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  int rc;
+  if ((rc = run(ctx, s, 2, 0, 0, 0, 0, nullptr, 0))) return rc;
+  if ((rc = run(ctx, s, 0, t, 0, 0, 0, nullptr, 0))) return rc;
+  if ((rc = run(ctx, s, 1, t, 0, 0.f, 0.f, s->tend.p, 0))) return rc;
+  if (dqdt) {
+    std::vector<float> f(s->q.n);
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(f.data(), s->tend.p, s->tend.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+    SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t k = 0; k < f.size(); ++k) dqdt[k] = f[k];
+  }
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return SELF_OK;
+}
+
+int rk3(self_dg2d* hd, State* s, double tn, int nsteps) {
+  self_ctx* ctx = handle_ctx(hd);
+  int rc;
+  if (!s->traces_valid) {
+    if ((rc = run(ctx, s, 2, 0, 0, 0, 0, nullptr, 0))) return rc;
+    s->traces_valid = true;
+  }
+  if (s->has_inflow) {
+    for (int k = 0; k < nsteps; ++k)
+      if ((rc = step(ctx, s, tn + k * s->dt))) return rc;
+    return SELF_OK;
+  }
+  if (!s->graph) {
+    cudaGraph_t g;
+    SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = step(ctx, s, tn);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    ctx->launches.fetch_sub(6);
+  }
+  for (int k = 0; k < nsteps; ++k) {
+    SELF_CUDA_TRY(ctx, cudaGraphLaunch(s->graph, ctx->stream));
+    ctx->launches.fetch_add(6);
+  }
+  return SELF_OK;
+}
+
+int time_kernels(self_dg2d* hd, State* s, int reps, size_t flush_bytes, double* ms) {
+  self_ctx* ctx = handle_ctx(hd);
+  DevBuf<float> q0, G0;
+  if (q0.alloc(s->q.n) || G0.alloc(s->G.n)) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(q0.p, s->q.p, s->q.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(G0.p, s->G.p, s->G.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  int rc;
+  if ((rc = run(ctx, s, 2, 0, 0, 0, 0, nullptr, 0))) return rc;
+  double te = 0, tv = 0, t;
+  for (int r = 0; r < reps; ++r) {
+    if ((rc = self_ctx_flush_l2(ctx, flush_bytes)) || (rc = self_ctx_timer_start(ctx))) return rc;
+    if ((rc = run(ctx, s, 0, 0.0, 0, 0, 0, nullptr, 0))) return rc;
+    if ((rc = self_ctx_timer_stop(ctx, &t))) return rc;
+    te += t;
+    if ((rc = self_ctx_flush_l2(ctx, flush_bytes)) || (rc = self_ctx_timer_start(ctx))) return rc;
+    if ((rc = run(ctx, s, 1, 0.0, 2, (float)kA[1], (float)(kG[1] * s->dt), nullptr, 1))) return rc;
+    if ((rc = self_ctx_timer_stop(ctx, &t))) return rc;
+    tv += t;
+  }
+  ms[0] = te / reps;
+  ms[1] = tv / reps;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->q.p, q0.p, s->q.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->G.p, G0.p, s->G.bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->traces_valid = false;
+  return SELF_OK;
+}
 
 }  // namespace dg32
 }  // namespace selfgpu

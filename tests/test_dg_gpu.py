@@ -137,3 +137,65 @@ def test_advection_config1_1000_steps(oracle, gpu_ctx):
     assert rel_inf(got, ref) <= TOLLONG
     ex = W.advection_exact(mesh.x, mesh.y, steps * dt)
     assert np.abs(got - ex).max() < 1e-4
+
+
+# ---------------------------------------------------------------------------------------------- FP32 form
+def test_fp32_sw_tendency_close_to_fp64(oracle, gpu_ctx):
+    """FP32 perturbation form: one tendency within 1e-4 relative (per variable) of the FP64 oracle."""
+    import self_gb300 as sg
+    N, nx = 7, 8
+    nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, _, _ = _sw_problem(oracle, N, nx, flow=False)
+    rng = np.random.default_rng(11)
+    qq = q.reshape(mesh.nEl, 3, -1)
+    qq[:, 0] = 20.0 * np.sin(2 * np.pi * mesh.y / 2e6).reshape(mesh.nEl, -1)
+    qq[:, 1] = 10.0 * np.cos(2 * np.pi * mesh.x / 2e6).reshape(mesh.nEl, -1)
+    q = qq.ravel()
+    sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy, precision=sg._native.PREC_FP32)
+    sw.SetSolution(q)
+    back = sw.GetSolution().reshape(mesh.nEl, 3, -1)
+    assert np.abs(back[:, 2] - qq[:, 2]).max() < 1e-6  # eta = H - h stored in FP32
+    got = sw.GlobalTimeDerivative(0.0)
+    errs = per_var_rel(got, P.tendency(q), 3, (N + 1) ** 2)
+    assert max(errs) <= 1e-4, errs
+
+
+def test_fp32_sw_height_error_after_1000_steps(gpu_ctx):
+    """North-star accuracy of the FP32 step: shallow-water height error <= 1e-6 relative to FP64 after 1000
+    steps on the 128x128, N=7 curvilinear workload."""
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    N, nx, steps = 7, 128, 1000
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, warp=W.SW_WARP, scale=(W.SW_L, W.SW_L))
+    q, h, fcor, dt = W.shallow_water(mesh, N, nx, seed=2)
+    dhdx, dhdy = sg.bathymetry_gradient(nod, mesh, h)
+    out = {}
+    for prec in (sg._native.PREC_FP64, sg._native.PREC_FP32):
+        sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy, precision=prec)
+        sw.SetSolution(q)
+        sw.ForwardStepRK3(0.0, steps)
+        out[prec] = sw.GetSolution().reshape(mesh.nEl, 3, -1)
+        sw.Trash()
+    H64, H32 = out[0][:, 2], out[1][:, 2]
+    err = np.abs(H32 - H64).max() / np.abs(H64).max()
+    assert err <= 1e-6, err
+    eta_err = np.abs(H32 - H64).max() / np.abs(H64 - h.reshape(mesh.nEl, -1)).max()
+    assert eta_err <= 1e-3, eta_err
+    for v in (0, 1):
+        assert rel_inf(out[1][:, v], out[0][:, v]) <= 1e-3
+
+
+def test_fp32_advection_1000_steps(gpu_ctx):
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    N, nx, steps = 7, 16, 1000
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, periodic=(True, True))
+    c0, u, v, dt = W.advection_periodic(mesh, N, nx)
+    res = []
+    for prec in (0, 1):
+        adv = sg.Advection(gpu_ctx, nod, mesh, u, v, dt, precision=prec)
+        adv.SetSolution(c0)
+        adv.ForwardStepRK3(0.0, steps)
+        res.append(adv.GetSolution())
+    assert rel_inf(res[1], res[0]) <= 1e-5
