@@ -451,9 +451,11 @@ namespace cg {
 
 
 // (P)CG iterations on the device from the current residual; returns ioerr and fills iters/resi.
+// abs_stop: the reference's early return when ||r0|| < TOL (CGsemElliptic_2D_Class.f90:1160-1162); the inner
+// solves of the iterative refinement use a purely relative stop.
 template <typename R>
 int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int maxIters, double tol, double r0,
-               double* resi_dev, int* iters, double* rel, const OpData<R>& od) {
+               double* resi_dev, int* iters, double* rel, const OpData<R>& od, bool abs_stop = true) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
   CGScalars hs{};
@@ -461,7 +463,7 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
   hs.tol = tol;
   hs.maxIters = maxIters;
   hs.iter = 0;
-  hs.done = (r0 < tol) || maxIters <= 0;
+  hs.done = (abs_stop && r0 < tol) || maxIters <= 0 || r0 == 0.0;
   hs.ioerr = hs.done ? 0 : -2;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
   int rc;
@@ -1088,7 +1090,7 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         int it_in = 0;
         double rel_in = 0;
         pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p, jac ? h->op32.dinv.p : nullptr,
-                          o->maxIters - total, inner_tol, rn, nullptr, &it_in, &rel_in, h->op32);
+                          o->maxIters - total, inner_tol, rn, nullptr, &it_in, &rel_in, h->op32, false);
         total += it_in;
         // x += d (FP64), r = b - A x in FP64
         convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->u32.p, nl);

@@ -302,6 +302,22 @@ __global__ void __launch_bounds__(256) tr32(const float* q, float* bs, int nEl, 
   if (e < nEl) traces32<N1, NEQ>(C, &sQ[le][0][0], bs, e, tid);
 }
 
+// FP64 E-vector <-> FP32 perturbation state (eta = H - h for shallow water), on the device
+__global__ void to_pert(float* __restrict__ q32, const double* __restrict__ q64, const double* __restrict__ h64,
+                        size_t nn, int nEq, int sw, size_t ntot) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < ntot; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = k / (nn * nEq), v = (k / nn) % nEq, t = k % nn;
+    q32[k] = (float)((sw && v == 2) ? q64[k] - h64[e * nn + t] : q64[k]);
+  }
+}
+__global__ void from_pert(double* __restrict__ q64, const float* __restrict__ q32, const double* __restrict__ h64,
+                          size_t nn, int nEq, int sw, size_t ntot) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < ntot; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = k / (nn * nEq), v = (k / nn) % nEq, t = k % nn;
+    q64[k] = (sw && v == 2) ? h64[e * nn + t] + (double)q32[k] : (double)q32[k];
+  }
+}
+
 // ----------------------------------------------------------------------------------- state
 struct State {
   int n = 0, nEq = 0, nEl = 0, nEdges = 0, sw = 0, naux = 0, has_drag = 0, has_relax = 0, has_inflow = 0;
@@ -310,6 +326,7 @@ struct State {
   std::vector<float> dS, dP, lW, lE, lS, lN, qwinv;
   std::vector<double> h;  // bathymetry per node (host, FP64) for the state conversion
   DevBuf<float> q, G, bs, bf, metrics, aux, egeo, R0, hb, tend;
+  DevBuf<double> stage64, h64;  // FP64 staging of host transfers, bathymetry for the state conversion
   const int* edges = nullptr;  // owned by the FP64 handle
   cudaGraphExec_t graph = nullptr;
   bool traces_valid = false;
@@ -536,17 +553,25 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
   return SELF_OK;
 }
 
+static int ensure_staging(self_ctx* ctx, State* s) {
+  if (s->stage64.n == 0 && s->stage64.alloc(s->q.n) != cudaSuccess)
+    return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  if (s->sw && s->h64.n == 0) {
+    if (s->h64.alloc(s->h.size()) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+    SELF_CUDA_TRY(ctx, cudaMemcpy(s->h64.p, s->h.data(), s->h64.bytes(), cudaMemcpyHostToDevice));
+  }
+  return SELF_OK;
+}
+
+// Host FP64 E-vector in, converted on the device (eta = H - h in FP64, then rounded to FP32).
 int set_state(self_dg2d* hd, State* s, const double* q) {
   self_ctx* ctx = handle_ctx(hd);
+  int rc = ensure_staging(ctx, s);
+  if (rc) return rc;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->stage64.p, q, s->stage64.bytes(), cudaMemcpyHostToDevice, ctx->stream));
   const size_t NN = (size_t)s->n * s->n;
-  std::vector<float> f(s->q.n);
-  for (size_t e = 0; e < (size_t)s->nEl; ++e)
-    for (int v = 0; v < s->nEq; ++v)
-      for (size_t k = 0; k < NN; ++k) {
-        const size_t id = (e * s->nEq + v) * NN + k;
-        f[id] = (float)(s->sw && v == 2 ? q[id] - s->h[e * NN + k] : q[id]);
-      }
-  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->q.p, f.data(), s->q.bytes(), cudaMemcpyHostToDevice, ctx->stream));
+  to_pert<<<2 * ctx->num_sms * 4, 256, 0, ctx->stream>>>(s->q.p, s->stage64.p, s->h64.p, NN, s->nEq, s->sw, s->q.n);
+  SELF_LAUNCHED(ctx);
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->traces_valid = false;
   return SELF_OK;
@@ -554,16 +579,13 @@ int set_state(self_dg2d* hd, State* s, const double* q) {
 
 int get_state(self_dg2d* hd, State* s, double* q) {
   self_ctx* ctx = handle_ctx(hd);
+  int rc = ensure_staging(ctx, s);
+  if (rc) return rc;
   const size_t NN = (size_t)s->n * s->n;
-  std::vector<float> f(s->q.n);
-  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(f.data(), s->q.p, s->q.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  from_pert<<<2 * ctx->num_sms * 4, 256, 0, ctx->stream>>>(s->stage64.p, s->q.p, s->h64.p, NN, s->nEq, s->sw, s->q.n);
+  SELF_LAUNCHED(ctx);
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(q, s->stage64.p, s->stage64.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  for (size_t e = 0; e < (size_t)s->nEl; ++e)
-    for (int v = 0; v < s->nEq; ++v)
-      for (size_t k = 0; k < NN; ++k) {
-        const size_t id = (e * s->nEq + v) * NN + k;
-        q[id] = (s->sw && v == 2) ? s->h[e * NN + k] + (double)f[id] : (double)f[id];
-      }
   return SELF_OK;
 }
 
