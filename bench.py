@@ -185,6 +185,54 @@ def run_reference(args):
         dist.destroy_process_group()
 
 
+def _time_steps(nat, L, ctx, sw, steps):
+    """Device time of `steps` single RK3 steps, each bracketed by CUDA events, L2 flushed in between."""
+    import ctypes as C
+    ms = C.c_double()
+    total = 0.0
+    for _ in range(steps):
+        nat.check(L.self_ctx_flush_l2(ctx.ptr, C.c_size_t(L2_FLUSH_BYTES)), ctx.ptr)
+        nat.check(L.self_ctx_timer_start(ctx.ptr), ctx.ptr)
+        sw.ForwardStepRK3_async(0.0, 1)
+        nat.check(L.self_ctx_timer_stop(ctx.ptr, C.byref(ms)), ctx.ptr)
+        total += ms.value
+    return total
+
+
+def _kernel_ms(nat, L, ctx, sw):
+    import ctypes as C
+    kms = (C.c_double * 2)()
+    nat.check(L.self_dg2d_time_kernels(sw.ptr, 20, C.c_size_t(L2_FLUSH_BYTES), kms), ctx.ptr)
+    return kms[0], kms[1]
+
+
+def _e2e(nat, L, ctx, sw, dof, steps, dist):
+    """Through the C ABI with pinned host buffers: upload state, one RK3 step, download state, per step."""
+    import ctypes as C
+    nbytes = dof * 8
+    hp = C.c_void_p()
+    nat.check(L.self_host_alloc(C.c_size_t(nbytes), C.byref(hp)))
+    hq = np.ctypeslib.as_array((C.c_double * dof).from_address(hp.value))
+    hq[:] = sw.GetSolution()
+    if dist:
+        dist.barrier()
+    ms = C.c_double()
+    t = 0.0
+    for _ in range(steps):
+        nat.check(L.self_ctx_timer_start(ctx.ptr), ctx.ptr)
+        nat.check(L.self_dg2d_set_state(sw.ptr, hq.ctypes.data_as(nat.dp)), ctx.ptr)
+        nat.check(L.self_dg2d_rk3(sw.ptr, C.c_double(0.0), 1), ctx.ptr)
+        nat.check(L.self_dg2d_get_state(sw.ptr, hq.ctypes.data_as(nat.dp)), ctx.ptr)
+        nat.check(L.self_ctx_timer_stop(ctx.ptr, C.byref(ms)), ctx.ptr)
+        t += ms.value
+    L.self_host_free(hp)
+    return t, nbytes
+
+
+FLOPS_PER_EL_STAGE_N7 = 14.0e3  # algorithmic FP64 flops of one element-stage at N=7 (traces, fluxes, contractions,
+#                                 lift, 1/J, sources, RK update, Riemann), the count of the design notes
+
+
 def run_gpu(args):
     dist, rank, ws, local = dist_init()
     import ctypes as C
@@ -192,65 +240,68 @@ def run_gpu(args):
     import self_gb300 as sg
     from self_gb300 import _native as nat
 
-    prec = nat.PREC_FP32 if args.precision == "fp32" else nat.PREC_FP64
+    head = nat.PREC_FP32 if args.precision == "fp32" else nat.PREC_FP64
     nod, mesh, q, h, fcor, dhdx, dhdy, dt = build_problem(sg)
     ctx = sg.Context(local)
-    sw = sg.ShallowWater(ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy, precision=prec)
-    sw.SetSolution(q)
     L = nat.lib()
     n = N_POLY + 1
     dof = q.size
+    forms = {}
+    for prec in (nat.PREC_FP64, nat.PREC_FP32):
+        sw = sg.ShallowWater(ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy, precision=prec)
+        sw.SetSolution(q)
+        forms[prec] = sw
 
-    for _ in range(args.warmup):
-        sw.ForwardStepRK3(0.0, 1)
-    ctx.synchronize()
-    if dist:
-        dist.barrier()
-    clocks = Clocks(local)
-    clocks.start()
-    launches0 = ctx.kernel_launches()
-    total_ms = 0.0
-    ms = C.c_double()
-    for _ in range(args.steps):
-        nat.check(L.self_ctx_flush_l2(ctx.ptr, C.c_size_t(L2_FLUSH_BYTES)), ctx.ptr)
-        nat.check(L.self_ctx_timer_start(ctx.ptr), ctx.ptr)
-        sw.ForwardStepRK3_async(0.0, 1)
-        nat.check(L.self_ctx_timer_stop(ctx.ptr, C.byref(ms)), ctx.ptr)
-        total_ms += ms.value
-    launches = ctx.kernel_launches() - launches0
-    ck = clocks.stop()
-    total_ms = allmax(dist, total_ms)
-    ms_step = total_ms / args.steps
-    value = ws * dof * args.steps / (total_ms * 1e-3)
+    # accuracy of the FP32 form against FP64 on this workload (device-resident runs from the same state)
+    acc_steps = args.accuracy_steps
+    res = {}
+    for prec, sw in forms.items():
+        sw.ForwardStepRK3(0.0, acc_steps)
+        res[prec] = sw.GetSolution().reshape(mesh.nEl, 3, -1)
+        sw.SetSolution(q)
+    H64, H32 = res[nat.PREC_FP64][:, 2], res[nat.PREC_FP32][:, 2]
+    h_err = float(np.abs(H32 - H64).max() / np.abs(H64).max())
+    eta_err = float(np.abs(H32 - H64).max() / np.abs(H64 - h.reshape(mesh.nEl, -1)).max())
 
-    # dominant kernel: volume + RK update, CUDA events around single launches (L2 flushed before each)
-    kms = (C.c_double * 2)()
-    nat.check(L.self_dg2d_time_kernels(sw.ptr, 20, C.c_size_t(L2_FLUSH_BYTES), kms), ctx.ptr)
-    pb = 8 if prec == nat.PREC_FP64 else 4
-    vbytes = bytes_per_volume_launch(mesh.nEl, n, pb)
-    achieved = vbytes / (kms[1] * 1e-3) / 1e9
+    out = {}
+    launches = 0
+    ck = None
+    for prec in (head, nat.PREC_FP64 if head == nat.PREC_FP32 else nat.PREC_FP32):
+        sw = forms[prec]
+        for _ in range(args.warmup):
+            sw.ForwardStepRK3(0.0, 1)
+        ctx.synchronize()
+        if dist:
+            dist.barrier()
+        if prec == head:
+            clocks = Clocks(local)
+            clocks.start()
+            l0 = ctx.kernel_launches()
+        total = _time_steps(nat, L, ctx, sw, args.steps)
+        if prec == head:
+            launches = ctx.kernel_launches() - l0
+            ck = clocks.stop()
+        total = allmax(dist, total)
+        e_ms, v_ms = _kernel_ms(nat, L, ctx, sw)
+        out[prec] = {"ms": total / args.steps, "value": ws * dof * args.steps / (total * 1e-3),
+                     "edge_ms": e_ms, "volume_ms": v_ms}
+
     peak, peak_kind = _peaks()
+    f64peak = C.c_double()
+    nat.check(L.self_probe_fma_peak(ctx.ptr, 1, C.byref(f64peak)), ctx.ptr)
 
-    # end to end through the C ABI with pinned host buffers
-    nbytes = dof * 8
-    hp = C.c_void_p()
-    nat.check(L.self_host_alloc(C.c_size_t(nbytes), C.byref(hp)))
-    hq = np.ctypeslib.as_array((C.c_double * dof).from_address(hp.value))
-    hq[:] = sw.GetSolution()
+    def roof(prec):
+        pb = 8 if prec == nat.PREC_FP64 else 4
+        vb = bytes_per_volume_launch(mesh.nEl, n, pb)
+        ach = vb / (out[prec]["volume_ms"] * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": None, "kernel": "dg_volume (volume + RK update + next-stage traces)",
+                "launch_ms": out[prec]["volume_ms"], "bytes_per_launch": vb, "peak_source": peak_kind,
+                "edge_kernel_ms": out[prec]["edge_ms"]}
+
     e2e_steps = max(3, min(args.steps, 50))
-    if dist:
-        dist.barrier()
-    t_e2e = 0.0
-    for _ in range(e2e_steps):
-        nat.check(L.self_ctx_timer_start(ctx.ptr), ctx.ptr)
-        nat.check(L.self_dg2d_set_state(sw.ptr, hq.ctypes.data_as(nat.dp)), ctx.ptr)
-        nat.check(L.self_dg2d_rk3(sw.ptr, C.c_double(0.0), 1), ctx.ptr)
-        nat.check(L.self_dg2d_get_state(sw.ptr, hq.ctypes.data_as(nat.dp)), ctx.ptr)
-        nat.check(L.self_ctx_timer_stop(ctx.ptr, C.byref(ms)), ctx.ptr)
-        t_e2e += ms.value
+    t_e2e, nbytes = _e2e(nat, L, ctx, forms[head], dof, e2e_steps, dist)
     t_e2e = allmax(dist, t_e2e)
-    e2e_value = ws * dof * e2e_steps / (t_e2e * 1e-3)
-    L.self_host_free(hp)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -259,27 +310,38 @@ def run_gpu(args):
         cpu = cpu_baseline(O, nod, mesh, q, h, fcor, dhdx, dhdy, dt)
 
     if rank == 0:
+        f64 = out[nat.PREC_FP64]
+        fl = FLOPS_PER_EL_STAGE_N7 * mesh.nEl
+        f64_gflops = fl / (f64["volume_ms"] * 1e-3) / 1e9
         line = {
-            "metric": "DG DOF-updates/s", "value": value, "unit": "DOF-updates/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == nat.PREC_FP64 else "f32",
+            "metric": "DG DOF-updates/s", "value": out[head]["value"], "unit": "DOF-updates/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out[head]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if head == nat.PREC_FP32 else "f64",
             "data": "synthetic (seeded; shapes of the shallow-water configuration)",
-            "config": {"workload": "DGSEM 2D conservative shallow water, 128x128 curvilinear quads, N=7 Legendre-Gauss,"
-                                   " 3 vars = 3,145,728 DOF, one LSRK3 step",
-                       "precision_form": "plain FP64 drop-in" if prec == nat.PREC_FP64 else "FP32 perturbation form",
+            "config": {"workload": "DGSEM 2D conservative shallow water, 128x128 curvilinear quads, N=7 Legendre-"
+                                   "Gauss, 3 vars = 3,145,728 DOF, one LSRK3 step",
+                       "precision_form": ("FP32 perturbation form about the lake at rest" if head == nat.PREC_FP32
+                                          else "plain FP64 drop-in"),
                        "l2": "flushed (512 MiB write) between timed steps", "parallelism": f"replicas x{ws}"},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "dg_volume (volume + RK update + traces)",
-                         "launch_ms": kms[1], "bytes_per_launch": vbytes, "peak_source": peak_kind,
-                         "edge_kernel_ms": kms[0]},
-            "e2e": {"value": e2e_value, "unit": "DOF-updates/s", "h2d_bytes_per_step": nbytes,
-                    "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
+            "roofline": roof(head),
+            "e2e": {"value": ws * dof * e2e_steps / (t_e2e * 1e-3), "unit": "DOF-updates/s",
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
+            "accuracy": {"steps": acc_steps, "height_rel_err_fp32_vs_fp64": h_err,
+                         "height_err_rel_to_max_eta": eta_err, "tolerance": 1e-6},
+            "fp64_plain": {"value": f64["value"], "ms_per_step": f64["ms"], "volume_ms": f64["volume_ms"],
+                           "edge_ms": f64["edge_ms"], "roofline_hbm": roof(nat.PREC_FP64),
+                           "fp64_pipe": {"achieved_tflops": f64_gflops / 1e3, "peak_tflops_measured": f64peak.value,
+                                         "frac": f64_gflops / 1e3 / f64peak.value,
+                                         "flops_per_element_stage": FLOPS_PER_EL_STAGE_N7}},
+            "fp32_form": {"value": out[nat.PREC_FP32]["value"], "ms_per_step": out[nat.PREC_FP32]["ms"],
+                          "volume_ms": out[nat.PREC_FP32]["volume_ms"], "edge_ms": out[nat.PREC_FP32]["edge_ms"]},
             "cpu_baseline": cpu,
             "clocks": ck,
         }
         print(json.dumps(line), flush=True)
-    sw.Trash()
+    for sw in forms.values():
+        sw.Trash()
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -291,7 +353,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"], help="form of the headline value")
+    ap.add_argument("--accuracy-steps", type=int, default=1000, help="FP32-vs-FP64 height check length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -69,6 +69,9 @@ int self_ctx_timer_start(self_ctx* ctx);
 int self_ctx_timer_stop(self_ctx* ctx, double* ms);
 /* Overwrite a scratch buffer of `bytes` on the context's stream (evicts L2 between timed steps). */
 int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
+/* Measured fused-multiply-add rate of the device (TFLOP/s, FP64 when fp64 != 0 else FP32): the compute
+ * roofline used for kernels bound by the FP64 pipe. */
+int self_probe_fma_peak(self_ctx* ctx, int fp64, double* tflops);
 /* Page-locked host memory for host<->device copies at full link speed. */
 int self_host_alloc(size_t bytes, void** ptr);
 int self_host_free(void* ptr);
