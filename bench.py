@@ -107,10 +107,13 @@ def build_problem(mod, N=N_POLY, nx=NX):
 
 
 def bytes_per_volume_launch(nEl, n, prec_bytes):
-    """Algorithmic HBM bytes of one volume + RK-update launch: q r/w, G r/w, 5 metric fields, 3 aux fields
-    (dhdx, dhdy, f), boundary fluxes read and new traces written (4 sides x n x 3 vars each)."""
+    """Algorithmic HBM bytes of one volume + RK-update launch (stages 2-3, G read): q r/w and G r/w (3 vars),
+    5 metric fields (dxds, dxdp, dyds, dydp, 1/J), the aux fields (FP64: dhdx, dhdy, f; FP32 perturbation form:
+    dhdx, dhdy, f, h and the 3 lake-at-rest tendency fields), boundary fluxes read and new traces written
+    (4 sides x n x 3 vars each)."""
     nn = n * n
-    per_el = prec_bytes * (4 * 3 * nn + 5 * nn + 3 * nn + 2 * 4 * n * 3)
+    aux = 3 if prec_bytes == 8 else 4 + 3
+    per_el = prec_bytes * (4 * 3 * nn + 5 * nn + aux * nn + 2 * 4 * n * 3)
     return per_el * nEl
 
 
