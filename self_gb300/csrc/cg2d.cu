@@ -27,6 +27,7 @@
 #include <memory>
 #include <vector>
 
+#include "cg2d_api.hpp"
 #include "internal.hpp"
 
 using namespace selfgpu;
@@ -360,6 +361,8 @@ struct self_cg2d {
   DevBuf<double> gm_H, gm_rho, gm_c, gm_s, gm_bhat;
   DevBuf<selfgpu::cg::GMScalars> GS;
   std::vector<double> h_J, h_w;
+  std::vector<double> h_fac, h_dinv;
+  bool upload_dev = true;  // false: compile the host arrays only (used by the batched solver)
   int nblk = 0;
 };
 
@@ -631,6 +634,7 @@ int compile_topology(self_cg2d* h, const self_cg2d_desc* d) {
     h->h_gdir.push_back(dir ? 1 : 0);
   }
   h->ngroups = (int)h->h_gdir.size();
+  if (!h->upload_dev) return SELF_OK;
   int rc;
   if ((rc = upload(h->ctx, h->src, h->h_src))) return rc;
   if ((rc = upload(h->ctx, h->gptr, h->h_gptr))) return rc;
@@ -694,6 +698,9 @@ int build_factors(self_cg2d* h, const self_cg2d_desc* d, std::vector<double>& Jw
     for (int k = a; k < b; ++k) dinv[h->h_gidx[k]] = 1.0;
     if (!h->h_gdir[g]) dinv[h->h_gidx[a]] = 1.0 / s;
   }
+  h->h_fac = fac;
+  h->h_dinv = dinv;
+  if (!h->upload_dev) return SELF_OK;
   int rc;
   if ((rc = upload(h->ctx, h->op64.fac, fac))) return rc;
   if ((rc = upload(h->ctx, h->op64.dinv, dinv))) return rc;
@@ -1127,3 +1134,44 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
 }
 
 }  // extern "C"
+
+namespace selfgpu {
+namespace cg {
+
+int compile_host(self_ctx* ctx, const self_cg2d_desc* d, HostCompiled& out) {
+  if (!d || d->N < 2 || d->N > 9 || d->nEl < 1 || d->op != 0)
+    return set_error(ctx, SELF_ERR_INVALID, "batched problems: Helmholtz operator, N in 2..9");
+  self_cg2d h;
+  h.ctx = ctx;
+  h.upload_dev = false;
+  h.N = d->N;
+  h.n = d->N + 1;
+  h.nEl = d->nEl;
+  h.nEdges = d->nEdges;
+  h.nNodes = d->nNodes;
+  h.op = 0;
+  h.nf = 4;
+  h.lambda = d->lambda;
+  h.nl = (size_t)h.n * h.n * h.nEl;
+  int rc = compile_topology(&h, d);
+  if (rc) return rc;
+  std::vector<double> Jww;
+  if ((rc = build_factors(&h, d, Jww))) return rc;
+  out.N = h.N;
+  out.n = h.n;
+  out.nEl = h.nEl;
+  out.ngroups = h.ngroups;
+  out.nl = h.nl;
+  out.src = std::move(h.h_src);
+  out.gptr = std::move(h.h_gptr);
+  out.gidx = std::move(h.h_gidx);
+  out.gdir = std::move(h.h_gdir);
+  out.fac = std::move(h.h_fac);
+  out.dinv = std::move(h.h_dinv);
+  out.Jww = std::move(Jww);
+  out.D.assign(d->dmat, d->dmat + (size_t)h.n * h.n);
+  return SELF_OK;
+}
+
+}  // namespace cg
+}  // namespace selfgpu

@@ -8,7 +8,9 @@ MappedGeometry_2D node positions (x, y flat arrays in element order).
 * shallow_water: [0, L]^2 with L = 2e6 m, beta-plane f = f0 + beta*y, depth 1000 m minus a 200 m Gaussian
   seamount (sigma 2e5 m) at the centre, free surface = 16 Gaussian bumps with amplitudes U(0.5, 1) m, centres
   uniform in the domain and widths U(5e4, 1.5e5) m, zero velocity.
-Time steps use dt = CFL * dx / ((2N+1) * s) with s = |u|+|v| (advection) or s = 2 sqrt(g Hmax) (shallow water).
+Time steps: advection dt = CFL * dx / ((2N+1) (|u|+|v|)); shallow water dt = CFL * 2 / ((2N+1) max over nodes of
+sqrt(g H) (|grad s| + |grad p|)), the contravariant gravity-wave speed of the mapped element (reduces to
+CFL * dx / ((2N+1) 2 sqrt(g H)) on uniform squares, and shrinks where the warp compresses the mesh).
 """
 import numpy as np
 
@@ -53,9 +55,18 @@ def shallow_water(mesh, N, nx, seed=2, cfl=0.5, L=SW_L, nbumps=16):
     n2 = (N + 1) ** 2
     q = np.zeros((nEl, 3, n2))
     q[:, 2, :] = (h + eta).reshape(nEl, n2)
-    Hmax = float((h + eta).max())
-    dt = cfl * (L / nx) / ((2 * N + 1) * 2.0 * np.sqrt(SW_G * Hmax))
+    dt = sw_dt(mesh, N, h + eta, cfl)
     return q.ravel(), h, fcor, dt
+
+
+def sw_dt(mesh, N, H, cfl=0.5, g=SW_G):
+    """CFL time step from the contravariant gravity-wave speeds: |grad s| = |(dydp, -dxdp)| / |J|,
+    |grad p| = |(-dyds, dxds)| / |J| on the reference element [-1, 1]^2."""
+    J = np.abs(mesh.J)
+    gs = np.hypot(mesh.dydp, mesh.dxdp) / J
+    gp = np.hypot(mesh.dyds, mesh.dxds) / J
+    lam = np.sqrt(g * H) * (gs + gp)
+    return float(cfl * 2.0 / ((2 * N + 1) * lam.max()))
 
 
 def sw_ensemble_member(mesh, N, nx, seed, cfl=0.5, L=SW_L):
