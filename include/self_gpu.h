@@ -199,6 +199,23 @@ int self_cg2d_unmask(self_cg2d* h, double* u);
 int self_cg2d_solve(self_cg2d* h, const self_solve_opts* opts, const double* source, const double* dirichlet,
                     double* solution, double* resi, self_solve_report* report);
 
+/* ---------------------------------------------------------------- batched uneven CGSEM solves
+ * Many independent Helmholtz problems (op 0; different meshes and degrees N = 2..9) solved together: one
+ * launch per phase covers every problem, inner iterations replay as CUDA graphs, converged problems skip their
+ * work.  Each problem is the PCG-Jacobi of self_cg2d_solve from a zero initial guess with homogeneous
+ * Dirichlet values; opts.precision = SELF_PREC_FP32 runs FP32 inner solves under FP64 iterative refinement. */
+typedef struct self_cgbatch self_cgbatch;
+int self_cgbatch_create(self_ctx* ctx, int nprob, const self_cg2d_desc* descs, self_cgbatch** out);
+int self_cgbatch_destroy(self_cgbatch* b);
+int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source);
+int self_cgbatch_problem_size(self_cgbatch* b, int p, long long* nlocal);
+int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* opts, self_solve_report* reports);
+int self_cgbatch_get_solution(self_cgbatch* b, int p, double* solution);
+/* Project autotuner: times elements-per-CTA choices of the element operator per (N, element-count bucket:
+ * <=256, <=1024, <=4096, larger) and keeps the fastest; cache_path (JSON) is read first and written after. */
+int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path);
+int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* epb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,7 +6,8 @@ mirror of the reference's Fortran types for Python drivers, tests and benchmarks
 from . import _native  # noqa: F401
 from .dgsem import Advection, Context, NodalStorage_2D, QuadMesh, ShallowWater, bathymetry_gradient  # noqa: F401
 from .cgsem import CGsemElliptic_2D  # noqa: F401
+from .batch import CGBatch  # noqa: F401
 from . import workloads  # noqa: F401
 
 __all__ = ["Context", "NodalStorage_2D", "QuadMesh", "ShallowWater", "Advection", "bathymetry_gradient",
-           "CGsemElliptic_2D", "workloads"]
+           "CGsemElliptic_2D", "CGBatch", "workloads"]

@@ -325,3 +325,441 @@ __global__ void batch_convert(const VTile* __restrict__ tiles, const Prob* __res
 
 }  // namespace cgb
 }  // namespace selfgpu
+
+// =============================================================================================== host side
+struct self_cgbatch {
+  self_ctx* ctx = nullptr;
+  int nprob = 0;
+  struct Mem {
+    DevBuf<float> fac32, dinv32, u32, r32, v32, w32, z32;
+    DevBuf<double> fac64, dinv64, f, x, r, v64, w64, z64;
+    DevBuf<int> src, gptr, gidx;
+    DevBuf<unsigned char> gdir;
+  };
+  std::vector<std::unique_ptr<Mem>> mem;
+  std::vector<selfgpu::cgb::Prob> hp;
+  std::vector<std::vector<double>> Jww;  // load assembly per problem (host)
+  std::vector<std::vector<int>> hsrc;    // unmask on download
+  std::vector<std::vector<int>> hdirnodes;
+  DevBuf<selfgpu::cgb::Prob> probs;
+  DevBuf<selfgpu::cgb::Scal> S;
+  DevBuf<double> red, partial;
+  DevBuf<selfgpu::cgb::DTable> DT;
+  DevBuf<selfgpu::cgb::ETile> et;
+  DevBuf<selfgpu::cgb::GTile> gt;
+  DevBuf<selfgpu::cgb::VTile> vt;
+  DevBuf<int> vt_ptr;
+  int n_et = 0, n_gt = 0, n_vt = 0;
+  int epb[10][4];  // elements per CTA for (N, element-count bucket); 0 = maximum
+  cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
+  int graph_k = 8;
+  ~self_cgbatch() {
+    if (inner32) cudaGraphExecDestroy(inner32);
+    if (inner64) cudaGraphExecDestroy(inner64);
+  }
+};
+
+namespace {
+
+using namespace selfgpu::cgb;
+
+int bucket_of(int nEl) { return nEl <= 256 ? 0 : nEl <= 1024 ? 1 : nEl <= 4096 ? 2 : 3; }
+int max_epb_rt(int N) {
+  const int nn = (N + 1) * (N + 1);
+  return nn >= 256 ? 1 : 256 / nn;
+}
+
+template <typename T>
+int put(self_ctx* ctx, DevBuf<T>& b, const T* src, size_t n) {
+  if (b.alloc(n) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "batch: device allocation failed");
+  if (src && n) SELF_CUDA_TRY(ctx, cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return SELF_OK;
+}
+template <typename T>
+int zeros(self_ctx* ctx, DevBuf<T>& b, size_t n) {
+  if (b.alloc(n) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "batch: device allocation failed");
+  if (n) SELF_CUDA_TRY(ctx, cudaMemset(b.p, 0, n * sizeof(T)));
+  return SELF_OK;
+}
+
+// element tiles for the problems selected by (N, bucket) filter (-1 = all), with the given override EPB
+int build_tiles(self_cgbatch* b, int onlyN, int onlyBucket, int forceEpb) {
+  std::vector<ETile> et;
+  std::vector<GTile> gt;
+  std::vector<VTile> vt;
+  std::vector<int> vptr(b->nprob + 1, 0);
+  for (int p = 0; p < b->nprob; ++p) {
+    const Prob& P = b->hp[p];
+    const int bk = bucket_of(P.nEl);
+    const bool sel = (onlyN < 0 || P.N == onlyN) && (onlyBucket < 0 || bk == onlyBucket);
+    int e = forceEpb > 0 ? forceEpb : (b->epb[P.N][bk] > 0 ? b->epb[P.N][bk] : max_epb_rt(P.N));
+    e = std::max(1, std::min(e, max_epb_rt(P.N)));
+    if (sel)
+      for (int e0 = 0; e0 < P.nEl; e0 += e) et.push_back(ETile{p, P.N, e0, std::min(e, P.nEl - e0)});
+    for (int g0 = 0; g0 < P.ngroups; g0 += kThreads) gt.push_back(GTile{p, g0, std::min(kThreads, P.ngroups - g0)});
+    vptr[p] = (int)vt.size();
+    for (long long s0 = 0; s0 < P.nl; s0 += kVecChunk) vt.push_back(VTile{p, s0, std::min<long long>(P.nl, s0 + kVecChunk)});
+  }
+  vptr[b->nprob] = (int)vt.size();
+  int rc;
+  if ((rc = put(b->ctx, b->et, et.data(), et.size()))) return rc;
+  if ((rc = put(b->ctx, b->gt, gt.data(), gt.size()))) return rc;
+  if ((rc = put(b->ctx, b->vt, vt.data(), vt.size()))) return rc;
+  if ((rc = put(b->ctx, b->vt_ptr, vptr.data(), vptr.size()))) return rc;
+  if (b->partial.n < vt.size() && (rc = zeros(b->ctx, b->partial, vt.size()))) return rc;
+  b->n_et = (int)et.size();
+  b->n_gt = (int)gt.size();
+  b->n_vt = (int)vt.size();
+  if (b->inner32) cudaGraphExecDestroy(b->inner32);
+  if (b->inner64) cudaGraphExecDestroy(b->inner64);
+  b->inner32 = b->inner64 = nullptr;
+  return SELF_OK;
+}
+
+template <typename R>
+int k_apply(self_cgbatch* b, int vin, int vout, int residual, int gate) {
+  if (!b->n_et) return SELF_OK;
+  batch_apply<R><<<b->n_et, kThreads, 0, b->ctx->stream>>>(b->et.p, b->probs.p, b->S.p, b->DT.p, vin, vout, residual,
+                                                           gate);
+  SELF_LAUNCHED(b->ctx);
+  return SELF_OK;
+}
+template <typename R>
+int k_dss(self_cgbatch* b, int v, int gate) {
+  if (!b->n_gt) return SELF_OK;
+  batch_dss<R><<<b->n_gt, kThreads, 0, b->ctx->stream>>>(b->gt.p, b->probs.p, b->S.p, v, gate);
+  SELF_LAUNCHED(b->ctx);
+  return SELF_OK;
+}
+template <typename R>
+int k_vec(self_cgbatch* b, int op, int gate, bool reduce) {
+  batch_vec<R><<<b->n_vt, kThreads, 0, b->ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, b->red.p, b->partial.p, op, 1,
+                                                         gate);
+  SELF_LAUNCHED(b->ctx);
+  if (reduce) {
+    batch_reduce<<<(b->nprob + 7) / 8, 256, 0, b->ctx->stream>>>(b->vt_ptr.p, b->partial.p, b->S.p, b->red.p, b->nprob,
+                                                                 gate);
+    SELF_LAUNCHED(b->ctx);
+  }
+  return SELF_OK;
+}
+int k_scal(self_cgbatch* b, int mode, int maxIters, int maxInner) {
+  batch_scal<<<(b->nprob + 127) / 128, 128, 0, b->ctx->stream>>>(b->S.p, b->red.p, b->nprob, mode, maxIters, maxInner);
+  SELF_LAUNCHED(b->ctx);
+  return SELF_OK;
+}
+
+// one inner (P)CG iteration for every problem whose inner solve is running
+template <typename R>
+int inner_iteration(self_cgbatch* b, int maxIters, int maxInner) {
+  int rc;
+  if ((rc = k_vec<R>(b, 0, 0, true)) || (rc = k_scal(b, 0, maxIters, maxInner))) return rc;
+  if ((rc = k_vec<R>(b, 1, 0, false))) return rc;
+  if ((rc = k_apply<R>(b, V_V, V_Z, 0, 0)) || (rc = k_dss<R>(b, V_Z, 0))) return rc;
+  if ((rc = k_vec<R>(b, 2, 0, true))) return rc;
+  if ((rc = k_vec<R>(b, 3, 0, true))) return rc;
+  return k_scal(b, 1, maxIters, maxInner);
+}
+
+int fp64_residual_norms(self_cgbatch* b, std::vector<double>& rn) {
+  int rc;
+  if ((rc = k_apply<double>(b, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, V_R, 1))) return rc;
+  if ((rc = k_vec<double>(b, 4, 1, true))) return rc;
+  rn.resize(b->nprob);
+  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(rn.data(), b->red.p, b->nprob * sizeof(double), cudaMemcpyDeviceToHost,
+                                        b->ctx->stream));
+  SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(b->ctx->stream));
+  for (auto& v : rn) v = std::sqrt(v);
+  return SELF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int self_cgbatch_create(self_ctx* ctx, int nprob, const self_cg2d_desc* descs, self_cgbatch** out) {
+  if (!ctx || nprob < 1 || !descs || !out) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  std::unique_ptr<self_cgbatch> b(new self_cgbatch());
+  b->ctx = ctx;
+  b->nprob = nprob;
+  std::memset(b->epb, 0, sizeof(b->epb));
+  DTable dt;
+  std::memset(&dt, 0, sizeof(dt));
+  std::vector<bool> haveD(10, false);
+  int rc;
+  for (int p = 0; p < nprob; ++p) {
+    selfgpu::cg::HostCompiled hc;
+    if ((rc = selfgpu::cg::compile_host(ctx, &descs[p], hc))) return rc;
+    const int n = hc.n;
+    if (!haveD[hc.N]) {
+      for (int k = 0; k < n * n; ++k) {
+        dt.d64[hc.N][k] = hc.D[k];
+        dt.d32[hc.N][k] = (float)hc.D[k];
+      }
+      haveD[hc.N] = true;
+    }
+    auto m = std::make_unique<self_cgbatch::Mem>();
+    const size_t nl = hc.nl;
+    std::vector<float> f32(hc.fac.begin(), hc.fac.end()), d32(hc.dinv.begin(), hc.dinv.end());
+    if ((rc = put(ctx, m->fac64, hc.fac.data(), hc.fac.size())) || (rc = put(ctx, m->fac32, f32.data(), f32.size())) ||
+        (rc = put(ctx, m->dinv64, hc.dinv.data(), nl)) || (rc = put(ctx, m->dinv32, d32.data(), nl)) ||
+        (rc = put(ctx, m->src, hc.src.data(), nl)) || (rc = put(ctx, m->gptr, hc.gptr.data(), hc.gptr.size())) ||
+        (rc = put(ctx, m->gidx, hc.gidx.data(), hc.gidx.size())) ||
+        (rc = put(ctx, m->gdir, hc.gdir.data(), hc.gdir.size())))
+      return rc;
+    if ((rc = zeros(ctx, m->f, nl)) || (rc = zeros(ctx, m->x, nl)) || (rc = zeros(ctx, m->r, nl)) ||
+        (rc = zeros(ctx, m->v64, nl)) || (rc = zeros(ctx, m->w64, nl)) || (rc = zeros(ctx, m->z64, nl)) ||
+        (rc = zeros(ctx, m->u32, nl)) || (rc = zeros(ctx, m->r32, nl)) || (rc = zeros(ctx, m->v32, nl)) ||
+        (rc = zeros(ctx, m->w32, nl)) || (rc = zeros(ctx, m->z32, nl)))
+      return rc;
+    Prob P;
+    P.N = hc.N;
+    P.n = n;
+    P.nEl = hc.nEl;
+    P.ngroups = hc.ngroups;
+    P.nl = (long long)nl;
+    P.fac32 = m->fac32.p;
+    P.fac64 = m->fac64.p;
+    P.dinv32 = m->dinv32.p;
+    P.dinv64 = m->dinv64.p;
+    P.src = m->src.p;
+    P.gptr = m->gptr.p;
+    P.gidx = m->gidx.p;
+    P.gdir = m->gdir.p;
+    P.f = m->f.p;
+    P.x = m->x.p;
+    P.r = m->r.p;
+    P.v64 = m->v64.p;
+    P.w64 = m->w64.p;
+    P.z64 = m->z64.p;
+    P.u32 = m->u32.p;
+    P.r32 = m->r32.p;
+    P.v32 = m->v32.p;
+    P.w32 = m->w32.p;
+    P.z32 = m->z32.p;
+    b->hp.push_back(P);
+    b->mem.push_back(std::move(m));
+    b->Jww.push_back(std::move(hc.Jww));
+    std::vector<int> dn;
+    for (int g = 0; g < hc.ngroups; ++g)
+      if (hc.gdir[g])
+        for (int k = hc.gptr[g]; k < hc.gptr[g + 1]; ++k) dn.push_back(hc.gidx[k]);
+    b->hdirnodes.push_back(std::move(dn));
+    b->hsrc.push_back(std::move(hc.src));
+  }
+  if ((rc = put(ctx, b->probs, b->hp.data(), b->hp.size())) || (rc = zeros(ctx, b->S, (size_t)nprob)) ||
+      (rc = zeros(ctx, b->red, (size_t)nprob)) || (rc = put(ctx, b->DT, &dt, 1)))
+    return rc;
+  if ((rc = build_tiles(b.get(), -1, -1, 0))) return rc;
+  *out = b.release();
+  return SELF_OK;
+}
+
+int self_cgbatch_destroy(self_cgbatch* b) {
+  if (!b) return SELF_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  delete b;
+  return SELF_OK;
+}
+
+int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source) {
+  if (!b || p < 0 || p >= b->nprob || !source) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
+  const auto& J = b->Jww[p];
+  std::vector<double> f(J.size());
+  for (size_t k = 0; k < f.size(); ++k) f[k] = source[k] * J[k];
+  SELF_CUDA_TRY(b->ctx, cudaMemcpy(b->hp[p].f, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return SELF_OK;
+}
+
+int self_cgbatch_problem_size(self_cgbatch* b, int p, long long* nl) {
+  if (!b || p < 0 || p >= b->nprob || !nl) return SELF_ERR_INVALID;
+  *nl = b->hp[p].nl;
+  return SELF_OK;
+}
+
+int self_cgbatch_get_solution(self_cgbatch* b, int p, double* solution) {
+  if (!b || p < 0 || p >= b->nprob || !solution) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
+  const size_t nl = (size_t)b->hp[p].nl;
+  std::vector<double> x(nl);
+  SELF_CUDA_TRY(b->ctx, cudaMemcpy(x.data(), b->hp[p].x, nl * sizeof(double), cudaMemcpyDeviceToHost));
+  const auto& src = b->hsrc[p];
+  for (size_t k = 0; k < nl; ++k) solution[k] = x[src[k]];  // UnMask
+  for (int l : b->hdirnodes[p]) solution[l] = 0.0;          // homogeneous Dirichlet values
+  return SELF_OK;
+}
+
+// Solve every problem: FP32 inner PCG-Jacobi under FP64 refinement (precision = SELF_PREC_FP32) or plain FP64
+// PCG-Jacobi (SELF_PREC_FP64), from a zero initial guess, to ||r||/||r0|| < tolerance.  Inner iterations run in
+// CUDA graphs of graph_k iterations.  reports: nprob entries (or NULL).
+int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* o, self_solve_report* reports) {
+  if (!b || !o || !(o->tolerance > 0) || o->maxIters < 1) return SELF_ERR_INVALID;
+  self_ctx* ctx = b->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const int np = b->nprob;
+  const bool fp32 = o->precision == SELF_PREC_FP32;
+  const double inner_tol = fp32 ? (o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4) : o->tolerance;
+  const int max_outer = fp32 ? (o->max_outer > 0 ? o->max_outer : 30) : 1;
+  const int maxInner = fp32 ? o->maxIters : o->maxIters;
+  int rc;
+  for (auto& P : b->hp) SELF_CUDA_TRY(ctx, cudaMemsetAsync(P.x, 0, P.nl * sizeof(double), ctx->stream));
+  std::vector<Scal> hs(np);
+  for (auto& s : hs) std::memset(&s, 0, sizeof(s));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, hs.data(), np * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<double> r0, rn;
+  if ((rc = fp64_residual_norms(b, r0))) return rc;
+  rn = r0;
+  std::vector<int> outer(np, 0), total(np, 0), conv(np, 0);
+  for (int p = 0; p < np; ++p) conv[p] = (r0[p] == 0.0);
+  for (int step = 0; step < max_outer; ++step) {
+    bool any = false;
+    for (int p = 0; p < np; ++p) {
+      if (!conv[p] && rn[p] / r0[p] < o->tolerance) conv[p] = 1;
+      if (!conv[p] && total[p] >= o->maxIters) conv[p] = 2;  // iteration budget spent
+      Scal& s = hs[p];
+      std::memset(&s, 0, sizeof(s));
+      s.conv = conv[p] ? 1 : 0;
+      s.done = s.conv;
+      s.r0 = r0[p];
+      s.rin0 = rn[p];
+      s.tol = inner_tol;
+      s.total = total[p];
+      if (!conv[p]) {
+        any = true;
+        outer[p]++;
+      }
+    }
+    if (!any) break;
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, hs.data(), np * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
+    if (fp32) {
+      batch_convert<<<b->n_vt, kThreads, 0, ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, 0);
+      SELF_LAUNCHED(ctx);
+    }
+    cudaGraphExec_t& G = fp32 ? b->inner32 : b->inner64;
+    if (!G) {
+      cudaGraph_t g;
+      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < b->graph_k && !rc; ++k)
+        rc = fp32 ? inner_iteration<float>(b, o->maxIters, maxInner) : inner_iteration<double>(b, o->maxIters, maxInner);
+      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+      if (rc) return rc;
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&G, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
+    }
+    const long long per_graph = 10LL * b->graph_k;  // kernels per captured chunk
+    for (int chunk = 0; chunk < 1000000; ++chunk) {
+      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
+      ctx->launches.fetch_add(per_graph);
+      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), b->S.p, np * sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
+      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      bool all = true;
+      for (int p = 0; p < np; ++p) all = all && (hs[p].done || hs[p].conv);
+      if (all) break;
+    }
+    for (int p = 0; p < np; ++p) total[p] = hs[p].total;
+    if (fp32) {
+      batch_convert<<<b->n_vt, kThreads, 0, ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, 1);
+      SELF_LAUNCHED(ctx);
+    }
+    if ((rc = fp64_residual_norms(b, rn))) return rc;
+    if (!fp32) {
+      for (int p = 0; p < np; ++p) conv[p] = conv[p] ? conv[p] : 1;
+      break;
+    }
+  }
+  int failed = 0;
+  for (int p = 0; p < np; ++p) {
+    const double rel = r0[p] > 0 ? rn[p] / r0[p] : 0.0;
+    const int ioerr = (rel < o->tolerance) ? 0 : -1;
+    failed += ioerr != 0;
+    if (reports) {
+      reports[p].ioerr = ioerr;
+      reports[p].iterations = total[p];
+      reports[p].outer_iterations = outer[p];
+      reports[p].r0 = r0[p];
+      reports[p].rel_residual = rel;
+    }
+  }
+  return SELF_OK;
+}
+
+// Measure elements-per-CTA choices of the element operator for each (N, element-count bucket) present and
+// keep the fastest; results are written to / read from a small JSON file when cache_path is given.
+int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
+  if (!b) return SELF_ERR_INVALID;
+  self_ctx* ctx = b->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  bool present[10][4] = {};
+  for (auto& P : b->hp) present[P.N][bucket_of(P.nEl)] = true;
+  // cache read: lines "N bucket epb"
+  if (cache_path) {
+    FILE* fp = fopen(cache_path, "r");
+    if (fp) {
+      char line[256];
+      while (fgets(line, sizeof(line), fp)) {
+        int N, bk, e;
+        if (sscanf(line, " { \"N\": %d, \"bucket\": %d, \"epb\": %d", &N, &bk, &e) == 3 && N >= 2 && N <= 9 && bk >= 0 &&
+            bk < 4)
+          b->epb[N][bk] = e;
+      }
+      fclose(fp);
+    }
+  }
+  std::vector<Scal> hs(b->nprob);
+  for (auto& s : hs) std::memset(&s, 0, sizeof(s));
+  SELF_CUDA_TRY(ctx, cudaMemcpy(b->S.p, hs.data(), hs.size() * sizeof(Scal), cudaMemcpyHostToDevice));
+  int rc;
+  for (int N = 2; N <= 9; ++N)
+    for (int bk = 0; bk < 4; ++bk) {
+      if (!present[N][bk] || b->epb[N][bk] > 0) continue;
+      const int mx = max_epb_rt(N);
+      int best = mx;
+      double best_ms = 1e30;
+      for (int e = mx; e >= 1; e = (e > 1 ? std::max(1, e / 2) : 0)) {
+        if ((rc = build_tiles(b, N, bk, e))) return rc;
+        for (int w = 0; w < 2; ++w)
+          if ((rc = k_apply<float>(b, V_V, V_Z, 0, 0))) return rc;
+        double ms = 0;
+        if ((rc = self_ctx_timer_start(ctx))) return rc;
+        for (int r = 0; r < 10; ++r)
+          if ((rc = k_apply<float>(b, V_V, V_Z, 0, 0))) return rc;
+        if ((rc = self_ctx_timer_stop(ctx, &ms))) return rc;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = e;
+        }
+        if (e == 1) break;
+      }
+      b->epb[N][bk] = best;
+    }
+  if ((rc = build_tiles(b, -1, -1, 0))) return rc;
+  if (cache_path) {
+    FILE* fp = fopen(cache_path, "w");
+    if (fp) {
+      fprintf(fp, "[\n");
+      bool first = true;
+      for (int N = 2; N <= 9; ++N)
+        for (int bk = 0; bk < 4; ++bk)
+          if (b->epb[N][bk] > 0) {
+            fprintf(fp, "%s  { \"N\": %d, \"bucket\": %d, \"epb\": %d }", first ? "" : ",\n", N, bk, b->epb[N][bk]);
+            first = false;
+          }
+      fprintf(fp, "\n]\n");
+      fclose(fp);
+    }
+  }
+  return SELF_OK;
+}
+
+int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* epb) {
+  if (!b || N < 2 || N > 9 || bucket < 0 || bucket > 3 || !epb) return SELF_ERR_INVALID;
+  *epb = b->epb[N][bucket] > 0 ? b->epb[N][bucket] : max_epb_rt(N);
+  return SELF_OK;
+}
+
+}  // extern "C"

@@ -90,3 +90,24 @@ def helmholtz(mesh, N, seed=3, nmodes=32, kmax=16):
     for m in range(nmodes):
         f += amp[m] * np.cos(2 * np.pi * (kx[m] * x + ky[m] * y) + ph[m])
     return k, f, -f
+
+
+def batched_specs(nprob=512, seed0=4, nmin=8, nmax=64, Nmin=3, Nmax=9):
+    """Mesh size n (n x n quads) uniform in [nmin, nmax] and degree N uniform in {Nmin..Nmax}, seed seed0 + i."""
+    specs = []
+    for i in range(nprob):
+        rng = np.random.default_rng(seed0 + i)
+        specs.append((int(rng.integers(nmin, nmax + 1)), int(rng.integers(Nmin, Nmax + 1)), seed0 + i))
+    return specs
+
+
+def batched_problem(mod, nx, N, seed, lam=0.1):
+    """One Helmholtz problem of the batched configuration: unit square, Dirichlet walls, its own coefficient
+    field k = 1 + 0.5 sin(4 pi x + a) cos(4 pi y + b) (seeded phases) and seeded Fourier right-hand side."""
+    nod = mod.NodalStorage_2D(N, -1, 2001)
+    mesh = mod.QuadMesh(nx, nx, N, -1, boundary_flag=-200)
+    rng = np.random.default_rng(seed + 100000)
+    a, b = rng.uniform(0, 2 * np.pi, 2)
+    k = 1.0 + 0.5 * np.sin(4 * np.pi * mesh.x + a) * np.cos(4 * np.pi * mesh.y + b)
+    _, f, source = helmholtz(mesh, N, seed=seed)
+    return {"nodal": nod, "mesh": mesh, "k": k, "source": source, "lam": lam}
