@@ -205,12 +205,24 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* opts, const double* sou
  * work.  Each problem is the PCG-Jacobi of self_cg2d_solve from a zero initial guess with homogeneous
  * Dirichlet values; opts.precision = SELF_PREC_FP32 runs FP32 inner solves under FP64 iterative refinement. */
 typedef struct self_cgbatch self_cgbatch;
+/* nprob problems in slots 0..nprob-1 (nprob may be 0 for an empty pool filled by self_cgbatch_add) */
 int self_cgbatch_create(self_ctx* ctx, int nprob, const self_cg2d_desc* descs, self_cgbatch** out);
 int self_cgbatch_destroy(self_cgbatch* b);
+/* set the source of slot p and restart its solve from a zero initial guess */
 int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source);
 int self_cgbatch_problem_size(self_cgbatch* b, int p, long long* nlocal);
+/* solve every problem in the pool (runs self_cgbatch_step until all finished); reports in slot order */
 int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* opts, self_solve_report* reports);
 int self_cgbatch_get_solution(self_cgbatch* b, int p, double* solution);
+/* continuous batching: add a problem to a free slot (its solve starts at the next step), remove a slot,
+ * advance every unfinished problem by one step (outer updates + graph-captured inner iterations), read a
+ * slot's report; footprint = device bytes a problem would take (admission control). */
+int self_cgbatch_add(self_cgbatch* b, const self_cg2d_desc* desc, const double* source, int* slot);
+int self_cgbatch_remove(self_cgbatch* b, int slot);
+int self_cgbatch_step(self_cgbatch* b, const self_solve_opts* opts, int* nfinished);
+int self_cgbatch_report(self_cgbatch* b, int slot, self_solve_report* report, int* finished);
+int self_cgbatch_footprint(const self_cg2d_desc* desc, long long* bytes);
+long long self_cgbatch_bytes(const self_cgbatch* b);
 /* Project autotuner: times elements-per-CTA choices of the element operator per (N, element-count bucket:
  * <=256, <=1024, <=4096, larger) and keeps the fastest; cache_path (JSON) is read first and written after. */
 int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path);

@@ -56,15 +56,23 @@ struct Prob {
   float* z32;
 };
 
-// Per-problem solver scalars.
-// done: the current inner solve of this problem finished; conv: the problem reached the outer tolerance.
+// Per-problem solver state.  phase: 0 inner iterations running, 1 waiting for the outer (FP64 residual)
+// update, 2 finished (converged or out of budget), 3 empty slot.
 struct Scal {
   double num, den, rr, r0, tol, rin0;
-  int iter, done, total, conv;
+  int iter, phase, total, fresh;  // fresh: no outer update yet (initial residual pending)
 };
 
-// gate 0 skips problems whose inner solve is done, gate 1 skips problems that converged
-__device__ __forceinline__ bool skip(const Scal& s, int gate) { return gate ? s.conv != 0 : s.done != 0; }
+// gate 0 runs problems in phase 0, gate 1 those in phase 1, gate 2 those in phase 1 that are not fresh,
+// gate 3 those in phase 0 that just entered it (iter == 0)
+__device__ __forceinline__ bool skip(const Scal& s, int gate) {
+  switch (gate) {
+    case 0: return s.phase != 0;
+    case 1: return s.phase != 1;
+    case 2: return s.phase != 1 || s.fresh;
+    default: return s.phase != 0 || s.iter != 0;
+  }
+}
 
 struct ETile {
   int prob, N, e0, ne;
@@ -288,13 +296,13 @@ __global__ void batch_reduce(const int* __restrict__ vt_ptr, const double* __res
 
 // Scalar updates per problem.
 // mode 0: num = red (after op 0);  mode 1: end of iteration: den = num, rr = red, convergence test
-// mode 0: num = red (after op 0); mode 1: end of an inner iteration (den = num, rr, inner stop test)
+// mode 0: num = red (after op 0); mode 1: end of an inner iteration (den = num, rr, inner stop test -> phase 1)
 __global__ void batch_scal(Scal* __restrict__ S, const double* __restrict__ red, int nprob, int mode, int maxIters,
                            int maxInner) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nprob) return;
   Scal& s = S[p];
-  if (s.done || s.conv) return;
+  if (s.phase != 0) return;
   if (mode == 0) {
     s.num = red[p];
   } else {
@@ -303,15 +311,16 @@ __global__ void batch_scal(Scal* __restrict__ S, const double* __restrict__ red,
     s.iter += 1;
     s.total += 1;
     s.rr = rn;
-    if (!(rn == rn) || rn / s.rin0 < s.tol || s.total >= maxIters || s.iter >= maxInner) s.done = 1;
+    if (!(rn == rn) || rn / s.rin0 < s.tol || s.total >= maxIters || s.iter >= maxInner) s.phase = 1;
   }
 }
 
 // FP64 -> FP32 residual, FP32 correction -> FP64 solution, zeroing the inner correction
+// dir 0 (gate 3, problems entering an inner solve): r32 = r, u32 = 0; dir 1 (gate 2): x += u32
 __global__ void batch_convert(const VTile* __restrict__ tiles, const Prob* __restrict__ probs,
                               const Scal* __restrict__ S, int dir) {
   const VTile t = tiles[blockIdx.x];
-  if (S[t.prob].conv) return;
+  if (skip(S[t.prob], dir == 0 ? 3 : 2)) return;
   const Prob& p = probs[t.prob];
   for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
     if (dir == 0) {
@@ -327,32 +336,43 @@ __global__ void batch_convert(const VTile* __restrict__ tiles, const Prob* __res
 }  // namespace selfgpu
 
 // =============================================================================================== host side
+// Slots are stable problem indices; an empty slot is in phase 3 and owns no memory.
 struct self_cgbatch {
   self_ctx* ctx = nullptr;
-  int nprob = 0;
   struct Mem {
     DevBuf<float> fac32, dinv32, u32, r32, v32, w32, z32;
     DevBuf<double> fac64, dinv64, f, x, r, v64, w64, z64;
     DevBuf<int> src, gptr, gidx;
     DevBuf<unsigned char> gdir;
   };
-  std::vector<std::unique_ptr<Mem>> mem;
+  struct Slot {
+    bool used = false;
+    std::unique_ptr<Mem> mem;
+    std::vector<double> Jww;
+    std::vector<int> src, dirnodes;
+    long long bytes = 0;
+    int outer = 0;
+  };
+  std::vector<Slot> slots;
   std::vector<selfgpu::cgb::Prob> hp;
-  std::vector<std::vector<double>> Jww;  // load assembly per problem (host)
-  std::vector<std::vector<int>> hsrc;    // unmask on download
-  std::vector<std::vector<int>> hdirnodes;
+  std::vector<selfgpu::cgb::Scal> hs;
+  int cap = 0;
   DevBuf<selfgpu::cgb::Prob> probs;
   DevBuf<selfgpu::cgb::Scal> S;
   DevBuf<double> red, partial;
   DevBuf<selfgpu::cgb::DTable> DT;
+  selfgpu::cgb::DTable hDT;
+  bool haveD[10] = {};
   DevBuf<selfgpu::cgb::ETile> et;
   DevBuf<selfgpu::cgb::GTile> gt;
   DevBuf<selfgpu::cgb::VTile> vt;
   DevBuf<int> vt_ptr;
   int n_et = 0, n_gt = 0, n_vt = 0;
-  int epb[10][4];  // elements per CTA for (N, element-count bucket); 0 = maximum
+  bool dirty = true;
+  int epb[10][4];
   cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
   int graph_k = 8;
+  long long bytes_in_use = 0;
   ~self_cgbatch() {
     if (inner32) cudaGraphExecDestroy(inner32);
     if (inner64) cudaGraphExecDestroy(inner64);
@@ -382,13 +402,41 @@ int zeros(self_ctx* ctx, DevBuf<T>& b, size_t n) {
   return SELF_OK;
 }
 
-// element tiles for the problems selected by (N, bucket) filter (-1 = all), with the given override EPB
+void drop_graphs(self_cgbatch* b) {
+  if (b->inner32) cudaGraphExecDestroy(b->inner32);
+  if (b->inner64) cudaGraphExecDestroy(b->inner64);
+  b->inner32 = b->inner64 = nullptr;
+}
+
+// grow the slot arrays (host and device) to hold at least `want` problems
+int ensure_cap(self_cgbatch* b, int want) {
+  if (want <= b->cap) return SELF_OK;
+  int nc = std::max(want, std::max(16, 2 * b->cap));
+  b->slots.resize(nc);
+  Prob empty;
+  std::memset(&empty, 0, sizeof(empty));
+  b->hp.resize(nc, empty);
+  Scal e;
+  std::memset(&e, 0, sizeof(e));
+  e.phase = 3;
+  b->hs.resize(nc, e);
+  b->cap = nc;
+  int rc;
+  if ((rc = zeros(b->ctx, b->probs, nc)) || (rc = zeros(b->ctx, b->S, nc)) || (rc = zeros(b->ctx, b->red, nc)))
+    return rc;
+  b->dirty = true;
+  return SELF_OK;
+}
+
+// element tiles for the problems selected by (N, bucket) filter (-1 = all), with an optional forced EPB
 int build_tiles(self_cgbatch* b, int onlyN, int onlyBucket, int forceEpb) {
   std::vector<ETile> et;
   std::vector<GTile> gt;
   std::vector<VTile> vt;
-  std::vector<int> vptr(b->nprob + 1, 0);
-  for (int p = 0; p < b->nprob; ++p) {
+  std::vector<int> vptr(b->cap + 1, 0);
+  for (int p = 0; p < b->cap; ++p) {
+    vptr[p] = (int)vt.size();
+    if (!b->slots[p].used) continue;
     const Prob& P = b->hp[p];
     const int bk = bucket_of(P.nEl);
     const bool sel = (onlyN < 0 || P.N == onlyN) && (onlyBucket < 0 || bk == onlyBucket);
@@ -397,22 +445,31 @@ int build_tiles(self_cgbatch* b, int onlyN, int onlyBucket, int forceEpb) {
     if (sel)
       for (int e0 = 0; e0 < P.nEl; e0 += e) et.push_back(ETile{p, P.N, e0, std::min(e, P.nEl - e0)});
     for (int g0 = 0; g0 < P.ngroups; g0 += kThreads) gt.push_back(GTile{p, g0, std::min(kThreads, P.ngroups - g0)});
-    vptr[p] = (int)vt.size();
-    for (long long s0 = 0; s0 < P.nl; s0 += kVecChunk) vt.push_back(VTile{p, s0, std::min<long long>(P.nl, s0 + kVecChunk)});
+    for (long long s0 = 0; s0 < P.nl; s0 += kVecChunk)
+      vt.push_back(VTile{p, s0, std::min<long long>(P.nl, s0 + kVecChunk)});
   }
-  vptr[b->nprob] = (int)vt.size();
+  vptr[b->cap] = (int)vt.size();
   int rc;
   if ((rc = put(b->ctx, b->et, et.data(), et.size()))) return rc;
   if ((rc = put(b->ctx, b->gt, gt.data(), gt.size()))) return rc;
   if ((rc = put(b->ctx, b->vt, vt.data(), vt.size()))) return rc;
   if ((rc = put(b->ctx, b->vt_ptr, vptr.data(), vptr.size()))) return rc;
-  if (b->partial.n < vt.size() && (rc = zeros(b->ctx, b->partial, vt.size()))) return rc;
+  if (b->partial.n < std::max<size_t>(1, vt.size()) && (rc = zeros(b->ctx, b->partial, std::max<size_t>(1, vt.size()))))
+    return rc;
   b->n_et = (int)et.size();
   b->n_gt = (int)gt.size();
   b->n_vt = (int)vt.size();
-  if (b->inner32) cudaGraphExecDestroy(b->inner32);
-  if (b->inner64) cudaGraphExecDestroy(b->inner64);
-  b->inner32 = b->inner64 = nullptr;
+  drop_graphs(b);
+  return SELF_OK;
+}
+
+int refresh(self_cgbatch* b) {
+  if (!b->dirty) return SELF_OK;
+  int rc;
+  if ((rc = put(b->ctx, b->probs, b->hp.data(), (size_t)b->cap))) return rc;
+  if ((rc = put(b->ctx, b->DT, &b->hDT, 1))) return rc;
+  if ((rc = build_tiles(b, -1, -1, 0))) return rc;
+  b->dirty = false;
   return SELF_OK;
 }
 
@@ -433,23 +490,29 @@ int k_dss(self_cgbatch* b, int v, int gate) {
 }
 template <typename R>
 int k_vec(self_cgbatch* b, int op, int gate, bool reduce) {
+  if (!b->n_vt) return SELF_OK;
   batch_vec<R><<<b->n_vt, kThreads, 0, b->ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, b->red.p, b->partial.p, op, 1,
                                                          gate);
   SELF_LAUNCHED(b->ctx);
   if (reduce) {
-    batch_reduce<<<(b->nprob + 7) / 8, 256, 0, b->ctx->stream>>>(b->vt_ptr.p, b->partial.p, b->S.p, b->red.p, b->nprob,
-                                                                 gate);
+    batch_reduce<<<(b->cap + 7) / 8, 256, 0, b->ctx->stream>>>(b->vt_ptr.p, b->partial.p, b->S.p, b->red.p, b->cap,
+                                                               gate);
     SELF_LAUNCHED(b->ctx);
   }
   return SELF_OK;
 }
 int k_scal(self_cgbatch* b, int mode, int maxIters, int maxInner) {
-  batch_scal<<<(b->nprob + 127) / 128, 128, 0, b->ctx->stream>>>(b->S.p, b->red.p, b->nprob, mode, maxIters, maxInner);
+  batch_scal<<<(b->cap + 127) / 128, 128, 0, b->ctx->stream>>>(b->S.p, b->red.p, b->cap, mode, maxIters, maxInner);
+  SELF_LAUNCHED(b->ctx);
+  return SELF_OK;
+}
+int k_convert(self_cgbatch* b, int dir) {
+  if (!b->n_vt) return SELF_OK;
+  batch_convert<<<b->n_vt, kThreads, 0, b->ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, dir);
   SELF_LAUNCHED(b->ctx);
   return SELF_OK;
 }
 
-// one inner (P)CG iteration for every problem whose inner solve is running
 template <typename R>
 int inner_iteration(self_cgbatch* b, int maxIters, int maxInner) {
   int rc;
@@ -461,15 +524,162 @@ int inner_iteration(self_cgbatch* b, int maxIters, int maxInner) {
   return k_scal(b, 1, maxIters, maxInner);
 }
 
-int fp64_residual_norms(self_cgbatch* b, std::vector<double>& rn) {
+// One tick: outer updates of the problems waiting for one, then graph_k inner iterations of the others.
+int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
+  self_ctx* ctx = b->ctx;
+  const bool fp32 = o->precision == SELF_PREC_FP32;
+  const double inner_tol = fp32 ? (o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4) : o->tolerance;
+  const int max_outer = fp32 ? (o->max_outer > 0 ? o->max_outer : 30) : 2;
   int rc;
-  if ((rc = k_apply<double>(b, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, V_R, 1))) return rc;
-  if ((rc = k_vec<double>(b, 4, 1, true))) return rc;
-  rn.resize(b->nprob);
-  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(rn.data(), b->red.p, b->nprob * sizeof(double), cudaMemcpyDeviceToHost,
-                                        b->ctx->stream));
-  SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(b->ctx->stream));
-  for (auto& v : rn) v = std::sqrt(v);
+  if ((rc = refresh(b))) return rc;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
+  bool any1 = false;
+  for (int p = 0; p < b->cap; ++p) any1 = any1 || (b->slots[p].used && b->hs[p].phase == 1);
+  if (any1) {
+    if (fp32 && (rc = k_convert(b, 1))) return rc;  // x += u32 for problems whose inner solve ended
+    if ((rc = k_apply<double>(b, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, V_R, 1))) return rc;
+    if ((rc = k_vec<double>(b, 4, 1, true))) return rc;
+    std::vector<double> rr(b->cap);
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(rr.data(), b->red.p, b->cap * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int p = 0; p < b->cap; ++p) {
+      Scal& s = b->hs[p];
+      if (!b->slots[p].used || s.phase != 1) continue;
+      const double rn = std::sqrt(rr[p]);
+      s.rr = rn;
+      if (s.fresh) {
+        s.r0 = rn;
+        s.fresh = 0;
+      }
+      const bool conv = s.r0 == 0.0 || rn / s.r0 < o->tolerance || !(rn == rn);
+      if (conv || s.total >= o->maxIters || b->slots[p].outer >= max_outer) {
+        s.phase = 2;
+        continue;
+      }
+      b->slots[p].outer++;
+      s.phase = 0;
+      s.iter = 0;
+      s.num = s.den = 0;
+      s.rin0 = rn;
+      s.tol = fp32 ? inner_tol : o->tolerance * s.r0 / rn;
+    }
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
+    if (fp32 && (rc = k_convert(b, 0))) return rc;  // r32 = r, u32 = 0 for problems entering an inner solve
+  }
+  bool any0 = false;
+  for (int p = 0; p < b->cap; ++p) any0 = any0 || (b->slots[p].used && b->hs[p].phase == 0);
+  if (any0) {
+    cudaGraphExec_t& G = fp32 ? b->inner32 : b->inner64;
+    if (!G) {
+      cudaGraph_t g;
+      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < b->graph_k && !rc; ++k)
+        rc = fp32 ? inner_iteration<float>(b, o->maxIters, o->maxIters) : inner_iteration<double>(b, o->maxIters, o->maxIters);
+      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+      if (rc) return rc;
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&G, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
+      ctx->launches.fetch_sub(13LL * b->graph_k);
+    }
+    SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
+    ctx->launches.fetch_add(13LL * b->graph_k);
+  }
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->hs.data(), b->S.p, b->cap * sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  int fin = 0;
+  for (int p = 0; p < b->cap; ++p) fin += b->slots[p].used && b->hs[p].phase == 2;
+  if (nfinished) *nfinished = fin;
+  return SELF_OK;
+}
+
+int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, int* slot_out) {
+  self_ctx* ctx = b->ctx;
+  selfgpu::cg::HostCompiled hc;
+  int rc;
+  if ((rc = selfgpu::cg::compile_host(ctx, d, hc))) return rc;
+  int slot = -1;
+  for (int p = 0; p < b->cap; ++p)
+    if (!b->slots[p].used) {
+      slot = p;
+      break;
+    }
+  if (slot < 0) {
+    slot = b->cap;
+    if ((rc = ensure_cap(b, b->cap + 1))) return rc;
+  }
+  const int n = hc.n;
+  if (!b->haveD[hc.N]) {
+    for (int k = 0; k < n * n; ++k) {
+      b->hDT.d64[hc.N][k] = hc.D[k];
+      b->hDT.d32[hc.N][k] = (float)hc.D[k];
+    }
+    b->haveD[hc.N] = true;
+  }
+  auto m = std::make_unique<self_cgbatch::Mem>();
+  const size_t nl = hc.nl;
+  std::vector<float> f32(hc.fac.begin(), hc.fac.end()), d32(hc.dinv.begin(), hc.dinv.end());
+  if ((rc = put(ctx, m->fac64, hc.fac.data(), hc.fac.size())) || (rc = put(ctx, m->fac32, f32.data(), f32.size())) ||
+      (rc = put(ctx, m->dinv64, hc.dinv.data(), nl)) || (rc = put(ctx, m->dinv32, d32.data(), nl)) ||
+      (rc = put(ctx, m->src, hc.src.data(), nl)) || (rc = put(ctx, m->gptr, hc.gptr.data(), hc.gptr.size())) ||
+      (rc = put(ctx, m->gidx, hc.gidx.data(), hc.gidx.size())) || (rc = put(ctx, m->gdir, hc.gdir.data(), hc.gdir.size())))
+    return rc;
+  if ((rc = zeros(ctx, m->f, nl)) || (rc = zeros(ctx, m->x, nl)) || (rc = zeros(ctx, m->r, nl)) ||
+      (rc = zeros(ctx, m->v64, nl)) || (rc = zeros(ctx, m->w64, nl)) || (rc = zeros(ctx, m->z64, nl)) ||
+      (rc = zeros(ctx, m->u32, nl)) || (rc = zeros(ctx, m->r32, nl)) || (rc = zeros(ctx, m->v32, nl)) ||
+      (rc = zeros(ctx, m->w32, nl)) || (rc = zeros(ctx, m->z32, nl)))
+    return rc;
+  Prob P;
+  P.N = hc.N;
+  P.n = n;
+  P.nEl = hc.nEl;
+  P.ngroups = hc.ngroups;
+  P.nl = (long long)nl;
+  P.fac32 = m->fac32.p;
+  P.fac64 = m->fac64.p;
+  P.dinv32 = m->dinv32.p;
+  P.dinv64 = m->dinv64.p;
+  P.src = m->src.p;
+  P.gptr = m->gptr.p;
+  P.gidx = m->gidx.p;
+  P.gdir = m->gdir.p;
+  P.f = m->f.p;
+  P.x = m->x.p;
+  P.r = m->r.p;
+  P.v64 = m->v64.p;
+  P.w64 = m->w64.p;
+  P.z64 = m->z64.p;
+  P.u32 = m->u32.p;
+  P.r32 = m->r32.p;
+  P.v32 = m->v32.p;
+  P.w32 = m->w32.p;
+  P.z32 = m->z32.p;
+  if (source) {
+    std::vector<double> f(nl);
+    for (size_t k = 0; k < nl; ++k) f[k] = source[k] * hc.Jww[k];
+    SELF_CUDA_TRY(ctx, cudaMemcpy(P.f, f.data(), nl * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  self_cgbatch::Slot& S = b->slots[slot];
+  S.used = true;
+  S.outer = 0;
+  S.bytes = (long long)(m->fac32.bytes() + m->dinv32.bytes() + 5 * nl * 4 + m->fac64.bytes() + m->dinv64.bytes() +
+                        6 * nl * 8 + m->src.bytes() + m->gptr.bytes() + m->gidx.bytes() + m->gdir.bytes());
+  b->bytes_in_use += S.bytes;
+  S.mem = std::move(m);
+  S.Jww = std::move(hc.Jww);
+  S.dirnodes.clear();
+  for (int g = 0; g < hc.ngroups; ++g)
+    if (hc.gdir[g])
+      for (int k = hc.gptr[g]; k < hc.gptr[g + 1]; ++k) S.dirnodes.push_back(hc.gidx[k]);
+  S.src = std::move(hc.src);
+  b->hp[slot] = P;
+  Scal& sc = b->hs[slot];
+  std::memset(&sc, 0, sizeof(sc));
+  sc.phase = 1;
+  sc.fresh = 1;
+  b->dirty = true;
+  *slot_out = slot;
   return SELF_OK;
 }
 
@@ -478,80 +688,18 @@ int fp64_residual_norms(self_cgbatch* b, std::vector<double>& rn) {
 extern "C" {
 
 int self_cgbatch_create(self_ctx* ctx, int nprob, const self_cg2d_desc* descs, self_cgbatch** out) {
-  if (!ctx || nprob < 1 || !descs || !out) return SELF_ERR_INVALID;
+  if (!ctx || nprob < 0 || (nprob > 0 && !descs) || !out) return SELF_ERR_INVALID;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   std::unique_ptr<self_cgbatch> b(new self_cgbatch());
   b->ctx = ctx;
-  b->nprob = nprob;
   std::memset(b->epb, 0, sizeof(b->epb));
-  DTable dt;
-  std::memset(&dt, 0, sizeof(dt));
-  std::vector<bool> haveD(10, false);
+  std::memset(&b->hDT, 0, sizeof(b->hDT));
   int rc;
+  if ((rc = ensure_cap(b.get(), std::max(nprob, 1)))) return rc;
   for (int p = 0; p < nprob; ++p) {
-    selfgpu::cg::HostCompiled hc;
-    if ((rc = selfgpu::cg::compile_host(ctx, &descs[p], hc))) return rc;
-    const int n = hc.n;
-    if (!haveD[hc.N]) {
-      for (int k = 0; k < n * n; ++k) {
-        dt.d64[hc.N][k] = hc.D[k];
-        dt.d32[hc.N][k] = (float)hc.D[k];
-      }
-      haveD[hc.N] = true;
-    }
-    auto m = std::make_unique<self_cgbatch::Mem>();
-    const size_t nl = hc.nl;
-    std::vector<float> f32(hc.fac.begin(), hc.fac.end()), d32(hc.dinv.begin(), hc.dinv.end());
-    if ((rc = put(ctx, m->fac64, hc.fac.data(), hc.fac.size())) || (rc = put(ctx, m->fac32, f32.data(), f32.size())) ||
-        (rc = put(ctx, m->dinv64, hc.dinv.data(), nl)) || (rc = put(ctx, m->dinv32, d32.data(), nl)) ||
-        (rc = put(ctx, m->src, hc.src.data(), nl)) || (rc = put(ctx, m->gptr, hc.gptr.data(), hc.gptr.size())) ||
-        (rc = put(ctx, m->gidx, hc.gidx.data(), hc.gidx.size())) ||
-        (rc = put(ctx, m->gdir, hc.gdir.data(), hc.gdir.size())))
-      return rc;
-    if ((rc = zeros(ctx, m->f, nl)) || (rc = zeros(ctx, m->x, nl)) || (rc = zeros(ctx, m->r, nl)) ||
-        (rc = zeros(ctx, m->v64, nl)) || (rc = zeros(ctx, m->w64, nl)) || (rc = zeros(ctx, m->z64, nl)) ||
-        (rc = zeros(ctx, m->u32, nl)) || (rc = zeros(ctx, m->r32, nl)) || (rc = zeros(ctx, m->v32, nl)) ||
-        (rc = zeros(ctx, m->w32, nl)) || (rc = zeros(ctx, m->z32, nl)))
-      return rc;
-    Prob P;
-    P.N = hc.N;
-    P.n = n;
-    P.nEl = hc.nEl;
-    P.ngroups = hc.ngroups;
-    P.nl = (long long)nl;
-    P.fac32 = m->fac32.p;
-    P.fac64 = m->fac64.p;
-    P.dinv32 = m->dinv32.p;
-    P.dinv64 = m->dinv64.p;
-    P.src = m->src.p;
-    P.gptr = m->gptr.p;
-    P.gidx = m->gidx.p;
-    P.gdir = m->gdir.p;
-    P.f = m->f.p;
-    P.x = m->x.p;
-    P.r = m->r.p;
-    P.v64 = m->v64.p;
-    P.w64 = m->w64.p;
-    P.z64 = m->z64.p;
-    P.u32 = m->u32.p;
-    P.r32 = m->r32.p;
-    P.v32 = m->v32.p;
-    P.w32 = m->w32.p;
-    P.z32 = m->z32.p;
-    b->hp.push_back(P);
-    b->mem.push_back(std::move(m));
-    b->Jww.push_back(std::move(hc.Jww));
-    std::vector<int> dn;
-    for (int g = 0; g < hc.ngroups; ++g)
-      if (hc.gdir[g])
-        for (int k = hc.gptr[g]; k < hc.gptr[g + 1]; ++k) dn.push_back(hc.gidx[k]);
-    b->hdirnodes.push_back(std::move(dn));
-    b->hsrc.push_back(std::move(hc.src));
+    int slot;
+    if ((rc = add_problem(b.get(), &descs[p], nullptr, &slot))) return rc;
   }
-  if ((rc = put(ctx, b->probs, b->hp.data(), b->hp.size())) || (rc = zeros(ctx, b->S, (size_t)nprob)) ||
-      (rc = zeros(ctx, b->red, (size_t)nprob)) || (rc = put(ctx, b->DT, &dt, 1)))
-    return rc;
-  if ((rc = build_tiles(b.get(), -1, -1, 0))) return rc;
   *out = b.release();
   return SELF_OK;
 }
@@ -564,126 +712,118 @@ int self_cgbatch_destroy(self_cgbatch* b) {
   return SELF_OK;
 }
 
-int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source) {
-  if (!b || p < 0 || p >= b->nprob || !source) return SELF_ERR_INVALID;
+int self_cgbatch_add(self_cgbatch* b, const self_cg2d_desc* desc, const double* source, int* slot) {
+  if (!b || !desc || !source || !slot) return SELF_ERR_INVALID;
   SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
-  const auto& J = b->Jww[p];
+  return add_problem(b, desc, source, slot);
+}
+
+int self_cgbatch_remove(self_cgbatch* b, int p) {
+  if (!b || p < 0 || p >= b->cap || !b->slots[p].used) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
+  SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(b->ctx->stream));
+  auto& S = b->slots[p];
+  b->bytes_in_use -= S.bytes;
+  S = self_cgbatch::Slot();
+  std::memset(&b->hp[p], 0, sizeof(Prob));
+  std::memset(&b->hs[p], 0, sizeof(Scal));
+  b->hs[p].phase = 3;
+  b->dirty = true;
+  return SELF_OK;
+}
+
+int self_cgbatch_footprint(const self_cg2d_desc* d, long long* bytes) {
+  if (!d || !bytes) return SELF_ERR_INVALID;
+  const long long nl = (long long)(d->N + 1) * (d->N + 1) * d->nEl;
+  // FP32: 4 factors + diag + 5 vectors; FP64: 4 factors + diag + 6 vectors; src + groups
+  *bytes = nl * (10 * 4 + 11 * 8 + 4 + 8) + 4096;
+  return SELF_OK;
+}
+
+int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source) {
+  if (!b || p < 0 || p >= b->cap || !b->slots[p].used || !source) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
+  const auto& J = b->slots[p].Jww;
   std::vector<double> f(J.size());
   for (size_t k = 0; k < f.size(); ++k) f[k] = source[k] * J[k];
   SELF_CUDA_TRY(b->ctx, cudaMemcpy(b->hp[p].f, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice));
+  Scal& s = b->hs[p];
+  std::memset(&s, 0, sizeof(s));
+  s.phase = 1;
+  s.fresh = 1;
+  b->slots[p].outer = 0;
+  SELF_CUDA_TRY(b->ctx, cudaMemset(b->hp[p].x, 0, b->hp[p].nl * sizeof(double)));
   return SELF_OK;
 }
 
 int self_cgbatch_problem_size(self_cgbatch* b, int p, long long* nl) {
-  if (!b || p < 0 || p >= b->nprob || !nl) return SELF_ERR_INVALID;
+  if (!b || p < 0 || p >= b->cap || !b->slots[p].used || !nl) return SELF_ERR_INVALID;
   *nl = b->hp[p].nl;
   return SELF_OK;
 }
 
 int self_cgbatch_get_solution(self_cgbatch* b, int p, double* solution) {
-  if (!b || p < 0 || p >= b->nprob || !solution) return SELF_ERR_INVALID;
+  if (!b || p < 0 || p >= b->cap || !b->slots[p].used || !solution) return SELF_ERR_INVALID;
   SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
   const size_t nl = (size_t)b->hp[p].nl;
   std::vector<double> x(nl);
   SELF_CUDA_TRY(b->ctx, cudaMemcpy(x.data(), b->hp[p].x, nl * sizeof(double), cudaMemcpyDeviceToHost));
-  const auto& src = b->hsrc[p];
+  const auto& src = b->slots[p].src;
   for (size_t k = 0; k < nl; ++k) solution[k] = x[src[k]];  // UnMask
-  for (int l : b->hdirnodes[p]) solution[l] = 0.0;          // homogeneous Dirichlet values
+  for (int l : b->slots[p].dirnodes) solution[l] = 0.0;      // homogeneous Dirichlet values
   return SELF_OK;
 }
 
-// Solve every problem: FP32 inner PCG-Jacobi under FP64 refinement (precision = SELF_PREC_FP32) or plain FP64
-// PCG-Jacobi (SELF_PREC_FP64), from a zero initial guess, to ||r||/||r0|| < tolerance.  Inner iterations run in
-// CUDA graphs of graph_k iterations.  reports: nprob entries (or NULL).
+int self_cgbatch_report(self_cgbatch* b, int p, self_solve_report* rep, int* finished) {
+  if (!b || p < 0 || p >= b->cap || !b->slots[p].used || !rep) return SELF_ERR_INVALID;
+  const Scal& s = b->hs[p];
+  const double rel = s.r0 > 0 ? s.rr / s.r0 : 0.0;
+  rep->ioerr = (s.phase == 2 && rel < 1e300 && (s.r0 == 0 || rel == rel)) ? 0 : -2;
+  rep->iterations = s.total;
+  rep->outer_iterations = b->slots[p].outer;
+  rep->r0 = s.r0;
+  rep->rel_residual = rel;
+  if (finished) *finished = s.phase == 2;
+  return SELF_OK;
+}
+
+int self_cgbatch_step(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
+  if (!b || !o || !(o->tolerance > 0) || o->maxIters < 1) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(b->ctx, cudaSetDevice(b->ctx->device));
+  return tick(b, o, nfinished);
+}
+
+long long self_cgbatch_bytes(const self_cgbatch* b) { return b ? b->bytes_in_use : 0; }
+
+// Solve every problem in the batch from a zero initial guess (ticks until all finished).
 int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* o, self_solve_report* reports) {
   if (!b || !o || !(o->tolerance > 0) || o->maxIters < 1) return SELF_ERR_INVALID;
   self_ctx* ctx = b->ctx;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-  const int np = b->nprob;
-  const bool fp32 = o->precision == SELF_PREC_FP32;
-  const double inner_tol = fp32 ? (o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4) : o->tolerance;
-  const int max_outer = fp32 ? (o->max_outer > 0 ? o->max_outer : 30) : 1;
-  const int maxInner = fp32 ? o->maxIters : o->maxIters;
-  int rc;
-  for (auto& P : b->hp) SELF_CUDA_TRY(ctx, cudaMemsetAsync(P.x, 0, P.nl * sizeof(double), ctx->stream));
-  std::vector<Scal> hs(np);
-  for (auto& s : hs) std::memset(&s, 0, sizeof(s));
-  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, hs.data(), np * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
-  std::vector<double> r0, rn;
-  if ((rc = fp64_residual_norms(b, r0))) return rc;
-  rn = r0;
-  std::vector<int> outer(np, 0), total(np, 0), conv(np, 0);
-  for (int p = 0; p < np; ++p) conv[p] = (r0[p] == 0.0);
-  for (int step = 0; step < max_outer; ++step) {
-    bool any = false;
-    for (int p = 0; p < np; ++p) {
-      if (!conv[p] && rn[p] / r0[p] < o->tolerance) conv[p] = 1;
-      if (!conv[p] && total[p] >= o->maxIters) conv[p] = 2;  // iteration budget spent
-      Scal& s = hs[p];
-      std::memset(&s, 0, sizeof(s));
-      s.conv = conv[p] ? 1 : 0;
-      s.done = s.conv;
-      s.r0 = r0[p];
-      s.rin0 = rn[p];
-      s.tol = inner_tol;
-      s.total = total[p];
-      if (!conv[p]) {
-        any = true;
-        outer[p]++;
-      }
-    }
-    if (!any) break;
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, hs.data(), np * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
-    if (fp32) {
-      batch_convert<<<b->n_vt, kThreads, 0, ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, 0);
-      SELF_LAUNCHED(ctx);
-    }
-    cudaGraphExec_t& G = fp32 ? b->inner32 : b->inner64;
-    if (!G) {
-      cudaGraph_t g;
-      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < b->graph_k && !rc; ++k)
-        rc = fp32 ? inner_iteration<float>(b, o->maxIters, maxInner) : inner_iteration<double>(b, o->maxIters, maxInner);
-      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
-      if (rc) return rc;
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&G, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
-    }
-    const long long per_graph = 10LL * b->graph_k;  // kernels per captured chunk
-    for (int chunk = 0; chunk < 1000000; ++chunk) {
-      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
-      ctx->launches.fetch_add(per_graph);
-      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), b->S.p, np * sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
-      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      bool all = true;
-      for (int p = 0; p < np; ++p) all = all && (hs[p].done || hs[p].conv);
-      if (all) break;
-    }
-    for (int p = 0; p < np; ++p) total[p] = hs[p].total;
-    if (fp32) {
-      batch_convert<<<b->n_vt, kThreads, 0, ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, 1);
-      SELF_LAUNCHED(ctx);
-    }
-    if ((rc = fp64_residual_norms(b, rn))) return rc;
-    if (!fp32) {
-      for (int p = 0; p < np; ++p) conv[p] = conv[p] ? conv[p] : 1;
-      break;
-    }
+  int nused = 0;
+  for (int p = 0; p < b->cap; ++p) {
+    if (!b->slots[p].used) continue;
+    ++nused;
+    Scal& s = b->hs[p];
+    std::memset(&s, 0, sizeof(s));
+    s.phase = 1;
+    s.fresh = 1;
+    b->slots[p].outer = 0;
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(b->hp[p].x, 0, b->hp[p].nl * sizeof(double), ctx->stream));
   }
-  int failed = 0;
-  for (int p = 0; p < np; ++p) {
-    const double rel = r0[p] > 0 ? rn[p] / r0[p] : 0.0;
-    const int ioerr = (rel < o->tolerance) ? 0 : -1;
-    failed += ioerr != 0;
-    if (reports) {
-      reports[p].ioerr = ioerr;
-      reports[p].iterations = total[p];
-      reports[p].outer_iterations = outer[p];
-      reports[p].r0 = r0[p];
-      reports[p].rel_residual = rel;
-    }
+  int rc, fin = 0;
+  const long long max_ticks = (long long)o->maxIters / std::max(1, b->graph_k) + 1000;
+  for (long long t = 0; t < max_ticks && fin < nused; ++t)
+    if ((rc = tick(b, o, &fin))) return rc;
+  int k = 0;
+  for (int p = 0; p < b->cap; ++p) {
+    if (!b->slots[p].used) continue;
+    int f;
+    self_solve_report r;
+    self_cgbatch_report(b, p, &r, &f);
+    if (r.rel_residual >= o->tolerance || !f) r.ioerr = -1;
+    if (reports) reports[k] = r;
+    ++k;
   }
   return SELF_OK;
 }
@@ -695,32 +835,36 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
   self_ctx* ctx = b->ctx;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   bool present[10][4] = {};
-  for (auto& P : b->hp) present[P.N][bucket_of(P.nEl)] = true;
-  // cache read: lines "N bucket epb"
+  for (int p = 0; p < b->cap; ++p)
+    if (b->slots[p].used) present[b->hp[p].N][bucket_of(b->hp[p].nEl)] = true;
   if (cache_path) {
     FILE* fp = fopen(cache_path, "r");
     if (fp) {
       char line[256];
       while (fgets(line, sizeof(line), fp)) {
         int N, bk, e;
-        if (sscanf(line, " { \"N\": %d, \"bucket\": %d, \"epb\": %d", &N, &bk, &e) == 3 && N >= 2 && N <= 9 && bk >= 0 &&
-            bk < 4)
+        if (sscanf(line, " { \"N\": %d, \"bucket\": %d, \"epb\": %d", &N, &bk, &e) == 3 && N >= 2 && N <= 9 &&
+            bk >= 0 && bk < 4 && e >= 1)
           b->epb[N][bk] = e;
       }
       fclose(fp);
     }
   }
-  std::vector<Scal> hs(b->nprob);
-  for (auto& s : hs) std::memset(&s, 0, sizeof(s));
-  SELF_CUDA_TRY(ctx, cudaMemcpy(b->S.p, hs.data(), hs.size() * sizeof(Scal), cudaMemcpyHostToDevice));
   int rc;
+  if ((rc = refresh(b))) return rc;
+  std::vector<Scal> hs(b->cap);
+  for (auto& s : hs) {
+    std::memset(&s, 0, sizeof(s));
+    s.phase = 0;  // every problem "running" for the timing launches
+  }
+  SELF_CUDA_TRY(ctx, cudaMemcpy(b->S.p, hs.data(), hs.size() * sizeof(Scal), cudaMemcpyHostToDevice));
   for (int N = 2; N <= 9; ++N)
     for (int bk = 0; bk < 4; ++bk) {
       if (!present[N][bk] || b->epb[N][bk] > 0) continue;
       const int mx = max_epb_rt(N);
       int best = mx;
       double best_ms = 1e30;
-      for (int e = mx; e >= 1; e = (e > 1 ? std::max(1, e / 2) : 0)) {
+      for (int e = mx;; e = std::max(1, e / 2)) {
         if ((rc = build_tiles(b, N, bk, e))) return rc;
         for (int w = 0; w < 2; ++w)
           if ((rc = k_apply<float>(b, V_V, V_Z, 0, 0))) return rc;
@@ -737,7 +881,9 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
       }
       b->epb[N][bk] = best;
     }
-  if ((rc = build_tiles(b, -1, -1, 0))) return rc;
+  b->dirty = true;
+  if ((rc = refresh(b))) return rc;
+  SELF_CUDA_TRY(ctx, cudaMemcpy(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice));
   if (cache_path) {
     FILE* fp = fopen(cache_path, "w");
     if (fp) {
