@@ -50,6 +50,7 @@ extern "C" {
 
 #define SELF_PREC_FP64 0 /* plain FP64 drop-in */
 #define SELF_PREC_FP32 1 /* FP32 arithmetic; shallow water in perturbation form about the lake at rest */
+#define SELF_PREC_FP64_EXACT 2 /* FP64 in the reference's statement order, no FMA contraction, true divisions */
 
 /* ---------------------------------------------------------------- context */
 typedef struct self_ctx self_ctx;

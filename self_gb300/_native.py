@@ -24,6 +24,7 @@ MODEL_SW_CONSERVATIVE = 1
 MODEL_ADVECTION = 2
 PREC_FP64 = 0
 PREC_FP32 = 1
+PREC_FP64_EXACT = 2
 
 dp = C.POINTER(C.c_double)
 fp = C.POINTER(C.c_float)

@@ -42,7 +42,8 @@ def build(verbose=False, force=False, extra_flags=()):
     cu, cpp = sources()
     headers = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".hpp", ".cuh", ".h"))]
     headers.append(os.path.join(HERE, "..", "include", "self_gpu.h"))
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing", "-lineinfo",
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing", "-Xcompiler",
+              "-ffp-contract=off", "-lineinfo",
               "--expt-relaxed-constexpr", "-DNDEBUG"] + list(extra_flags)
     jobs = []
     objs = []

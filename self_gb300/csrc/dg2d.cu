@@ -39,6 +39,7 @@ struct NodalConst {
   double dP[N1 * N1];  // p direction
   double lW[N1], lE[N1], lS[N1], lN[N1];
   double qwinv[N1];  // 1 / quadrature weight
+  double qw[N1];     // quadrature weight (bit-faithful mode divides)
 };
 
 struct VolArgs {
@@ -65,35 +66,63 @@ struct EdgeArgs {
   double g, t;
 };
 
+// ------------------------------------------------------------------------------------ arithmetic
+// EX = true is the bit-faithful FP64 mode: no FMA contraction (__dmul_rn/__dadd_rn), true divisions by J, H
+// and the quadrature weights, and the reference's statement order, so the result equals the Fortran-order
+// CPU restatement bit for bit.  EX = false lets the compiler contract and uses precomputed reciprocals.
+template <bool EX>
+struct Ar {
+  static __device__ __forceinline__ double mul(double a, double b) { return EX ? __dmul_rn(a, b) : a * b; }
+  static __device__ __forceinline__ double add(double a, double b) { return EX ? __dadd_rn(a, b) : a + b; }
+  static __device__ __forceinline__ double sub(double a, double b) { return EX ? __dsub_rn(a, b) : a - b; }
+};
+
 // ------------------------------------------------------------------------------------ physics
 struct SWFlux {
-  template <int NEQ>
+  template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
                                                  double un_adv, double g, double* f) {
     (void)un_adv;
     // RiemannSolver (ConservativeShallowWaterClass.f90:1555-1604), g taken from the parameters
+    using A = Ar<EX>;
     const double uL = in[0], vL = in[1], pL = in[2];
     const double uR = ex[0], vR = ex[1], pR = ex[2];
-    const double uOut = uR * nx + vR * ny;
-    const double uIn = uL * nx + vL * ny;
-    const double ipR = 1.0 / pR, ipL = 1.0 / pL;
-    const double cR = sqrt(g * pR), cL = sqrt(g * pL);
-    const double wR = uOut * ipR, wL = uIn * ipL;
-    const double fac = fmax(fmax(fabs(wR + cR), fabs(wR - cR)), fmax(fabs(wL + cL), fabs(wL - cL)));
-    const double a0 = wR * uR + 0.5 * g * pR * pR * nx + wL * uL + 0.5 * g * pL * pL * nx;
-    const double a1 = wR * vR + 0.5 * g * pR * pR * ny + wL * vL + 0.5 * g * pL * pL * ny;
-    const double a2 = uOut + uIn;
-    f[0] = 0.5 * (a0 - fac * (uR - uL));
-    f[1] = 0.5 * (a1 - fac * (vR - vL));
-    f[2] = 0.5 * (a2 - fac * (pR - pL));
+    const double uOut = A::add(A::mul(uR, nx), A::mul(vR, ny));
+    const double uIn = A::add(A::mul(uL, nx), A::mul(vL, ny));
+    if (EX) {
+      const double oR = uOut / pR, oL = uIn / pL;
+      const double cR = sqrt(A::mul(g, pR)), cL = sqrt(A::mul(g, pL));
+      const double fac =
+          fmax(fmax(fmax(fabs(A::add(oR, cR)), fabs(A::sub(oR, cR))), fabs(A::add(oL, cL))), fabs(A::sub(oL, cL)));
+      const double hgR = A::mul(A::mul(A::mul(0.5, g), pR), pR), hgL = A::mul(A::mul(A::mul(0.5, g), pL), pL);
+      const double a0 = A::add(A::add(A::add(A::mul(oR, uR), A::mul(hgR, nx)), A::mul(oL, uL)), A::mul(hgL, nx));
+      const double a1 = A::add(A::add(A::add(A::mul(oR, vR), A::mul(hgR, ny)), A::mul(oL, vL)), A::mul(hgL, ny));
+      const double a2 = A::add(uOut, uIn);
+      f[0] = A::mul(0.5, A::sub(a0, A::mul(fac, A::sub(uR, uL))));
+      f[1] = A::mul(0.5, A::sub(a1, A::mul(fac, A::sub(vR, vL))));
+      f[2] = A::mul(0.5, A::sub(a2, A::mul(fac, A::sub(pR, pL))));
+    } else {
+      const double ipR = 1.0 / pR, ipL = 1.0 / pL;
+      const double cR = sqrt(g * pR), cL = sqrt(g * pL);
+      const double wR = uOut * ipR, wL = uIn * ipL;
+      const double fac = fmax(fmax(fabs(wR + cR), fabs(wR - cR)), fmax(fabs(wL + cL), fabs(wL - cL)));
+      const double a0 = wR * uR + 0.5 * g * pR * pR * nx + wL * uL + 0.5 * g * pL * pL * nx;
+      const double a1 = wR * vR + 0.5 * g * pR * pR * ny + wL * vL + 0.5 * g * pL * pL * ny;
+      const double a2 = uOut + uIn;
+      f[0] = 0.5 * (a0 - fac * (uR - uL));
+      f[1] = 0.5 * (a1 - fac * (vR - vL));
+      f[2] = 0.5 * (a2 - fac * (pR - pL));
+    }
   }
-  template <int NEQ>
+  template <int NEQ, bool EX>
   static __device__ __forceinline__ void external(int bc, double nx, double ny, double t, const double* in,
                                                   double* ex) {
     (void)t;
+    using A = Ar<EX>;
     if (bc == SELF_NO_NORMAL_FLOW) {  // GetExternalState (:1698-1729)
-      ex[0] = (ny * ny - nx * nx) * in[0] - 2.0 * nx * ny * in[1];
-      ex[1] = (nx * nx - ny * ny) * in[1] - 2.0 * nx * ny * in[0];
+      const double c = A::mul(A::mul(2.0, nx), ny);
+      ex[0] = A::sub(A::mul(A::sub(A::mul(ny, ny), A::mul(nx, nx)), in[0]), A::mul(c, in[1]));
+      ex[1] = A::sub(A::mul(A::sub(A::mul(nx, nx), A::mul(ny, ny)), in[1]), A::mul(c, in[0]));
       ex[2] = in[2];
     } else {
       ex[0] = ex[1] = ex[2] = 0.0;
@@ -102,17 +131,19 @@ struct SWFlux {
 };
 
 struct AdvFlux {
-  template <int NEQ>
+  template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
                                                  double un, double g, double* f) {
     (void)nx;
     (void)ny;
     (void)g;
+    using A = Ar<EX>;
     // RiemannSolver (AdvectionClass.f90:1756-1787) with kappa = 0
 #pragma unroll
-    for (int v = 0; v < NEQ; ++v) f[v] = 0.5 * (un * (ex[v] + in[v]) - fabs(un) * (ex[v] - in[v]));
+    for (int v = 0; v < NEQ; ++v)
+      f[v] = A::mul(0.5, A::sub(A::mul(un, A::add(ex[v], in[v])), A::mul(fabs(un), A::sub(ex[v], in[v]))));
   }
-  template <int NEQ>
+  template <int NEQ, bool EX>
   static __device__ __forceinline__ void external(int bc, double nx, double ny, double t, const double* in,
                                                   double* ex) {
     (void)nx;
@@ -126,7 +157,7 @@ struct AdvFlux {
 };
 
 // ------------------------------------------------------------------------------------ edge kernel
-template <int N1, int NEQ, class Phys>
+template <int N1, int NEQ, class Phys, bool EX>
 __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = gid / N1;
@@ -146,21 +177,21 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
     const double* b2 = A.bs + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
-    Phys::template riemann<NEQ>(in, ex, nx, ny, un, A.g, f);
+    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, A.g, f);
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
     double* o2 = A.bf + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) {
-      const double fl = f[v] * len;
+      const double fl = Ar<EX>::mul(f[v], len);
       o1[i + N1 * v] = fl;
       o2[kk + N1 * v] = -fl;
     }
   } else {
-    Phys::template external<NEQ>(e2f, nx, ny, A.t, in, ex);
-    Phys::template riemann<NEQ>(in, ex, nx, ny, un, A.g, f);
+    Phys::template external<NEQ, EX>(e2f, nx, ny, A.t, in, ex);
+    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, A.g, f);
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
 #pragma unroll
-    for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = f[v] * len;
+    for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = Ar<EX>::mul(f[v], len);
   }
 }
 
@@ -170,10 +201,11 @@ constexpr int elems_per_block() {
   return (N1 * N1 >= 256) ? 1 : (256 / (N1 * N1));
 }
 
-template <int N1, int NEQ>
+template <int N1, int NEQ, bool EX>
 __device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const double* sq /*[EPB][NEQ][N1*N1]*/,
                                              double* bs, int e, int tid) {
   // 4 sides x NEQ x N1 values per element; side 0..3 = S,E,N,W (CalculateSolutionAtBoundaries)
+  using A = Ar<EX>;
   constexpr int NV = 4 * NEQ * N1;
   for (int t = tid; t < NV; t += N1 * N1) {
     const int k = t % N1;
@@ -184,18 +216,19 @@ __device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const doub
     if (side == 0 || side == 2) {
       const double* L = (side == 0) ? C.lS : C.lN;
 #pragma unroll
-      for (int m = 0; m < N1; ++m) acc += L[m] * Q[k + N1 * m];
+      for (int m = 0; m < N1; ++m) acc = A::add(acc, A::mul(L[m], Q[k + N1 * m]));
     } else {
       const double* L = (side == 1) ? C.lE : C.lW;
 #pragma unroll
-      for (int m = 0; m < N1; ++m) acc += L[m] * Q[m + N1 * k];
+      for (int m = 0; m < N1; ++m) acc = A::add(acc, A::mul(L[m], Q[m + N1 * k]));
     }
     bs[(size_t)N1 * NEQ * (side + 4 * (size_t)e) + k + N1 * v] = acc;
   }
 }
 
-template <int N1, int NEQ, bool SW>
+template <int N1, int NEQ, bool SW, bool EX>
 __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
+  using X = Ar<EX>;
   constexpr int NN = N1 * N1;
   constexpr int EPB = elems_per_block<N1>();
   __shared__ NodalConst<N1> C;
@@ -216,7 +249,7 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
   }
   const int i = tid % N1, j = tid / N1;
   double qv[NEQ];
-  double dxds = 0, dxdp = 0, dyds = 0, dydp = 0, invJ = 0;
+  double dxds = 0, dxdp = 0, dyds = 0, dydp = 0, jac = 0;  // jac: 1/J (fast) or J (exact)
   if (active) {
     const double* qe = A.q + (size_t)e * NEQ * NN;
 #pragma unroll
@@ -226,7 +259,7 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
     dxdp = me[NN + tid];
     dyds = me[2 * NN + tid];
     dydp = me[3 * NN + tid];
-    invJ = me[4 * NN + tid];
+    jac = me[4 * NN + tid];
     // boundary fluxes of this element into shared memory
     const double* be = A.bf + (size_t)e * 4 * NEQ * N1;
     double* sb = &sB[le][0][0][0];
@@ -234,27 +267,37 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
     double xF[NEQ], yF[NEQ];
     if (SW) {
       // XFlux / YFlux (:1608-1658)
-      const double iH = 1.0 / qv[2];
-      const double p = A.g * 0.5 * qv[2] * qv[2];
-      xF[0] = qv[0] * qv[0] * iH + p;
-      xF[1] = qv[0] * qv[1] * iH;
-      xF[2] = qv[0];
-      yF[0] = qv[1] * qv[0] * iH;
-      yF[1] = qv[1] * qv[1] * iH + p;
-      yF[2] = qv[1];
+      if (EX) {
+        const double p = X::mul(X::mul(X::mul(A.g, 0.5), qv[2]), qv[2]);
+        xF[0] = X::add(X::mul(qv[0], qv[0]) / qv[2], p);
+        xF[1] = X::mul(qv[0], qv[1]) / qv[2];
+        xF[2] = qv[0];
+        yF[0] = X::mul(qv[1], qv[0]) / qv[2];
+        yF[1] = X::add(X::mul(qv[1], qv[1]) / qv[2], p);
+        yF[2] = qv[1];
+      } else {
+        const double iH = 1.0 / qv[2];
+        const double p = A.g * 0.5 * qv[2] * qv[2];
+        xF[0] = qv[0] * qv[0] * iH + p;
+        xF[1] = qv[0] * qv[1] * iH;
+        xF[2] = qv[0];
+        yF[0] = qv[1] * qv[0] * iH;
+        yF[1] = qv[1] * qv[1] * iH + p;
+        yF[2] = qv[1];
+      }
     } else {
       const double* ae = A.aux + (size_t)e * A.naux * NN;
       const double u = ae[tid], vv = ae[NN + tid];
 #pragma unroll
       for (int v = 0; v < NEQ; ++v) {
-        xF[v] = qv[v] * u;
-        yF[v] = qv[v] * vv;
+        xF[v] = X::mul(qv[v], u);
+        yF[v] = X::mul(qv[v], vv);
       }
     }
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) {
-      sF[le][v][tid] = dydp * xF[v] - dxdp * yF[v];
-      sG[le][v][tid] = -dyds * xF[v] + dxds * yF[v];
+      sF[le][v][tid] = X::sub(X::mul(dydp, xF[v]), X::mul(dxdp, yF[v]));
+      sG[le][v][tid] = X::add(X::mul(-dyds, xF[v]), X::mul(dxds, yF[v]));
     }
   }
   __syncthreads();
@@ -262,43 +305,55 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
   if (active) {
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) {
-      // s direction: MATMUL(dMatS, F(:,j)) + lift, along the row j
-      double ds = 0.0;
+      // s direction: MATMUL(dMatS, F(:,j)) + lift, along the row j; then the p direction and 1/J
+      double ds = 0.0, dp = 0.0;
 #pragma unroll
-      for (int m = 0; m < N1; ++m) ds += C.dS[i + N1 * m] * sF[le][v][m + N1 * j];
-      ds += (sB[le][1][v][j] * C.lE[i] + sB[le][3][v][j] * C.lW[i]) * C.qwinv[i];
-      double dp = 0.0;
+      for (int m = 0; m < N1; ++m) ds = X::add(ds, X::mul(C.dS[i + N1 * m], sF[le][v][m + N1 * j]));
 #pragma unroll
-      for (int m = 0; m < N1; ++m) dp += C.dP[j + N1 * m] * sG[le][v][i + N1 * m];
-      dp += (sB[le][2][v][i] * C.lN[j] + sB[le][0][v][i] * C.lS[j]) * C.qwinv[j];
-      tend[v] = (-ds - dp) * invJ;
+      for (int m = 0; m < N1; ++m) dp = X::add(dp, X::mul(C.dP[j + N1 * m], sG[le][v][i + N1 * m]));
+      if (EX) {
+        ds = X::add(ds, X::add(X::mul(sB[le][1][v][j], C.lE[i]), X::mul(sB[le][3][v][j], C.lW[i])) / C.qw[i]);
+        dp = X::add(dp, X::add(X::mul(sB[le][2][v][i], C.lN[j]), X::mul(sB[le][0][v][i], C.lS[j])) / C.qw[j]);
+        tend[v] = X::sub(-ds, dp) / jac;
+      } else {
+        ds += (sB[le][1][v][j] * C.lE[i] + sB[le][3][v][j] * C.lW[i]) * C.qwinv[i];
+        dp += (sB[le][2][v][i] * C.lN[j] + sB[le][0][v][i] * C.lS[j]) * C.qwinv[j];
+        tend[v] = (-ds - dp) * jac;
+      }
     }
     const double* ae = A.aux + (size_t)e * A.naux * NN;
     if (SW) {
-      // Source (:1662-1694)
+      // Source (:1662-1694): ((f V + g H dh/dx) - drag U/h) - (U - relax) ts, left to right
       const double dhdx = ae[tid], dhdy = ae[NN + tid], f = ae[2 * NN + tid];
-      double s0 = f * qv[1] + A.g * qv[2] * dhdx;
-      double s1 = -f * qv[0] + A.g * qv[2] * dhdy;
+      double s0 = X::add(X::mul(f, qv[1]), X::mul(X::mul(A.g, qv[2]), dhdx));
+      double s1 = X::add(X::mul(-f, qv[0]), X::mul(X::mul(A.g, qv[2]), dhdy));
       double s2 = 0.0;
       int o = 3;
       if (A.has_drag) {
-        const double ih = 1.0 / ae[3 * NN + tid];
-        s0 -= A.drag * qv[0] * ih;
-        s1 -= A.drag * qv[1] * ih;
+        const double hh = ae[3 * NN + tid];
+        if (EX) {
+          s0 = X::sub(s0, X::mul(A.drag, qv[0]) / hh);
+          s1 = X::sub(s1, X::mul(A.drag, qv[1]) / hh);
+        } else {
+          const double ih = 1.0 / hh;
+          s0 -= A.drag * qv[0] * ih;
+          s1 -= A.drag * qv[1] * ih;
+        }
         o = 4;
       }
       if (A.has_relax) {
         const double ts = ae[(o + 3) * NN + tid];
-        s0 -= (qv[0] - ae[o * NN + tid]) * ts;
-        s1 -= (qv[1] - ae[(o + 1) * NN + tid]) * ts;
-        s2 -= (qv[2] - ae[(o + 2) * NN + tid]) * ts;
+        s0 = X::sub(s0, X::mul(X::sub(qv[0], ae[o * NN + tid]), ts));
+        s1 = X::sub(s1, X::mul(X::sub(qv[1], ae[(o + 1) * NN + tid]), ts));
+        s2 = -X::mul(X::sub(qv[2], ae[(o + 2) * NN + tid]), ts);
       }
-      tend[0] += s0;
-      tend[1] += s1;
-      if (NEQ > 2) tend[NEQ > 2 ? 2 : 0] += s2;
+      tend[0] = X::add(tend[0], s0);
+      tend[1] = X::add(tend[1], s1);
+      if (NEQ > 2 && A.has_relax) tend[NEQ > 2 ? 2 : 0] = X::add(tend[NEQ > 2 ? 2 : 0], s2);
     } else if (A.has_relax) {
 #pragma unroll
-      for (int v = 0; v < NEQ; ++v) tend[v] += (ae[(2 + v) * NN + tid] - qv[v]) * ae[(2 + NEQ + v) * NN + tid];
+      for (int v = 0; v < NEQ; ++v)
+        tend[v] = X::add(tend[v], X::mul(X::sub(ae[(2 + v) * NN + tid], qv[v]), ae[(2 + NEQ + v) * NN + tid]));
     }
     if (A.mode == 0) {
       double* te = A.tend + (size_t)e * NEQ * NN;
@@ -309,9 +364,9 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
       double* qo = A.qout + (size_t)e * NEQ * NN;
 #pragma unroll
       for (int v = 0; v < NEQ; ++v) {
-        double g = (A.mode == 2) ? (A.a * Ge[v * NN + tid] + tend[v]) : tend[v];
+        double g = (A.mode == 2) ? X::add(X::mul(A.a, Ge[v * NN + tid]), tend[v]) : tend[v];
         Ge[v * NN + tid] = g;
-        qv[v] = qv[v] + A.gdt * g;
+        qv[v] = X::add(qv[v], X::mul(A.gdt, g));
         qo[v * NN + tid] = qv[v];
       }
     }
@@ -323,12 +378,12 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
       for (int v = 0; v < NEQ; ++v) sF[le][v][tid] = qv[v];
     }
     __syncthreads();
-    if (active) write_traces<N1, NEQ>(C, &sF[le][0][0], A.bs, e, tid);
+    if (active) write_traces<N1, NEQ, EX>(C, &sF[le][0][0], A.bs, e, tid);
   }
 }
 
 // Boundary traces of q alone (start of a run, and the tendency entry point).
-template <int N1, int NEQ>
+template <int N1, int NEQ, bool EX>
 __global__ void __launch_bounds__(256) dg_traces(const double* q, double* bs, int nEl, NodalConst<N1> Cg) {
   constexpr int NN = N1 * N1;
   constexpr int EPB = elems_per_block<N1>();
@@ -348,7 +403,7 @@ __global__ void __launch_bounds__(256) dg_traces(const double* q, double* bs, in
     for (int v = 0; v < NEQ; ++v) sQ[le][v][tid] = q[(size_t)e * NEQ * NN + v * NN + tid];
   }
   __syncthreads();
-  if (e < nEl) write_traces<N1, NEQ>(C, &sQ[le][0][0], bs, e, tid);
+  if (e < nEl) write_traces<N1, NEQ, EX>(C, &sQ[le][0][0], bs, e, tid);
 }
 
 }  // namespace dg
@@ -389,11 +444,12 @@ NodalConst<N1> make_const(const self_dg2d* h) {
     C.lS[k] = h->lS[k];
     C.lN[k] = h->lN[k];
     C.qwinv[k] = 1.0 / h->qw[k];
+    C.qw[k] = h->qw[k];
   }
   return C;
 }
 
-template <int N1, int NEQ, bool SW>
+template <int N1, int NEQ, bool SW, bool EX>
 int launch_edge_t(self_dg2d* h, double t) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
@@ -407,14 +463,14 @@ int launch_edge_t(self_dg2d* h, double t) {
   EA.t = t;
   const int nthr = h->nEdges * N1;
   if (SW)
-    dg_edge_flux<N1, NEQ, SWFlux><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
+    dg_edge_flux<N1, NEQ, SWFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   else
-    dg_edge_flux<N1, NEQ, AdvFlux><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
+    dg_edge_flux<N1, NEQ, AdvFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   SELF_LAUNCHED(ctx);
   return SELF_OK;
 }
 
-template <int N1, int NEQ, bool SW>
+template <int N1, int NEQ, bool SW, bool EX>
 int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend,
                     int write_traces) {
   self_ctx* ctx = h->ctx;
@@ -440,72 +496,93 @@ int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* 
   VA.write_traces = write_traces;
   constexpr int EPB = elems_per_block<N1>();
   dim3 blk(N1 * N1, EPB);
-  dg_volume<N1, NEQ, SW><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(VA, make_const<N1>(h));
+  dg_volume<N1, NEQ, SW, EX><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(VA, make_const<N1>(h));
   SELF_LAUNCHED(ctx);
   return SELF_OK;
 }
 
-template <int N1, int NEQ, bool SW>
+template <int N1, int NEQ, bool SW, bool EX>
 int launch_stage_t(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout,
                    double* tend, int write_traces) {
-  int rc = launch_edge_t<N1, NEQ, SW>(h, t);
+  int rc = launch_edge_t<N1, NEQ, SW, EX>(h, t);
   if (rc) return rc;
-  return launch_volume_t<N1, NEQ, SW>(h, mode, a, gdt, qin, qout, tend, write_traces);
+  return launch_volume_t<N1, NEQ, SW, EX>(h, mode, a, gdt, qin, qout, tend, write_traces);
 }
 
-template <int N1, int NEQ>
+template <int N1, int NEQ, bool EX>
 int launch_traces_t(self_dg2d* h, const double* q) {
   constexpr int EPB = elems_per_block<N1>();
   dim3 blk(N1 * N1, EPB);
-  dg_traces<N1, NEQ><<<(h->nEl + EPB - 1) / EPB, blk, 0, h->ctx->stream>>>(q, h->bs.p, h->nEl, make_const<N1>(h));
+  dg_traces<N1, NEQ, EX><<<(h->nEl + EPB - 1) / EPB, blk, 0, h->ctx->stream>>>(q, h->bs.p, h->nEl, make_const<N1>(h));
   SELF_LAUNCHED(h->ctx);
   return SELF_OK;
 }
 
-// dispatch over (N+1, nEq, model)
+// dispatch over (N+1, nEq, model, exactness)
+template <int N1, bool EX>
+int stage_nx(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout, double* tend,
+             int wt) {
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE)
+    return launch_stage_t<N1, 3, true, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  switch (h->nEq) {
+    case 1: return launch_stage_t<N1, 1, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 2: return launch_stage_t<N1, 2, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 3: return launch_stage_t<N1, 3, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 4: return launch_stage_t<N1, 4, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  }
+  return SELF_ERR_UNSUPPORTED;
+}
 template <int N1>
 int stage_n(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout, double* tend,
             int wt) {
-  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_stage_t<N1, 3, true>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  if (h->precision == SELF_PREC_FP64_EXACT) return stage_nx<N1, true>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  return stage_nx<N1, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
+}
+template <int N1, bool EX>
+int edge_nx(self_dg2d* h, double t) {
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_edge_t<N1, 3, true, EX>(h, t);
   switch (h->nEq) {
-    case 1: return launch_stage_t<N1, 1, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
-    case 2: return launch_stage_t<N1, 2, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
-    case 3: return launch_stage_t<N1, 3, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
-    case 4: return launch_stage_t<N1, 4, false>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 1: return launch_edge_t<N1, 1, false, EX>(h, t);
+    case 2: return launch_edge_t<N1, 2, false, EX>(h, t);
+    case 3: return launch_edge_t<N1, 3, false, EX>(h, t);
+    case 4: return launch_edge_t<N1, 4, false, EX>(h, t);
   }
   return SELF_ERR_UNSUPPORTED;
 }
 template <int N1>
 int edge_n(self_dg2d* h, double t) {
-  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_edge_t<N1, 3, true>(h, t);
+  return h->precision == SELF_PREC_FP64_EXACT ? edge_nx<N1, true>(h, t) : edge_nx<N1, false>(h, t);
+}
+template <int N1, bool EX>
+int volume_nx(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend, int wt) {
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE)
+    return launch_volume_t<N1, 3, true, EX>(h, mode, a, gdt, qin, qout, tend, wt);
   switch (h->nEq) {
-    case 1: return launch_edge_t<N1, 1, false>(h, t);
-    case 2: return launch_edge_t<N1, 2, false>(h, t);
-    case 3: return launch_edge_t<N1, 3, false>(h, t);
-    case 4: return launch_edge_t<N1, 4, false>(h, t);
+    case 1: return launch_volume_t<N1, 1, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 2: return launch_volume_t<N1, 2, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 3: return launch_volume_t<N1, 3, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 4: return launch_volume_t<N1, 4, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
   }
   return SELF_ERR_UNSUPPORTED;
 }
 template <int N1>
 int volume_n(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend, int wt) {
-  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_volume_t<N1, 3, true>(h, mode, a, gdt, qin, qout, tend, wt);
+  if (h->precision == SELF_PREC_FP64_EXACT) return volume_nx<N1, true>(h, mode, a, gdt, qin, qout, tend, wt);
+  return volume_nx<N1, false>(h, mode, a, gdt, qin, qout, tend, wt);
+}
+template <int N1, bool EX>
+int traces_nx(self_dg2d* h, const double* q) {
   switch (h->nEq) {
-    case 1: return launch_volume_t<N1, 1, false>(h, mode, a, gdt, qin, qout, tend, wt);
-    case 2: return launch_volume_t<N1, 2, false>(h, mode, a, gdt, qin, qout, tend, wt);
-    case 3: return launch_volume_t<N1, 3, false>(h, mode, a, gdt, qin, qout, tend, wt);
-    case 4: return launch_volume_t<N1, 4, false>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 1: return launch_traces_t<N1, 1, EX>(h, q);
+    case 2: return launch_traces_t<N1, 2, EX>(h, q);
+    case 3: return launch_traces_t<N1, 3, EX>(h, q);
+    case 4: return launch_traces_t<N1, 4, EX>(h, q);
   }
   return SELF_ERR_UNSUPPORTED;
 }
 template <int N1>
 int traces_n(self_dg2d* h, const double* q) {
-  switch (h->nEq) {
-    case 1: return launch_traces_t<N1, 1>(h, q);
-    case 2: return launch_traces_t<N1, 2>(h, q);
-    case 3: return launch_traces_t<N1, 3>(h, q);
-    case 4: return launch_traces_t<N1, 4>(h, q);
-  }
-  return SELF_ERR_UNSUPPORTED;
+  return h->precision == SELF_PREC_FP64_EXACT ? traces_nx<N1, true>(h, q) : traces_nx<N1, false>(h, q);
 }
 
 #define SELF_DISPATCH_N(FN, ...)                       \
@@ -595,7 +672,7 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   } else {
     return set_error(ctx, SELF_ERR_INVALID, "unknown model %d", d->model);
   }
-  if (d->precision != SELF_PREC_FP64 && d->precision != SELF_PREC_FP32)
+  if (d->precision != SELF_PREC_FP64 && d->precision != SELF_PREC_FP32 && d->precision != SELF_PREC_FP64_EXACT)
     return set_error(ctx, SELF_ERR_INVALID, "unknown precision");
   if (d->precision == SELF_PREC_FP32 && d->model != SELF_MODEL_SW_CONSERVATIVE && d->model != SELF_MODEL_ADVECTION)
     return set_error(ctx, SELF_ERR_UNSUPPORTED, "FP32 form");
@@ -645,7 +722,7 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
       met[(e * 5 + 1) * NN + k] = d->dxdp[id];
       met[(e * 5 + 2) * NN + k] = d->dyds[id];
       met[(e * 5 + 3) * NN + k] = d->dydp[id];
-      met[(e * 5 + 4) * NN + k] = 1.0 / d->J[id];
+      met[(e * 5 + 4) * NN + k] = d->precision == SELF_PREC_FP64_EXACT ? d->J[id] : 1.0 / d->J[id];
     }
   // aux block
   std::vector<const double*> fields;
@@ -705,7 +782,7 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   int rc;
   if ((rc = upload(ctx, h->edges, ed))) return rc;
   if ((rc = upload(ctx, h->egeo, eg))) return rc;
-  if (d->precision == SELF_PREC_FP64) {
+  if (d->precision != SELF_PREC_FP32) {
     if ((rc = upload(ctx, h->metrics, met))) return rc;
     if ((rc = upload(ctx, h->aux, aux))) return rc;
     const size_t nq = NN * d->nEq * nEl, nb = (size_t)n * d->nEq * 4 * nEl;

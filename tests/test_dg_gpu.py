@@ -199,3 +199,33 @@ def test_fp32_advection_1000_steps(gpu_ctx):
         adv.ForwardStepRK3(0.0, steps)
         res.append(adv.GetSolution())
     assert rel_inf(res[1], res[0]) <= 1e-5
+
+
+
+# ---------------------------------------------------------------------------------------------- exact FP64 mode
+@pytest.mark.parametrize("N,nx,warp,drag,relax", [(3, 4, 0.05, 0.0, False), (7, 16, 0.05, 0.0, False),
+                                                  (5, 6, 0.0, 1e-3, True)])
+def test_sw_exact_mode_is_bitwise_oracle(oracle, gpu_ctx, N, nx, warp, drag, relax):
+    """SELF_PREC_FP64_EXACT (no FMA contraction, true divisions, the reference's statement order) reproduces the
+    Fortran-order oracle bit for bit: tendency and a 10-step RK3 trajectory."""
+    import self_gb300 as sg
+    nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, rl, ts = _sw_problem(oracle, N, nx, warp, drag=drag, relax=relax)
+    sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, linear_drag=drag, dhdx=dhdx, dhdy=dhdy, relax=rl,
+                         timescale=ts, precision=sg._native.PREC_FP64_EXACT)
+    sw.SetSolution(q)
+    assert np.array_equal(sw.GlobalTimeDerivative(0.0), P.tendency(q))
+    sw.ForwardStepRK3(0.0, 10)
+    assert np.array_equal(sw.GetSolution(), P.rk3(q, 10))
+
+
+def test_advection_exact_mode_1000_steps_bitwise(oracle, gpu_ctx):
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    N, nx, steps = 7, 16, 1000
+    nod = sg.NodalStorage_2D(N)
+    mesh = sg.QuadMesh(nx, nx, N, periodic=(True, True))
+    c0, u, v, dt = W.advection_periodic(mesh, N, nx)
+    adv = sg.Advection(gpu_ctx, nod, mesh, u, v, dt, precision=sg._native.PREC_FP64_EXACT)
+    adv.SetSolution(c0)
+    adv.ForwardStepRK3(0.0, steps)
+    assert np.array_equal(adv.GetSolution(), oracle.DGProblem(nod, mesh, 2, 1, dt, u=u, v=v).rk3(c0, steps))
