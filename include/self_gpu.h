@@ -229,6 +229,19 @@ long long self_cgbatch_bytes(const self_cgbatch* b);
 int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path);
 int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* epb);
 
+/* ---------------------------------------------------------------- dot product without allocation
+ * No counterpart in the reference.  For callers that cannot allocate device memory where they need an inner
+ * product -- Fortran codes whose device arrays live in their own OpenACC / CUDA Fortran data regions and forbid
+ * allocation inside the time loop, code running while a stream is captured into a CUDA graph, latency-bound
+ * loops -- this computes result = sum_k x[k]*y[k] in FP64 on the current device with the same two-pass tile
+ * reduction as self_cg2d_dot, keeping its partial sums in a fixed static device array (32 KiB, held by every
+ * GPU that loads the library until exit) instead of cudaMalloc'd memory.  x, y (n doubles) and result (one
+ * double) are device pointers; stream may be NULL.  n <= 67,108,864 (4096 partials x 16384 elements), larger n
+ * returns SELF_ERR_INVALID.  The call allocates nothing; its first call on a device looks up the array's
+ * address and should come before any stream capture.  Calls that overlap on the GPU share the array and race;
+ * serialise them.  Errors: self_last_error(NULL, ...). */
+int self_dot_noalloc(const double* x, const double* y, long long n, double* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
