@@ -929,6 +929,7 @@ int self_dg2d_rk3(self_dg2d* h, double tn, int nsteps) {
   int rc = self_dg2d_rk3_async(h, tn, nsteps);
   if (rc) return rc;
   SELF_CUDA_TRY(h->ctx, cudaStreamSynchronize(h->ctx->stream));
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::check_error(h, h->f32);
   return SELF_OK;
 }
 

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "dg2d_fp32.cuh"
+#include "sw32_fused.cuh"
 
 namespace selfgpu {
 namespace dg32 {
@@ -327,6 +328,13 @@ struct State {
   std::vector<double> h;  // bathymetry per node (host, FP64) for the state conversion
   DevBuf<float> q, G, bs, bf, metrics, aux, egeo, R0, hb, tend;
   DevBuf<double> stage64, h64;  // FP64 staging of host transfers, bathymetry for the state conversion
+  // fused TMA-pipelined stage (shallow water, N = 7): per-side edge data, 3 rotating trace buffers, error flag
+  bool fused = false;
+  DevBuf<float> egF, bs1, bs2;
+  DevBuf<selfgpu::sw32::ESide> esides;
+  DevBuf<int> err;
+  int fused_grid = 0;
+  size_t fused_smem = 0;
   const int* edges = nullptr;  // owned by the FP64 handle
   cudaGraphExec_t graph = nullptr;
   bool traces_valid = false;
@@ -452,12 +460,58 @@ int run(self_ctx* ctx, State* s, int op, double t, int mode, float a, float gdt,
   return SELF_ERR_UNSUPPORTED;
 }
 
+int launch_fused(self_ctx* ctx, State* s, int stage, int mode, float a, float gdt) {
+  using namespace selfgpu::sw32;
+  float* T[3] = {s->bs.p, s->bs1.p, s->bs2.p};
+  FusedArgs A;
+  A.q = s->q.p;
+  A.qout = s->q.p;
+  A.G = s->G.p;
+  A.met = s->metrics.p;
+  A.aux = s->aux.p;
+  A.R0 = s->R0.p;
+  A.eg = s->egF.p;
+  A.es = s->esides.p;
+  A.bs_in = T[stage % 3];
+  A.bs_out = T[(stage + 1) % 3];
+  A.err = s->err.p;
+  A.nEl = s->nEl;
+  A.naux = s->naux;
+  A.has_drag = s->has_drag;
+  A.has_relax = s->has_relax;
+  A.mode = mode;
+  A.g = s->g;
+  A.drag = s->drag;
+  A.a = a;
+  A.gdt = gdt;
+  FConst<8> C;
+  for (int k = 0; k < 64; ++k) {
+    C.dS[k] = s->dS[k];
+    C.dP[k] = s->dP[k];
+  }
+  for (int k = 0; k < 8; ++k) {
+    C.lW[k] = s->lW[k];
+    C.lE[k] = s->lE[k];
+    C.lS[k] = s->lS[k];
+    C.lN[k] = s->lN[k];
+    C.qwinv[k] = s->qwinv[k];
+  }
+  sw32_fused<8><<<s->fused_grid, dim3(64, fused_epb<8>()), s->fused_smem, ctx->stream>>>(A, C);
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
 const double kA[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
 const double kB[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
 const double kG[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
 
 int step(self_ctx* ctx, State* s, double t0) {
   int rc;
+  if (s->fused) {  // traces rotate T0 -> T1 -> T2 -> T0 over the three stages
+    for (int m = 0; m < 3; ++m)
+      if ((rc = launch_fused(ctx, s, m, m == 0 ? 1 : 2, (float)kA[m], (float)(kG[m] * s->dt)))) return rc;
+    return SELF_OK;
+  }
   for (int m = 0; m < 3; ++m) {
     if ((rc = run(ctx, s, 0, t0 + kB[m] * s->dt, 0, 0.f, 0.f, nullptr, 0))) return rc;
     if ((rc = run(ctx, s, 1, 0.0, m == 0 ? 1 : 2, (float)kA[m], (float)(kG[m] * s->dt), nullptr, 1))) return rc;
@@ -534,6 +588,60 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
         hb[k + n * (3 + 4 * e)] = sW;
       }
     if ((rc = up(ctx, s->hb, tof(hb)))) return rc;
+    // fused stage data: per element side the neighbour map and the primary side's geometry (N = 7 only)
+    bool walls_only = true;
+    for (int k = 0; k < d->nEdges; ++k)
+      if (d->edges[6 * k + 2] <= 0 && d->edges[6 * k + 2] != SELF_NO_NORMAL_FLOW) walls_only = false;
+    if (n == 8 && walls_only) {
+      using selfgpu::sw32::ESide;
+      std::vector<ESide> es((size_t)4 * nEl);
+      for (auto& x : es) x = ESide{-1, 0, 0, 0};
+      std::vector<double> egv((size_t)nEl * 4 * 5 * n, 0.0);
+      auto put5 = [&](size_t e, int side, int k, size_t pe, int ps, int pk, double hP, double hS) {
+        const size_t ib = (size_t)pk + n * (ps + 4 * pe);
+        double* o = &egv[(e * 4 + side) * 5 * n];
+        o[k] = d->nhx[ib];
+        o[n + k] = d->nhy[ib];
+        o[2 * n + k] = d->nlen[ib];
+        o[3 * n + k] = hP;
+        o[4 * n + k] = hS;
+      };
+      for (int k = 0; k < d->nEdges; ++k) {
+        const int* E = d->edges + 6 * k;
+        const int e1 = E[0] - 1, s1 = E[1] - 1;
+        if (E[2] > 0) {
+          const int e2 = E[2] - 1, s2 = std::abs(E[3]) - 1, st = E[4], inc = E[5];
+          es[(size_t)e1 * 4 + s1] = ESide{e2, s2, st - inc, (inc << 8) | 1};
+          es[(size_t)e2 * 4 + s2] = ESide{e1, s1, (inc - st) * inc, (inc << 8)};
+          for (int i = 0; i < n; ++i) {
+            const int kk = st - inc + i * inc;
+            const double hP = hb[i + n * (s1 + 4 * (size_t)e1)], hS = hb[kk + n * (s2 + 4 * (size_t)e2)];
+            put5(e1, s1, i, e1, s1, i, hP, hS);
+            put5(e2, s2, kk, e1, s1, i, hP, hS);
+          }
+        } else {
+          es[(size_t)e1 * 4 + s1] = ESide{-1, 0, 0, (1 << 8) | 3};
+          for (int i = 0; i < n; ++i) {
+            const double hP = hb[i + n * (s1 + 4 * (size_t)e1)];
+            put5(e1, s1, i, e1, s1, i, hP, hP);
+          }
+        }
+      }
+      if ((rc = up(ctx, s->esides, es)) || (rc = up(ctx, s->egF, tof(egv)))) return rc;
+      const size_t nb = (size_t)n * 3 * 4 * nEl;
+      if (s->bs1.alloc(nb) || s->bs2.alloc(nb) || s->err.alloc(1))
+        return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+      SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
+      s->fused_smem = sizeof(selfgpu::sw32::SwSmem<8>);
+      SELF_CUDA_TRY(ctx, cudaFuncSetAttribute(selfgpu::sw32::sw32_fused<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)s->fused_smem));
+      int per_sm = 0;
+      SELF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, selfgpu::sw32::sw32_fused<8>, 256,
+                                                                      s->fused_smem));
+      const int nchunks = (int)((nEl + 3) / 4);
+      s->fused_grid = std::max(1, std::min(nchunks, std::max(1, per_sm) * ctx->num_sms));
+      s->fused = true;
+    }
     std::vector<double> R0;
     if ((rc = fp64_lake_tendency(d, ctx, R0))) return rc;
     if ((rc = up(ctx, s->R0, tof(R0)))) return rc;
@@ -644,6 +752,20 @@ int rk3(self_dg2d* hd, State* s, double tn, int nsteps) {
   return SELF_OK;
 }
 
+int is_fused(State* s) { return s->fused ? 1 : 0; }
+
+int check_error(self_dg2d* hd, State* s) {
+  if (!s->fused) return SELF_OK;
+  self_ctx* ctx = handle_ctx(hd);
+  int e = 0;
+  SELF_CUDA_TRY(ctx, cudaMemcpy(&e, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
+    return set_error(ctx, SELF_ERR_TIMEOUT, "fused stage: a bulk-copy barrier wait ran out (code %d)", e);
+  }
+  return SELF_OK;
+}
+
 int time_kernels(self_dg2d* hd, State* s, int reps, size_t flush_bytes, double* ms) {
   self_ctx* ctx = handle_ctx(hd);
   DevBuf<float> q0, G0;
@@ -654,6 +776,13 @@ int time_kernels(self_dg2d* hd, State* s, int reps, size_t flush_bytes, double* 
   if ((rc = run(ctx, s, 2, 0, 0, 0, 0, nullptr, 0))) return rc;
   double te = 0, tv = 0, t;
   for (int r = 0; r < reps; ++r) {
+    if (s->fused) {  // one fused launch per stage (edge fluxes inside): ms[0] = 0
+      if ((rc = self_ctx_flush_l2(ctx, flush_bytes)) || (rc = self_ctx_timer_start(ctx))) return rc;
+      if ((rc = launch_fused(ctx, s, 0, 2, (float)kA[1], (float)(kG[1] * s->dt)))) return rc;
+      if ((rc = self_ctx_timer_stop(ctx, &t))) return rc;
+      tv += t;
+      continue;
+    }
     if ((rc = self_ctx_flush_l2(ctx, flush_bytes)) || (rc = self_ctx_timer_start(ctx))) return rc;
     if ((rc = run(ctx, s, 0, 0.0, 0, 0, 0, nullptr, 0))) return rc;
     if ((rc = self_ctx_timer_stop(ctx, &t))) return rc;
