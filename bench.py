@@ -125,7 +125,7 @@ def bytes_per_fused_launch(nEl, n):
     return 4 * (4 * 3 * nn + 5 * nn + 4 * nn + 3 * nn + 4 * 5 * n + 2 * 4 * 3 * n) * nEl
 
 
-def cpu_baseline(oracle, nod, mesh, q, h, fcor, dhdx, dhdy, dt, budget_s=15.0, max_steps=20):
+def cpu_baseline(oracle, nod, mesh, q, h, fcor, dhdx, dhdy, dt, budget_s=12.0, max_steps=5000):
     import multiprocessing
     cores = os.cpu_count() or multiprocessing.cpu_count()
     oracle.set_threads(cores)
