@@ -244,6 +244,145 @@ FLOPS_PER_EL_STAGE_N7 = 14.0e3  # algorithmic FP64 flops of one element-stage at
 #                                 lift, 1/J, sources, RK update, Riemann), the count of the design notes
 
 
+# ------------------------------------------------------------------------------------------ elliptic legs
+def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=3000):
+    """256x256 N=7 variable-coefficient Helmholtz (k = 1 + 0.5 sin 4pi x cos 4pi y, lambda = 0.1, Dirichlet 0,
+    Jacobi): plain FP64 PCG vs FP32-inner PCG under FP64 refinement, both to ||r||/||r0|| < 1e-10; GMRES(30) on the
+    advection-diffusion operator (v = (1, 0.5), kappa = 1e-3)."""
+    from self_gb300 import workloads as W
+    from self_gb300 import _native as nat
+    nod = sg.NodalStorage_2D(N, nat.GAUSS_LOBATTO, nat.CG)
+    mesh = sg.QuadMesh(nx, nx, N, nat.GAUSS_LOBATTO, boundary_flag=nat.DIRICHLET)
+    k, f, source = W.helmholtz(mesh, N, seed=3)
+    cg = sg.CGsemElliptic_2D(ctx, nod, mesh, k, lam=0.1)
+    out = {"workload": f"CGSEM Helmholtz {nx}x{nx} N={N} GLL, {mesh.nEl * (N + 1) ** 2} local nodes"}
+    for prec in ("fp64", "fp32"):
+        cg.Solve(source, method="pcg", precision=prec, tolerance=1e-10, maxIters=200)  # warm-up (graphs, buffers)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        sol, rep = cg.Solve(source, method="pcg", precision=prec, tolerance=1e-10, maxIters=50000)
+        el = time.perf_counter() - t0
+        out["pcg_" + prec] = {"seconds": el, "solves_per_s": 1.0 / el, "iterations": rep["iterations"],
+                              "outer": rep["outer_iterations"], "rel_residual": rep["rel_residual"],
+                              "ioerr": rep["ioerr"]}
+        if prec == "fp64":
+            s64 = sol
+        else:
+            out["pcg_fp32"]["max_rel_diff_vs_fp64"] = float(np.abs(sol - s64).max() / np.abs(s64).max())
+    out["speedup_fp32_ir_vs_fp64"] = out["pcg_fp64"]["seconds"] / out["pcg_fp32"]["seconds"]
+    cg.Trash()
+    ad = sg.CGsemElliptic_2D(ctx, nod, mesh, np.full_like(k, 1e-3), lam=0.0, op=1, vel=(1.0, 0.5))
+    t0 = time.perf_counter()
+    sol, rep = ad.Solve(source, method="gmres", m=30, tolerance=1e-10, maxIters=gmres_iters)
+    el = time.perf_counter() - t0
+    out["gmres30_fp64"] = {"seconds": el, "arnoldi_steps": rep["iterations"], "rel_residual": rep["rel_residual"],
+                           "ioerr": rep["ioerr"], "operator": "-kappa Lap u + v.grad u, kappa 1e-3, v (1, 0.5)"}
+    ad.Trash()
+    return out, (nod, mesh, k, source)
+
+
+def elliptic_cpu(oracle, nod, mesh, k, source, iters_gpu, budget_s=10.0):
+    """Oracle PCG-Jacobi (restated CGsemElliptic_2D%Solve) on the same problem for a bounded number of
+    iterations; solves/s extrapolated with the GPU's iteration count."""
+    P = oracle.CGProblem(nod, mesh, k, lam=0.1)
+    oracle.set_threads(os.cpu_count())
+    n_it = 5
+    while True:
+        t0 = time.perf_counter()
+        P.solve_pcg(source, maxIters=n_it, tol=1e-30, precond=1)
+        el = time.perf_counter() - t0
+        if el > budget_s / 3 or n_it >= 400:
+            break
+        n_it *= 2
+    per_it = el / n_it
+    return {"value": 1.0 / (per_it * iters_gpu), "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{n_it} PCG iterations of the 256x256 N=7 Helmholtz solve ({el:.1f} s), scaled to "
+                      f"{iters_gpu} iterations"}
+
+
+def batched_leg(sg, ctx, nprob=512, fp64_sample=32):
+    """512 uneven Helmholtz problems (n x n, n in [8, 64], N in {3..9}, own k and f): one batched FP32-inner /
+    FP64-refined solve of all of them (autotuned tiles) vs plain FP64 one-solve-per-launch (sampled)."""
+    from self_gb300 import workloads as W
+    specs = W.batched_specs(nprob)
+    t0 = time.perf_counter()
+    probs = [W.batched_problem(sg, nx, N, seed) for nx, N, seed in specs]
+    setup = time.perf_counter() - t0
+    B = sg.CGBatch(ctx, probs)
+    tune = B.autotune(os.path.join(ROOT, "self_gb300", "_build", "cgbatch_tuning.json"))
+    B.Solve(precision="fp32", tolerance=1e-10, maxIters=64)  # warm-up: graphs
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    reps = B.Solve(precision="fp32", tolerance=1e-10)
+    el32 = time.perf_counter() - t0
+    ok = sum(1 for r in reps if r["ioerr"] == 0 and r["rel_residual"] < 1e-10)
+    t0 = time.perf_counter()
+    reps64 = B.Solve(precision="fp64", tolerance=1e-10)
+    el64b = time.perf_counter() - t0
+    B.Trash()
+    idx = np.linspace(0, nprob - 1, min(fp64_sample, nprob)).astype(int)
+    t_single = 0.0
+    for i in idx:
+        pr = probs[i]
+        cg = sg.CGsemElliptic_2D(ctx, pr["nodal"], pr["mesh"], pr["k"], lam=pr["lam"])
+        t0 = time.perf_counter()
+        cg.Solve(pr["source"], method="pcg", precision="fp64", tolerance=1e-10)
+        t_single += time.perf_counter() - t0
+        cg.Trash()
+    single_rate = len(idx) / t_single
+    nodes = sum(pr["mesh"].nEl * (pr["nodal"].N + 1) ** 2 for pr in probs)
+    return {"problems": nprob, "local_nodes": int(nodes), "host_setup_s": setup,
+            "fp32_ir_batched": {"seconds": el32, "solves_per_s": nprob / el32, "converged": ok,
+                                "max_rel_residual": max(r["rel_residual"] for r in reps)},
+            "fp64_batched": {"seconds": el64b, "solves_per_s": nprob / el64b},
+            "fp64_one_solve_per_launch": {"solves_per_s": single_rate, "sampled_problems": int(len(idx))},
+            "speedup_vs_fp64_single": (nprob / el32) / single_rate,
+            "autotuned_elements_per_cta": {f"N{N}_b{b}": e for (N, b), e in tune.items()}}
+
+
+def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, fp64_sample=60):
+    """Poisson stream (mean 2000 req/s, seed 5): 70 % Helmholtz from the batched distribution, 30 % shallow-water
+    ensemble members (64x64, N=5, 100 steps).  Continuous batching (FP32 inner + FP64 refinement, FP32 members)
+    vs the plain FP64 path serving the same stream one request at a time (service times measured on a sample)."""
+    from self_gb300 import serving as S
+    reqs = S.make_requests(sg, nreq, rate=rate, seed=seed)
+    srv = S.Server(ctx)
+    srv.keep_results = False
+    srv.run(reqs)
+    srv.close()
+    st = S.latency_stats(reqs)
+    # plain FP64 path: FIFO single-request service; service time of each request measured on a sample
+    idx = np.linspace(0, nreq - 1, min(fp64_sample, nreq)).astype(int)
+    svc = {}
+    for i in idx:
+        r = reqs[i]
+        pr = r.payload
+        t0 = time.perf_counter()
+        if r.kind == "helmholtz":
+            cg = sg.CGsemElliptic_2D(ctx, pr["nodal"], pr["mesh"], pr["k"], lam=pr["lam"])
+            cg.Solve(pr["source"], method="pcg", precision="fp64", tolerance=1e-10)
+            cg.Trash()
+        else:
+            sw = sg.ShallowWater(ctx, pr["nodal"], pr["mesh"], pr["h"], pr["fcor"], pr["dt"], dhdx=pr["dhdx"],
+                                 dhdy=pr["dhdy"])
+            sw.SetSolution(pr["q"])
+            sw.ForwardStepRK3(0.0, pr["steps"])
+            sw.GetSolution()
+            sw.Trash()
+        svc[i] = time.perf_counter() - t0
+    kinds = {k: np.mean([svc[i] for i in idx if reqs[i].kind == k]) for k in ("helmholtz", "sw")
+             if any(reqs[i].kind == k for i in idx)}
+    t, lat = 0.0, []
+    for r in reqs:  # FIFO queue simulation with sampled service times (sample value where measured)
+        t = max(t, r.arrival) + svc.get(r.rid, kinds[r.kind])
+        lat.append(t - r.arrival)
+    lat = np.array(lat)
+    base = {"p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+            "throughput_req_s": nreq / (t - reqs[0].arrival), "service_sampled": int(len(idx))}
+    return {"requests": nreq, "rate_req_s": rate, "continuous_batching": st, "fp64_sequential": base,
+            "throughput_ratio": st["throughput_req_s"] / base["throughput_req_s"]}
+
+
 def run_gpu(args):
     dist, rank, ws, local = dist_init()
     import ctypes as C
@@ -323,6 +462,20 @@ def run_gpu(args):
         O.build()
         cpu = cpu_baseline(O, nod, mesh, q, h, fcor, dhdx, dhdy, dt)
 
+    for sw in forms.values():
+        sw.Trash()
+    forms = {}
+    elliptic = batched = serving = None
+    if args.elliptic:
+        elliptic, eprob = elliptic_leg(sg, ctx)
+        if rank == 0 and not args.no_cpu:
+            from oracle import oracle as O
+            elliptic["cpu_baseline_pcg_fp64"] = elliptic_cpu(O, *eprob, elliptic["pcg_fp64"]["iterations"])
+    if args.batched_n > 0:
+        batched = batched_leg(sg, ctx, nprob=args.batched_n)
+    if args.serve_n > 0:
+        serving = serving_leg(sg, ctx, nreq=args.serve_n)
+
     if rank == 0:
         f64 = out[nat.PREC_FP64]
         fl = FLOPS_PER_EL_STAGE_N7 * mesh.nEl
@@ -352,10 +505,11 @@ def run_gpu(args):
                           "volume_ms": out[nat.PREC_FP32]["volume_ms"], "edge_ms": out[nat.PREC_FP32]["edge_ms"]},
             "cpu_baseline": cpu,
             "clocks": ck,
+            "elliptic": elliptic,
+            "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
-    for sw in forms.values():
-        sw.Trash()
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -370,6 +524,9 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"], help="form of the headline value")
     ap.add_argument("--accuracy-steps", type=int, default=1000, help="FP32-vs-FP64 height check length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-elliptic", dest="elliptic", action="store_false", help="skip the CGSEM solve leg")
+    ap.add_argument("--batched-n", type=int, default=512, help="problems of the batched leg (0 skips it)")
+    ap.add_argument("--serve-n", type=int, default=300, help="requests of the serving leg (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

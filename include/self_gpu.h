@@ -68,6 +68,8 @@ long long self_ctx_kernel_launches(const self_ctx* ctx);
  * synchronises and returns the elapsed milliseconds between them. */
 int self_ctx_timer_start(self_ctx* ctx);
 int self_ctx_timer_stop(self_ctx* ctx, double* ms);
+/* 1 when all work enqueued on the context's stream has completed, 0 otherwise (cudaStreamQuery). */
+int self_ctx_query(self_ctx* ctx);
 /* Overwrite a scratch buffer of `bytes` on the context's stream (evicts L2 between timed steps). */
 int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
 /* Measured fused-multiply-add rate of the device (TFLOP/s, FP64 when fp64 != 0 else FP32): the compute
@@ -127,6 +129,8 @@ int self_dg2d_tendency(self_dg2d* h, double t, double* dqdt);
 int self_dg2d_rk3(self_dg2d* h, double tn, int nsteps);
 /* Same as self_dg2d_rk3 but enqueued only (no host synchronisation); pair with self_ctx_synchronize. */
 int self_dg2d_rk3_async(self_dg2d* h, double tn, int nsteps);
+/* Device bytes held by the handle (admission control of the serving loop). */
+long long self_dg2d_bytes(const self_dg2d* h);
 /* Device address of the resident state (FP64: double, FP32: float perturbation form). */
 int self_dg2d_state_device(self_dg2d* h, void** dptr, size_t* bytes);
 /* Measurement helper: average CUDA-event time (ms) of one launch of each kernel of an RK stage, each launch

@@ -8,6 +8,7 @@ from .dgsem import Advection, Context, NodalStorage_2D, QuadMesh, ShallowWater, 
 from .cgsem import CGsemElliptic_2D  # noqa: F401
 from .batch import CGBatch  # noqa: F401
 from . import workloads  # noqa: F401
+from . import serving  # noqa: F401
 
 __all__ = ["Context", "NodalStorage_2D", "QuadMesh", "ShallowWater", "Advection", "bathymetry_gradient",
            "CGsemElliptic_2D", "CGBatch", "workloads"]

@@ -829,6 +829,14 @@ int self_dg2d_get_state(self_dg2d* h, double* q) {
   return SELF_OK;
 }
 
+long long self_dg2d_bytes(const self_dg2d* h) {
+  if (!h) return 0;
+  long long b = (long long)(h->q.bytes() + h->G.bytes() + h->bs.bytes() + h->bf.bytes() + h->metrics.bytes() +
+                            h->aux.bytes() + h->egeo.bytes() + h->tend.bytes() + h->edges.bytes());
+  if (h->f32) b += selfgpu::dg32::bytes(h->f32);
+  return b;
+}
+
 int self_dg2d_state_device(self_dg2d* h, void** dptr, size_t* bytes) {
   if (!h || !dptr) return SELF_ERR_INVALID;
   if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::state_device(h, h->f32, dptr, bytes);

@@ -754,6 +754,13 @@ int rk3(self_dg2d* hd, State* s, double tn, int nsteps) {
 
 int is_fused(State* s) { return s->fused ? 1 : 0; }
 
+long long bytes(const State* s) {
+  return (long long)(s->q.bytes() + s->G.bytes() + s->bs.bytes() + s->bf.bytes() + s->metrics.bytes() +
+                     s->aux.bytes() + s->egeo.bytes() + s->R0.bytes() + s->hb.bytes() + s->tend.bytes() +
+                     s->stage64.bytes() + s->h64.bytes() + s->egF.bytes() + s->bs1.bytes() + s->bs2.bytes() +
+                     s->esides.bytes());
+}
+
 int check_error(self_dg2d* hd, State* s) {
   if (!s->fused) return SELF_OK;
   self_ctx* ctx = handle_ctx(hd);

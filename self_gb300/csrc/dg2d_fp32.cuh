@@ -25,6 +25,7 @@ int time_kernels(self_dg2d* h, State* s, int reps, size_t flush_bytes, double* m
 int check_error(self_dg2d* h, State* s);
 // 1 when the fused TMA-pipelined stage is in use
 int is_fused(State* s);
+long long bytes(const State* s);
 void destroy(State* s);
 
 }  // namespace dg32

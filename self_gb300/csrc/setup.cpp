@@ -270,6 +270,14 @@ int self_ctx_timer_stop(self_ctx* ctx, double* ms) {
   return SELF_OK;
 }
 
+int self_ctx_query(self_ctx* ctx) {
+  if (!ctx) return SELF_ERR_INVALID;
+  cudaError_t e = cudaStreamQuery(ctx->stream);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return set_error(ctx, SELF_ERR_CUDA, "stream query: %s", cudaGetErrorString(e));
+}
+
 int self_ctx_flush_l2(self_ctx* ctx, size_t bytes) {
   if (!ctx) return SELF_ERR_INVALID;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
