@@ -236,8 +236,19 @@ def _e2e(nat, L, ctx, sw, dof, steps, dist):
         nat.check(L.self_dg2d_get_state(sw.ptr, hq.ctypes.data_as(nat.dp)), ctx.ptr)
         nat.check(L.self_ctx_timer_stop(ctx.ptr, C.byref(ms)), ctx.ptr)
         t += ms.value
+    # the same three calls timed one by one (not part of the reported value)
+    parts = {"set_state_ms": 0.0, "rk3_ms": 0.0, "get_state_ms": 0.0}
+    calls = (("set_state_ms", lambda: L.self_dg2d_set_state(sw.ptr, hq.ctypes.data_as(nat.dp))),
+             ("rk3_ms", lambda: L.self_dg2d_rk3(sw.ptr, C.c_double(0.0), 1)),
+             ("get_state_ms", lambda: L.self_dg2d_get_state(sw.ptr, hq.ctypes.data_as(nat.dp))))
+    for _ in range(steps):
+        for key, fn in calls:
+            nat.check(L.self_ctx_timer_start(ctx.ptr), ctx.ptr)
+            nat.check(fn(), ctx.ptr)
+            nat.check(L.self_ctx_timer_stop(ctx.ptr, C.byref(ms)), ctx.ptr)
+            parts[key] += ms.value / steps
     L.self_host_free(hp)
-    return t, nbytes
+    return t, nbytes, parts
 
 
 FLOPS_PER_EL_STAGE_N7 = 14.0e3  # algorithmic FP64 flops of one element-stage at N=7 (traces, fluxes, contractions,
@@ -453,7 +464,7 @@ def run_gpu(args):
                 "edge_kernel_ms": out[prec]["edge_ms"]}
 
     e2e_steps = max(3, min(args.steps, 50))
-    t_e2e, nbytes = _e2e(nat, L, ctx, forms[head], dof, e2e_steps, dist)
+    t_e2e, nbytes, e2e_parts = _e2e(nat, L, ctx, forms[head], dof, e2e_steps, dist)
     t_e2e = allmax(dist, t_e2e)
 
     cpu = None
@@ -493,7 +504,8 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "roofline": roof(head),
             "e2e": {"value": ws * dof * e2e_steps / (t_e2e * 1e-3), "unit": "DOF-updates/s",
-                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
+                    "per_call": e2e_parts},
             "accuracy": {"steps": acc_steps, "height_rel_err_fp32_vs_fp64": h_err,
                          "height_err_rel_to_max_eta": eta_err, "tolerance": 1e-6},
             "fp64_plain": {"value": f64["value"], "ms_per_step": f64["ms"], "volume_ms": f64["volume_ms"],

@@ -371,6 +371,7 @@ struct self_cgbatch {
   bool dirty = true;
   int epb[10][4];
   cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
+  int inner32_max = -1, inner64_max = -1;  // iteration limit baked into each captured graph
   int graph_k = 8;
   long long bytes_in_use = 0;
   ~self_cgbatch() {
@@ -570,7 +571,13 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
   for (int p = 0; p < b->cap; ++p) any0 = any0 || (b->slots[p].used && b->hs[p].phase == 0);
   if (any0) {
     cudaGraphExec_t& G = fp32 ? b->inner32 : b->inner64;
+    int& gmax = fp32 ? b->inner32_max : b->inner64_max;
+    if (G && gmax != o->maxIters) {  // the per-problem iteration limit is a kernel argument inside the graph
+      cudaGraphExecDestroy(G);
+      G = nullptr;
+    }
     if (!G) {
+      gmax = o->maxIters;
       cudaGraph_t g;
       SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < b->graph_k && !rc; ++k)

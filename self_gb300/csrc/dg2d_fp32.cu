@@ -13,10 +13,14 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "dg2d_fp32.cuh"
 #include "sw32_fused.cuh"
+
+// warps (independent element workers) per CTA of the fused stage, for 2- and 3-deep per-warp pipelines
+constexpr int kFusedWarps = 4, kFusedWarps3 = 3;
 
 namespace selfgpu {
 namespace dg32 {
@@ -333,7 +337,7 @@ struct State {
   DevBuf<float> egF, bs1, bs2;
   DevBuf<selfgpu::sw32::ESide> esides;
   DevBuf<int> err;
-  int fused_grid = 0;
+  int fused_grid = 0, fused_nbuf = 2;
   size_t fused_smem = 0;
   const int* edges = nullptr;  // owned by the FP64 handle
   cudaGraphExec_t graph = nullptr;
@@ -488,6 +492,7 @@ int launch_fused(self_ctx* ctx, State* s, int stage, int mode, float a, float gd
   for (int k = 0; k < 64; ++k) {
     C.dS[k] = s->dS[k];
     C.dP[k] = s->dP[k];
+    C.dPt[(k % 8) * 8 + k / 8] = s->dP[k];
   }
   for (int k = 0; k < 8; ++k) {
     C.lW[k] = s->lW[k];
@@ -496,7 +501,10 @@ int launch_fused(self_ctx* ctx, State* s, int stage, int mode, float a, float gd
     C.lN[k] = s->lN[k];
     C.qwinv[k] = s->qwinv[k];
   }
-  sw32_fused<8><<<s->fused_grid, dim3(64, fused_epb<8>()), s->fused_smem, ctx->stream>>>(A, C);
+  if (s->fused_nbuf == 3)
+    sw32_fused<8, 3, kFusedWarps3><<<s->fused_grid, 32 * kFusedWarps3, s->fused_smem, ctx->stream>>>(A, C);
+  else
+    sw32_fused<8, 2, kFusedWarps><<<s->fused_grid, 32 * kFusedWarps, s->fused_smem, ctx->stream>>>(A, C);
   SELF_LAUNCHED(ctx);
   return SELF_OK;
 }
@@ -632,14 +640,19 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
       if (s->bs1.alloc(nb) || s->bs2.alloc(nb) || s->err.alloc(1))
         return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
       SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
-      s->fused_smem = sizeof(selfgpu::sw32::SwSmem<8>);
-      SELF_CUDA_TRY(ctx, cudaFuncSetAttribute(selfgpu::sw32::sw32_fused<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)s->fused_smem));
+      // pipeline depth per warp: 2 element buffers (16 warps per SM) unless SELF_FUSED_STAGES=3 (12 warps)
+      const char* depth = getenv("SELF_FUSED_STAGES");
+      s->fused_nbuf = (depth && atoi(depth) == 3) ? 3 : 2;
+      const void* kfn = s->fused_nbuf == 3 ? (const void*)selfgpu::sw32::sw32_fused<8, 3, kFusedWarps3>
+                                           : (const void*)selfgpu::sw32::sw32_fused<8, 2, kFusedWarps>;
+      s->fused_smem = s->fused_nbuf == 3 ? selfgpu::sw32::fused_smem_bytes<8, 3, kFusedWarps3>()
+                                         : selfgpu::sw32::fused_smem_bytes<8, 2, kFusedWarps>();
+      SELF_CUDA_TRY(ctx, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->fused_smem));
       int per_sm = 0;
-      SELF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, selfgpu::sw32::sw32_fused<8>, 256,
-                                                                      s->fused_smem));
-      const int nchunks = (int)((nEl + 3) / 4);
-      s->fused_grid = std::max(1, std::min(nchunks, std::max(1, per_sm) * ctx->num_sms));
+      const int wpb = s->fused_nbuf == 3 ? kFusedWarps3 : kFusedWarps;
+      SELF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 32 * wpb, s->fused_smem));
+      const int nblocks = (int)((nEl + wpb - 1) / wpb);
+      s->fused_grid = std::max(1, std::min(nblocks, std::max(1, per_sm) * ctx->num_sms));
       s->fused = true;
     }
     std::vector<double> R0;

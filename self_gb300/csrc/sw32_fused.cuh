@@ -1,18 +1,21 @@
 // Fused, TMA-pipelined RK stage of the FP32 shallow-water form (perturbation about the lake at rest).
 //
-// One persistent kernel per RK stage replaces the edge-flux + volume pair.  Each CTA owns EPB elements at a
-// time (64 threads per element at N = 7) and walks over element chunks with a two-deep pipeline: warp 0
-// issues 1-D TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx) of the next chunk's element-contiguous
-// blocks -- state q, RK register G, metrics, aux fields, lake-at-rest tendency, per-side edge data and the
-// neighbours' boundary traces -- into shared memory while the CTA computes the current chunk.  Per chunk:
-//   1. traces of the element's own state (from shared memory);
-//   2. LLF flux on each of its 4 sides, evaluated exactly as the edge's primary element sees it (primary trace
-//      "in", secondary trace "ex", primary normal and length), +flux on the primary side and -flux on the
-//      secondary side, so both elements use bitwise-identical values as in EdgeFlux
+// One persistent kernel per RK stage replaces the edge-flux + volume pair.  Each warp is an independent
+// worker that owns one element at a time (N = 7: 64 nodes, two per lane) and walks over the elements
+// e = warp, warp + total warps, ... with its own NBUF-deep pipeline: lanes of the warp issue 1-D TMA bulk
+// copies (cp.async.bulk ... mbarrier::complete_tx) of the element blocks of a later element -- state q, RK
+// register G, metrics, aux fields, lake-at-rest tendency, per-side edge data and the neighbours' boundary
+// traces -- into the warp's shared-memory buffers while the warp computes the current one.  No block-wide
+// barrier is used after set-up; phases inside an element synchronise with __syncwarp.  Per element:
+//   1. traces of the element's own state (shared memory, 3 values per lane);
+//   2. LLF flux at the 32 side nodes (one per lane), evaluated exactly as the edge's primary element sees it
+//      (primary trace "in", secondary trace "ex", primary normal and length), +flux on the primary side and
+//      -flux on the secondary side, so both elements use bitwise-identical values as in EdgeFlux
 //      (ConservativeShallowWaterClass.f90:1266-1360);
-//   3. contravariant fluxes, the two weak-derivative contractions, lift, 1/J, sources, RK update;
+//   3. contravariant fluxes, the two weak-derivative contractions (derivative-matrix rows held in registers,
+//      flux rows read as float4), lift, 1/J, sources, RK update;
 //   4. new traces into the next trace buffer (three buffers rotate over the 3 stages of a step).
-// Every mbarrier wait is bounded; on time-out the CTA records an error code, drains its own copies with a
+// Every mbarrier wait is bounded; on time-out the warp records an error code, drains its own copies with a
 // second bounded wait and returns (the host reports SELF_ERR_TIMEOUT).
 #pragma once
 
@@ -84,43 +87,9 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 template <int N1>
 struct FConst {
   float dS[N1 * N1], dP[N1 * N1];
+  float dPt[N1 * N1];  // dPt[j * N1 + m] = dP[j + N1 * m] (rows read as float4)
   float lW[N1], lE[N1], lS[N1], lN[N1];
   float qwinv[N1];
-};
-
-template <int N1>
-constexpr int fused_epb() {
-  return (N1 * N1 >= 256) ? 1 : (256 / (N1 * N1));
-}
-
-// floats staged per element
-template <int N1>
-struct Stage {
-  static constexpr int NN = N1 * N1;
-  static constexpr int Q = 3 * NN, G = 3 * NN, M = 5 * NN, R = 3 * NN, EG = 4 * 5 * N1, NB = 4 * 3 * N1;
-  static constexpr int AUXMAX = 5 * NN;
-};
-
-template <int N1>
-struct SwSmem {
-  static constexpr int EPB = fused_epb<N1>();
-  static constexpr int NN = N1 * N1;
-  struct Buf {
-    float q[EPB][3 * NN];
-    float G[EPB][3 * NN];
-    float met[EPB][5 * NN];
-    float aux[EPB][5 * NN];
-    float R0[EPB][3 * NN];
-    float eg[EPB][4 * 5 * N1];
-    float nb[EPB][4][3 * N1];  // neighbour traces (primary-or-secondary side), neighbour node order
-  };
-  Buf buf[2];
-  alignas(8) uint64_t bar[2];
-  FConst<N1> C;
-  float sT[EPB][4][3][N1];  // own traces
-  float sB[EPB][4][3][N1];  // boundary fluxes
-  float sF[EPB][3][NN];
-  float sG[EPB][3][NN];
 };
 
 __device__ __forceinline__ void riemann_pert(const float* in, const float* ex, float hL, float hR, float nx, float ny,
@@ -140,181 +109,257 @@ __device__ __forceinline__ void riemann_pert(const float* in, const float* ex, f
 }
 
 template <int N1>
-__global__ void __launch_bounds__(256) sw32_fused(FusedArgs A, FConst<N1> Cg) {
-  constexpr int NN = N1 * N1, EPB = fused_epb<N1>();
-  // 16-byte granularity of the bulk copies: every staged block is a multiple of 16 bytes for N1 = 4 and 8
-  static_assert(N1 == 8, "fused stage: 16-byte bulk-copy granularity and warp-0 lane map are laid out for N1 = 8");
-  static_assert(EPB * 4 <= 32, "one warp-0 lane per (element, side) neighbour copy");
-  using S = Stage<N1>;
+struct WarpStage {  // floats staged per element, one block per field (all multiples of 16 bytes for N1 = 8)
+  static constexpr int NN = N1 * N1;
+  static constexpr int Q = 3 * NN, M = 5 * NN, G = 3 * NN, AUX = 5 * NN, R = 3 * NN, EG = 4 * 5 * N1,
+                       NB = 4 * 3 * N1;
+};
+
+// One element's staging buffer.  q and met are adjacent: once their values are in registers the 8 * NN floats
+// are reused as scratch (contravariant fluxes F in natural order, G transposed with a padded row of 12 floats,
+// then the new state).
+template <int N1>
+struct alignas(16) WarpBuf {
+  using S = WarpStage<N1>;
+  float q[S::Q];
+  float met[S::M];
+  float G[S::G];
+  float aux[S::AUX];
+  float R0[S::R];
+  float eg[S::EG];
+  float nb[S::NB];  // neighbour traces per side (the neighbour's side, neighbour node order)
+};
+
+template <int N1, int NBUF>
+struct alignas(16) WarpSmem {
+  WarpBuf<N1> buf[NBUF];
+  ESide es[NBUF][4];
+  float sT[4 * 3 * N1];  // own traces, t = k + N1 * v + 3 * N1 * side
+  float sB[4 * 3 * N1];  // side fluxes, same order
+  uint64_t bar[NBUF];
+  uint64_t pad[NBUF & 1];
+};
+
+template <int N1, int NBUF, int W>
+struct FusedSmem {
+  WarpSmem<N1, NBUF> w[W];
+  FConst<N1> C;
+};
+
+template <int N1, int NBUF, int W>
+constexpr size_t fused_smem_bytes() {
+  return sizeof(FusedSmem<N1, NBUF, W>);
+}
+
+// trace value t = k + N1 * v + 3 * N1 * side of the 3-variable state Q[v * NN + i + N1 * j]
+template <int N1>
+__device__ __forceinline__ float trace_value(const float* Q, const FConst<N1>& C, int t) {
+  constexpr int NN = N1 * N1;
+  const int k = t % N1, v = (t / N1) % 3, side = t / (3 * N1);
+  const float* L = (side == 0) ? C.lS : (side == 1) ? C.lE : (side == 2) ? C.lN : C.lW;
+  const int base = v * NN + ((side & 1) ? N1 * k : k);
+  const int stride = (side & 1) ? 1 : N1;
+  float acc = 0.f;
+#pragma unroll
+  for (int m = 0; m < N1; ++m) acc += L[m] * Q[base + stride * m];
+  return acc;
+}
+
+// NBUF = 2 with W = 4 fits 16 warps per SM (128 registers, 51 KB of shared memory per CTA); NBUF = 3 with W = 3
+// fits 12 warps (55 KB per CTA)
+template <int N1, int NBUF, int W>
+__global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> Cg) {
+  constexpr int NN = N1 * N1;
+  static_assert(N1 == 8, "fused stage: lane map (2 nodes per lane, 32 side nodes) and 16-byte bulk granularity");
+  using S = WarpStage<N1>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  SwSmem<N1>& sm = *reinterpret_cast<SwSmem<N1>*>(smem_raw);
-  const int tid = threadIdx.x, le = threadIdx.y;
-  const int flat = tid + NN * le, nthr = NN * EPB;
+  FusedSmem<N1, NBUF, W>& sm = *reinterpret_cast<FusedSmem<N1, NBUF, W>*>(smem_raw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpSmem<N1, NBUF>& ws = sm.w[wid];
   {
     constexpr int NC = sizeof(FConst<N1>) / sizeof(float);
     const float* src = reinterpret_cast<const float*>(&Cg);
     float* dst = reinterpret_cast<float*>(&sm.C);
-    for (int t = flat; t < NC; t += nthr) dst[t] = src[t];
+    for (int t = threadIdx.x; t < NC; t += 32 * W) dst[t] = src[t];
   }
-  if (flat == 0) {
-    mbar_init(&sm.bar[0], 1);
-    mbar_init(&sm.bar[1], 1);
+  if (lane == 0) {
+    for (int b = 0; b < NBUF; ++b) mbar_init(&ws.bar[b], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncthreads();
-  const int nchunks = (A.nEl + EPB - 1) / EPB;
-  const long long kMaxSpin = 1LL << 20;  // try_wait polls; normal waits end within microseconds
+  __syncthreads();  // the only block-wide barrier: constants and barrier initialisation
+  const FConst<N1>& C = sm.C;
+  const int i = lane & 7, j = lane >> 3;  // nodes (i, j) and (i, j + 4)
+  float cS[N1];
+#pragma unroll
+  for (int m = 0; m < N1; ++m) cS[m] = C.dS[i + N1 * m];
+  const float lEi = C.lE[i], lWi = C.lW[i], qwi = C.qwinv[i];
+  const float lN0 = C.lN[j], lS0 = C.lS[j], qw0 = C.qwinv[j];
+  const float lN1 = C.lN[j + 4], lS1 = C.lS[j + 4], qw1 = C.qwinv[j + 4];
 
-  // warp 0: issue the bulk copies of chunk c into buffer b (lane 0 the element blocks, lanes 4l+s the
-  // neighbour traces of element l, side s); the byte count is posted before any copy is issued
-  auto issue = [&](int c, int b) {
-    const int lane = flat & 31;
-    const int e0 = c * EPB;
-    const int ne = min(EPB, A.nEl - e0);
-    typename SwSmem<N1>::Buf& B = sm.buf[b];
-    const int l = lane >> 2, sd = lane & 3;
+  const int nwarps = gridDim.x * W;
+  const int gw = blockIdx.x * W + wid;
+  const long long kMaxSpin = 1LL << 20;  // try_wait polls; normal waits end within microseconds
+  const uint32_t base_bytes = 4u * (S::Q + S::M + (uint32_t)A.naux * NN + S::R + S::EG) + (A.mode == 2 ? 4u * S::G : 0u);
+
+  // issue the bulk copies of element e into buffer b: lanes 0-3 the neighbour traces of side = lane, lanes
+  // 4-9 the element blocks; the byte count is posted before any copy is issued
+  auto issue = [&](int e, int b) {
     ESide es;
     es.nbr = -1;
-    if (l < ne && l < EPB) es = A.es[(size_t)(e0 + l) * 4 + sd];
-    const bool hasnb = (l < ne && l < EPB) && es.nbr >= 0;
-    const unsigned nb = __popc(__ballot_sync(0xffffffffu, hasnb));
-    if (lane == 0) {
-      uint32_t bytes = (uint32_t)ne * 4u * (S::Q + S::M + A.naux * NN + S::R + S::EG) + nb * 4u * 3u * N1;
-      if (A.mode == 2) bytes += (uint32_t)ne * 4u * S::G;
-      fence_proxy_async();
-      mbar_expect_tx(&sm.bar[b], bytes);
+    if (lane < 4) {
+      es = A.es[(size_t)e * 4 + lane];
+      ws.es[b][lane] = es;
     }
+    const bool hasnb = lane < 4 && es.nbr >= 0;
+    const unsigned nbm = __ballot_sync(0xffffffffu, hasnb);
+    fence_proxy_async();  // earlier generic accesses of this buffer before the async-proxy writes
     __syncwarp();
-    if (lane == 0) {
-      bulk_g2s(&B.q[0][0], A.q + (size_t)e0 * S::Q, ne * 4u * S::Q, &sm.bar[b]);
-      if (A.mode == 2) bulk_g2s(&B.G[0][0], A.G + (size_t)e0 * S::G, ne * 4u * S::G, &sm.bar[b]);
-      bulk_g2s(&B.met[0][0], A.met + (size_t)e0 * S::M, ne * 4u * S::M, &sm.bar[b]);
-      // aux rows are naux*NN per element; the staging rows are 5*NN wide, so copy element by element
-      for (int k = 0; k < ne; ++k)
-        bulk_g2s(&B.aux[k][0], A.aux + (size_t)(e0 + k) * A.naux * NN, 4u * A.naux * NN, &sm.bar[b]);
-      bulk_g2s(&B.R0[0][0], A.R0 + (size_t)e0 * S::R, ne * 4u * S::R, &sm.bar[b]);
-      bulk_g2s(&B.eg[0][0], A.eg + (size_t)e0 * S::EG, ne * 4u * S::EG, &sm.bar[b]);
-    }
-    if (hasnb) {
-      fence_proxy_async();
-      bulk_g2s(&B.nb[l][sd][0], A.bs_in + (size_t)3 * N1 * (es.nside + 4 * (size_t)es.nbr), 4u * 3u * N1,
-               &sm.bar[b]);
-    }
+    if (lane == 0) mbar_expect_tx(&ws.bar[b], base_bytes + (uint32_t)__popc(nbm) * 4u * 3u * N1);
+    __syncwarp();
+    WarpBuf<N1>& B = ws.buf[b];
+    if (hasnb)
+      bulk_g2s(&B.nb[lane * 3 * N1], A.bs_in + (size_t)3 * N1 * (es.nside + 4 * (size_t)es.nbr), 4u * 3u * N1,
+               &ws.bar[b]);
+    else if (lane == 4)
+      bulk_g2s(B.q, A.q + (size_t)e * S::Q, 4u * S::Q, &ws.bar[b]);
+    else if (lane == 5)
+      bulk_g2s(B.met, A.met + (size_t)e * S::M, 4u * S::M, &ws.bar[b]);
+    else if (lane == 6)
+      bulk_g2s(B.aux, A.aux + (size_t)e * A.naux * NN, 4u * A.naux * NN, &ws.bar[b]);
+    else if (lane == 7)
+      bulk_g2s(B.R0, A.R0 + (size_t)e * S::R, 4u * S::R, &ws.bar[b]);
+    else if (lane == 8)
+      bulk_g2s(B.eg, A.eg + (size_t)e * S::EG, 4u * S::EG, &ws.bar[b]);
+    else if (lane == 9 && A.mode == 2)
+      bulk_g2s(B.G, A.G + (size_t)e * S::G, 4u * S::G, &ws.bar[b]);
   };
 
+  // prologue: elements of iterations 0 .. NBUF-2
+#pragma unroll
+  for (int k = 0; k < NBUF - 1; ++k) {
+    const int e = gw + k * nwarps;
+    if (e < A.nEl) issue(e, k);
+  }
   int it = 0;
-  int c = blockIdx.x;
-  if (c < nchunks && flat < 32) issue(c, 0);
-  for (; c < nchunks; c += gridDim.x, ++it) {
-    const int b = it & 1;
-    const int cn = c + gridDim.x;
-    if (cn < nchunks && flat < 32) issue(cn, b ^ 1);  // buffer b^1 was released at the end of iteration it-1
-    const bool ok = mbar_wait(&sm.bar[b], (uint32_t)((it >> 1) & 1), kMaxSpin);
-    if (__syncthreads_or(!ok)) {
-      if (flat == 0) atomicExch(A.err, 1);
-      // drain: give outstanding copies of both buffers a second bounded wait, then leave
-      mbar_wait(&sm.bar[b], (uint32_t)((it >> 1) & 1), kMaxSpin);
-      if (cn < nchunks) mbar_wait(&sm.bar[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kMaxSpin);
+  for (int e = gw; e < A.nEl; e += nwarps, ++it) {
+    const int b = it % NBUF;
+    {
+      const int ef = e + (NBUF - 1) * nwarps;  // buffer (b + NBUF - 1) % NBUF was released by iteration it - 1
+      if (ef < A.nEl) issue(ef, (b + NBUF - 1) % NBUF);
+    }
+    const bool ok = mbar_wait(&ws.bar[b], (uint32_t)((it / NBUF) & 1), kMaxSpin);
+    if (!__all_sync(0xffffffffu, ok)) {
+      if (lane == 0) atomicExch(A.err, 1);
+      // drain: a second bounded wait on every buffer with copies in flight, then leave
+      for (int k = 0; k < NBUF; ++k) {
+        const int ek = e + k * nwarps;
+        if (ek < A.nEl) mbar_wait(&ws.bar[(it + k) % NBUF], (uint32_t)(((it + k) / NBUF) & 1), kMaxSpin);
+      }
       return;
     }
-    typename SwSmem<N1>::Buf& B = sm.buf[b];
-    const int e = c * EPB + le;
-    const bool active = e < A.nEl;
-    const int i = tid % N1, j = tid / N1;
+    WarpBuf<N1>& B = ws.buf[b];
+    // registers: state and metrics of the two nodes
+    float q0[3], q1[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      q0[v] = B.q[v * NN + lane];
+      q1[v] = B.q[v * NN + lane + 32];
+    }
+    float m0[5], m1[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      m0[c] = B.met[c * NN + lane];
+      m1[c] = B.met[c * NN + lane + 32];
+    }
+    const float h0 = B.aux[3 * NN + lane], h1 = B.aux[3 * NN + lane + 32];
     // 1. own traces
-    if (active) {
-      const FConst<N1>& C = sm.C;
-      for (int t = tid; t < 4 * 3 * N1; t += NN) {
-        const int k = t % N1, v = (t / N1) % 3, side = t / (3 * N1);
-        const float* Qv = &B.q[le][v * NN];
-        float acc = 0.f;
-        if (side == 0 || side == 2) {
-          const float* L = (side == 0) ? C.lS : C.lN;
 #pragma unroll
-          for (int m = 0; m < N1; ++m) acc += L[m] * Qv[k + N1 * m];
+    for (int r = 0; r < 3; ++r) ws.sT[lane + 32 * r] = trace_value<N1>(B.q, C, lane + 32 * r);
+    __syncwarp();  // q and met are free (scratch) and the own traces are visible
+    float* sF = B.q;             // [3][NN], natural order
+    float* sGt = B.q + 3 * NN;   // [3][N1 rows of 12]: sGt[v][m + 12 i] = G_v(i, m)
+    // 2. side fluxes: lane = (side, k)
+    {
+      const int side = lane >> 3, k = lane & 7;
+      const ESide es = ws.es[b][side];
+      const int flags = es.b_flags & 0xff, bb = es.b_flags >> 8;
+      const float* egs = &B.eg[side * 5 * N1];
+      const float nx = egs[k], ny = egs[N1 + k], len = egs[2 * N1 + k], hP = egs[3 * N1 + k], hS = egs[4 * N1 + k];
+      float own[3], oth[3], f[3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) own[v] = ws.sT[k + N1 * v + 3 * N1 * side];
+      float sgn = 1.f;
+      if (es.nbr >= 0) {
+        const int kn = es.a + bb * k;
+#pragma unroll
+        for (int v = 0; v < 3; ++v) oth[v] = B.nb[side * 3 * N1 + v * N1 + kn];
+        if (flags & 1) {
+          riemann_pert(own, oth, hP, hS, nx, ny, A.g, f);
         } else {
-          const float* L = (side == 1) ? C.lE : C.lW;
-#pragma unroll
-          for (int m = 0; m < N1; ++m) acc += L[m] * Qv[m + N1 * k];
+          riemann_pert(oth, own, hP, hS, nx, ny, A.g, f);
+          sgn = -1.f;
         }
-        sm.sT[le][side][v][k] = acc;
+      } else {
+        oth[0] = (ny * ny - nx * nx) * own[0] - 2.0f * nx * ny * own[1];  // mirror (NO_NORMAL_FLOW)
+        oth[1] = (nx * nx - ny * ny) * own[1] - 2.0f * nx * ny * own[0];
+        oth[2] = own[2];
+        riemann_pert(own, oth, hP, hP, nx, ny, A.g, f);
       }
+#pragma unroll
+      for (int v = 0; v < 3; ++v) ws.sB[k + N1 * v + 3 * N1 * side] = sgn * (f[v] * len);
     }
-    __syncthreads();
-    float qv[3], dxds = 0, dxdp = 0, dyds = 0, dydp = 0, invJ = 0, hn = 0;
-    if (active) {
-      // 2. fluxes on the 4 sides (threads 0..4*N1-1 of the element)
-      if (tid < 4 * N1) {
-        const int side = tid / N1, k = tid % N1;
-        const ESide es = A.es[(size_t)e * 4 + side];
-        const int flags = es.b_flags & 0xff, bb = es.b_flags >> 8;
-        const float* egs = &B.eg[le][side * 5 * N1];
-        const float nx = egs[k], ny = egs[N1 + k], len = egs[2 * N1 + k], hP = egs[3 * N1 + k], hS = egs[4 * N1 + k];
-        float own[3], oth[3], f[3];
+    // 3. contravariant fluxes of the two nodes
+    {
+      auto cflux = [&](const float* qv, const float* me, float hn, int node, int ii, int jj) {
+        const float iH = 1.0f / (hn + qv[2]);
+        const float p = A.g * qv[2] * (hn + 0.5f * qv[2]);
+        float xF[3], yF[3];
+        xF[0] = qv[0] * qv[0] * iH + p;
+        xF[1] = qv[0] * qv[1] * iH;
+        xF[2] = qv[0];
+        yF[0] = qv[1] * qv[0] * iH;
+        yF[1] = qv[1] * qv[1] * iH + p;
+        yF[2] = qv[1];
 #pragma unroll
-        for (int v = 0; v < 3; ++v) own[v] = sm.sT[le][side][v][k];
-        float sgn = 1.f;
-        if (es.nbr >= 0) {
-          const int kn = es.a + bb * k;
-#pragma unroll
-          for (int v = 0; v < 3; ++v) oth[v] = B.nb[le][side][v * N1 + kn];
-          if (flags & 1) {
-            riemann_pert(own, oth, hP, hS, nx, ny, A.g, f);
-          } else {
-            riemann_pert(oth, own, hP, hS, nx, ny, A.g, f);
-            sgn = -1.f;
-          }
-        } else {
-          oth[0] = (ny * ny - nx * nx) * own[0] - 2.0f * nx * ny * own[1];  // mirror (NO_NORMAL_FLOW)
-          oth[1] = (nx * nx - ny * ny) * own[1] - 2.0f * nx * ny * own[0];
-          oth[2] = own[2];
-          riemann_pert(own, oth, hP, hP, nx, ny, A.g, f);
+        for (int v = 0; v < 3; ++v) {
+          sF[v * NN + node] = me[3] * xF[v] - me[1] * yF[v];           // dydp xF - dxdp yF
+          sGt[v * 12 * N1 + jj + 12 * ii] = -me[2] * xF[v] + me[0] * yF[v];  // -dyds xF + dxds yF
         }
-#pragma unroll
-        for (int v = 0; v < 3; ++v) sm.sB[le][side][v][k] = sgn * (f[v] * len);
-      }
-      // 3. contravariant fluxes
-#pragma unroll
-      for (int v = 0; v < 3; ++v) qv[v] = B.q[le][v * NN + tid];
-      const float* me = &B.met[le][0];
-      dxds = me[tid];
-      dxdp = me[NN + tid];
-      dyds = me[2 * NN + tid];
-      dydp = me[3 * NN + tid];
-      invJ = me[4 * NN + tid];
-      hn = B.aux[le][3 * NN + tid];
-      const float iH = 1.0f / (hn + qv[2]);
-      const float p = A.g * qv[2] * (hn + 0.5f * qv[2]);
-      float xF[3], yF[3];
-      xF[0] = qv[0] * qv[0] * iH + p;
-      xF[1] = qv[0] * qv[1] * iH;
-      xF[2] = qv[0];
-      yF[0] = qv[1] * qv[0] * iH;
-      yF[1] = qv[1] * qv[1] * iH + p;
-      yF[2] = qv[1];
-#pragma unroll
-      for (int v = 0; v < 3; ++v) {
-        sm.sF[le][v][tid] = dydp * xF[v] - dxdp * yF[v];
-        sm.sG[le][v][tid] = -dyds * xF[v] + dxds * yF[v];
-      }
+      };
+      cflux(q0, m0, h0, lane, i, j);
+      cflux(q1, m1, h1, lane + 32, i, j + 4);
     }
-    __syncthreads();
-    if (active) {
-      const FConst<N1>& C = sm.C;
+    __syncwarp();
+    // 4. contractions, lift, sources, RK update
+    float* Ge = A.G + (size_t)e * 3 * NN;
+    float* qo = A.qout + (size_t)e * 3 * NN;
+    const float* ae = B.aux;
+    float qn0[3], qn1[3];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int jj = j + 4 * half, node = lane + 32 * half;
+      const float4 cpa = reinterpret_cast<const float4*>(&C.dPt[N1 * jj])[0];
+      const float4 cpb = reinterpret_cast<const float4*>(&C.dPt[N1 * jj])[1];
+      const float lN = half ? lN1 : lN0, lS = half ? lS1 : lS0, qwj = half ? qw1 : qw0;
+      const float* qv = half ? q1 : q0;
+      const float invJ = half ? m1[4] : m0[4];
+      const float hn = half ? h1 : h0;
       float tend[3];
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
+        const float4* Fr = reinterpret_cast<const float4*>(&sF[v * NN + N1 * jj]);
+        const float4* Gr = reinterpret_cast<const float4*>(&sGt[v * 12 * N1 + 12 * i]);
+        const float4 f0 = Fr[0], f1 = Fr[1], g0 = Gr[0], g1 = Gr[1];
         float ds = 0.f, dp = 0.f;
-#pragma unroll
-        for (int m = 0; m < N1; ++m) ds += C.dS[i + N1 * m] * sm.sF[le][v][m + N1 * j];
-        ds += (sm.sB[le][1][v][j] * C.lE[i] + sm.sB[le][3][v][j] * C.lW[i]) * C.qwinv[i];
-#pragma unroll
-        for (int m = 0; m < N1; ++m) dp += C.dP[j + N1 * m] * sm.sG[le][v][i + N1 * m];
-        dp += (sm.sB[le][2][v][i] * C.lN[j] + sm.sB[le][0][v][i] * C.lS[j]) * C.qwinv[j];
+        ds += cS[0] * f0.x; ds += cS[1] * f0.y; ds += cS[2] * f0.z; ds += cS[3] * f0.w;
+        ds += cS[4] * f1.x; ds += cS[5] * f1.y; ds += cS[6] * f1.z; ds += cS[7] * f1.w;
+        ds += (ws.sB[jj + N1 * v + 3 * N1 * 1] * lEi + ws.sB[jj + N1 * v + 3 * N1 * 3] * lWi) * qwi;
+        dp += cpa.x * g0.x; dp += cpa.y * g0.y; dp += cpa.z * g0.z; dp += cpa.w * g0.w;
+        dp += cpb.x * g1.x; dp += cpb.y * g1.y; dp += cpb.z * g1.z; dp += cpb.w * g1.w;
+        dp += (ws.sB[i + N1 * v + 3 * N1 * 2] * lN + ws.sB[i + N1 * v + 3 * N1 * 0] * lS) * qwj;
         tend[v] = (-ds - dp) * invJ;
       }
-      const float* ae = &B.aux[le][0];
-      const float dhdx = ae[tid], dhdy = ae[NN + tid], fc = ae[2 * NN + tid];
+      const float dhdx = ae[node], dhdy = ae[NN + node], fc = ae[2 * NN + node];
       float s0 = fc * qv[1] + A.g * qv[2] * dhdx;
       float s1 = -fc * qv[0] + A.g * qv[2] * dhdy;
       float s2 = 0.f;
@@ -323,50 +368,35 @@ __global__ void __launch_bounds__(256) sw32_fused(FusedArgs A, FConst<N1> Cg) {
         s1 -= A.drag * qv[1] / hn;
       }
       if (A.has_relax) {
-        const float ts = ae[4 * NN + tid];
+        const float ts = ae[4 * NN + node];
         s0 -= qv[0] * ts;
         s1 -= qv[1] * ts;
         s2 -= qv[2] * ts;
       }
-      const float* r0 = &B.R0[le][0];
-      tend[0] += s0 + r0[tid];
-      tend[1] += s1 + r0[NN + tid];
-      tend[2] += s2 + r0[2 * NN + tid];
-      float* Ge = A.G + (size_t)e * 3 * NN;
-      float* qo = A.qout + (size_t)e * 3 * NN;
+      tend[0] += s0 + B.R0[node];
+      tend[1] += s1 + B.R0[NN + node];
+      tend[2] += s2 + B.R0[2 * NN + node];
+      float* qn = half ? qn1 : qn0;
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
-        const float gg = (A.mode == 2) ? (A.a * B.G[le][v * NN + tid] + tend[v]) : tend[v];
-        Ge[v * NN + tid] = gg;
-        qv[v] = qv[v] + A.gdt * gg;
-        qo[v * NN + tid] = qv[v];
+        const float gg = (A.mode == 2) ? (A.a * B.G[v * NN + node] + tend[v]) : tend[v];
+        Ge[v * NN + node] = gg;
+        qn[v] = qv[v] + A.gdt * gg;
+        qo[v * NN + node] = qn[v];
       }
     }
-    __syncthreads();  // sF reused for the new state
-    if (active) {
+    __syncwarp();  // scratch reads done: the new state goes into the same floats
 #pragma unroll
-      for (int v = 0; v < 3; ++v) sm.sF[le][v][tid] = qv[v];
+    for (int v = 0; v < 3; ++v) {
+      sF[v * NN + lane] = qn0[v];
+      sF[v * NN + lane + 32] = qn1[v];
     }
-    __syncthreads();
-    if (active) {
-      const FConst<N1>& C = sm.C;
-      for (int t = tid; t < 4 * 3 * N1; t += NN) {
-        const int k = t % N1, v = (t / N1) % 3, side = t / (3 * N1);
-        const float* Qv = &sm.sF[le][v][0];
-        float acc = 0.f;
-        if (side == 0 || side == 2) {
-          const float* L = (side == 0) ? C.lS : C.lN;
+    __syncwarp();
+    // 5. traces of the new state
+    float* bo = A.bs_out + (size_t)3 * N1 * 4 * e;
 #pragma unroll
-          for (int m = 0; m < N1; ++m) acc += L[m] * Qv[k + N1 * m];
-        } else {
-          const float* L = (side == 1) ? C.lE : C.lW;
-#pragma unroll
-          for (int m = 0; m < N1; ++m) acc += L[m] * Qv[m + N1 * k];
-        }
-        A.bs_out[(size_t)3 * N1 * (side + 4 * (size_t)e) + k + N1 * v] = acc;
-      }
-    }
-    __syncthreads();  // buffer b and the scratch arrays are free for the next chunk
+    for (int r = 0; r < 3; ++r) bo[lane + 32 * r] = trace_value<N1>(sF, C, lane + 32 * r);
+    __syncwarp();  // this buffer's floats are read; the next issue into it follows a proxy fence
   }
 }
 
