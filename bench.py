@@ -4,16 +4,24 @@
 Workload (the configuration the DG metric is quoted on): conservative shallow water on [0, 2e6 m]^2,
 128 x 128 curvilinear quads (x,y += 0.05 L sin(2 pi x/L) sin(2 pi y/L)), N = 7 Legendre-Gauss nodes,
 3 variables = 3,145,728 DOF, beta-plane, seamount bathymetry, 16 seeded Gaussian bumps, mirror walls.
-A step is one LSRK3 step (3 stages x {edge-flux kernel, volume+update kernel}).
+A step is one LSRK3 step: 3 stages, each one fused kernel in the FP32 form (edge fluxes + volume + RK update +
+traces) or an edge-flux kernel and a volume + update kernel in the FP64 form.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--precision fp64|fp32]
+                  [--no-cpu] [--no-elliptic] [--batched-n P] [--serve-n R]
 
 value      DOF-updates/s of the device-resident step (inputs in HBM, L2 flushed between timed steps),
            whole job (sum over ranks; ranks are independent replicas).
 e2e        the same metric through the C ABI with host (pinned) buffers: every step uploads the state,
            advances one step and downloads the state, copies inside the timed region.
-roofline   dominant kernel (volume + RK update): algorithmic bytes per launch / CUDA-event launch time.
+roofline   dominant kernel: algorithmic bytes per launch / CUDA-event launch time, against the measured copy
+           bandwidth.
 cpu_baseline  the CPU oracle (C++ restatement of the reference's Fortran, OpenMP) on a bounded sample.
+elliptic   CGSEM Helmholtz 256x256 N=7: FP64 PCG vs FP32-inner PCG under FP64 refinement (solves/s to 1e-10),
+           GMRES(30) on advection-diffusion, the oracle's PCG rate on the same problem.
+batched    512 uneven Helmholtz problems solved together vs one FP64 solve per launch.
+serving    seeded Poisson stream of Helmholtz solves and shallow-water ensemble members: continuous batching
+           latency (p50/p99) and throughput vs plain FP64 one request at a time.
 --impl reference  times the oracle alone on the host cores (the reference itself is Fortran with no compiler
            on this image; the oracle is its restatement).
 """

@@ -7,13 +7,13 @@
 // register G, metrics, aux fields, lake-at-rest tendency, per-side edge data and the neighbours' boundary
 // traces -- into the warp's shared-memory buffers while the warp computes the current one.  No block-wide
 // barrier is used after set-up; phases inside an element synchronise with __syncwarp.  Per element:
-//   1. traces of the element's own state (shared memory, 3 values per lane);
+//   1. traces of the element's own state (shared memory, 3 values per lane, bank-conflict-free order);
 //   2. LLF flux at the 32 side nodes (one per lane), evaluated exactly as the edge's primary element sees it
 //      (primary trace "in", secondary trace "ex", primary normal and length), +flux on the primary side and
 //      -flux on the secondary side, so both elements use bitwise-identical values as in EdgeFlux
 //      (ConservativeShallowWaterClass.f90:1266-1360);
-//   3. contravariant fluxes, the two weak-derivative contractions (derivative-matrix rows held in registers,
-//      flux rows read as float4), lift, 1/J, sources, RK update;
+//   3. contravariant fluxes, the two weak-derivative contractions (each lane owns a node pair; derivative-matrix
+//      rows held in registers, flux rows read as float4), lift, 1/J, sources, RK update;
 //   4. new traces into the next trace buffer (three buffers rotate over the 3 stages of a step).
 // Every mbarrier wait is bounded; on time-out the warp records an error code, drains its own copies with a
 // second bounded wait and returns (the host reports SELF_ERR_TIMEOUT).
@@ -151,26 +151,52 @@ constexpr size_t fused_smem_bytes() {
   return sizeof(FusedSmem<N1, NBUF, W>);
 }
 
-// trace value t = k + N1 * v + 3 * N1 * side of the 3-variable state Q[v * NN + i + N1 * j]
+// Boundary traces of a 3-variable state Q[v * NN + i + N1 * j] (N1 = 8), three per lane.  Round r gives lane
+// (g = lane / 8, k = lane % 8) one (side, v) pair; the S/N partners and the E/W partners of a round read the same
+// words, and each lane starts its 8-term sum at a lane-dependent offset (skew), so that every shared-memory read of
+// the 32 lanes is free of bank conflicts:
+//   round 0: S0 N0 S1 N1 (skew v);  round 1: E0 W0 E1 W1 (skew v + 4 [k >= 4]);
+//   round 2: S2 N2 E2 W2 (skew (-k) mod 4 for S/N, (2 - k) mod 4 + 4 [k >= 4] for E/W).
+// The trace (side, v, k) lands at index k + N1 * v + 3 * N1 * side of `out` (shared or global).
 template <int N1>
-__device__ __forceinline__ float trace_value(const float* Q, const FConst<N1>& C, int t) {
+__device__ __forceinline__ void traces3(const float* Q, const FConst<N1>& C, int lane, float* out) {
   constexpr int NN = N1 * N1;
-  const int k = t % N1, v = (t / N1) % 3, side = t / (3 * N1);
-  const float* L = (side == 0) ? C.lS : (side == 1) ? C.lE : (side == 2) ? C.lN : C.lW;
-  const int base = v * NN + ((side & 1) ? N1 * k : k);
-  const int stride = (side & 1) ? 1 : N1;
-  float acc = 0.f;
+  const int g = lane >> 3, k = lane & 7;
 #pragma unroll
-  for (int m = 0; m < N1; ++m) acc += L[m] * Q[base + stride * m];
-  return acc;
+  for (int r = 0; r < 3; ++r) {
+    int side, v, skew;
+    if (r == 0) {
+      side = (g & 1) ? 2 : 0;
+      v = g >> 1;
+      skew = v;
+    } else if (r == 1) {
+      side = (g & 1) ? 3 : 1;
+      v = g >> 1;
+      skew = v + ((k >> 2) << 2);
+    } else {
+      side = (g < 2) ? 2 * g : 2 * g - 3;  // 0, 2, 1, 3
+      v = 2;
+      skew = (side & 1) ? (((2 - k) & 3) + ((k >> 2) << 2)) : ((-k) & 3);
+    }
+    const float* L = (side == 0) ? C.lS : (side == 1) ? C.lE : (side == 2) ? C.lN : C.lW;
+    const float* Qv = Q + v * NN + ((side & 1) ? N1 * k : k);
+    const int stride = (side & 1) ? 1 : N1;
+    float acc = 0.f;
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      const int mm = (m + skew) & (N1 - 1);
+      acc += L[mm] * Qv[stride * mm];
+    }
+    out[k + N1 * v + 3 * N1 * side] = acc;
+  }
 }
 
-// NBUF = 2 with W = 4 fits 16 warps per SM (128 registers, 51 KB of shared memory per CTA); NBUF = 3 with W = 3
-// fits 12 warps (55 KB per CTA)
+// Lane map (N1 = 8): lane owns the node pair (i, j), (i + 1, j) with i = 2 (lane % 4), j = lane / 4, i.e. the
+// flat nodes 2 lane and 2 lane + 1, so every per-node field moves as a float2.
 template <int N1, int NBUF, int W>
 __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> Cg) {
   constexpr int NN = N1 * N1;
-  static_assert(N1 == 8, "fused stage: lane map (2 nodes per lane, 32 side nodes) and 16-byte bulk granularity");
+  static_assert(N1 == 8, "fused stage: lane map (node pairs, 32 side nodes) and 16-byte bulk granularity");
   using S = WarpStage<N1>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   FusedSmem<N1, NBUF, W>& sm = *reinterpret_cast<FusedSmem<N1, NBUF, W>*>(smem_raw);
@@ -188,13 +214,17 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   }
   __syncthreads();  // the only block-wide barrier: constants and barrier initialisation
   const FConst<N1>& C = sm.C;
-  const int i = lane & 7, j = lane >> 3;  // nodes (i, j) and (i, j + 4)
-  float cS[N1];
+  const int i = 2 * (lane & 3), j = lane >> 2;
+  const int node = 2 * lane;  // = i + N1 * j
+  float cS0[N1], cS1[N1];
 #pragma unroll
-  for (int m = 0; m < N1; ++m) cS[m] = C.dS[i + N1 * m];
-  const float lEi = C.lE[i], lWi = C.lW[i], qwi = C.qwinv[i];
-  const float lN0 = C.lN[j], lS0 = C.lS[j], qw0 = C.qwinv[j];
-  const float lN1 = C.lN[j + 4], lS1 = C.lS[j + 4], qw1 = C.qwinv[j + 4];
+  for (int m = 0; m < N1; ++m) {
+    cS0[m] = C.dS[i + N1 * m];
+    cS1[m] = C.dS[i + 1 + N1 * m];
+  }
+  const float lEa = C.lE[i], lWa = C.lW[i], qwa = C.qwinv[i];
+  const float lEb = C.lE[i + 1], lWb = C.lW[i + 1], qwb = C.qwinv[i + 1];
+  const float lNj = C.lN[j], lSj = C.lS[j], qwj = C.qwinv[j];
 
   const int nwarps = gridDim.x * W;
   const int gw = blockIdx.x * W + wid;
@@ -258,26 +288,18 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       return;
     }
     WarpBuf<N1>& B = ws.buf[b];
-    // registers: state and metrics of the two nodes
-    float q0[3], q1[3];
+    // registers: state, metrics and bathymetry of the node pair
+    float2 q2[3], m2[5];
 #pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      q0[v] = B.q[v * NN + lane];
-      q1[v] = B.q[v * NN + lane + 32];
-    }
-    float m0[5], m1[5];
+    for (int v = 0; v < 3; ++v) q2[v] = *reinterpret_cast<const float2*>(&B.q[v * NN + node]);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      m0[c] = B.met[c * NN + lane];
-      m1[c] = B.met[c * NN + lane + 32];
-    }
-    const float h0 = B.aux[3 * NN + lane], h1 = B.aux[3 * NN + lane + 32];
+    for (int c = 0; c < 5; ++c) m2[c] = *reinterpret_cast<const float2*>(&B.met[c * NN + node]);
+    const float2 h2 = *reinterpret_cast<const float2*>(&B.aux[3 * NN + node]);
     // 1. own traces
-#pragma unroll
-    for (int r = 0; r < 3; ++r) ws.sT[lane + 32 * r] = trace_value<N1>(B.q, C, lane + 32 * r);
+    traces3<N1>(B.q, C, lane, ws.sT);
     __syncwarp();  // q and met are free (scratch) and the own traces are visible
-    float* sF = B.q;             // [3][NN], natural order
-    float* sGt = B.q + 3 * NN;   // [3][N1 rows of 12]: sGt[v][m + 12 i] = G_v(i, m)
+    float* sF = B.q;            // [3][NN], natural order
+    float* sGt = B.q + 3 * NN;  // [3][N1 rows of 12]: sGt[v][m + 12 i] = G_v(i, m)
     // 2. side fluxes: lane = (side, k)
     {
       const int side = lane >> 3, k = lane & 7;
@@ -308,94 +330,119 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
 #pragma unroll
       for (int v = 0; v < 3; ++v) ws.sB[k + N1 * v + 3 * N1 * side] = sgn * (f[v] * len);
     }
-    // 3. contravariant fluxes of the two nodes
+    // 3. contravariant fluxes of the node pair
     {
-      auto cflux = [&](const float* qv, const float* me, float hn, int node, int ii, int jj) {
-        const float iH = 1.0f / (hn + qv[2]);
-        const float p = A.g * qv[2] * (hn + 0.5f * qv[2]);
+      auto cflux = [&](float U, float V, float eta, float hn, float dxds, float dxdp, float dyds, float dydp,
+                       float* Ft, float* Gt) {
+        const float iH = 1.0f / (hn + eta);
+        const float p = A.g * eta * (hn + 0.5f * eta);
         float xF[3], yF[3];
-        xF[0] = qv[0] * qv[0] * iH + p;
-        xF[1] = qv[0] * qv[1] * iH;
-        xF[2] = qv[0];
-        yF[0] = qv[1] * qv[0] * iH;
-        yF[1] = qv[1] * qv[1] * iH + p;
-        yF[2] = qv[1];
+        xF[0] = U * U * iH + p;
+        xF[1] = U * V * iH;
+        xF[2] = U;
+        yF[0] = V * U * iH;
+        yF[1] = V * V * iH + p;
+        yF[2] = V;
 #pragma unroll
         for (int v = 0; v < 3; ++v) {
-          sF[v * NN + node] = me[3] * xF[v] - me[1] * yF[v];           // dydp xF - dxdp yF
-          sGt[v * 12 * N1 + jj + 12 * ii] = -me[2] * xF[v] + me[0] * yF[v];  // -dyds xF + dxds yF
+          Ft[v] = dydp * xF[v] - dxdp * yF[v];
+          Gt[v] = -dyds * xF[v] + dxds * yF[v];
         }
       };
-      cflux(q0, m0, h0, lane, i, j);
-      cflux(q1, m1, h1, lane + 32, i, j + 4);
+      float Fa[3], Ga[3], Fb[3], Gb[3];
+      cflux(q2[0].x, q2[1].x, q2[2].x, h2.x, m2[0].x, m2[1].x, m2[2].x, m2[3].x, Fa, Ga);
+      cflux(q2[0].y, q2[1].y, q2[2].y, h2.y, m2[0].y, m2[1].y, m2[2].y, m2[3].y, Fb, Gb);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        *reinterpret_cast<float2*>(&sF[v * NN + node]) = make_float2(Fa[v], Fb[v]);
+        sGt[v * 12 * N1 + j + 12 * i] = Ga[v];
+        sGt[v * 12 * N1 + j + 12 * (i + 1)] = Gb[v];
+      }
     }
     __syncwarp();
     // 4. contractions, lift, sources, RK update
-    float* Ge = A.G + (size_t)e * 3 * NN;
-    float* qo = A.qout + (size_t)e * 3 * NN;
-    const float* ae = B.aux;
-    float qn0[3], qn1[3];
+    const float4 cPa = reinterpret_cast<const float4*>(&C.dPt[N1 * j])[0];  // dP[j + N1 m], m = 0..7
+    const float4 cPb = reinterpret_cast<const float4*>(&C.dPt[N1 * j])[1];
+    const float cP[N1] = {cPa.x, cPa.y, cPa.z, cPa.w, cPb.x, cPb.y, cPb.z, cPb.w};
+    float2 tend[3];
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int jj = j + 4 * half, node = lane + 32 * half;
-      const float4 cpa = reinterpret_cast<const float4*>(&C.dPt[N1 * jj])[0];
-      const float4 cpb = reinterpret_cast<const float4*>(&C.dPt[N1 * jj])[1];
-      const float lN = half ? lN1 : lN0, lS = half ? lS1 : lS0, qwj = half ? qw1 : qw0;
-      const float* qv = half ? q1 : q0;
-      const float invJ = half ? m1[4] : m0[4];
-      const float hn = half ? h1 : h0;
-      float tend[3];
+    for (int v = 0; v < 3; ++v) {
+      const float4* Fr = reinterpret_cast<const float4*>(&sF[v * NN + N1 * j]);
+      const float4* Ga4 = reinterpret_cast<const float4*>(&sGt[v * 12 * N1 + 12 * i]);
+      const float4* Gb4 = reinterpret_cast<const float4*>(&sGt[v * 12 * N1 + 12 * (i + 1)]);
+      const float4 f0 = Fr[0], f1 = Fr[1];
+      const float4 ga0 = Ga4[0], ga1 = Ga4[1], gb0 = Gb4[0], gb1 = Gb4[1];
+      float dsa = 0.f, dsb = 0.f, dpa = 0.f, dpb = 0.f;
+      dsa += cS0[0] * f0.x; dsa += cS0[1] * f0.y; dsa += cS0[2] * f0.z; dsa += cS0[3] * f0.w;
+      dsa += cS0[4] * f1.x; dsa += cS0[5] * f1.y; dsa += cS0[6] * f1.z; dsa += cS0[7] * f1.w;
+      dsb += cS1[0] * f0.x; dsb += cS1[1] * f0.y; dsb += cS1[2] * f0.z; dsb += cS1[3] * f0.w;
+      dsb += cS1[4] * f1.x; dsb += cS1[5] * f1.y; dsb += cS1[6] * f1.z; dsb += cS1[7] * f1.w;
+      const float bE = ws.sB[j + N1 * v + 3 * N1 * 1], bW = ws.sB[j + N1 * v + 3 * N1 * 3];
+      dsa += (bE * lEa + bW * lWa) * qwa;
+      dsb += (bE * lEb + bW * lWb) * qwb;
+      dpa += cP[0] * ga0.x; dpa += cP[1] * ga0.y; dpa += cP[2] * ga0.z; dpa += cP[3] * ga0.w;
+      dpa += cP[4] * ga1.x; dpa += cP[5] * ga1.y; dpa += cP[6] * ga1.z; dpa += cP[7] * ga1.w;
+      dpb += cP[0] * gb0.x; dpb += cP[1] * gb0.y; dpb += cP[2] * gb0.z; dpb += cP[3] * gb0.w;
+      dpb += cP[4] * gb1.x; dpb += cP[5] * gb1.y; dpb += cP[6] * gb1.z; dpb += cP[7] * gb1.w;
+      const float2 bN = *reinterpret_cast<const float2*>(&ws.sB[i + N1 * v + 3 * N1 * 2]);
+      const float2 bS = *reinterpret_cast<const float2*>(&ws.sB[i + N1 * v + 3 * N1 * 0]);
+      dpa += (bN.x * lNj + bS.x * lSj) * qwj;
+      dpb += (bN.y * lNj + bS.y * lSj) * qwj;
+      tend[v].x = (-dsa - dpa) * m2[4].x;
+      tend[v].y = (-dsb - dpb) * m2[4].y;
+    }
+    {
+      const float2 dhdx = *reinterpret_cast<const float2*>(&B.aux[node]);
+      const float2 dhdy = *reinterpret_cast<const float2*>(&B.aux[NN + node]);
+      const float2 fc = *reinterpret_cast<const float2*>(&B.aux[2 * NN + node]);
+      auto source = [&](float U, float V, float eta, float hn, float dx, float dy, float f, float ts, float* s) {
+        s[0] = f * V + A.g * eta * dx;
+        s[1] = -f * U + A.g * eta * dy;
+        s[2] = 0.f;
+        if (A.has_drag) {
+          s[0] -= A.drag * U / hn;
+          s[1] -= A.drag * V / hn;
+        }
+        if (A.has_relax) {
+          s[0] -= U * ts;
+          s[1] -= V * ts;
+          s[2] -= eta * ts;
+        }
+      };
+      float2 ts2 = make_float2(0.f, 0.f);
+      if (A.has_relax) ts2 = *reinterpret_cast<const float2*>(&B.aux[4 * NN + node]);
+      float sa[3], sb[3];
+      source(q2[0].x, q2[1].x, q2[2].x, h2.x, dhdx.x, dhdy.x, fc.x, ts2.x, sa);
+      source(q2[0].y, q2[1].y, q2[2].y, h2.y, dhdx.y, dhdy.y, fc.y, ts2.y, sb);
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
-        const float4* Fr = reinterpret_cast<const float4*>(&sF[v * NN + N1 * jj]);
-        const float4* Gr = reinterpret_cast<const float4*>(&sGt[v * 12 * N1 + 12 * i]);
-        const float4 f0 = Fr[0], f1 = Fr[1], g0 = Gr[0], g1 = Gr[1];
-        float ds = 0.f, dp = 0.f;
-        ds += cS[0] * f0.x; ds += cS[1] * f0.y; ds += cS[2] * f0.z; ds += cS[3] * f0.w;
-        ds += cS[4] * f1.x; ds += cS[5] * f1.y; ds += cS[6] * f1.z; ds += cS[7] * f1.w;
-        ds += (ws.sB[jj + N1 * v + 3 * N1 * 1] * lEi + ws.sB[jj + N1 * v + 3 * N1 * 3] * lWi) * qwi;
-        dp += cpa.x * g0.x; dp += cpa.y * g0.y; dp += cpa.z * g0.z; dp += cpa.w * g0.w;
-        dp += cpb.x * g1.x; dp += cpb.y * g1.y; dp += cpb.z * g1.z; dp += cpb.w * g1.w;
-        dp += (ws.sB[i + N1 * v + 3 * N1 * 2] * lN + ws.sB[i + N1 * v + 3 * N1 * 0] * lS) * qwj;
-        tend[v] = (-ds - dp) * invJ;
+        const float2 r0 = *reinterpret_cast<const float2*>(&B.R0[v * NN + node]);
+        tend[v].x += sa[v] + r0.x;
+        tend[v].y += sb[v] + r0.y;
       }
-      const float dhdx = ae[node], dhdy = ae[NN + node], fc = ae[2 * NN + node];
-      float s0 = fc * qv[1] + A.g * qv[2] * dhdx;
-      float s1 = -fc * qv[0] + A.g * qv[2] * dhdy;
-      float s2 = 0.f;
-      if (A.has_drag) {
-        s0 -= A.drag * qv[0] / hn;
-        s1 -= A.drag * qv[1] / hn;
-      }
-      if (A.has_relax) {
-        const float ts = ae[4 * NN + node];
-        s0 -= qv[0] * ts;
-        s1 -= qv[1] * ts;
-        s2 -= qv[2] * ts;
-      }
-      tend[0] += s0 + B.R0[node];
-      tend[1] += s1 + B.R0[NN + node];
-      tend[2] += s2 + B.R0[2 * NN + node];
-      float* qn = half ? qn1 : qn0;
+    }
+    float2* Ge = reinterpret_cast<float2*>(A.G + (size_t)e * 3 * NN);
+    float2* qo = reinterpret_cast<float2*>(A.qout + (size_t)e * 3 * NN);
+    float2 qn[3];
 #pragma unroll
-      for (int v = 0; v < 3; ++v) {
-        const float gg = (A.mode == 2) ? (A.a * B.G[v * NN + node] + tend[v]) : tend[v];
-        Ge[v * NN + node] = gg;
-        qn[v] = qv[v] + A.gdt * gg;
-        qo[v * NN + node] = qn[v];
+    for (int v = 0; v < 3; ++v) {
+      float2 gg = tend[v];
+      if (A.mode == 2) {
+        const float2 g0 = *reinterpret_cast<const float2*>(&B.G[v * NN + node]);
+        gg.x = A.a * g0.x + tend[v].x;
+        gg.y = A.a * g0.y + tend[v].y;
       }
+      Ge[(v * NN + node) / 2] = gg;
+      qn[v].x = q2[v].x + A.gdt * gg.x;
+      qn[v].y = q2[v].y + A.gdt * gg.y;
+      qo[(v * NN + node) / 2] = qn[v];
     }
     __syncwarp();  // scratch reads done: the new state goes into the same floats
 #pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      sF[v * NN + lane] = qn0[v];
-      sF[v * NN + lane + 32] = qn1[v];
-    }
+    for (int v = 0; v < 3; ++v) *reinterpret_cast<float2*>(&sF[v * NN + node]) = qn[v];
     __syncwarp();
     // 5. traces of the new state
-    float* bo = A.bs_out + (size_t)3 * N1 * 4 * e;
-#pragma unroll
-    for (int r = 0; r < 3; ++r) bo[lane + 32 * r] = trace_value<N1>(sF, C, lane + 32 * r);
+    traces3<N1>(sF, C, lane, A.bs_out + (size_t)3 * N1 * 4 * e);
     __syncwarp();  // this buffer's floats are read; the next issue into it follows a proxy fence
   }
 }
