@@ -7,14 +7,14 @@
 // register G, metrics, aux fields, lake-at-rest tendency, per-side edge data and the neighbours' boundary
 // traces -- into the warp's shared-memory buffers while the warp computes the current one.  No block-wide
 // barrier is used after set-up; phases inside an element synchronise with __syncwarp.  Per element:
-//   1. traces of the element's own state (shared memory, 3 values per lane, bank-conflict-free order);
+//   1. traces of the element's own state (warp shuffles over the registers of the node pairs);
 //   2. LLF flux at the 32 side nodes (one per lane), evaluated exactly as the edge's primary element sees it
 //      (primary trace "in", secondary trace "ex", primary normal and length), +flux on the primary side and
 //      -flux on the secondary side, so both elements use bitwise-identical values as in EdgeFlux
 //      (ConservativeShallowWaterClass.f90:1266-1360);
 //   3. contravariant fluxes, the two weak-derivative contractions (each lane owns a node pair; derivative-matrix
 //      rows held in registers, flux rows read as float4), lift, 1/J, sources, RK update;
-//   4. new traces into the next trace buffer (three buffers rotate over the 3 stages of a step).
+//   4. new traces (shuffles) into the next trace buffer (three buffers rotate over the 3 stages of a step).
 // Every mbarrier wait is bounded; on time-out the warp records an error code, drains its own copies with a
 // second bounded wait and returns (the host reports SELF_ERR_TIMEOUT).
 #pragma once
@@ -92,16 +92,22 @@ struct FConst {
   float qwinv[N1];
 };
 
+// Square root and quotient on the special-function unit (rsqrt / reciprocal, 2 ulp): depths and gravity-wave
+// speeds are positive, and the same inputs give the same outputs, so the lake-at-rest cancellation
+// (fac = fac0 when eta = 0) stays exact.
+__device__ __forceinline__ float sqrt_sfu(float x) { return x * rsqrtf(x); }
+__device__ __forceinline__ float div_sfu(float a, float b) { return __fdividef(a, b); }
+
 __device__ __forceinline__ void riemann_pert(const float* in, const float* ex, float hL, float hR, float nx, float ny,
                                              float g, float* f) {
   const float UL = in[0], VL = in[1], eL = in[2];
   const float UR = ex[0], VR = ex[1], eR = ex[2];
   const float pL = hL + eL, pR = hR + eR;
   const float uOut = UR * nx + VR * ny, uIn = UL * nx + VL * ny;
-  const float wR = uOut / pR, wL = uIn / pL;
-  const float cR = sqrtf(g * pR), cL = sqrtf(g * pL);
+  const float wR = div_sfu(uOut, pR), wL = div_sfu(uIn, pL);
+  const float cR = sqrt_sfu(g * pR), cL = sqrt_sfu(g * pL);
   const float fac = fmaxf(fmaxf(fabsf(wR + cR), fabsf(wR - cR)), fmaxf(fabsf(wL + cL), fabsf(wL - cL)));
-  const float fac0 = fmaxf(sqrtf(g * hR), sqrtf(g * hL));
+  const float fac0 = fmaxf(sqrt_sfu(g * hR), sqrt_sfu(g * hL));
   const float pr = 0.5f * g * eR * (2.0f * hR + eR), pl = 0.5f * g * eL * (2.0f * hL + eL);
   f[0] = 0.5f * ((wR * UR + pr * nx + wL * UL + pl * nx) - fac * (UR - UL));
   f[1] = 0.5f * ((wR * VR + pr * ny + wL * VL + pl * ny) - fac * (VR - VL));
@@ -151,43 +157,31 @@ constexpr size_t fused_smem_bytes() {
   return sizeof(FusedSmem<N1, NBUF, W>);
 }
 
-// Boundary traces of a 3-variable state Q[v * NN + i + N1 * j] (N1 = 8), three per lane.  Round r gives lane
-// (g = lane / 8, k = lane % 8) one (side, v) pair; the S/N partners and the E/W partners of a round read the same
-// words, and each lane starts its 8-term sum at a lane-dependent offset (skew), so that every shared-memory read of
-// the 32 lanes is free of bank conflicts:
-//   round 0: S0 N0 S1 N1 (skew v);  round 1: E0 W0 E1 W1 (skew v + 4 [k >= 4]);
-//   round 2: S2 N2 E2 W2 (skew (-k) mod 4 for S/N, (2 - k) mod 4 + 4 [k >= 4] for E/W).
-// The trace (side, v, k) lands at index k + N1 * v + 3 * N1 * side of `out` (shared or global).
-template <int N1>
-__device__ __forceinline__ void traces3(const float* Q, const FConst<N1>& C, int lane, float* out) {
-  constexpr int NN = N1 * N1;
-  const int g = lane >> 3, k = lane & 7;
+// Boundary traces of the 3-variable state held in registers (lane = node pair (i, j), (i + 1, j), i = 2 (lane % 4),
+// j = lane / 4; N1 = 8), by warp shuffles.  S/N traces sum over j (lane bits 2-4), E/W traces over i (lane bits
+// 0-1); each butterfly level splits the values still being summed between the two partners (reduce-scatter),
+// so after the last level lane bit 4 selects S or N, bit 3 the node i or i + 1, and lane bit 0 selects E or W.
+// The trace (side, v, k) is written at index k + N1 * v + 3 * N1 * side of `out` (shared or global memory).
+__device__ __forceinline__ void traces_shfl(const float2 (&q)[3], float lSj, float lNj, float lEa, float lEb,
+                                            float lWa, float lWb, int lane, int i, int j, float* out) {
+  constexpr int N1 = 8;
+  const bool b4 = lane & 16, b3 = lane & 8, b0 = lane & 1;
 #pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    int side, v, skew;
-    if (r == 0) {
-      side = (g & 1) ? 2 : 0;
-      v = g >> 1;
-      skew = v;
-    } else if (r == 1) {
-      side = (g & 1) ? 3 : 1;
-      v = g >> 1;
-      skew = v + ((k >> 2) << 2);
-    } else {
-      side = (g < 2) ? 2 * g : 2 * g - 3;  // 0, 2, 1, 3
-      v = 2;
-      skew = (side & 1) ? (((2 - k) & 3) + ((k >> 2) << 2)) : ((-k) & 3);
-    }
-    const float* L = (side == 0) ? C.lS : (side == 1) ? C.lE : (side == 2) ? C.lN : C.lW;
-    const float* Qv = Q + v * NN + ((side & 1) ? N1 * k : k);
-    const int stride = (side & 1) ? 1 : N1;
-    float acc = 0.f;
-#pragma unroll
-    for (int m = 0; m < N1; ++m) {
-      const int mm = (m + skew) & (N1 - 1);
-      acc += L[mm] * Qv[stride * mm];
-    }
-    out[k + N1 * v + 3 * N1 * side] = acc;
+  for (int v = 0; v < 3; ++v) {
+    const float qa = q[v].x, qb = q[v].y;
+    // S / N: sum over j
+    const float sa = lSj * qa, sb = lSj * qb, na = lNj * qa, nb = lNj * qb;
+    const float k0 = b4 ? na : sa, k1 = b4 ? nb : sb;
+    const float x0 = k0 + __shfl_xor_sync(0xffffffffu, b4 ? sa : na, 16);
+    const float x1 = k1 + __shfl_xor_sync(0xffffffffu, b4 ? sb : nb, 16);
+    float y = (b3 ? x1 : x0) + __shfl_xor_sync(0xffffffffu, b3 ? x0 : x1, 8);
+    y += __shfl_xor_sync(0xffffffffu, y, 4);
+    if ((lane & 4) == 0) out[i + (b3 ? 1 : 0) + N1 * v + 3 * N1 * (b4 ? 2 : 0)] = y;
+    // E / W: sum over i
+    const float ev = lEa * qa + lEb * qb, wv = lWa * qa + lWb * qb;
+    float z = (b0 ? wv : ev) + __shfl_xor_sync(0xffffffffu, b0 ? ev : wv, 1);
+    z += __shfl_xor_sync(0xffffffffu, z, 2);
+    if ((lane & 2) == 0) out[j + N1 * v + 3 * N1 * (b0 ? 3 : 1)] = z;
   }
 }
 
@@ -296,7 +290,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
     for (int c = 0; c < 5; ++c) m2[c] = *reinterpret_cast<const float2*>(&B.met[c * NN + node]);
     const float2 h2 = *reinterpret_cast<const float2*>(&B.aux[3 * NN + node]);
     // 1. own traces
-    traces3<N1>(B.q, C, lane, ws.sT);
+    traces_shfl(q2, lSj, lNj, lEa, lEb, lWa, lWb, lane, i, j, ws.sT);
     __syncwarp();  // q and met are free (scratch) and the own traces are visible
     float* sF = B.q;            // [3][NN], natural order
     float* sGt = B.q + 3 * NN;  // [3][N1 rows of 12]: sGt[v][m + 12 i] = G_v(i, m)
@@ -334,7 +328,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
     {
       auto cflux = [&](float U, float V, float eta, float hn, float dxds, float dxdp, float dyds, float dydp,
                        float* Ft, float* Gt) {
-        const float iH = 1.0f / (hn + eta);
+        const float iH = div_sfu(1.0f, hn + eta);
         const float p = A.g * eta * (hn + 0.5f * eta);
         float xF[3], yF[3];
         xF[0] = U * U * iH + p;
@@ -437,12 +431,8 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       qn[v].y = q2[v].y + A.gdt * gg.y;
       qo[(v * NN + node) / 2] = qn[v];
     }
-    __syncwarp();  // scratch reads done: the new state goes into the same floats
-#pragma unroll
-    for (int v = 0; v < 3; ++v) *reinterpret_cast<float2*>(&sF[v * NN + node]) = qn[v];
-    __syncwarp();
     // 5. traces of the new state
-    traces3<N1>(sF, C, lane, A.bs_out + (size_t)3 * N1 * 4 * e);
+    traces_shfl(qn, lSj, lNj, lEa, lEb, lWa, lWb, lane, i, j, A.bs_out + (size_t)3 * N1 * 4 * e);
     __syncwarp();  // this buffer's floats are read; the next issue into it follows a proxy fence
   }
 }
