@@ -372,6 +372,7 @@ struct self_cgbatch {
   int epb[10][4];
   cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
   int inner32_max = -1, inner64_max = -1;  // iteration limit baked into each captured graph
+  long long inner32_launches = 0, inner64_launches = 0;  // kernels per captured graph
   int graph_k = 8;
   long long bytes_in_use = 0;
   ~self_cgbatch() {
@@ -579,6 +580,7 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
     if (!G) {
       gmax = o->maxIters;
       cudaGraph_t g;
+      const long long l0 = ctx->launches.load();
       SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < b->graph_k && !rc; ++k)
         rc = fp32 ? inner_iteration<float>(b, o->maxIters, o->maxIters) : inner_iteration<double>(b, o->maxIters, o->maxIters);
@@ -588,10 +590,11 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
       ce = cudaGraphInstantiate(&G, g, 0);
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
-      ctx->launches.fetch_sub(13LL * b->graph_k);
+      (fp32 ? b->inner32_launches : b->inner64_launches) = ctx->launches.load() - l0;
+      ctx->launches.fetch_sub(fp32 ? b->inner32_launches : b->inner64_launches);
     }
     SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
-    ctx->launches.fetch_add(13LL * b->graph_k);
+    ctx->launches.fetch_add(fp32 ? b->inner32_launches : b->inner64_launches);
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->hs.data(), b->S.p, b->cap * sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -177,77 +177,180 @@ struct GMScalars {
 struct CGScalars {
   double num, den, vz, rr, r0, tol;
   int iter, done, ioerr, maxIters;
+  double* resi;  // residual history (resi[iter] = ||r||), or null
 };
 
-// w = r * dinv (dinv = 1 when no preconditioner) ; partial <r,w>  (also <r,r> in slot 1)
-template <typename R>
-__global__ void __launch_bounds__(kRedThreads) pcg_precond(const R* __restrict__ r, const R* __restrict__ dinv,
-                                                           R* __restrict__ w, size_t n, double* __restrict__ partial,
-                                                           const CGScalars* __restrict__ S) {
-  if (S->done) return;
-  double s0 = 0;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-    R wk = dinv ? r[k] * dinv[k] : r[k];
-    w[k] = wk;
-    s0 += (double)r[k] * (double)wk;
+// ---------------------------------------------------------------------------------- fused (P)CG iteration
+// One iteration is three launches, captured in a CUDA graph of several iterations:
+//   pcg_apply_fused : v_new = w + beta v_old (beta = num/den, v_new = w on the first iteration), z = L(v_new)
+//                     per element (before the direct-stiffness sum), partial sums of <v_new, z>;
+//   cg_dss_mask     : z = Mask(GlobalSum(z));
+//   pcg_update_fused: a = num/<v,z>, u += a v, r -= a z, w = dinv r, partial sums of <r,w> and <r,r>, and the
+//                     end-of-iteration scalar update (den = num, num = <r,w>, ||r||, stop tests).
+// <v, Mask(GlobalSum(Lv))> equals the element-local sum of v(src[l]) * (Lv)_l because v is zero on Dirichlet
+// nodes and on non-primary copies.  The grid-wide sums are deterministic: every block writes its partial, and the
+// last block to finish (atomic ticket) adds the partials in block order and updates the scalars.
+
+// Sum of one value per thread over a block of any size up to 256 threads (fixed tree order); result in thread 0.
+__device__ __forceinline__ double block_sum_any(double v) {
+  __shared__ double sh[256];
+  const int nthr = blockDim.x * blockDim.y;
+  const int t = threadIdx.x + blockDim.x * threadIdx.y;
+  sh[t] = v;
+  for (int k = nthr + t; k < 256; k += nthr) sh[k] = 0.0;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (t < st) sh[t] += sh[t + st];
+    __syncthreads();
   }
-  s0 = block_sum(s0);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
+  const double r = sh[0];
+  __syncthreads();
+  return r;
 }
 
-// v = w + beta v (beta = num/den, first iteration v = w), from the reduced <r,w>
-template <typename R>
-__global__ void __launch_bounds__(kRedThreads) pcg_update_v(const R* __restrict__ w, R* __restrict__ v, size_t n,
-                                                            const double* __restrict__ red, CGScalars* S) {
-  if (S->done) return;
-  const double num = red[0];
-  const bool first = (S->iter == 0);
-  const R beta = first ? R(0) : (R)(num / S->den);
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-    v[k] = first ? w[k] : w[k] + beta * v[k];
-  if (blockIdx.x == 0 && threadIdx.x == 0) S->num = num;
+// Grid-wide sums of NS values per thread: returns true in the last block, with the sums in tot (all threads).
+template <int NS>
+__device__ __forceinline__ bool grid_sums_last(const double (&v)[NS], double* __restrict__ partial,
+                                               unsigned int* __restrict__ ticket, double (&tot)[NS]) {
+  __shared__ bool s_last;
+  const int t = threadIdx.x + blockDim.x * threadIdx.y;
+  const int nthr = blockDim.x * blockDim.y;
+  const int nb = gridDim.x;
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    const double b = block_sum_any(v[s]);
+    if (t == 0) partial[(size_t)s * nb + blockIdx.x] = b;
+  }
+  if (t == 0) {
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == (unsigned)(nb - 1);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    double a = 0.0;
+    for (int k = t; k < nb; k += nthr) a += __ldcg(&partial[(size_t)s * nb + k]);
+    tot[s] = block_sum_any(a);
+  }
+  if (t == 0) *ticket = 0u;
+  return true;
 }
 
-// u += a v ; r -= a z  with a = num / <v,z>; partial <r,r>
-template <typename R>
-__global__ void __launch_bounds__(kRedThreads) pcg_update_ur(R* __restrict__ u, R* __restrict__ r,
-                                                             const R* __restrict__ v, const R* __restrict__ z,
-                                                             size_t n, const double* __restrict__ red_vz,
-                                                             const CGScalars* __restrict__ S,
-                                                             double* __restrict__ partial) {
+template <int N1, typename R, int NF>
+__global__ void __launch_bounds__(256) pcg_apply_fused(const R* __restrict__ w, const R* __restrict__ vold,
+                                                       R* __restrict__ vnew, const int* __restrict__ src,
+                                                       const R* __restrict__ fac, R* __restrict__ z, int nEl,
+                                                       CGConst<N1, R> Cg, CGScalars* S, double* __restrict__ partial,
+                                                       unsigned int* __restrict__ ticket) {
   if (S->done) return;
-  const R a = (R)(S->num / red_vz[0]);
-  double s0 = 0;
+  constexpr int NN = N1 * N1;
+  constexpr int EPB = cg_epb<N1>();
+  __shared__ R D[N1 * N1];
+  __shared__ R su[EPB][NN];
+  __shared__ R s1[EPB][NN];
+  __shared__ R s2[EPB][NN];
+  const int tid = threadIdx.x, le = threadIdx.y;
+  const int e = blockIdx.x * EPB + le;
+  for (int t = tid + NN * le; t < N1 * N1; t += NN * EPB) D[t] = Cg.D[t];
+  const bool first = S->iter == 0;
+  const R beta = first ? R(0) : (R)(S->num / S->den);
+  const bool active = e < nEl;
+  const int i = tid % N1, j = tid / N1;
+  const size_t l = (size_t)e * NN + tid;
+  R u = 0;
+  if (active) {
+    const int sl = src[l];
+    u = first ? w[sl] : w[sl] + beta * vold[sl];
+    vnew[l] = first ? w[l] : w[l] + beta * vold[l];
+    su[le][tid] = u;
+  }
+  __syncthreads();
+  R us = 0, up = 0;
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      us += D[i + N1 * m] * su[le][m + N1 * j];
+      up += D[j + N1 * m] * su[le][i + N1 * m];
+    }
+    const R* fe = fac + (size_t)e * NF * NN;
+    const R G11 = fe[tid], G12 = fe[NN + tid], G22 = fe[2 * NN + tid];
+    s1[le][tid] = G11 * us + G12 * up;
+    s2[le][tid] = G12 * us + G22 * up;
+  }
+  __syncthreads();
+  double acc[1] = {0.0};
+  if (active) {
+    R a = 0, b = 0;
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      a += D[m + N1 * i] * s1[le][m + N1 * j];
+      b += D[m + N1 * j] * s2[le][i + N1 * m];
+    }
+    const R* fe = fac + (size_t)e * NF * NN;
+    R Lu = -(a + b) - fe[3 * NN + tid] * u;
+    if (NF == 6) Lu -= fe[4 * NN + tid] * us + fe[5 * NN + tid] * up;
+    z[l] = Lu;
+    acc[0] = (double)u * (double)Lu;
+  }
+  double tot[1];
+  if (grid_sums_last<1>(acc, partial, ticket, tot) && tid == 0 && le == 0) S->vz = tot[0];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ u, R* __restrict__ r,
+                                                                R* __restrict__ w, const R* __restrict__ v,
+                                                                const R* __restrict__ z, const R* __restrict__ dinv,
+                                                                size_t n, CGScalars* S, double* __restrict__ partial,
+                                                                unsigned int* __restrict__ ticket) {
+  if (S->done) return;
+  const R a = (R)(S->num / S->vz);
+  double acc[2] = {0.0, 0.0};
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
     u[k] += a * v[k];
-    R rk = r[k] - a * z[k];
+    const R rk = r[k] - a * z[k];
     r[k] = rk;
-    s0 += (double)rk * (double)rk;
+    const R wk = dinv ? rk * dinv[k] : rk;
+    w[k] = wk;
+    acc[0] += (double)rk * (double)wk;
+    acc[1] += (double)rk * (double)rk;
   }
-  s0 = block_sum(s0);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
-}
-
-// end of iteration: den = num, resi(iter) = ||r||, convergence test ||r||/||r0|| < tol
-__global__ void pcg_end_iter(const double* __restrict__ red_rr, CGScalars* S, double* __restrict__ resi) {
-  if (S->done) return;
-  const double rn = sqrt(red_rr[0]);
+  double tot[2];
+  if (!grid_sums_last<2>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
+  const double rn = sqrt(tot[1]);
   S->den = S->num;
+  S->num = tot[0];
   S->iter += 1;
-  if (resi) resi[S->iter] = rn;
+  if (S->resi) S->resi[S->iter] = rn;
   S->rr = rn;
   if (!(rn == rn) || isinf(rn)) {  // non-finite residual
     S->done = 1;
     S->ioerr = -7;
-    return;
-  }
-  if (rn / S->r0 < S->tol) {
+  } else if (rn / S->r0 < S->tol) {
     S->done = 1;
     S->ioerr = 0;
   } else if (S->iter >= S->maxIters) {
     S->done = 1;
     S->ioerr = -1;
   }
+}
+
+// w = dinv r and num = <r, w> before the first iteration
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) pcg_start_fused(const R* __restrict__ r, const R* __restrict__ dinv,
+                                                               R* __restrict__ w, size_t n, CGScalars* S,
+                                                               double* __restrict__ partial,
+                                                               unsigned int* __restrict__ ticket) {
+  if (S->done) return;
+  double acc[1] = {0.0};
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const R wk = dinv ? r[k] * dinv[k] : r[k];
+    w[k] = wk;
+    acc[0] += (double)r[k] * (double)wk;
+  }
+  double tot[1];
+  if (grid_sums_last<1>(acc, partial, ticket, tot) && threadIdx.x == 0) S->num = tot[0];
 }
 
 // ---------------------------------------------------------------------------------- generic vector ops
@@ -327,6 +430,14 @@ namespace selfgpu {
 namespace cg {
 
 // Operator data on the device in precision R.
+// Buffers a captured PCG iteration graph was built on.
+struct PcgGraphKey {
+  const void *u, *r, *v, *v2, *w, *z, *dinv, *fac;
+  bool operator==(const PcgGraphKey& o) const {
+    return u == o.u && r == o.r && v == o.v && v2 == o.v2 && w == o.w && z == o.z && dinv == o.dinv && fac == o.fac;
+  }
+};
+
 template <typename R>
 struct OpData {
   DevBuf<R> fac;   // NF * n^2 per element
@@ -364,6 +475,19 @@ struct self_cg2d {
   std::vector<double> h_fac, h_dinv;
   bool upload_dev = true;  // false: compile the host arrays only (used by the batched solver)
   int nblk = 0;
+  // fused (P)CG: second direction buffer, block ticket of the grid-wide sums, one captured iteration graph per
+  // (precision, preconditioner)
+  DevBuf<double> v2;
+  DevBuf<float> v2_32;
+  DevBuf<unsigned int> ticket;
+  cudaGraphExec_t pcg_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  selfgpu::cg::PcgGraphKey pcg_key[2][2] = {};
+  long long pcg_graph_launches = 0;  // kernels in a captured PCG graph
+  ~self_cg2d() {
+    for (auto& row : pcg_graph)
+      for (auto& g : row)
+        if (g) cudaGraphExecDestroy(g);
+  }
 };
 
 namespace {
@@ -415,6 +539,45 @@ int launch_dss(self_cg2d* h, R* v) {
   return SELF_OK;
 }
 
+template <int N1, typename R, int NF>
+void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, const R* fac, R* z,
+                          const std::vector<R>& D) {
+  CGConst<N1, R> C;
+  for (int k = 0; k < N1 * N1; ++k) C.D[k] = D[k];
+  constexpr int EPB = cg_epb<N1>();
+  dim3 blk(N1 * N1, EPB);
+  pcg_apply_fused<N1, R, NF><<<(h->nEl + EPB - 1) / EPB, blk, 0, h->ctx->stream>>>(
+      w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
+}
+
+template <typename R>
+int launch_apply_fused(self_cg2d* h, const R* w, const R* vold, R* vnew, R* z, const selfgpu::cg::OpData<R>& od) {
+  const R* fac = od.fac.p;
+  const bool adv = h->nf == 6;
+#define SELF_CG_CASE(NV)                                                   \
+  case NV:                                                                 \
+    if (adv)                                                               \
+      launch_apply_fused_t<NV, R, 6>(h, w, vold, vnew, fac, z, od.D);      \
+    else                                                                   \
+      launch_apply_fused_t<NV, R, 4>(h, w, vold, vnew, fac, z, od.D);      \
+    break;
+  switch (h->n) {
+    SELF_CG_CASE(3)
+    SELF_CG_CASE(4)
+    SELF_CG_CASE(5)
+    SELF_CG_CASE(6)
+    SELF_CG_CASE(7)
+    SELF_CG_CASE(8)
+    SELF_CG_CASE(9)
+    SELF_CG_CASE(10)
+    default:
+      return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "CG degree %d", h->N);
+  }
+#undef SELF_CG_CASE
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
 // MatrixAction: out = Mask(GlobalSum(L(UnMask(x))))
 template <typename R>
 int matrix_action(self_cg2d* h, const R* x, R* out, const selfgpu::cg::OpData<R>& od) {
@@ -456,11 +619,17 @@ namespace cg {
 // (P)CG iterations on the device from the current residual; returns ioerr and fills iters/resi.
 // abs_stop: the reference's early return when ||r0|| < TOL (CGsemElliptic_2D_Class.f90:1160-1162); the inner
 // solves of the iterative refinement use a purely relative stop.
+// The iterations run as a captured graph of kGraphIters fused iterations (three launches each, the two direction
+// buffers alternating); the host reads the scalar block after each graph launch.
+constexpr int kGraphIters = 16;  // even: the current direction is back in `v` after every graph launch
+
 template <typename R>
 int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int maxIters, double tol, double r0,
                double* resi_dev, int* iters, double* rel, const OpData<R>& od, bool abs_stop = true) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
+  R* v2 = (sizeof(R) == 4) ? reinterpret_cast<R*>(h->v2_32.p) : reinterpret_cast<R*>(h->v2.p);
+  if (!v2) return set_error(ctx, SELF_ERR_INVALID, "PCG direction buffer missing");
   CGScalars hs{};
   hs.r0 = r0;
   hs.tol = tol;
@@ -468,25 +637,48 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
   hs.iter = 0;
   hs.done = (abs_stop && r0 < tol) || maxIters <= 0 || r0 == 0.0;
   hs.ioerr = hs.done ? 0 : -2;
+  hs.resi = resi_dev;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
-  int rc;
-  const int check_every = 16;
-  for (int it = 0; it < maxIters; ++it) {
-    pcg_precond<R><<<h->nblk, kRedThreads, 0, st>>>(r, dinv, w, h->nl, h->partial.p, h->S.p);
+  if (!hs.done) {
+    pcg_start_fused<R><<<h->nblk, kRedThreads, 0, st>>>(r, dinv, w, h->nl, h->S.p, h->partial.p, h->ticket.p);
     SELF_LAUNCHED(ctx);
-    reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, 1, h->red.p);
-    SELF_LAUNCHED(ctx);
-    pcg_update_v<R><<<h->nblk, kRedThreads, 0, st>>>(w, v, h->nl, h->red.p, h->S.p);
-    SELF_LAUNCHED(ctx);
-    if ((rc = matrix_action<R>(h, v, z, od))) return rc;
-    if ((rc = dots<R>(h, v, z, nullptr, nullptr, h->red.p + 1))) return rc;
-    pcg_update_ur<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, v, z, h->nl, h->red.p + 1, h->S.p, h->partial.p);
-    SELF_LAUNCHED(ctx);
-    reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, 1, h->red.p + 2);
-    SELF_LAUNCHED(ctx);
-    pcg_end_iter<<<1, 1, 0, st>>>(h->red.p + 2, h->S.p, resi_dev);
-    SELF_LAUNCHED(ctx);
-    if ((it + 1) % check_every == 0 || it + 1 == maxIters) {
+    PcgGraphKey key{u, r, v, v2, w, z, dinv, od.fac.p};
+    cudaGraphExec_t& G = h->pcg_graph[sizeof(R) == 4 ? 1 : 0][dinv ? 1 : 0];
+    PcgGraphKey& gk = h->pcg_key[sizeof(R) == 4 ? 1 : 0][dinv ? 1 : 0];
+    if (G && !(gk == key)) {
+      cudaGraphExecDestroy(G);
+      G = nullptr;
+    }
+    if (!G) {
+      cudaGraph_t g;
+      int rc = SELF_OK;
+      const long long l0 = ctx->launches.load();
+      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < kGraphIters && !rc; ++k) {
+        R* vold = (k % 2 == 0) ? v : v2;
+        R* vnew = (k % 2 == 0) ? v2 : v;
+        if (!rc) rc = launch_apply_fused<R>(h, w, vold, vnew, z, od);
+        if (!rc) rc = launch_dss<R>(h, z);
+        if (!rc) {
+          pcg_update_fused<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, w, vnew, z, dinv, h->nl, h->S.p, h->partial.p,
+                                                              h->ticket.p);
+          SELF_LAUNCHED(ctx);
+        }
+      }
+      cudaError_t ce = cudaStreamEndCapture(st, &g);
+      if (rc) return rc;
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&G, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
+      gk = key;
+      h->pcg_graph_launches = ctx->launches.load() - l0;
+      ctx->launches.fetch_sub(h->pcg_graph_launches);
+    }
+    const long long max_launches = (long long)maxIters / kGraphIters + 2;
+    for (long long gl = 0; gl < max_launches; ++gl) {
+      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
+      ctx->launches.fetch_add(h->pcg_graph_launches);
       SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
       SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (hs.done) break;
@@ -754,7 +946,11 @@ int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* d, self_cg2d** out) {
   h->h_J.assign(d->J, d->J + h->nl);
   h->h_w.assign(d->qweight, d->qweight + h->n);
   h->nblk = grid_for(ctx, h->nl);
-  if ((rc = ensure(ctx, h->partial, (size_t)2 * h->nblk))) return rc;
+  const int epb = (h->n * h->n >= 256) ? 1 : 256 / (h->n * h->n);
+  const size_t apply_blocks = ((size_t)h->nEl + epb - 1) / epb;
+  if ((rc = ensure(ctx, h->partial, std::max((size_t)2 * h->nblk, apply_blocks)))) return rc;
+  if (h->ticket.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
+  SELF_CUDA_TRY(ctx, cudaMemset(h->ticket.p, 0, sizeof(unsigned int)));
   if ((rc = ensure(ctx, h->red, 8))) return rc;
   if (h->S.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
   if ((rc = ensure(ctx, h->t, h->nl))) return rc;
@@ -1048,7 +1244,7 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   std::vector<double> load = make_load(h, source);
   if ((rc = upload_vec(h, h->f, load.data())) || (rc = upload_vec(h, h->u, x0.data())) ||
       (rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->v, nl)) || (rc = ensure(ctx, h->w, nl)) ||
-      (rc = ensure(ctx, h->z, nl)))
+      (rc = ensure(ctx, h->z, nl)) || (o->method != SELF_SOLVE_GMRES && (rc = ensure(ctx, h->v2, nl))))
     return rc;
   if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
   self_solve_report R{};
@@ -1081,7 +1277,7 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
     } else {
       // FP32 inner (P)CG under FP64 iterative refinement: x += A32^-1 r64, r64 = b - A64 x
       if ((rc = ensuref(ctx, h->u32, nl)) || (rc = ensuref(ctx, h->r32, nl)) || (rc = ensuref(ctx, h->v32, nl)) ||
-          (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)))
+          (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)) || (rc = ensuref(ctx, h->v2_32, nl)))
         return rc;
       const double inner_tol = o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4;
       const int max_outer = o->max_outer > 0 ? o->max_outer : 30;

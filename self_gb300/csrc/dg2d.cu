@@ -420,6 +420,7 @@ struct self_dg2d {
   DevBuf<int> edges;
   bool traces_valid = false;
   cudaGraphExec_t step_graph = nullptr;
+  long long step_graph_launches = 0;  // kernels in the captured step graph
   selfgpu::dg32::State* f32 = nullptr;  // FP32 form
   ~self_dg2d() {
     if (step_graph) cudaGraphExecDestroy(step_graph);
@@ -880,6 +881,7 @@ int self_dg2d_rk3_async(self_dg2d* h, double tn, int nsteps) {
   }
   if (!h->step_graph) {  // capture one RK3 step (6 kernels) once, replay it nsteps times
     cudaGraph_t g;
+    const long long l0 = ctx->launches.load();
     SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     rc = enqueue_step(h, tn);
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
@@ -888,11 +890,12 @@ int self_dg2d_rk3_async(self_dg2d* h, double tn, int nsteps) {
     ce = cudaGraphInstantiate(&h->step_graph, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-    ctx->launches.fetch_sub(6);  // captured, not launched
+    h->step_graph_launches = ctx->launches.load() - l0;
+    ctx->launches.fetch_sub(h->step_graph_launches);  // captured, not launched
   }
   for (int s = 0; s < nsteps; ++s) {
     SELF_CUDA_TRY(ctx, cudaGraphLaunch(h->step_graph, ctx->stream));
-    ctx->launches.fetch_add(6);
+    ctx->launches.fetch_add(h->step_graph_launches);
   }
   return SELF_OK;
 }
@@ -936,8 +939,8 @@ int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* m
 int self_dg2d_rk3(self_dg2d* h, double tn, int nsteps) {
   int rc = self_dg2d_rk3_async(h, tn, nsteps);
   if (rc) return rc;
+  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::sync_and_check(h, h->f32);
   SELF_CUDA_TRY(h->ctx, cudaStreamSynchronize(h->ctx->stream));
-  if (h->precision == SELF_PREC_FP32) return selfgpu::dg32::check_error(h, h->f32);
   return SELF_OK;
 }
 

@@ -338,12 +338,15 @@ struct State {
   DevBuf<selfgpu::sw32::ESide> esides;
   DevBuf<int> err;
   int fused_grid = 0, fused_nbuf = 2;
+  long long graph_launches = 0;  // kernels in the captured step graph
   size_t fused_smem = 0;
   const int* edges = nullptr;  // owned by the FP64 handle
   cudaGraphExec_t graph = nullptr;
   bool traces_valid = false;
+  int* err_host = nullptr;  // page-locked copy of the error flag, read back in the same stream as the work
   ~State() {
     if (graph) cudaGraphExecDestroy(graph);
+    if (err_host) cudaFreeHost(err_host);
   }
 };
 
@@ -640,6 +643,8 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
       if (s->bs1.alloc(nb) || s->bs2.alloc(nb) || s->err.alloc(1))
         return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
       SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
+      SELF_CUDA_TRY(ctx, cudaHostAlloc(reinterpret_cast<void**>(&s->err_host), sizeof(int), cudaHostAllocDefault));
+      *s->err_host = 0;
       // pipeline depth per warp: 2 element buffers (16 warps per SM) unless SELF_FUSED_STAGES=3 (12 warps)
       const char* depth = getenv("SELF_FUSED_STAGES");
       s->fused_nbuf = (depth && atoi(depth) == 3) ? 3 : 2;
@@ -748,6 +753,7 @@ int rk3(self_dg2d* hd, State* s, double tn, int nsteps) {
   }
   if (!s->graph) {
     cudaGraph_t g;
+    const long long l0 = ctx->launches.load();
     SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     rc = step(ctx, s, tn);
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
@@ -756,11 +762,12 @@ int rk3(self_dg2d* hd, State* s, double tn, int nsteps) {
     ce = cudaGraphInstantiate(&s->graph, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-    ctx->launches.fetch_sub(6);
+    s->graph_launches = ctx->launches.load() - l0;  // 3 fused stages, or 3 x (edge, volume)
+    ctx->launches.fetch_sub(s->graph_launches);
   }
   for (int k = 0; k < nsteps; ++k) {
     SELF_CUDA_TRY(ctx, cudaGraphLaunch(s->graph, ctx->stream));
-    ctx->launches.fetch_add(6);
+    ctx->launches.fetch_add(s->graph_launches);
   }
   return SELF_OK;
 }
@@ -774,12 +781,17 @@ long long bytes(const State* s) {
                      s->esides.bytes());
 }
 
-int check_error(self_dg2d* hd, State* s) {
-  if (!s->fused) return SELF_OK;
+// Waits for the stream and reports a time-out recorded by the fused stage (the flag is copied back in the same
+// stream, so one synchronisation covers the work and the flag).
+int sync_and_check(self_dg2d* hd, State* s) {
   self_ctx* ctx = handle_ctx(hd);
-  int e = 0;
-  SELF_CUDA_TRY(ctx, cudaMemcpy(&e, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (s->fused)
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->err_host, s->err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (!s->fused) return SELF_OK;
+  const int e = *s->err_host;
   if (e) {
+    *s->err_host = 0;
     SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
     return set_error(ctx, SELF_ERR_TIMEOUT, "fused stage: a bulk-copy barrier wait ran out (code %d)", e);
   }

@@ -22,7 +22,7 @@ int tendency(self_dg2d* h, State* s, double t, double* dqdt);
 int rk3(self_dg2d* h, State* s, double tn, int nsteps);
 int time_kernels(self_dg2d* h, State* s, int reps, size_t flush_bytes, double* ms);
 // reports a bounded-wait time-out recorded by the fused stage kernel (after synchronisation)
-int check_error(self_dg2d* h, State* s);
+int sync_and_check(self_dg2d* h, State* s);
 // 1 when the fused TMA-pipelined stage is in use
 int is_fused(State* s);
 long long bytes(const State* s);
