@@ -282,6 +282,7 @@ def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=3000):
         sol, rep = cg.Solve(source, method="pcg", precision=prec, tolerance=1e-10, maxIters=50000)
         el = time.perf_counter() - t0
         out["pcg_" + prec] = {"seconds": el, "solves_per_s": 1.0 / el, "iterations": rep["iterations"],
+                              "ms_per_iteration": 1e3 * el / max(1, rep["iterations"]),
                               "outer": rep["outer_iterations"], "rel_residual": rep["rel_residual"],
                               "ioerr": rep["ioerr"]}
         if prec == "fp64":

@@ -191,37 +191,19 @@ struct CGScalars {
 // nodes and on non-primary copies.  The grid-wide sums are deterministic: every block writes its partial, and the
 // last block to finish (atomic ticket) adds the partials in block order and updates the scalars.
 
-// Sum of one value per thread over a block of any size up to 256 threads (fixed tree order); result in thread 0.
-__device__ __forceinline__ double block_sum_any(double v) {
-  __shared__ double sh[256];
-  const int nthr = blockDim.x * blockDim.y;
-  const int t = threadIdx.x + blockDim.x * threadIdx.y;
-  sh[t] = v;
-  for (int k = nthr + t; k < 256; k += nthr) sh[k] = 0.0;
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (t < st) sh[t] += sh[t + st];
-    __syncthreads();
-  }
-  const double r = sh[0];
-  __syncthreads();
-  return r;
-}
-
-// Grid-wide sums of NS values per thread: returns true in the last block, with the sums in tot (all threads).
+// Grid-wide sums of NS values per thread (1-D blocks of kRedThreads threads): returns true in the last block to
+// finish, with the sums (block order, fixed tree order inside each block) in thread 0's tot.
 template <int NS>
 __device__ __forceinline__ bool grid_sums_last(const double (&v)[NS], double* __restrict__ partial,
                                                unsigned int* __restrict__ ticket, double (&tot)[NS]) {
   __shared__ bool s_last;
-  const int t = threadIdx.x + blockDim.x * threadIdx.y;
-  const int nthr = blockDim.x * blockDim.y;
   const int nb = gridDim.x;
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
-    const double b = block_sum_any(v[s]);
-    if (t == 0) partial[(size_t)s * nb + blockIdx.x] = b;
+    const double b = block_sum(v[s]);
+    if (threadIdx.x == 0) partial[(size_t)s * nb + blockIdx.x] = b;
   }
-  if (t == 0) {
+  if (threadIdx.x == 0) {
     __threadfence();
     s_last = atomicAdd(ticket, 1u) == (unsigned)(nb - 1);
   }
@@ -231,71 +213,79 @@ __device__ __forceinline__ bool grid_sums_last(const double (&v)[NS], double* __
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
     double a = 0.0;
-    for (int k = t; k < nb; k += nthr) a += __ldcg(&partial[(size_t)s * nb + k]);
-    tot[s] = block_sum_any(a);
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) a += __ldcg(&partial[(size_t)s * nb + k]);
+    tot[s] = block_sum(a);
   }
-  if (t == 0) *ticket = 0u;
+  if (threadIdx.x == 0) *ticket = 0u;
   return true;
 }
 
+// Element groups of EPB elements per pass, grid-stride over the groups (1-D blocks of 256 threads: thread t works
+// on node t % NN of element t / NN of the group; threads beyond EPB * NN only join the reductions).
 template <int N1, typename R, int NF>
-__global__ void __launch_bounds__(256) pcg_apply_fused(const R* __restrict__ w, const R* __restrict__ vold,
-                                                       R* __restrict__ vnew, const int* __restrict__ src,
-                                                       const R* __restrict__ fac, R* __restrict__ z, int nEl,
-                                                       CGConst<N1, R> Cg, CGScalars* S, double* __restrict__ partial,
-                                                       unsigned int* __restrict__ ticket) {
+__global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restrict__ w, const R* __restrict__ vold,
+                                                               R* __restrict__ vnew, const int* __restrict__ src,
+                                                               const R* __restrict__ fac, R* __restrict__ z, int nEl,
+                                                               CGConst<N1, R> Cg, CGScalars* S,
+                                                               double* __restrict__ partial,
+                                                               unsigned int* __restrict__ ticket) {
   if (S->done) return;
   constexpr int NN = N1 * N1;
   constexpr int EPB = cg_epb<N1>();
+  static_assert(EPB * NN <= kRedThreads, "one element group per block pass");
   __shared__ R D[N1 * N1];
   __shared__ R su[EPB][NN];
   __shared__ R s1[EPB][NN];
   __shared__ R s2[EPB][NN];
-  const int tid = threadIdx.x, le = threadIdx.y;
-  const int e = blockIdx.x * EPB + le;
-  for (int t = tid + NN * le; t < N1 * N1; t += NN * EPB) D[t] = Cg.D[t];
+  const int tid = threadIdx.x % NN, le = threadIdx.x / NN;
+  for (int t = threadIdx.x; t < N1 * N1; t += kRedThreads) D[t] = Cg.D[t];
   const bool first = S->iter == 0;
   const R beta = first ? R(0) : (R)(S->num / S->den);
-  const bool active = e < nEl;
   const int i = tid % N1, j = tid / N1;
-  const size_t l = (size_t)e * NN + tid;
-  R u = 0;
-  if (active) {
-    const int sl = src[l];
-    u = first ? w[sl] : w[sl] + beta * vold[sl];
-    vnew[l] = first ? w[l] : w[l] + beta * vold[l];
-    su[le][tid] = u;
-  }
-  __syncthreads();
-  R us = 0, up = 0;
-  if (active) {
-#pragma unroll
-    for (int m = 0; m < N1; ++m) {
-      us += D[i + N1 * m] * su[le][m + N1 * j];
-      up += D[j + N1 * m] * su[le][i + N1 * m];
-    }
-    const R* fe = fac + (size_t)e * NF * NN;
-    const R G11 = fe[tid], G12 = fe[NN + tid], G22 = fe[2 * NN + tid];
-    s1[le][tid] = G11 * us + G12 * up;
-    s2[le][tid] = G12 * us + G22 * up;
-  }
-  __syncthreads();
+  const int ngroups = (nEl + EPB - 1) / EPB;
   double acc[1] = {0.0};
-  if (active) {
-    R a = 0, b = 0;
-#pragma unroll
-    for (int m = 0; m < N1; ++m) {
-      a += D[m + N1 * i] * s1[le][m + N1 * j];
-      b += D[m + N1 * j] * s2[le][i + N1 * m];
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int e = grp * EPB + le;
+    const bool active = le < EPB && e < nEl;
+    const size_t l = (size_t)e * NN + tid;
+    R u = 0;
+    __syncthreads();  // D loaded / previous pass done with the scratch arrays
+    if (active) {
+      const int sl = src[l];
+      u = first ? w[sl] : w[sl] + beta * vold[sl];
+      vnew[l] = first ? w[l] : w[l] + beta * vold[l];
+      su[le][tid] = u;
     }
-    const R* fe = fac + (size_t)e * NF * NN;
-    R Lu = -(a + b) - fe[3 * NN + tid] * u;
-    if (NF == 6) Lu -= fe[4 * NN + tid] * us + fe[5 * NN + tid] * up;
-    z[l] = Lu;
-    acc[0] = (double)u * (double)Lu;
+    __syncthreads();
+    R us = 0, up = 0;
+    if (active) {
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        us += D[i + N1 * m] * su[le][m + N1 * j];
+        up += D[j + N1 * m] * su[le][i + N1 * m];
+      }
+      const R* fe = fac + (size_t)e * NF * NN;
+      const R G11 = fe[tid], G12 = fe[NN + tid], G22 = fe[2 * NN + tid];
+      s1[le][tid] = G11 * us + G12 * up;
+      s2[le][tid] = G12 * us + G22 * up;
+    }
+    __syncthreads();
+    if (active) {
+      R a = 0, b = 0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        a += D[m + N1 * i] * s1[le][m + N1 * j];
+        b += D[m + N1 * j] * s2[le][i + N1 * m];
+      }
+      const R* fe = fac + (size_t)e * NF * NN;
+      R Lu = -(a + b) - fe[3 * NN + tid] * u;
+      if (NF == 6) Lu -= fe[4 * NN + tid] * us + fe[5 * NN + tid] * up;
+      z[l] = Lu;
+      acc[0] += (double)u * (double)Lu;
+    }
   }
   double tot[1];
-  if (grid_sums_last<1>(acc, partial, ticket, tot) && tid == 0 && le == 0) S->vz = tot[0];
+  if (grid_sums_last<1>(acc, partial, ticket, tot) && threadIdx.x == 0) S->vz = tot[0];
 }
 
 template <typename R>
@@ -483,6 +473,7 @@ struct self_cg2d {
   cudaGraphExec_t pcg_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   selfgpu::cg::PcgGraphKey pcg_key[2][2] = {};
   long long pcg_graph_launches = 0;  // kernels in a captured PCG graph
+  int apply_grid = 0;                // blocks of the fused apply (grid-stride over element groups)
   ~self_cg2d() {
     for (auto& row : pcg_graph)
       for (auto& g : row)
@@ -544,9 +535,7 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
                           const std::vector<R>& D) {
   CGConst<N1, R> C;
   for (int k = 0; k < N1 * N1; ++k) C.D[k] = D[k];
-  constexpr int EPB = cg_epb<N1>();
-  dim3 blk(N1 * N1, EPB);
-  pcg_apply_fused<N1, R, NF><<<(h->nEl + EPB - 1) / EPB, blk, 0, h->ctx->stream>>>(
+  pcg_apply_fused<N1, R, NF><<<h->apply_grid, kRedThreads, 0, h->ctx->stream>>>(
       w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
 }
 
@@ -947,8 +936,9 @@ int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* d, self_cg2d** out) {
   h->h_w.assign(d->qweight, d->qweight + h->n);
   h->nblk = grid_for(ctx, h->nl);
   const int epb = (h->n * h->n >= 256) ? 1 : 256 / (h->n * h->n);
-  const size_t apply_blocks = ((size_t)h->nEl + epb - 1) / epb;
-  if ((rc = ensure(ctx, h->partial, std::max((size_t)2 * h->nblk, apply_blocks)))) return rc;
+  const size_t groups = ((size_t)h->nEl + epb - 1) / epb;
+  h->apply_grid = (int)std::max<size_t>(1, std::min(groups, (size_t)std::max(1, ctx->num_sms) * 8));
+  if ((rc = ensure(ctx, h->partial, (size_t)2 * std::max(h->nblk, h->apply_grid)))) return rc;
   if (h->ticket.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation failed");
   SELF_CUDA_TRY(ctx, cudaMemset(h->ticket.p, 0, sizeof(unsigned int)));
   if ((rc = ensure(ctx, h->red, 8))) return rc;

@@ -504,10 +504,25 @@ int launch_fused(self_ctx* ctx, State* s, int stage, int mode, float a, float gd
     C.lN[k] = s->lN[k];
     C.qwinv[k] = s->qwinv[k];
   }
-  if (s->fused_nbuf == 3)
-    sw32_fused<8, 3, kFusedWarps3><<<s->fused_grid, 32 * kFusedWarps3, s->fused_smem, ctx->stream>>>(A, C);
-  else
-    sw32_fused<8, 2, kFusedWarps><<<s->fused_grid, 32 * kFusedWarps, s->fused_smem, ctx->stream>>>(A, C);
+  // launched with programmatic stream serialisation: consecutive stages overlap set-up with the previous tail
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = dim3(s->fused_grid);
+  cfg.dynamicSmemBytes = s->fused_smem;
+  cfg.stream = ctx->stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t le;
+  if (s->fused_nbuf == 3) {
+    cfg.blockDim = dim3(32 * kFusedWarps3);
+    le = cudaLaunchKernelEx(&cfg, sw32_fused<8, 3, kFusedWarps3>, A, C);
+  } else {
+    cfg.blockDim = dim3(32 * kFusedWarps);
+    le = cudaLaunchKernelEx(&cfg, sw32_fused<8, 2, kFusedWarps>, A, C);
+  }
+  if (le != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "fused stage launch: %s", cudaGetErrorString(le));
   SELF_LAUNCHED(ctx);
   return SELF_OK;
 }

@@ -220,6 +220,11 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   const float lEb = C.lE[i + 1], lWb = C.lW[i + 1], qwb = C.qwinv[i + 1];
   const float lNj = C.lN[j], lSj = C.lS[j], qwj = C.qwinv[j];
 
+  // Programmatic dependent launch: the next stage's CTAs may be scheduled as this grid's CTAs retire, and this
+  // grid's set-up above overlaps the previous stage's tail; every read or write of data the previous stage
+  // touches (state, RK register, traces) comes after the wait for that stage's completion.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nwarps = gridDim.x * W;
   const int gw = blockIdx.x * W + wid;
   const long long kMaxSpin = 1LL << 20;  // try_wait polls; normal waits end within microseconds
@@ -227,13 +232,15 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
 
   // issue the bulk copies of element e into buffer b: lanes 0-3 the neighbour traces of side = lane, lanes
   // 4-9 the element blocks; the byte count is posted before any copy is issued
-  auto issue = [&](int e, int b) {
+  // side records of element e (lanes 0-3), loaded one iteration before the element's copies are issued
+  auto load_es = [&](int e) {
     ESide es;
     es.nbr = -1;
-    if (lane < 4) {
-      es = A.es[(size_t)e * 4 + lane];
-      ws.es[b][lane] = es;
-    }
+    if (lane < 4 && e < A.nEl) es = A.es[(size_t)e * 4 + lane];
+    return es;
+  };
+  auto issue = [&](int e, int b, const ESide& es) {
+    if (lane < 4) ws.es[b][lane] = es;
     const bool hasnb = lane < 4 && es.nbr >= 0;
     const unsigned nbm = __ballot_sync(0xffffffffu, hasnb);
     fence_proxy_async();  // earlier generic accesses of this buffer before the async-proxy writes
@@ -262,14 +269,18 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
 #pragma unroll
   for (int k = 0; k < NBUF - 1; ++k) {
     const int e = gw + k * nwarps;
-    if (e < A.nEl) issue(e, k);
+    if (e < A.nEl) issue(e, k, load_es(e));
   }
+  ESide es_next = load_es(gw + (NBUF - 1) * nwarps);
   int it = 0;
   for (int e = gw; e < A.nEl; e += nwarps, ++it) {
     const int b = it % NBUF;
     {
       const int ef = e + (NBUF - 1) * nwarps;  // buffer (b + NBUF - 1) % NBUF was released by iteration it - 1
-      if (ef < A.nEl) issue(ef, (b + NBUF - 1) % NBUF);
+      if (ef < A.nEl) {
+        issue(ef, (b + NBUF - 1) % NBUF, es_next);
+        es_next = load_es(ef + nwarps);
+      }
     }
     const bool ok = mbar_wait(&ws.bar[b], (uint32_t)((it / NBUF) & 1), kMaxSpin);
     if (!__all_sync(0xffffffffu, ok)) {
