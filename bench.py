@@ -259,6 +259,10 @@ def _e2e(nat, L, ctx, sw, dof, steps, dist):
     return t, nbytes, parts
 
 
+# DRAM bytes (read + write) of one launch from the ncu --set full captures summarised in
+# profiles/sw32_fused_sw128_n7.md (launch 0) and profiles/dg_volume_fp64_sw128_n7.md (launch 1)
+NCU_TRAFFIC_BYTES = {"sw32_fused": 85.29e6, "dg_volume": 128.2e6}
+
 FLOPS_PER_EL_STAGE_N7 = 14.0e3  # algorithmic FP64 flops of one element-stage at N=7 (traces, fluxes, contractions,
 #                                 lift, 1/J, sources, RK update, Riemann), the count of the design notes
 
@@ -466,7 +470,7 @@ def run_gpu(args):
         vb = bytes_per_fused_launch(mesh.nEl, n) if fused else bytes_per_volume_launch(mesh.nEl, n, pb)
         ach = vb / (out[prec]["volume_ms"] * 1e-3) / 1e9
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": None,
+                "traffic": NCU_TRAFFIC_BYTES["sw32_fused" if fused else "dg_volume"], "traffic_unit": "B",
                 "kernel": ("sw32_fused (TMA-staged edge fluxes + volume + RK update + traces)" if fused
                            else "dg_volume (volume + RK update + next-stage traces)"),
                 "launch_ms": out[prec]["volume_ms"], "bytes_per_launch": vb, "peak_source": peak_kind,
