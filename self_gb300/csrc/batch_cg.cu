@@ -1,16 +1,25 @@
 // Batched CGSEM solves of many uneven problems (mixed mesh sizes and polynomial degrees) on one GPU.
 //
-// Each problem keeps its own device arrays (operator factors, topology, vectors); the batch is driven by
-// device-resident work tables: per-CTA tiles (problem, N, first element, count) for the element operator,
-// (problem, first group, count) for the direct-stiffness sum, (problem, first node, count) for the vector
-// phases, and a per-problem scalar block.  One launch per phase covers every active problem whatever its
-// degree (a switch on N selects the compile-time-specialised element body inside the kernel), and a CUDA
-// graph replays a chunk of iterations; problems that converged skip their tiles.  Elements per CTA for each
-// (N, element-count bucket) come from a measured autotuning table (self_cgbatch_autotune).
+// Each problem keeps its own device arrays (operator factors, topology, vectors).  Work is described by tile
+// tables: ETile (problem, N, first element, count) for the element operator, GTile (problem, first group, count)
+// for the direct-stiffness sum, VTile (problem, first node, last node) for vector phases.  Two compacted table
+// sets live on the device -- "inner" (problems running inner iterations) and "outer" (problems waiting for their
+// FP64 residual) -- with their tile counts in device memory; every kernel is a fixed-size grid that strides over
+// the tiles, so a change of the active set only re-uploads table contents and the captured iteration graph stays
+// valid.  One inner PCG iteration is three launches over all active problems (a switch on N selects the
+// compile-time element body):
+//   bk_apply : v_new = w + beta v_old (per-problem parity picks the buffers), z = L(v_new) per element, tile
+//              partial <v_new, z>;
+//   bk_dss   : z = Mask(GlobalSum(z));
+//   bk_update: a = num/<v,z>, u += a v, r -= a z, w = dinv r, tile partials <r,w>, <r,r>.
+// The last tile of a problem to finish (per-problem atomic ticket) adds that problem's tile partials in tile
+// order and updates its scalars, so every sum is deterministic and independent of the other problems.
+// Elements per CTA for each (N, element-count bucket) come from a measured autotuning table
+// (self_cgbatch_autotune).
 //
 // Solver: FP32-inner preconditioned CG under FP64 iterative refinement (the FP32 form of self_cg2d_solve),
-// or plain FP64 PCG.  Per problem it is the same recurrence as CGsemElliptic_2D%Solve (:1114-1207) with the
-// Jacobi preconditioner; dot products accumulate in FP64 per tile and are reduced per problem in tile order.
+// or plain FP64 PCG.  Per problem it is the recurrence of CGsemElliptic_2D%Solve (:1114-1207) with the Jacobi
+// preconditioner.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,6 +39,7 @@ namespace cgb {
 
 constexpr int kThreads = 256;
 constexpr int kVecChunk = kThreads * 8;  // nodes per vector tile
+constexpr int kElemTileNodes = 1024;      // nodes per element tile (several rounds of one node per thread)
 
 // Device descriptor of one problem.
 struct Prob {
@@ -54,13 +64,18 @@ struct Prob {
   float* v32;
   float* w32;
   float* z32;
+  double* v2_64;  // second direction buffers (v and v2 alternate with the iteration parity)
+  float* v2_32;
 };
 
 // Per-problem solver state.  phase: 0 inner iterations running, 1 waiting for the outer (FP64 residual)
 // update, 2 finished (converged or out of budget), 3 empty slot.
 struct Scal {
-  double num, den, rr, r0, tol, rin0;
+  double num, den, rr, r0, tol, rin0, vz;
+  double alpha, beta;             // step lengths, formed once per problem by its last tile (no per-thread division)
+  float alpha32, beta32;
   int iter, phase, total, fresh;  // fresh: no outer update yet (initial residual pending)
+  int max_total, max_inner;       // iteration limits of the current solve
 };
 
 // gate 0 runs problems in phase 0, gate 1 those in phase 1, gate 2 those in phase 1 that are not fresh,
@@ -75,7 +90,7 @@ __device__ __forceinline__ bool skip(const Scal& s, int gate) {
 }
 
 struct ETile {
-  int prob, N, e0, ne;
+  int prob, N, e0, ne, epr;  // ne elements from e0, processed epr at a time (one node per thread)
 };
 struct GTile {
   int prob, g0, ng;
@@ -162,66 +177,30 @@ __device__ __forceinline__ void apply_body(const Prob& p, const R* D, int e0, in
   }
 }
 
-// out = L(unmask(in)) [or rhs - L(...)] for every tile; D matrices for N = 2..9 in one table
+// D matrices for N = 2..9 in one table
 struct DTable {
   float d32[10][100];
   double d64[10][100];
 };
 
-template <typename R>
-__global__ void __launch_bounds__(kThreads) batch_apply(const ETile* __restrict__ tiles, const Prob* __restrict__ probs,
-                                                        const Scal* __restrict__ S, const DTable* __restrict__ DT,
-                                                        int vin, int vout, int residual, int gate) {
-  __shared__ R sh[3 * 256];
-  __shared__ R D[100];
-  const ETile t = tiles[blockIdx.x];
-  if (skip(S[t.prob], gate)) return;
-  const Prob& p = probs[t.prob];
-  const int n = t.N + 1;
-  for (int k = threadIdx.x; k < n * n; k += blockDim.x)
-    D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
-  __syncthreads();
-  const R* x = vec<R>(p, vin);
-  R* out = vec<R>(p, vout);
-  const double* rhs = residual ? p.f : nullptr;
-  switch (n) {
-    case 3: apply_body<3, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 4: apply_body<4, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 5: apply_body<5, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 6: apply_body<6, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 7: apply_body<7, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 8: apply_body<8, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 9: apply_body<9, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    case 10: apply_body<10, R>(p, D, t.e0, t.ne, x, rhs, out, sh); break;
-    default: break;
-  }
-}
+// Device view of one compacted tile-table set.  cnt[0..2]: ETiles, GTiles, VTiles; eptr/vptr[p]: first tile of
+// problem p (eptr[p + 1] - eptr[p] tiles; zero for problems outside the set).
+struct TileView {
+  const ETile* et;
+  const GTile* gt;
+  const VTile* vt;
+  const int* cnt;
+  const int* eptr;
+  const int* vptr;
+};
 
+// Sum over a 256-thread block: warp sums in the working precision, the 8 warp sums in FP64 (valid in thread 0).
 template <typename R>
-__global__ void __launch_bounds__(kThreads) batch_dss(const GTile* __restrict__ tiles, const Prob* __restrict__ probs,
-                                                      const Scal* __restrict__ S, int vsel, int gate) {
-  const GTile t = tiles[blockIdx.x];
-  if (skip(S[t.prob], gate)) return;
-  const Prob& p = probs[t.prob];
-  R* v = vec<R>(p, vsel);
-  for (int g = t.g0 + threadIdx.x; g < t.g0 + t.ng; g += blockDim.x) {
-    const int a = p.gptr[g], b = p.gptr[g + 1];
-    if (p.gdir[g]) {
-      for (int k = a; k < b; ++k) v[p.gidx[k]] = 0;
-      continue;
-    }
-    R s = 0;
-    for (int k = a; k < b; ++k) s += v[p.gidx[k]];
-    v[p.gidx[a]] = s;
-    for (int k = a + 1; k < b; ++k) v[p.gidx[k]] = 0;
-  }
-}
-
-__device__ __forceinline__ double block_sum(double v) {
+__device__ __forceinline__ double block_sum_r(R v) {
   __shared__ double sh[kThreads / 32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  if (ln == 0) sh[w] = v;
+  if (ln == 0) sh[w] = (double)v;
   __syncthreads();
   double r = 0;
   if (w == 0) {
@@ -232,103 +211,318 @@ __device__ __forceinline__ double block_sum(double v) {
   return r;
 }
 
-// Vector phases of the (P)CG iteration, per tile, with the tile's partial dot written to partial[tile].
-// op 0: w = r*dinv, partial <r,w>            op 1: v = w + beta v (beta from the problem's num/den)
-// op 2: partial <v,z>                         op 3: u += a v, r -= a z, partial <r,r>   (a = num / vz)
-// op 4: partial <r,r>
+// Tile partial(s) of problem p (NS sums; thread 0 holds the block values): written at partial[s * stride + t];
+// the last of the problem's `count` tiles adds the problem's partials (tile order, from `first`) into tot
+// (thread 0) and returns true (block-uniform).
+template <int NS>
+__device__ __forceinline__ bool tile_last(const double (&bv)[NS], double* __restrict__ partial, size_t stride, int t,
+                                          unsigned int* __restrict__ ticket, int first, int count, double (&tot)[NS]) {
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) partial[s * stride + t] = bv[s];
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == (unsigned)(count - 1);
+  }
+  __syncthreads();
+  const bool last = s_last;
+  __syncthreads();  // s_last is rewritten by the next tile of this block
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    double a = 0;
+    for (int k = threadIdx.x; k < count; k += kThreads) a += __ldcg(&partial[s * stride + first + k]);
+    tot[s] = block_sum_r<double>(a);
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+  return true;
+}
+
+// out = L(unmask(in)) [or rhs - L(...)] for the view's element tiles (outer residual, autotuning)
 template <typename R>
-__global__ void __launch_bounds__(kThreads) batch_vec(const VTile* __restrict__ tiles, const Prob* __restrict__ probs,
-                                                      const Scal* __restrict__ S, const double* __restrict__ red,
-                                                      double* __restrict__ partial, int op, int precond,
-                                                      int gate) {
-  const VTile t = tiles[blockIdx.x];
-  const Scal& s = S[t.prob];
-  if (skip(s, gate)) return;
-  const Prob& p = probs[t.prob];
-  R* r = vec<R>(p, V_R);
-  R* v = vec<R>(p, V_V);
-  R* w = vec<R>(p, V_W);
-  R* z = vec<R>(p, V_Z);
-  R* u = (sizeof(R) == 4) ? (R*)p.u32 : (R*)p.x;
-  const R* dinv = (sizeof(R) == 4) ? (const R*)p.dinv32 : (const R*)p.dinv64;
-  double acc = 0;
-  if (op == 0) {
-    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
-      const R wk = precond ? r[k] * dinv[k] : r[k];
-      w[k] = wk;
-      acc += (double)r[k] * (double)wk;
+__global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Prob* __restrict__ probs,
+                                                           const Scal* __restrict__ S, const DTable* __restrict__ DT,
+                                                           int vin, int vout, int residual, int gate) {
+  __shared__ R sh[3 * 256];
+  __shared__ R D[100];
+  const int nt = V.cnt[0];
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const ETile t = V.et[ti];
+    if (skip(S[t.prob], gate)) continue;
+    const Prob& p = probs[t.prob];
+    const int n = t.N + 1;
+    __syncthreads();  // previous tile done with D and the scratch
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x)
+      D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
+    __syncthreads();
+    const R* x = vec<R>(p, vin);
+    R* out = vec<R>(p, vout);
+    const double* rhs = residual ? p.f : nullptr;
+    for (int r0 = 0; r0 < t.ne; r0 += t.epr) {
+      const int ne = min(t.epr, t.ne - r0);
+      if (r0 > 0) __syncthreads();
+      switch (n) {
+        case 3: apply_body<3, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 4: apply_body<4, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 5: apply_body<5, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 6: apply_body<6, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 7: apply_body<7, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 8: apply_body<8, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 9: apply_body<9, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        case 10: apply_body<10, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
+        default: break;
+      }
     }
-  } else if (op == 1) {
+  }
+}
+
+// v_new = w + beta v_old on the tile's nodes, z = L(v_new gathered through src), returns the thread's u * Lu
+template <int N1, typename R>
+__device__ __forceinline__ R apply_fused_body(const Prob& p, const R* D, int e0, int ne, const R* w, const R* vold,
+                                              R* vnew, R beta, bool first, R* z, R* sh) {
+  constexpr int NN = N1 * N1;
+  constexpr int EPBM = max_epb<N1>();
+  const int tid = threadIdx.x % NN, le = threadIdx.x / NN;
+  const bool active = (le < EPBM) && (le < ne);
+  R* su = sh;
+  R* s1 = sh + EPBM * NN;
+  R* s2 = sh + 2 * EPBM * NN;
+  const int e = e0 + le;
+  const int i = tid % N1, j = tid / N1;
+  const size_t l = (size_t)e * NN + tid;
+  const R* fac = (sizeof(R) == 4) ? (const R*)p.fac32 : (const R*)p.fac64;
+  R u = 0, us = 0, up = 0, prod = 0;
+  if (active) {
+    const int sl = p.src[l];
+    u = first ? w[sl] : w[sl] + beta * vold[sl];
+    vnew[l] = first ? w[l] : w[l] + beta * vold[l];
+    su[le * NN + tid] = u;
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      us += D[i + N1 * m] * su[le * NN + m + N1 * j];
+      up += D[j + N1 * m] * su[le * NN + i + N1 * m];
+    }
+    const R* fe = fac + (size_t)e * 4 * NN;
+    const R G11 = fe[tid], G12 = fe[NN + tid], G22 = fe[2 * NN + tid];
+    s1[le * NN + tid] = G11 * us + G12 * up;
+    s2[le * NN + tid] = G12 * us + G22 * up;
+  }
+  __syncthreads();
+  if (active) {
+    R a = 0, b = 0;
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      a += D[m + N1 * i] * s1[le * NN + m + N1 * j];
+      b += D[m + N1 * j] * s2[le * NN + i + N1 * m];
+    }
+    const R M = fac[(size_t)e * 4 * NN + 3 * NN + tid];
+    const R Lu = -(a + b) - M * u;
+    z[l] = Lu;
+    prod = u * Lu;
+  }
+  return prod;
+}
+
+template <typename R>
+__device__ __forceinline__ void dirs(const Prob& p, int iter, R*& vold, R*& vnew) {
+  R* a = vec<R>(p, V_V);
+  R* b = (sizeof(R) == 4) ? (R*)p.v2_32 : (R*)p.v2_64;
+  vold = (iter & 1) ? b : a;
+  vnew = (iter & 1) ? a : b;
+}
+
+// inner iteration, part 1 (problems in phase 0)
+template <typename R>
+__global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __restrict__ probs, Scal* __restrict__ S,
+                                                     const DTable* __restrict__ DT, double* __restrict__ partial,
+                                                     unsigned int* __restrict__ ticket) {
+  __shared__ R sh[3 * 256];
+  __shared__ R D[100];
+  const int nt = V.cnt[0];
+  int curN = -1;
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const ETile t = V.et[ti];
+    Scal& s = S[t.prob];
+    if (skip(s, 0)) continue;
+    const Prob& p = probs[t.prob];
+    const int n = t.N + 1;
+    __syncthreads();  // previous tile done with D and the scratch
+    if (t.N != curN) {
+      for (int k = threadIdx.x; k < n * n; k += blockDim.x)
+        D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
+      curN = t.N;
+      __syncthreads();
+    }
     const bool first = s.iter == 0;
-    const R beta = first ? R(0) : (R)(red[t.prob] / s.den);
-    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) v[k] = first ? w[k] : w[k] + beta * v[k];
-  } else if (op == 2) {
-    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) acc += (double)v[k] * (double)z[k];
-  } else if (op == 3) {
-    const R a = (R)(s.num / red[t.prob]);
+    const R beta = first ? R(0) : (sizeof(R) == 4 ? (R)s.beta32 : (R)s.beta);
+    R *vold, *vnew;
+    dirs<R>(p, s.iter, vold, vnew);
+    const R* w = vec<R>(p, V_W);
+    R* z = vec<R>(p, V_Z);
+    R prod = 0;
+    const int epr = t.epr;  // elements per round (one node per thread); the tile holds several rounds
+    for (int r0 = 0; r0 < t.ne; r0 += epr) {
+      const int ne = min(epr, t.ne - r0);
+      if (r0 > 0) __syncthreads();  // scratch reuse between rounds
+      switch (n) {
+        case 3: prod += apply_fused_body<3, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 4: prod += apply_fused_body<4, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 5: prod += apply_fused_body<5, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 6: prod += apply_fused_body<6, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 7: prod += apply_fused_body<7, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 8: prod += apply_fused_body<8, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 9: prod += apply_fused_body<9, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        case 10: prod += apply_fused_body<10, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        default: break;
+      }
+    }
+    const double bv[1] = {block_sum_r<R>(prod)};
+    double tot[1];
+    const int first_t = V.eptr[t.prob], count = V.eptr[t.prob + 1] - first_t;
+    if (tile_last<1>(bv, partial, 0, ti, ticket + t.prob, first_t, count, tot) && threadIdx.x == 0) {
+      s.vz = tot[0];
+      s.alpha = s.num / tot[0];
+      s.alpha32 = (float)s.alpha;
+    }
+  }
+}
+
+// direct-stiffness sum + mask of vector vsel on the view's group tiles
+template <typename R>
+__global__ void __launch_bounds__(kThreads) bk_dss(TileView V, const Prob* __restrict__ probs,
+                                                   const Scal* __restrict__ S, int vsel, int gate) {
+  const int nt = V.cnt[1];
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const GTile t = V.gt[ti];
+    if (skip(S[t.prob], gate)) continue;
+    const Prob& p = probs[t.prob];
+    R* v = vec<R>(p, vsel);
+    for (int g = t.g0 + threadIdx.x; g < t.g0 + t.ng; g += blockDim.x) {
+      const int a = p.gptr[g], b = p.gptr[g + 1];
+      if (p.gdir[g]) {
+        for (int k = a; k < b; ++k) v[p.gidx[k]] = 0;
+        continue;
+      }
+      R sum = 0;
+      for (int k = a; k < b; ++k) sum += v[p.gidx[k]];
+      v[p.gidx[a]] = sum;
+      for (int k = a + 1; k < b; ++k) v[p.gidx[k]] = 0;
+    }
+  }
+}
+
+// inner iteration, part 3: a = num / <v,z>; u += a v_new; r -= a z; w = dinv r; <r,w>, <r,r>; the problem's last
+// tile closes the iteration (den = num, num = <r,w>, ||r||, inner stop test -> phase 1)
+template <typename R>
+__global__ void __launch_bounds__(kThreads) bk_update(TileView V, const Prob* __restrict__ probs, Scal* __restrict__ S,
+                                                      double* __restrict__ partial, size_t pstride,
+                                                      unsigned int* __restrict__ ticket) {
+  const int nt = V.cnt[2];
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const VTile t = V.vt[ti];
+    Scal& s = S[t.prob];
+    if (skip(s, 0)) continue;
+    const Prob& p = probs[t.prob];
+    R *vold, *v;
+    dirs<R>(p, s.iter, vold, v);
+    R* r = vec<R>(p, V_R);
+    R* w = vec<R>(p, V_W);
+    const R* z = vec<R>(p, V_Z);
+    R* u = (sizeof(R) == 4) ? (R*)p.u32 : (R*)p.x;
+    const R* dinv = (sizeof(R) == 4) ? (const R*)p.dinv32 : (const R*)p.dinv64;
+    const R a = sizeof(R) == 4 ? (R)s.alpha32 : (R)s.alpha;
+    R rw = 0, rr = 0;
     for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
       u[k] += a * v[k];
       const R rk = r[k] - a * z[k];
       r[k] = rk;
-      acc += (double)rk * (double)rk;
+      const R wk = rk * dinv[k];
+      w[k] = wk;
+      rw += rk * wk;
+      rr += rk * rk;
     }
-  } else {
-    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) acc += (double)r[k] * (double)r[k];
-  }
-  if (op != 1) {
-    acc = block_sum(acc);
-    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
-  }
-}
-
-// Per-problem reduction of its tiles' partials (tile order), one warp per problem.
-__global__ void batch_reduce(const int* __restrict__ vt_ptr, const double* __restrict__ partial,
-                             const Scal* __restrict__ S, double* __restrict__ red, int nprob, int gate) {
-  const int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  const int ln = threadIdx.x & 31;
-  if (p >= nprob) return;
-  if (skip(S[p], gate)) return;
-  double v = 0;
-  for (int k = vt_ptr[p] + ln; k < vt_ptr[p + 1]; k += 32) v += partial[k];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if (ln == 0) red[p] = v;
-}
-
-// Scalar updates per problem.
-// mode 0: num = red (after op 0);  mode 1: end of iteration: den = num, rr = red, convergence test
-// mode 0: num = red (after op 0); mode 1: end of an inner iteration (den = num, rr, inner stop test -> phase 1)
-__global__ void batch_scal(Scal* __restrict__ S, const double* __restrict__ red, int nprob, int mode, int maxIters,
-                           int maxInner) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nprob) return;
-  Scal& s = S[p];
-  if (s.phase != 0) return;
-  if (mode == 0) {
-    s.num = red[p];
-  } else {
-    const double rn = sqrt(red[p]);
-    s.den = s.num;
-    s.iter += 1;
-    s.total += 1;
-    s.rr = rn;
-    if (!(rn == rn) || rn / s.rin0 < s.tol || s.total >= maxIters || s.iter >= maxInner) s.phase = 1;
-  }
-}
-
-// FP64 -> FP32 residual, FP32 correction -> FP64 solution, zeroing the inner correction
-// dir 0 (gate 3, problems entering an inner solve): r32 = r, u32 = 0; dir 1 (gate 2): x += u32
-__global__ void batch_convert(const VTile* __restrict__ tiles, const Prob* __restrict__ probs,
-                              const Scal* __restrict__ S, int dir) {
-  const VTile t = tiles[blockIdx.x];
-  if (skip(S[t.prob], dir == 0 ? 3 : 2)) return;
-  const Prob& p = probs[t.prob];
-  for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
-    if (dir == 0) {
-      p.r32[k] = (float)p.r[k];
-      p.u32[k] = 0.f;
-    } else {
-      p.x[k] += (double)p.u32[k];
+    const double bv[2] = {block_sum_r<R>(rw), block_sum_r<R>(rr)};
+    double tot[2];
+    const int first_t = V.vptr[t.prob], count = V.vptr[t.prob + 1] - first_t;
+    if (tile_last<2>(bv, partial, pstride, ti, ticket + t.prob, first_t, count, tot) && threadIdx.x == 0) {
+      const double rn = sqrt(tot[1]);
+      s.den = s.num;
+      s.num = tot[0];
+      s.beta = s.num / s.den;
+      s.beta32 = (float)s.beta;
+      s.iter += 1;
+      s.total += 1;
+      s.rr = rn;
+      if (!(rn == rn) || rn / s.rin0 < s.tol || s.total >= s.max_total || s.iter >= s.max_inner) s.phase = 1;
     }
+  }
+}
+
+// start of an inner solve (problems in phase 0 with iter 0): FP32: r32 = r, u32 = 0; then w = dinv r, num = <r,w>
+template <typename R>
+__global__ void __launch_bounds__(kThreads) bk_start(TileView V, const Prob* __restrict__ probs, Scal* __restrict__ S,
+                                                     double* __restrict__ partial, unsigned int* __restrict__ ticket) {
+  const int nt = V.cnt[2];
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const VTile t = V.vt[ti];
+    Scal& s = S[t.prob];
+    if (skip(s, 3)) continue;
+    const Prob& p = probs[t.prob];
+    R* r = vec<R>(p, V_R);
+    R* w = vec<R>(p, V_W);
+    const R* dinv = (sizeof(R) == 4) ? (const R*)p.dinv32 : (const R*)p.dinv64;
+    R acc = 0;
+    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
+      R rk;
+      if (sizeof(R) == 4) {
+        rk = (R)p.r[k];
+        r[k] = rk;
+        p.u32[k] = 0.f;
+      } else {
+        rk = r[k];
+      }
+      const R wk = rk * dinv[k];
+      w[k] = wk;
+      acc += rk * wk;
+    }
+    const double bv[1] = {block_sum_r<R>(acc)};
+    double tot[1];
+    const int first_t = V.vptr[t.prob], count = V.vptr[t.prob + 1] - first_t;
+    if (tile_last<1>(bv, partial, 0, ti, ticket + t.prob, first_t, count, tot) && threadIdx.x == 0) s.num = tot[0];
+  }
+}
+
+// outer step (problems in phase 1): FP32 form adds the inner correction (x += u32) unless the problem is fresh
+__global__ void __launch_bounds__(kThreads) bk_correct(TileView V, const Prob* __restrict__ probs,
+                                                       const Scal* __restrict__ S) {
+  const int nt = V.cnt[2];
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const VTile t = V.vt[ti];
+    if (skip(S[t.prob], 2)) continue;
+    const Prob& p = probs[t.prob];
+    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) p.x[k] += (double)p.u32[k];
+  }
+}
+
+// outer step: red[p] = <r, r> (FP64) of every problem in phase 1
+__global__ void __launch_bounds__(kThreads) bk_rr(TileView V, const Prob* __restrict__ probs,
+                                                  const Scal* __restrict__ S, double* __restrict__ partial,
+                                                  unsigned int* __restrict__ ticket, double* __restrict__ red) {
+  const int nt = V.cnt[2];
+  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+    const VTile t = V.vt[ti];
+    if (skip(S[t.prob], 1)) continue;
+    const Prob& p = probs[t.prob];
+    double acc = 0;
+    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) acc += p.r[k] * p.r[k];
+    const double bv[1] = {block_sum_r<double>(acc)};
+    double tot[1];
+    const int first_t = V.vptr[t.prob], count = V.vptr[t.prob + 1] - first_t;
+    if (tile_last<1>(bv, partial, 0, ti, ticket + t.prob, first_t, count, tot) && threadIdx.x == 0) red[t.prob] = tot[0];
   }
 }
 
@@ -340,8 +534,8 @@ __global__ void batch_convert(const VTile* __restrict__ tiles, const Prob* __res
 struct self_cgbatch {
   self_ctx* ctx = nullptr;
   struct Mem {
-    DevBuf<float> fac32, dinv32, u32, r32, v32, w32, z32;
-    DevBuf<double> fac64, dinv64, f, x, r, v64, w64, z64;
+    DevBuf<float> fac32, dinv32, u32, r32, v32, w32, z32, v2_32;
+    DevBuf<double> fac64, dinv64, f, x, r, v64, w64, z64, v2_64;
     DevBuf<int> src, gptr, gidx;
     DevBuf<unsigned char> gdir;
   };
@@ -353,6 +547,16 @@ struct self_cgbatch {
     long long bytes = 0;
     int outer = 0;
   };
+  // one compacted tile-table set on the device (fixed capacity; contents re-uploaded when the set changes)
+  struct View {
+    DevBuf<selfgpu::cgb::ETile> et;
+    DevBuf<selfgpu::cgb::GTile> gt;
+    DevBuf<selfgpu::cgb::VTile> vt;
+    DevBuf<int> cnt, eptr, vptr;
+    std::vector<int> members;  // problems of the set at the last upload
+    bool valid = false;
+    selfgpu::cgb::TileView dev() const { return {et.p, gt.p, vt.p, cnt.p, eptr.p, vptr.p}; }
+  };
   std::vector<Slot> slots;
   std::vector<selfgpu::cgb::Prob> hp;
   std::vector<selfgpu::cgb::Scal> hs;
@@ -360,18 +564,16 @@ struct self_cgbatch {
   DevBuf<selfgpu::cgb::Prob> probs;
   DevBuf<selfgpu::cgb::Scal> S;
   DevBuf<double> red, partial;
+  DevBuf<unsigned int> ticket;
   DevBuf<selfgpu::cgb::DTable> DT;
   selfgpu::cgb::DTable hDT;
   bool haveD[10] = {};
-  DevBuf<selfgpu::cgb::ETile> et;
-  DevBuf<selfgpu::cgb::GTile> gt;
-  DevBuf<selfgpu::cgb::VTile> vt;
-  DevBuf<int> vt_ptr;
-  int n_et = 0, n_gt = 0, n_vt = 0;
+  View inner, outer, tune;
+  size_t cap_et = 0, cap_gt = 0, cap_vt = 0;  // table capacities (tiles of every problem in the pool)
+  int grid = 0;                               // blocks of every grid-stride launch
   bool dirty = true;
   int epb[10][4];
   cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
-  int inner32_max = -1, inner64_max = -1;  // iteration limit baked into each captured graph
   long long inner32_launches = 0, inner64_launches = 0;  // kernels per captured graph
   int graph_k = 8;
   long long bytes_in_use = 0;
@@ -424,109 +626,150 @@ int ensure_cap(self_cgbatch* b, int want) {
   b->hs.resize(nc, e);
   b->cap = nc;
   int rc;
-  if ((rc = zeros(b->ctx, b->probs, nc)) || (rc = zeros(b->ctx, b->S, nc)) || (rc = zeros(b->ctx, b->red, nc)))
+  if ((rc = zeros(b->ctx, b->probs, nc)) || (rc = zeros(b->ctx, b->S, nc)) || (rc = zeros(b->ctx, b->red, nc)) ||
+      (rc = zeros(b->ctx, b->ticket, nc)))
     return rc;
+  drop_graphs(b);  // the captured graphs hold the old arrays
+  b->cap_et = b->cap_gt = b->cap_vt = 0;  // per-problem pointer tables are sized by the slot count
   b->dirty = true;
   return SELF_OK;
 }
 
-// element tiles for the problems selected by (N, bucket) filter (-1 = all), with an optional forced EPB
-int build_tiles(self_cgbatch* b, int onlyN, int onlyBucket, int forceEpb) {
+int tile_epb(const self_cgbatch* b, const Prob& P, int forceEpb) {
+  const int bk = bucket_of(P.nEl);
+  int e = forceEpb > 0 ? forceEpb : (b->epb[P.N][bk] > 0 ? b->epb[P.N][bk] : max_epb_rt(P.N));
+  return std::max(1, std::min(e, max_epb_rt(P.N)));
+}
+
+// Upload the compacted tile tables of the problems in `members` (ascending slots) into view v.  With onlyN >= 0
+// only element tiles of that degree and bucket are listed, at forceEpb elements per tile (autotuning).
+int upload_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& members, int onlyN = -1,
+                int onlyBucket = -1, int forceEpb = 0) {
   std::vector<ETile> et;
   std::vector<GTile> gt;
   std::vector<VTile> vt;
-  std::vector<int> vptr(b->cap + 1, 0);
+  std::vector<int> eptr(b->cap + 1, 0), vptr(b->cap + 1, 0);
+  size_t m = 0;
   for (int p = 0; p < b->cap; ++p) {
+    eptr[p] = (int)et.size();
     vptr[p] = (int)vt.size();
-    if (!b->slots[p].used) continue;
+    if (m >= members.size() || members[m] != p) continue;
+    ++m;
     const Prob& P = b->hp[p];
-    const int bk = bucket_of(P.nEl);
-    const bool sel = (onlyN < 0 || P.N == onlyN) && (onlyBucket < 0 || bk == onlyBucket);
-    int e = forceEpb > 0 ? forceEpb : (b->epb[P.N][bk] > 0 ? b->epb[P.N][bk] : max_epb_rt(P.N));
-    e = std::max(1, std::min(e, max_epb_rt(P.N)));
+    const bool sel = (onlyN < 0 || P.N == onlyN) && (onlyBucket < 0 || bucket_of(P.nEl) == onlyBucket);
+    const int e = tile_epb(b, P, forceEpb);
+    const int nn = (P.N + 1) * (P.N + 1);
+    const int rounds = std::max(1, kElemTileNodes / (e * nn));
     if (sel)
-      for (int e0 = 0; e0 < P.nEl; e0 += e) et.push_back(ETile{p, P.N, e0, std::min(e, P.nEl - e0)});
+      for (int e0 = 0; e0 < P.nEl; e0 += e * rounds)
+        et.push_back(ETile{p, P.N, e0, std::min(e * rounds, P.nEl - e0), e});
     for (int g0 = 0; g0 < P.ngroups; g0 += kThreads) gt.push_back(GTile{p, g0, std::min(kThreads, P.ngroups - g0)});
     for (long long s0 = 0; s0 < P.nl; s0 += kVecChunk)
       vt.push_back(VTile{p, s0, std::min<long long>(P.nl, s0 + kVecChunk)});
   }
+  eptr[b->cap] = (int)et.size();
   vptr[b->cap] = (int)vt.size();
-  int rc;
-  if ((rc = put(b->ctx, b->et, et.data(), et.size()))) return rc;
-  if ((rc = put(b->ctx, b->gt, gt.data(), gt.size()))) return rc;
-  if ((rc = put(b->ctx, b->vt, vt.data(), vt.size()))) return rc;
-  if ((rc = put(b->ctx, b->vt_ptr, vptr.data(), vptr.size()))) return rc;
-  if (b->partial.n < std::max<size_t>(1, vt.size()) && (rc = zeros(b->ctx, b->partial, std::max<size_t>(1, vt.size()))))
-    return rc;
-  b->n_et = (int)et.size();
-  b->n_gt = (int)gt.size();
-  b->n_vt = (int)vt.size();
-  drop_graphs(b);
+  if (et.size() > b->cap_et || gt.size() > b->cap_gt || vt.size() > b->cap_vt)
+    return set_error(b->ctx, SELF_ERR_INVALID, "batch: tile tables exceed their capacity");
+  const int cnt[3] = {(int)et.size(), (int)gt.size(), (int)vt.size()};
+  cudaStream_t st = b->ctx->stream;
+  // the copies are ordered before the next launches of the stream (host vectors are copied synchronously
+  // with respect to the host for pageable memory)
+  if (!et.empty()) SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.et.p, et.data(), et.size() * sizeof(ETile), cudaMemcpyHostToDevice, st));
+  if (!gt.empty()) SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.gt.p, gt.data(), gt.size() * sizeof(GTile), cudaMemcpyHostToDevice, st));
+  if (!vt.empty()) SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.vt.p, vt.data(), vt.size() * sizeof(VTile), cudaMemcpyHostToDevice, st));
+  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.cnt.p, cnt, sizeof(cnt), cudaMemcpyHostToDevice, st));
+  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.eptr.p, eptr.data(), eptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.vptr.p, vptr.data(), vptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(st));  // host vectors go out of scope
+  v.members = members;
+  v.valid = onlyN < 0;
   return SELF_OK;
 }
 
+int alloc_view(self_cgbatch* b, self_cgbatch::View& v) {
+  int rc;
+  if ((rc = zeros(b->ctx, v.et, std::max<size_t>(1, b->cap_et))) || (rc = zeros(b->ctx, v.gt, std::max<size_t>(1, b->cap_gt))) ||
+      (rc = zeros(b->ctx, v.vt, std::max<size_t>(1, b->cap_vt))) || (rc = zeros(b->ctx, v.cnt, 3)) ||
+      (rc = zeros(b->ctx, v.eptr, (size_t)b->cap + 1)) || (rc = zeros(b->ctx, v.vptr, (size_t)b->cap + 1)))
+    return rc;
+  v.members.clear();
+  v.valid = false;
+  return SELF_OK;
+}
+
+// After the pool changed: upload the problem descriptors, size the tables for every problem (at the largest
+// tile count any element-per-tile choice gives) and drop the captured graphs if the table buffers moved.
 int refresh(self_cgbatch* b) {
   if (!b->dirty) return SELF_OK;
   int rc;
-  if ((rc = put(b->ctx, b->probs, b->hp.data(), (size_t)b->cap))) return rc;
-  if ((rc = put(b->ctx, b->DT, &b->hDT, 1))) return rc;
-  if ((rc = build_tiles(b, -1, -1, 0))) return rc;
+  // descriptors and derivative tables are copied into the existing arrays (the captured graphs hold them)
+  SELF_CUDA_TRY(b->ctx, cudaMemcpy(b->probs.p, b->hp.data(), (size_t)b->cap * sizeof(Prob), cudaMemcpyHostToDevice));
+  if (!b->DT.p) {
+    if ((rc = put(b->ctx, b->DT, &b->hDT, 1))) return rc;
+  } else {
+    SELF_CUDA_TRY(b->ctx, cudaMemcpy(b->DT.p, &b->hDT, sizeof(DTable), cudaMemcpyHostToDevice));
+  }
+  size_t ne = 0, ng = 0, nv = 0;
+  for (int p = 0; p < b->cap; ++p) {
+    if (!b->slots[p].used) continue;
+    const Prob& P = b->hp[p];
+    ne += (size_t)P.nEl;  // one element per tile is the most tiles any choice gives
+    ng += ((size_t)P.ngroups + kThreads - 1) / kThreads;
+    nv += ((size_t)P.nl + kVecChunk - 1) / kVecChunk;
+  }
+  if (ne > b->cap_et || ng > b->cap_gt || nv > b->cap_vt || !b->inner.et.p) {
+    b->cap_et = std::max(ne, 2 * b->cap_et);
+    b->cap_gt = std::max(ng, 2 * b->cap_gt);
+    b->cap_vt = std::max(nv, 2 * b->cap_vt);
+    if ((rc = alloc_view(b, b->inner)) || (rc = alloc_view(b, b->outer)) || (rc = alloc_view(b, b->tune))) return rc;
+    if ((rc = zeros(b->ctx, b->partial, std::max(b->cap_et, 2 * b->cap_vt)))) return rc;
+    drop_graphs(b);
+  } else {
+    b->inner.valid = b->outer.valid = false;  // same buffers, new contents on the next use
+  }
+  if (b->grid == 0) b->grid = std::max(1, b->ctx->num_sms) * 8;
   b->dirty = false;
   return SELF_OK;
 }
 
+int ensure_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& members) {
+  if (v.valid && v.members == members) return SELF_OK;
+  return upload_view(b, v, members);
+}
+
 template <typename R>
-int k_apply(self_cgbatch* b, int vin, int vout, int residual, int gate) {
-  if (!b->n_et) return SELF_OK;
-  batch_apply<R><<<b->n_et, kThreads, 0, b->ctx->stream>>>(b->et.p, b->probs.p, b->S.p, b->DT.p, vin, vout, residual,
-                                                           gate);
+int k_apply_plain(self_cgbatch* b, const self_cgbatch::View& v, int vin, int vout, int residual, int gate) {
+  bk_apply_plain<R><<<b->grid, kThreads, 0, b->ctx->stream>>>(v.dev(), b->probs.p, b->S.p, b->DT.p, vin, vout,
+                                                              residual, gate);
   SELF_LAUNCHED(b->ctx);
   return SELF_OK;
 }
 template <typename R>
-int k_dss(self_cgbatch* b, int v, int gate) {
-  if (!b->n_gt) return SELF_OK;
-  batch_dss<R><<<b->n_gt, kThreads, 0, b->ctx->stream>>>(b->gt.p, b->probs.p, b->S.p, v, gate);
+int k_dss(self_cgbatch* b, const self_cgbatch::View& v, int vsel, int gate) {
+  bk_dss<R><<<b->grid, kThreads, 0, b->ctx->stream>>>(v.dev(), b->probs.p, b->S.p, vsel, gate);
   SELF_LAUNCHED(b->ctx);
   return SELF_OK;
 }
+
+// inner iterations: graph = start (problems entering an inner solve) + graph_k x (apply, dss, update)
 template <typename R>
-int k_vec(self_cgbatch* b, int op, int gate, bool reduce) {
-  if (!b->n_vt) return SELF_OK;
-  batch_vec<R><<<b->n_vt, kThreads, 0, b->ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, b->red.p, b->partial.p, op, 1,
-                                                         gate);
+int enqueue_inner(self_cgbatch* b) {
+  cudaStream_t st = b->ctx->stream;
+  const TileView V = b->inner.dev();
+  bk_start<R><<<b->grid, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p);
   SELF_LAUNCHED(b->ctx);
-  if (reduce) {
-    batch_reduce<<<(b->cap + 7) / 8, 256, 0, b->ctx->stream>>>(b->vt_ptr.p, b->partial.p, b->S.p, b->red.p, b->cap,
-                                                               gate);
+  for (int k = 0; k < b->graph_k; ++k) {
+    bk_apply<R><<<b->grid, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->DT.p, b->partial.p, b->ticket.p);
+    SELF_LAUNCHED(b->ctx);
+    int rc;
+    if ((rc = k_dss<R>(b, b->inner, V_Z, 0))) return rc;
+    bk_update<R><<<b->grid, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->cap_vt, b->ticket.p);
     SELF_LAUNCHED(b->ctx);
   }
   return SELF_OK;
 }
-int k_scal(self_cgbatch* b, int mode, int maxIters, int maxInner) {
-  batch_scal<<<(b->cap + 127) / 128, 128, 0, b->ctx->stream>>>(b->S.p, b->red.p, b->cap, mode, maxIters, maxInner);
-  SELF_LAUNCHED(b->ctx);
-  return SELF_OK;
-}
-int k_convert(self_cgbatch* b, int dir) {
-  if (!b->n_vt) return SELF_OK;
-  batch_convert<<<b->n_vt, kThreads, 0, b->ctx->stream>>>(b->vt.p, b->probs.p, b->S.p, dir);
-  SELF_LAUNCHED(b->ctx);
-  return SELF_OK;
-}
 
-template <typename R>
-int inner_iteration(self_cgbatch* b, int maxIters, int maxInner) {
-  int rc;
-  if ((rc = k_vec<R>(b, 0, 0, true)) || (rc = k_scal(b, 0, maxIters, maxInner))) return rc;
-  if ((rc = k_vec<R>(b, 1, 0, false))) return rc;
-  if ((rc = k_apply<R>(b, V_V, V_Z, 0, 0)) || (rc = k_dss<R>(b, V_Z, 0))) return rc;
-  if ((rc = k_vec<R>(b, 2, 0, true))) return rc;
-  if ((rc = k_vec<R>(b, 3, 0, true))) return rc;
-  return k_scal(b, 1, maxIters, maxInner);
-}
-
-// One tick: outer updates of the problems waiting for one, then graph_k inner iterations of the others.
 int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
   self_ctx* ctx = b->ctx;
   const bool fp32 = o->precision == SELF_PREC_FP32;
@@ -534,19 +777,29 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
   const int max_outer = fp32 ? (o->max_outer > 0 ? o->max_outer : 30) : 2;
   int rc;
   if ((rc = refresh(b))) return rc;
+  for (int p = 0; p < b->cap; ++p) {
+    b->hs[p].max_total = o->maxIters;
+    b->hs[p].max_inner = o->maxIters;
+  }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
-  bool any1 = false;
-  for (int p = 0; p < b->cap; ++p) any1 = any1 || (b->slots[p].used && b->hs[p].phase == 1);
-  if (any1) {
-    if (fp32 && (rc = k_convert(b, 1))) return rc;  // x += u32 for problems whose inner solve ended
-    if ((rc = k_apply<double>(b, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, V_R, 1))) return rc;
-    if ((rc = k_vec<double>(b, 4, 1, true))) return rc;
+  std::vector<int> outer_set;
+  for (int p = 0; p < b->cap; ++p)
+    if (b->slots[p].used && b->hs[p].phase == 1) outer_set.push_back(p);
+  if (!outer_set.empty()) {
+    if ((rc = ensure_view(b, b->outer, outer_set))) return rc;
+    const TileView V = b->outer.dev();
+    if (fp32) {  // x += u32 for problems whose inner solve ended
+      bk_correct<<<b->grid, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p);
+      SELF_LAUNCHED(ctx);
+    }
+    if ((rc = k_apply_plain<double>(b, b->outer, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, b->outer, V_R, 1))) return rc;
+    bk_rr<<<b->grid, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p, b->red.p);
+    SELF_LAUNCHED(ctx);
     std::vector<double> rr(b->cap);
     SELF_CUDA_TRY(ctx, cudaMemcpyAsync(rr.data(), b->red.p, b->cap * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int p = 0; p < b->cap; ++p) {
+    for (int p : outer_set) {
       Scal& s = b->hs[p];
-      if (!b->slots[p].used || s.phase != 1) continue;
       const double rn = std::sqrt(rr[p]);
       s.rr = rn;
       if (s.fresh) {
@@ -561,40 +814,35 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
       b->slots[p].outer++;
       s.phase = 0;
       s.iter = 0;
-      s.num = s.den = 0;
+      s.num = s.den = s.vz = 0;
       s.rin0 = rn;
       s.tol = fp32 ? inner_tol : o->tolerance * s.r0 / rn;
     }
     SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
-    if (fp32 && (rc = k_convert(b, 0))) return rc;  // r32 = r, u32 = 0 for problems entering an inner solve
   }
-  bool any0 = false;
-  for (int p = 0; p < b->cap; ++p) any0 = any0 || (b->slots[p].used && b->hs[p].phase == 0);
-  if (any0) {
+  std::vector<int> inner_set;
+  for (int p = 0; p < b->cap; ++p)
+    if (b->slots[p].used && b->hs[p].phase == 0) inner_set.push_back(p);
+  if (!inner_set.empty()) {
+    if ((rc = ensure_view(b, b->inner, inner_set))) return rc;
     cudaGraphExec_t& G = fp32 ? b->inner32 : b->inner64;
-    int& gmax = fp32 ? b->inner32_max : b->inner64_max;
-    if (G && gmax != o->maxIters) {  // the per-problem iteration limit is a kernel argument inside the graph
-      cudaGraphExecDestroy(G);
-      G = nullptr;
-    }
+    long long& nk = fp32 ? b->inner32_launches : b->inner64_launches;
     if (!G) {
-      gmax = o->maxIters;
       cudaGraph_t g;
       const long long l0 = ctx->launches.load();
       SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < b->graph_k && !rc; ++k)
-        rc = fp32 ? inner_iteration<float>(b, o->maxIters, o->maxIters) : inner_iteration<double>(b, o->maxIters, o->maxIters);
+      rc = fp32 ? enqueue_inner<float>(b) : enqueue_inner<double>(b);
       cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
       if (rc) return rc;
       if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
       ce = cudaGraphInstantiate(&G, g, 0);
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
-      (fp32 ? b->inner32_launches : b->inner64_launches) = ctx->launches.load() - l0;
-      ctx->launches.fetch_sub(fp32 ? b->inner32_launches : b->inner64_launches);
+      nk = ctx->launches.load() - l0;
+      ctx->launches.fetch_sub(nk);
     }
     SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
-    ctx->launches.fetch_add(fp32 ? b->inner32_launches : b->inner64_launches);
+    ctx->launches.fetch_add(nk);
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->hs.data(), b->S.p, b->cap * sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -638,7 +886,8 @@ int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, 
   if ((rc = zeros(ctx, m->f, nl)) || (rc = zeros(ctx, m->x, nl)) || (rc = zeros(ctx, m->r, nl)) ||
       (rc = zeros(ctx, m->v64, nl)) || (rc = zeros(ctx, m->w64, nl)) || (rc = zeros(ctx, m->z64, nl)) ||
       (rc = zeros(ctx, m->u32, nl)) || (rc = zeros(ctx, m->r32, nl)) || (rc = zeros(ctx, m->v32, nl)) ||
-      (rc = zeros(ctx, m->w32, nl)) || (rc = zeros(ctx, m->z32, nl)))
+      (rc = zeros(ctx, m->w32, nl)) || (rc = zeros(ctx, m->z32, nl)) || (rc = zeros(ctx, m->v2_32, nl)) ||
+      (rc = zeros(ctx, m->v2_64, nl)))
     return rc;
   Prob P;
   P.N = hc.N;
@@ -665,6 +914,8 @@ int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, 
   P.v32 = m->v32.p;
   P.w32 = m->w32.p;
   P.z32 = m->z32.p;
+  P.v2_32 = m->v2_32.p;
+  P.v2_64 = m->v2_64.p;
   if (source) {
     std::vector<double> f(nl);
     for (size_t k = 0; k < nl; ++k) f[k] = source[k] * hc.Jww[k];
@@ -673,8 +924,8 @@ int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, 
   self_cgbatch::Slot& S = b->slots[slot];
   S.used = true;
   S.outer = 0;
-  S.bytes = (long long)(m->fac32.bytes() + m->dinv32.bytes() + 5 * nl * 4 + m->fac64.bytes() + m->dinv64.bytes() +
-                        6 * nl * 8 + m->src.bytes() + m->gptr.bytes() + m->gidx.bytes() + m->gdir.bytes());
+  S.bytes = (long long)(m->fac32.bytes() + m->dinv32.bytes() + 6 * nl * 4 + m->fac64.bytes() + m->dinv64.bytes() +
+                        7 * nl * 8 + m->src.bytes() + m->gptr.bytes() + m->gidx.bytes() + m->gdir.bytes());
   b->bytes_in_use += S.bytes;
   S.mem = std::move(m);
   S.Jww = std::move(hc.Jww);
@@ -745,8 +996,8 @@ int self_cgbatch_remove(self_cgbatch* b, int p) {
 int self_cgbatch_footprint(const self_cg2d_desc* d, long long* bytes) {
   if (!d || !bytes) return SELF_ERR_INVALID;
   const long long nl = (long long)(d->N + 1) * (d->N + 1) * d->nEl;
-  // FP32: 4 factors + diag + 5 vectors; FP64: 4 factors + diag + 6 vectors; src + groups
-  *bytes = nl * (10 * 4 + 11 * 8 + 4 + 8) + 4096;
+  // FP32: 4 factors + diag + 6 vectors; FP64: 4 factors + diag + 7 vectors; src + groups
+  *bytes = nl * (11 * 4 + 12 * 8 + 4 + 8) + 4096;
   return SELF_OK;
 }
 
@@ -862,6 +1113,9 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
   }
   int rc;
   if ((rc = refresh(b))) return rc;
+  std::vector<int> used;
+  for (int p = 0; p < b->cap; ++p)
+    if (b->slots[p].used) used.push_back(p);
   std::vector<Scal> hs(b->cap);
   for (auto& s : hs) {
     std::memset(&s, 0, sizeof(s));
@@ -875,13 +1129,13 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
       int best = mx;
       double best_ms = 1e30;
       for (int e = mx;; e = std::max(1, e / 2)) {
-        if ((rc = build_tiles(b, N, bk, e))) return rc;
+        if ((rc = upload_view(b, b->tune, used, N, bk, e))) return rc;
         for (int w = 0; w < 2; ++w)
-          if ((rc = k_apply<float>(b, V_V, V_Z, 0, 0))) return rc;
+          if ((rc = k_apply_plain<float>(b, b->tune, V_V, V_Z, 0, 0))) return rc;
         double ms = 0;
         if ((rc = self_ctx_timer_start(ctx))) return rc;
         for (int r = 0; r < 10; ++r)
-          if ((rc = k_apply<float>(b, V_V, V_Z, 0, 0))) return rc;
+          if ((rc = k_apply_plain<float>(b, b->tune, V_V, V_Z, 0, 0))) return rc;
         if ((rc = self_ctx_timer_stop(ctx, &ms))) return rc;
         if (ms < best_ms) {
           best_ms = ms;

@@ -177,7 +177,9 @@ struct GMScalars {
 struct CGScalars {
   double num, den, vz, rr, r0, tol;
   int iter, done, ioerr, maxIters;
-  double* resi;  // residual history (resi[iter] = ||r||), or null
+  double* resi;         // residual history (resi[iter] = ||r||), or null
+  double alpha, beta;   // step lengths of the current iteration, formed once by the last block of the kernel
+  float alpha32, beta32;  // before (no per-thread FP64 division); FP32 copies for the FP32 kernels
 };
 
 // ---------------------------------------------------------------------------------- fused (P)CG iteration
@@ -191,16 +193,34 @@ struct CGScalars {
 // nodes and on non-primary copies.  The grid-wide sums are deterministic: every block writes its partial, and the
 // last block to finish (atomic ticket) adds the partials in block order and updates the scalars.
 
-// Grid-wide sums of NS values per thread (1-D blocks of kRedThreads threads): returns true in the last block to
+// Sum over a 256-thread block of one value per thread: warp sums in the working precision R, the 8 warp sums in
+// FP64 (result in thread 0).  FP32 kernels keep the narrow FP64 pipe out of the per-node work.
+template <typename R>
+__device__ __forceinline__ double block_sum_mixed(R v) {
+  __shared__ double sh[kRedThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) sh[w] = (double)v;
+  __syncthreads();
+  double r = 0;
+  if (w == 0) {
+    r = (ln < kRedThreads / 32) ? sh[ln] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;
+}
+
+// Grid-wide sums of NS per-thread values (1-D blocks of kRedThreads threads): returns true in the last block to
 // finish, with the sums (block order, fixed tree order inside each block) in thread 0's tot.
-template <int NS>
-__device__ __forceinline__ bool grid_sums_last(const double (&v)[NS], double* __restrict__ partial,
+template <int NS, typename R>
+__device__ __forceinline__ bool grid_sums_last(const R (&v)[NS], double* __restrict__ partial,
                                                unsigned int* __restrict__ ticket, double (&tot)[NS]) {
   __shared__ bool s_last;
   const int nb = gridDim.x;
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
-    const double b = block_sum(v[s]);
+    const double b = block_sum_mixed<R>(v[s]);
     if (threadIdx.x == 0) partial[(size_t)s * nb + blockIdx.x] = b;
   }
   if (threadIdx.x == 0) {
@@ -214,7 +234,7 @@ __device__ __forceinline__ bool grid_sums_last(const double (&v)[NS], double* __
   for (int s = 0; s < NS; ++s) {
     double a = 0.0;
     for (int k = threadIdx.x; k < nb; k += blockDim.x) a += __ldcg(&partial[(size_t)s * nb + k]);
-    tot[s] = block_sum(a);
+    tot[s] = block_sum_mixed<double>(a);
   }
   if (threadIdx.x == 0) *ticket = 0u;
   return true;
@@ -240,22 +260,34 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
   const int tid = threadIdx.x % NN, le = threadIdx.x / NN;
   for (int t = threadIdx.x; t < N1 * N1; t += kRedThreads) D[t] = Cg.D[t];
   const bool first = S->iter == 0;
-  const R beta = first ? R(0) : (R)(S->num / S->den);
+  const R beta = first ? R(0) : (sizeof(R) == 4 ? (R)S->beta32 : (R)S->beta);
   const int i = tid % N1, j = tid / N1;
   const int ngroups = (nEl + EPB - 1) / EPB;
-  double acc[1] = {0.0};
+  R pa = 0;
   for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
     const int e = grp * EPB + le;
     const bool active = le < EPB && e < nEl;
     const size_t l = (size_t)e * NN + tid;
-    R u = 0;
-    __syncthreads();  // D loaded / previous pass done with the scratch arrays
+    // every independent load of the node first (index, own w and v, folded factors), then the gathers
+    R u = 0, G11 = 0, G12 = 0, G22 = 0, M = 0, B1 = 0, B2 = 0;
     if (active) {
       const int sl = src[l];
-      u = first ? w[sl] : w[sl] + beta * vold[sl];
-      vnew[l] = first ? w[l] : w[l] + beta * vold[l];
-      su[le][tid] = u;
+      const R wl = w[l], vl = first ? R(0) : vold[l];
+      const R* fe = fac + (size_t)e * NF * NN;
+      G11 = fe[tid];
+      G12 = fe[NN + tid];
+      G22 = fe[2 * NN + tid];
+      M = fe[3 * NN + tid];
+      if (NF == 6) {
+        B1 = fe[4 * NN + tid];
+        B2 = fe[5 * NN + tid];
+      }
+      const R ws = w[sl], vs = first ? R(0) : vold[sl];
+      u = first ? ws : ws + beta * vs;
+      vnew[l] = first ? wl : wl + beta * vl;
     }
+    __syncthreads();  // D loaded / previous pass done with the scratch arrays
+    if (active) su[le][tid] = u;
     __syncthreads();
     R us = 0, up = 0;
     if (active) {
@@ -264,8 +296,6 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
         us += D[i + N1 * m] * su[le][m + N1 * j];
         up += D[j + N1 * m] * su[le][i + N1 * m];
       }
-      const R* fe = fac + (size_t)e * NF * NN;
-      const R G11 = fe[tid], G12 = fe[NN + tid], G22 = fe[2 * NN + tid];
       s1[le][tid] = G11 * us + G12 * up;
       s2[le][tid] = G12 * us + G22 * up;
     }
@@ -277,15 +307,19 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
         a += D[m + N1 * i] * s1[le][m + N1 * j];
         b += D[m + N1 * j] * s2[le][i + N1 * m];
       }
-      const R* fe = fac + (size_t)e * NF * NN;
-      R Lu = -(a + b) - fe[3 * NN + tid] * u;
-      if (NF == 6) Lu -= fe[4 * NN + tid] * us + fe[5 * NN + tid] * up;
+      R Lu = -(a + b) - M * u;
+      if (NF == 6) Lu -= B1 * us + B2 * up;
       z[l] = Lu;
-      acc[0] += (double)u * (double)Lu;
+      pa += u * Lu;
     }
   }
+  const R acc[1] = {pa};
   double tot[1];
-  if (grid_sums_last<1>(acc, partial, ticket, tot) && threadIdx.x == 0) S->vz = tot[0];
+  if (grid_sums_last<1, R>(acc, partial, ticket, tot) && threadIdx.x == 0) {
+    S->vz = tot[0];
+    S->alpha = S->num / tot[0];
+    S->alpha32 = (float)S->alpha;
+  }
 }
 
 template <typename R>
@@ -295,22 +329,51 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ 
                                                                 size_t n, CGScalars* S, double* __restrict__ partial,
                                                                 unsigned int* __restrict__ ticket) {
   if (S->done) return;
-  const R a = (R)(S->num / S->vz);
-  double acc[2] = {0.0, 0.0};
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+  const R a = sizeof(R) == 4 ? (R)S->alpha32 : (R)S->alpha;
+  R prw = 0, prr = 0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int U = 4;  // four independent nodes per pass: their loads are all in flight together
+  for (; k + (U - 1) * stride < n; k += U * stride) {
+    R uu[U], vv[U], rr[U], zz[U], dd[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const size_t x = k + q * stride;
+      uu[q] = u[x];
+      vv[q] = v[x];
+      rr[q] = r[x];
+      zz[q] = z[x];
+      dd[q] = dinv ? dinv[x] : R(1);
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const size_t x = k + q * stride;
+      u[x] = uu[q] + a * vv[q];
+      const R rk = rr[q] - a * zz[q];
+      r[x] = rk;
+      const R wk = dinv ? rk * dd[q] : rk;
+      w[x] = wk;
+      prw += rk * wk;
+      prr += rk * rk;
+    }
+  }
+  for (; k < n; k += stride) {
     u[k] += a * v[k];
     const R rk = r[k] - a * z[k];
     r[k] = rk;
     const R wk = dinv ? rk * dinv[k] : rk;
     w[k] = wk;
-    acc[0] += (double)rk * (double)wk;
-    acc[1] += (double)rk * (double)rk;
+    prw += rk * wk;
+    prr += rk * rk;
   }
+  const R acc[2] = {prw, prr};
   double tot[2];
-  if (!grid_sums_last<2>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
+  if (!grid_sums_last<2, R>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
   const double rn = sqrt(tot[1]);
   S->den = S->num;
   S->num = tot[0];
+  S->beta = S->num / S->den;
+  S->beta32 = (float)S->beta;
   S->iter += 1;
   if (S->resi) S->resi[S->iter] = rn;
   S->rr = rn;
@@ -333,14 +396,15 @@ __global__ void __launch_bounds__(kRedThreads) pcg_start_fused(const R* __restri
                                                                double* __restrict__ partial,
                                                                unsigned int* __restrict__ ticket) {
   if (S->done) return;
-  double acc[1] = {0.0};
+  R pa = 0;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
     const R wk = dinv ? r[k] * dinv[k] : r[k];
     w[k] = wk;
-    acc[0] += (double)r[k] * (double)wk;
+    pa += r[k] * wk;
   }
+  const R acc[1] = {pa};
   double tot[1];
-  if (grid_sums_last<1>(acc, partial, ticket, tot) && threadIdx.x == 0) S->num = tot[0];
+  if (grid_sums_last<1, R>(acc, partial, ticket, tot) && threadIdx.x == 0) S->num = tot[0];
 }
 
 // ---------------------------------------------------------------------------------- generic vector ops
