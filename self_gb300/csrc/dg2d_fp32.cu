@@ -19,8 +19,16 @@
 #include "dg2d_fp32.cuh"
 #include "sw32_fused.cuh"
 
-// warps (independent element workers) per CTA of the fused stage, for 2- and 3-deep per-warp pipelines
-constexpr int kFusedWarps = 4, kFusedWarps3 = 3;
+// warps (independent element workers) per CTA of the fused stage, two element buffers per warp
+constexpr int kFusedWarps = 4;
+
+// the fused stage kernel for an RK mode (1: first stage) and whether drag or relaxation terms are present
+const void* fused_kernel(int mode, bool extra) {
+  using namespace selfgpu::sw32;
+  if (mode == 1) return extra ? (const void*)sw32_fused<8, 2, kFusedWarps, 1, true>
+                              : (const void*)sw32_fused<8, 2, kFusedWarps, 1, false>;
+  return extra ? (const void*)sw32_fused<8, 2, kFusedWarps, 2, true> : (const void*)sw32_fused<8, 2, kFusedWarps, 2, false>;
+}
 
 namespace selfgpu {
 namespace dg32 {
@@ -337,7 +345,7 @@ struct State {
   DevBuf<float> egF, bs1, bs2;
   DevBuf<selfgpu::sw32::ESide> esides;
   DevBuf<int> err;
-  int fused_grid = 0, fused_nbuf = 2;
+  int fused_grid = 0;
   long long graph_launches = 0;  // kernels in the captured step graph
   size_t fused_smem = 0;
   const int* edges = nullptr;  // owned by the FP64 handle
@@ -514,14 +522,9 @@ int launch_fused(self_ctx* ctx, State* s, int stage, int mode, float a, float gd
   cfg.stream = ctx->stream;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t le;
-  if (s->fused_nbuf == 3) {
-    cfg.blockDim = dim3(32 * kFusedWarps3);
-    le = cudaLaunchKernelEx(&cfg, sw32_fused<8, 3, kFusedWarps3>, A, C);
-  } else {
-    cfg.blockDim = dim3(32 * kFusedWarps);
-    le = cudaLaunchKernelEx(&cfg, sw32_fused<8, 2, kFusedWarps>, A, C);
-  }
+  cfg.blockDim = dim3(32 * kFusedWarps);
+  void* kargs[2] = {&A, &C};
+  const cudaError_t le = cudaLaunchKernelExC(&cfg, fused_kernel(mode, s->has_drag || s->has_relax), kargs);
   if (le != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "fused stage launch: %s", cudaGetErrorString(le));
   SELF_LAUNCHED(ctx);
   return SELF_OK;
@@ -618,7 +621,8 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
     bool walls_only = true;
     for (int k = 0; k < d->nEdges; ++k)
       if (d->edges[6 * k + 2] <= 0 && d->edges[6 * k + 2] != SELF_NO_NORMAL_FLOW) walls_only = false;
-    if (n == 8 && walls_only) {
+    // fused stage: N = 7, mirror walls only, element offsets within 32 bits (5 * 64 floats per element)
+    if (n == 8 && walls_only && (long long)nEl * 5 * 64 < (1LL << 31)) {
       using selfgpu::sw32::ESide;
       std::vector<ESide> es((size_t)4 * nEl);
       for (auto& x : es) x = ESide{-1, 0, 0, 0};
@@ -660,17 +664,17 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
       SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
       SELF_CUDA_TRY(ctx, cudaHostAlloc(reinterpret_cast<void**>(&s->err_host), sizeof(int), cudaHostAllocDefault));
       *s->err_host = 0;
-      // pipeline depth per warp: 2 element buffers (16 warps per SM) unless SELF_FUSED_STAGES=3 (12 warps)
-      const char* depth = getenv("SELF_FUSED_STAGES");
-      s->fused_nbuf = (depth && atoi(depth) == 3) ? 3 : 2;
-      const void* kfn = s->fused_nbuf == 3 ? (const void*)selfgpu::sw32::sw32_fused<8, 3, kFusedWarps3>
-                                           : (const void*)selfgpu::sw32::sw32_fused<8, 2, kFusedWarps>;
-      s->fused_smem = s->fused_nbuf == 3 ? selfgpu::sw32::fused_smem_bytes<8, 3, kFusedWarps3>()
-                                         : selfgpu::sw32::fused_smem_bytes<8, 2, kFusedWarps>();
-      SELF_CUDA_TRY(ctx, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->fused_smem));
-      int per_sm = 0;
-      const int wpb = s->fused_nbuf == 3 ? kFusedWarps3 : kFusedWarps;
-      SELF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 32 * wpb, s->fused_smem));
+      s->fused_smem = selfgpu::sw32::fused_smem_bytes<8, 2, kFusedWarps>();
+      int per_sm = 4;
+      for (int mode = 1; mode <= 2; ++mode)
+        for (int extra = 0; extra <= 1; ++extra) {
+          const void* kfn = fused_kernel(mode, extra != 0);
+          SELF_CUDA_TRY(ctx, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->fused_smem));
+          int ps = 0;
+          SELF_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, kfn, 32 * kFusedWarps, s->fused_smem));
+          per_sm = std::min(per_sm, ps);
+        }
+      const int wpb = kFusedWarps;
       const int nblocks = (int)((nEl + wpb - 1) / wpb);
       s->fused_grid = std::max(1, std::min(nblocks, std::max(1, per_sm) * ctx->num_sms));
       s->fused = true;

@@ -187,7 +187,8 @@ __device__ __forceinline__ void traces_shfl(const float2 (&q)[3], float lSj, flo
 
 // Lane map (N1 = 8): lane owns the node pair (i, j), (i + 1, j) with i = 2 (lane % 4), j = lane / 4, i.e. the
 // flat nodes 2 lane and 2 lane + 1, so every per-node field moves as a float2.
-template <int N1, int NBUF, int W>
+// MODE 1: G = tendency (first RK stage), 2: G = a G + tendency; EXTRA: linear drag and/or relaxation present.
+template <int N1, int NBUF, int W, int MODE, bool EXTRA>
 __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> Cg) {
   constexpr int NN = N1 * N1;
   static_assert(N1 == 8, "fused stage: lane map (node pairs, 32 side nodes) and 16-byte bulk granularity");
@@ -228,7 +229,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   const int nwarps = gridDim.x * W;
   const int gw = blockIdx.x * W + wid;
   const long long kMaxSpin = 1LL << 20;  // try_wait polls; normal waits end within microseconds
-  const uint32_t base_bytes = 4u * (S::Q + S::M + (uint32_t)A.naux * NN + S::R + S::EG) + (A.mode == 2 ? 4u * S::G : 0u);
+  const uint32_t base_bytes = 4u * (S::Q + S::M + (uint32_t)A.naux * NN + S::R + S::EG) + (MODE == 2 ? 4u * S::G : 0u);
 
   // issue the bulk copies of element e into buffer b: lanes 0-3 the neighbour traces of side = lane, lanes
   // 4-9 the element blocks; the byte count is posted before any copy is issued
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   auto load_es = [&](int e) {
     ESide es;
     es.nbr = -1;
-    if (lane < 4 && e < A.nEl) es = A.es[(size_t)e * 4 + lane];
+    if (lane < 4 && e < A.nEl) es = A.es[e * 4 + lane];
     return es;
   };
   auto issue = [&](int e, int b, const ESide& es) {
@@ -249,20 +250,20 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
     __syncwarp();
     WarpBuf<N1>& B = ws.buf[b];
     if (hasnb)
-      bulk_g2s(&B.nb[lane * 3 * N1], A.bs_in + (size_t)3 * N1 * (es.nside + 4 * (size_t)es.nbr), 4u * 3u * N1,
+      bulk_g2s(&B.nb[lane * 3 * N1], A.bs_in + 3 * N1 * (es.nside + 4 * es.nbr), 4u * 3u * N1,
                &ws.bar[b]);
     else if (lane == 4)
-      bulk_g2s(B.q, A.q + (size_t)e * S::Q, 4u * S::Q, &ws.bar[b]);
+      bulk_g2s(B.q, A.q + e * S::Q, 4u * S::Q, &ws.bar[b]);
     else if (lane == 5)
-      bulk_g2s(B.met, A.met + (size_t)e * S::M, 4u * S::M, &ws.bar[b]);
+      bulk_g2s(B.met, A.met + e * S::M, 4u * S::M, &ws.bar[b]);
     else if (lane == 6)
-      bulk_g2s(B.aux, A.aux + (size_t)e * A.naux * NN, 4u * A.naux * NN, &ws.bar[b]);
+      bulk_g2s(B.aux, A.aux + e * A.naux * NN, 4u * A.naux * NN, &ws.bar[b]);
     else if (lane == 7)
-      bulk_g2s(B.R0, A.R0 + (size_t)e * S::R, 4u * S::R, &ws.bar[b]);
+      bulk_g2s(B.R0, A.R0 + e * S::R, 4u * S::R, &ws.bar[b]);
     else if (lane == 8)
-      bulk_g2s(B.eg, A.eg + (size_t)e * S::EG, 4u * S::EG, &ws.bar[b]);
-    else if (lane == 9 && A.mode == 2)
-      bulk_g2s(B.G, A.G + (size_t)e * S::G, 4u * S::G, &ws.bar[b]);
+      bulk_g2s(B.eg, A.eg + e * S::EG, 4u * S::EG, &ws.bar[b]);
+    else if (MODE == 2 && lane == 9)
+      bulk_g2s(B.G, A.G + e * S::G, 4u * S::G, &ws.bar[b]);
   };
 
   // prologue: elements of iterations 0 .. NBUF-2
@@ -404,18 +405,18 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
         s[0] = f * V + A.g * eta * dx;
         s[1] = -f * U + A.g * eta * dy;
         s[2] = 0.f;
-        if (A.has_drag) {
+        if (EXTRA && A.has_drag) {
           s[0] -= A.drag * U / hn;
           s[1] -= A.drag * V / hn;
         }
-        if (A.has_relax) {
+        if (EXTRA && A.has_relax) {
           s[0] -= U * ts;
           s[1] -= V * ts;
           s[2] -= eta * ts;
         }
       };
       float2 ts2 = make_float2(0.f, 0.f);
-      if (A.has_relax) ts2 = *reinterpret_cast<const float2*>(&B.aux[4 * NN + node]);
+      if (EXTRA && A.has_relax) ts2 = *reinterpret_cast<const float2*>(&B.aux[4 * NN + node]);
       float sa[3], sb[3];
       source(q2[0].x, q2[1].x, q2[2].x, h2.x, dhdx.x, dhdy.x, fc.x, ts2.x, sa);
       source(q2[0].y, q2[1].y, q2[2].y, h2.y, dhdx.y, dhdy.y, fc.y, ts2.y, sb);
@@ -426,13 +427,13 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
         tend[v].y += sb[v] + r0.y;
       }
     }
-    float2* Ge = reinterpret_cast<float2*>(A.G + (size_t)e * 3 * NN);
-    float2* qo = reinterpret_cast<float2*>(A.qout + (size_t)e * 3 * NN);
+    float2* Ge = reinterpret_cast<float2*>(A.G + e * 3 * NN);
+    float2* qo = reinterpret_cast<float2*>(A.qout + e * 3 * NN);
     float2 qn[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
       float2 gg = tend[v];
-      if (A.mode == 2) {
+      if (MODE == 2) {
         const float2 g0 = *reinterpret_cast<const float2*>(&B.G[v * NN + node]);
         gg.x = A.a * g0.x + tend[v].x;
         gg.y = A.a * g0.y + tend[v].y;
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       qo[(v * NN + node) / 2] = qn[v];
     }
     // 5. traces of the new state
-    traces_shfl(qn, lSj, lNj, lEa, lEb, lWa, lWb, lane, i, j, A.bs_out + (size_t)3 * N1 * 4 * e);
+    traces_shfl(qn, lSj, lNj, lEa, lEb, lWa, lWb, lane, i, j, A.bs_out + 3 * N1 * 4 * e);
     __syncwarp();  // this buffer's floats are read; the next issue into it follows a proxy fence
   }
 }
