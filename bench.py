@@ -361,7 +361,7 @@ def batched_leg(sg, ctx, nprob=512, fp64_sample=32):
             "fp64_batched": {"seconds": el64b, "solves_per_s": nprob / el64b},
             "fp64_one_solve_per_launch": {"solves_per_s": single_rate, "sampled_problems": int(len(idx))},
             "speedup_vs_fp64_single": (nprob / el32) / single_rate,
-            "autotuned_elements_per_cta": {f"N{N}_b{b}": e for (N, b), e in tune.items()}}
+            "autotuned_elements_per_tile": {f"N{N}_b{b}": e for (N, b), e in tune.items()}}
 
 
 def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, fp64_sample=60):

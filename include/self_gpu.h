@@ -228,10 +228,11 @@ int self_cgbatch_step(self_cgbatch* b, const self_solve_opts* opts, int* nfinish
 int self_cgbatch_report(self_cgbatch* b, int slot, self_solve_report* report, int* finished);
 int self_cgbatch_footprint(const self_cg2d_desc* desc, long long* bytes);
 long long self_cgbatch_bytes(const self_cgbatch* b);
-/* Project autotuner: times elements-per-CTA choices of the element operator per (N, element-count bucket:
- * <=256, <=1024, <=4096, larger) and keeps the fastest; cache_path (JSON) is read first and written after. */
+/* Project autotuner: times element-tile sizes of the element operator (1, 2, 4, ... 32 rounds of one node per
+ * thread) per (N, element-count bucket: <=256, <=1024, <=4096, larger) and keeps the fastest; cache_path (JSON)
+ * is read first and written after.  self_cgbatch_tuning returns the elements per tile in use. */
 int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path);
-int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* epb);
+int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* elements_per_tile);
 
 /* ---------------------------------------------------------------- dot product without allocation
  * No counterpart in the reference.  For callers that cannot allocate device memory where they need an inner

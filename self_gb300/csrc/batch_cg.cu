@@ -14,7 +14,7 @@
 //   bk_update: a = num/<v,z>, u += a v, r -= a z, w = dinv r, tile partials <r,w>, <r,r>.
 // The last tile of a problem to finish (per-problem atomic ticket) adds that problem's tile partials in tile
 // order and updates its scalars, so every sum is deterministic and independent of the other problems.
-// Elements per CTA for each (N, element-count bucket) come from a measured autotuning table
+// Elements per element tile for each (N, element-count bucket) come from a measured autotuning table
 // (self_cgbatch_autotune).
 //
 // Solver: FP32-inner preconditioned CG under FP64 iterative refinement (the FP32 form of self_cg2d_solve),
@@ -40,6 +40,7 @@ namespace cgb {
 constexpr int kThreads = 256;
 constexpr int kVecChunk = kThreads * 8;  // nodes per vector tile
 constexpr int kElemTileNodes = 1024;      // nodes per element tile (several rounds of one node per thread)
+constexpr int kRoundsInFlight = 1;        // rounds of an element tile processed together (loads in flight)
 
 // Device descriptor of one problem.
 struct Prob {
@@ -247,12 +248,13 @@ __global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Pro
   __shared__ R sh[3 * 256];
   __shared__ R D[100];
   const int nt = V.cnt[0];
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const ETile t = V.et[ti];
-    if (skip(S[t.prob], gate)) continue;
+    if (skip(S[t.prob], gate)) return;
     const Prob& p = probs[t.prob];
     const int n = t.N + 1;
-    __syncthreads();  // previous tile done with D and the scratch
     for (int k = threadIdx.x; k < n * n; k += blockDim.x)
       D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
     __syncthreads();
@@ -277,53 +279,78 @@ __global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Pro
   }
 }
 
-// v_new = w + beta v_old on the tile's nodes, z = L(v_new gathered through src), returns the thread's u * Lu
-template <int N1, typename R>
-__device__ __forceinline__ R apply_fused_body(const Prob& p, const R* D, int e0, int ne, const R* w, const R* vold,
-                                              R* vnew, R beta, bool first, R* z, R* sh) {
+// v_new = w + beta v_old on the nodes of P consecutive rounds (round q: elements e0 + q epr .. of at most epr),
+// z = L(v_new gathered through src); returns the thread's sum of u * Lu.  All independent loads of the P rounds
+// are issued before the gathers, so each thread keeps P chains of loads in flight.
+template <int N1, typename R, int P>
+__device__ __noinline__ R apply_fused_rounds(const Prob& p, const R* D, int e0, int ne, int epr, const R* w,
+                                                const R* vold, R* vnew, R beta, bool first, R* z, R* sh) {
   constexpr int NN = N1 * N1;
   constexpr int EPBM = max_epb<N1>();
   const int tid = threadIdx.x % NN, le = threadIdx.x / NN;
-  const bool active = (le < EPBM) && (le < ne);
-  R* su = sh;
-  R* s1 = sh + EPBM * NN;
-  R* s2 = sh + 2 * EPBM * NN;
-  const int e = e0 + le;
   const int i = tid % N1, j = tid / N1;
-  const size_t l = (size_t)e * NN + tid;
   const R* fac = (sizeof(R) == 4) ? (const R*)p.fac32 : (const R*)p.fac64;
-  R u = 0, us = 0, up = 0, prod = 0;
-  if (active) {
-    const int sl = p.src[l];
-    u = first ? w[sl] : w[sl] + beta * vold[sl];
-    vnew[l] = first ? w[l] : w[l] + beta * vold[l];
-    su[le * NN + tid] = u;
-  }
-  __syncthreads();
-  if (active) {
+  bool act[P];
+  int e[P], sl[P];
+  size_t l[P];
+  R u[P], wl[P], vl[P], G11[P], G12[P], G22[P], M[P];
 #pragma unroll
-    for (int m = 0; m < N1; ++m) {
-      us += D[i + N1 * m] * su[le * NN + m + N1 * j];
-      up += D[j + N1 * m] * su[le * NN + i + N1 * m];
+  for (int q = 0; q < P; ++q) {
+    const int nq = min(epr, ne - q * epr);
+    e[q] = e0 + q * epr + le;
+    act[q] = (le < EPBM) && (le < nq);
+    l[q] = (size_t)e[q] * NN + tid;
+    u[q] = G11[q] = G12[q] = G22[q] = M[q] = R(0);
+    if (act[q]) {
+      sl[q] = p.src[l[q]];
+      wl[q] = w[l[q]];
+      vl[q] = first ? R(0) : vold[l[q]];
+      const R* fe = fac + (size_t)e[q] * 4 * NN;
+      G11[q] = fe[tid];
+      G12[q] = fe[NN + tid];
+      G22[q] = fe[2 * NN + tid];
+      M[q] = fe[3 * NN + tid];
     }
-    const R* fe = fac + (size_t)e * 4 * NN;
-    const R G11 = fe[tid], G12 = fe[NN + tid], G22 = fe[2 * NN + tid];
-    s1[le * NN + tid] = G11 * us + G12 * up;
-    s2[le * NN + tid] = G12 * us + G22 * up;
   }
-  __syncthreads();
-  if (active) {
-    R a = 0, b = 0;
 #pragma unroll
-    for (int m = 0; m < N1; ++m) {
-      a += D[m + N1 * i] * s1[le * NN + m + N1 * j];
-      b += D[m + N1 * j] * s2[le * NN + i + N1 * m];
+  for (int q = 0; q < P; ++q)
+    if (act[q]) {
+      const R ws = w[sl[q]], vs = first ? R(0) : vold[sl[q]];
+      u[q] = first ? ws : ws + beta * vs;
+      vnew[l[q]] = first ? wl[q] : wl[q] + beta * vl[q];
+      sh[(q * 3) * EPBM * NN + le * NN + tid] = u[q];
     }
-    const R M = fac[(size_t)e * 4 * NN + 3 * NN + tid];
-    const R Lu = -(a + b) - M * u;
-    z[l] = Lu;
-    prod = u * Lu;
-  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < P; ++q)
+    if (act[q]) {
+      const R* su = sh + (q * 3) * EPBM * NN + le * NN;
+      R us = 0, up = 0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        us += D[i + N1 * m] * su[m + N1 * j];
+        up += D[j + N1 * m] * su[i + N1 * m];
+      }
+      sh[(q * 3 + 1) * EPBM * NN + le * NN + tid] = G11[q] * us + G12[q] * up;
+      sh[(q * 3 + 2) * EPBM * NN + le * NN + tid] = G12[q] * us + G22[q] * up;
+    }
+  __syncthreads();
+  R prod = 0;
+#pragma unroll
+  for (int q = 0; q < P; ++q)
+    if (act[q]) {
+      const R* s1 = sh + (q * 3 + 1) * EPBM * NN + le * NN;
+      const R* s2 = sh + (q * 3 + 2) * EPBM * NN + le * NN;
+      R a = 0, b = 0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        a += D[m + N1 * i] * s1[m + N1 * j];
+        b += D[m + N1 * j] * s2[i + N1 * m];
+      }
+      const R Lu = -(a + b) - M[q] * u[q];
+      z[l[q]] = Lu;
+      prod += u[q] * Lu;
+    }
   return prod;
 }
 
@@ -340,23 +367,20 @@ template <typename R>
 __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __restrict__ probs, Scal* __restrict__ S,
                                                      const DTable* __restrict__ DT, double* __restrict__ partial,
                                                      unsigned int* __restrict__ ticket) {
-  __shared__ R sh[3 * 256];
+  __shared__ R sh[kRoundsInFlight * 3 * 256];
   __shared__ R D[100];
   const int nt = V.cnt[0];
-  int curN = -1;
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const ETile t = V.et[ti];
     Scal& s = S[t.prob];
-    if (skip(s, 0)) continue;
+    if (skip(s, 0)) return;
     const Prob& p = probs[t.prob];
     const int n = t.N + 1;
-    __syncthreads();  // previous tile done with D and the scratch
-    if (t.N != curN) {
-      for (int k = threadIdx.x; k < n * n; k += blockDim.x)
-        D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
-      curN = t.N;
-      __syncthreads();
-    }
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x)
+      D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
+    __syncthreads();
     const bool first = s.iter == 0;
     const R beta = first ? R(0) : (sizeof(R) == 4 ? (R)s.beta32 : (R)s.beta);
     R *vold, *vnew;
@@ -365,20 +389,26 @@ __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __r
     R* z = vec<R>(p, V_Z);
     R prod = 0;
     const int epr = t.epr;  // elements per round (one node per thread); the tile holds several rounds
-    for (int r0 = 0; r0 < t.ne; r0 += epr) {
-      const int ne = min(epr, t.ne - r0);
-      if (r0 > 0) __syncthreads();  // scratch reuse between rounds
+    for (int r0 = 0; r0 < t.ne; r0 += kRoundsInFlight * epr) {
+      const int ne = min(kRoundsInFlight * epr, t.ne - r0);
+      if (r0 > 0) __syncthreads();  // scratch reuse between passes
+#define SELF_BK_CASE(NV)                                                                                       \
+  case NV:                                                                                                     \
+    prod += apply_fused_rounds<NV, R, kRoundsInFlight>(p, D, t.e0 + r0, ne, epr, w, vold, vnew, beta, first, z, \
+                                                       sh);                                                    \
+    break;
       switch (n) {
-        case 3: prod += apply_fused_body<3, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 4: prod += apply_fused_body<4, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 5: prod += apply_fused_body<5, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 6: prod += apply_fused_body<6, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 7: prod += apply_fused_body<7, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 8: prod += apply_fused_body<8, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 9: prod += apply_fused_body<9, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
-        case 10: prod += apply_fused_body<10, R>(p, D, t.e0 + r0, ne, w, vold, vnew, beta, first, z, sh); break;
+        SELF_BK_CASE(3)
+        SELF_BK_CASE(4)
+        SELF_BK_CASE(5)
+        SELF_BK_CASE(6)
+        SELF_BK_CASE(7)
+        SELF_BK_CASE(8)
+        SELF_BK_CASE(9)
+        SELF_BK_CASE(10)
         default: break;
       }
+#undef SELF_BK_CASE
     }
     const double bv[1] = {block_sum_r<R>(prod)};
     double tot[1];
@@ -396,16 +426,18 @@ template <typename R>
 __global__ void __launch_bounds__(kThreads) bk_dss(TileView V, const Prob* __restrict__ probs,
                                                    const Scal* __restrict__ S, int vsel, int gate) {
   const int nt = V.cnt[1];
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const GTile t = V.gt[ti];
-    if (skip(S[t.prob], gate)) continue;
+    if (skip(S[t.prob], gate)) return;
     const Prob& p = probs[t.prob];
     R* v = vec<R>(p, vsel);
     for (int g = t.g0 + threadIdx.x; g < t.g0 + t.ng; g += blockDim.x) {
       const int a = p.gptr[g], b = p.gptr[g + 1];
       if (p.gdir[g]) {
         for (int k = a; k < b; ++k) v[p.gidx[k]] = 0;
-        continue;
+        return;
       }
       R sum = 0;
       for (int k = a; k < b; ++k) sum += v[p.gidx[k]];
@@ -422,10 +454,12 @@ __global__ void __launch_bounds__(kThreads) bk_update(TileView V, const Prob* __
                                                       double* __restrict__ partial, size_t pstride,
                                                       unsigned int* __restrict__ ticket) {
   const int nt = V.cnt[2];
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const VTile t = V.vt[ti];
     Scal& s = S[t.prob];
-    if (skip(s, 0)) continue;
+    if (skip(s, 0)) return;
     const Prob& p = probs[t.prob];
     R *vold, *v;
     dirs<R>(p, s.iter, vold, v);
@@ -436,14 +470,32 @@ __global__ void __launch_bounds__(kThreads) bk_update(TileView V, const Prob* __
     const R* dinv = (sizeof(R) == 4) ? (const R*)p.dinv32 : (const R*)p.dinv64;
     const R a = sizeof(R) == 4 ? (R)s.alpha32 : (R)s.alpha;
     R rw = 0, rr = 0;
-    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
-      u[k] += a * v[k];
-      const R rk = r[k] - a * z[k];
-      r[k] = rk;
-      const R wk = rk * dinv[k];
-      w[k] = wk;
-      rw += rk * wk;
-      rr += rk * rk;
+    // all loads of the thread's kVecChunk / kThreads nodes first (independent), then the updates
+    constexpr int Q = kVecChunk / kThreads;
+    R uu[Q], vv[Q], rq[Q], zz[Q], dd[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const long long k = t.s0 + threadIdx.x + (long long)q * kThreads;
+      if (k < t.s1) {
+        uu[q] = u[k];
+        vv[q] = v[k];
+        rq[q] = r[k];
+        zz[q] = z[k];
+        dd[q] = dinv[k];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const long long k = t.s0 + threadIdx.x + (long long)q * kThreads;
+      if (k < t.s1) {
+        u[k] = uu[q] + a * vv[q];
+        const R rk = rq[q] - a * zz[q];
+        r[k] = rk;
+        const R wk = rk * dd[q];
+        w[k] = wk;
+        rw += rk * wk;
+        rr += rk * rk;
+      }
     }
     const double bv[2] = {block_sum_r<R>(rw), block_sum_r<R>(rr)};
     double tot[2];
@@ -467,27 +519,39 @@ template <typename R>
 __global__ void __launch_bounds__(kThreads) bk_start(TileView V, const Prob* __restrict__ probs, Scal* __restrict__ S,
                                                      double* __restrict__ partial, unsigned int* __restrict__ ticket) {
   const int nt = V.cnt[2];
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const VTile t = V.vt[ti];
     Scal& s = S[t.prob];
-    if (skip(s, 3)) continue;
+    if (skip(s, 3)) return;
     const Prob& p = probs[t.prob];
     R* r = vec<R>(p, V_R);
     R* w = vec<R>(p, V_W);
     const R* dinv = (sizeof(R) == 4) ? (const R*)p.dinv32 : (const R*)p.dinv64;
     R acc = 0;
-    for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) {
-      R rk;
-      if (sizeof(R) == 4) {
-        rk = (R)p.r[k];
-        r[k] = rk;
-        p.u32[k] = 0.f;
-      } else {
-        rk = r[k];
+    constexpr int Q = kVecChunk / kThreads;
+    R rq[Q], dd[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const long long k = t.s0 + threadIdx.x + (long long)q * kThreads;
+      if (k < t.s1) {
+        rq[q] = (sizeof(R) == 4) ? (R)p.r[k] : r[k];
+        dd[q] = dinv[k];
       }
-      const R wk = rk * dinv[k];
-      w[k] = wk;
-      acc += rk * wk;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const long long k = t.s0 + threadIdx.x + (long long)q * kThreads;
+      if (k < t.s1) {
+        if (sizeof(R) == 4) {
+          r[k] = rq[q];
+          p.u32[k] = 0.f;
+        }
+        const R wk = rq[q] * dd[q];
+        w[k] = wk;
+        acc += rq[q] * wk;
+      }
     }
     const double bv[1] = {block_sum_r<R>(acc)};
     double tot[1];
@@ -500,9 +564,11 @@ __global__ void __launch_bounds__(kThreads) bk_start(TileView V, const Prob* __r
 __global__ void __launch_bounds__(kThreads) bk_correct(TileView V, const Prob* __restrict__ probs,
                                                        const Scal* __restrict__ S) {
   const int nt = V.cnt[2];
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const VTile t = V.vt[ti];
-    if (skip(S[t.prob], 2)) continue;
+    if (skip(S[t.prob], 2)) return;
     const Prob& p = probs[t.prob];
     for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) p.x[k] += (double)p.u32[k];
   }
@@ -513,9 +579,11 @@ __global__ void __launch_bounds__(kThreads) bk_rr(TileView V, const Prob* __rest
                                                   const Scal* __restrict__ S, double* __restrict__ partial,
                                                   unsigned int* __restrict__ ticket, double* __restrict__ red) {
   const int nt = V.cnt[2];
-  for (int ti = blockIdx.x; ti < nt; ti += gridDim.x) {
+  {  // one tile per block
+    const int ti = blockIdx.x;
+    if (ti >= nt) return;
     const VTile t = V.vt[ti];
-    if (skip(S[t.prob], 1)) continue;
+    if (skip(S[t.prob], 1)) return;
     const Prob& p = probs[t.prob];
     double acc = 0;
     for (long long k = t.s0 + threadIdx.x; k < t.s1; k += blockDim.x) acc += p.r[k] * p.r[k];
@@ -555,6 +623,8 @@ struct self_cgbatch {
     DevBuf<int> cnt, eptr, vptr;
     std::vector<int> members;  // problems of the set at the last upload
     bool valid = false;
+    size_t cap_e = 0, cap_g = 0, cap_v = 0;  // table capacities
+    int n_e = 0, n_g = 0, n_v = 0;           // tiles at the last upload
     selfgpu::cgb::TileView dev() const { return {et.p, gt.p, vt.p, cnt.p, eptr.p, vptr.p}; }
   };
   std::vector<Slot> slots;
@@ -570,11 +640,11 @@ struct self_cgbatch {
   bool haveD[10] = {};
   View inner, outer, tune;
   size_t cap_et = 0, cap_gt = 0, cap_vt = 0;  // table capacities (tiles of every problem in the pool)
-  int grid = 0;                               // blocks of every grid-stride launch
   bool dirty = true;
   int epb[10][4];
   cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
   long long inner32_launches = 0, inner64_launches = 0;  // kernels per captured graph
+  const double* partial_graph = nullptr;                 // partial-sum array the graphs were captured with
   int graph_k = 8;
   long long bytes_in_use = 0;
   ~self_cgbatch() {
@@ -635,10 +705,17 @@ int ensure_cap(self_cgbatch* b, int want) {
   return SELF_OK;
 }
 
-int tile_epb(const self_cgbatch* b, const Prob& P, int forceEpb) {
+// Elements per element tile: a multiple of the round size max_epb_rt(N) (one node per thread); the default gives
+// about kElemTileNodes nodes per tile, the autotuner may choose another multiple.
+int default_tile_elems(int N) {
+  const int r = max_epb_rt(N), nn = (N + 1) * (N + 1);
+  return r * std::max(1, kElemTileNodes / (r * nn));
+}
+int tile_elems(const self_cgbatch* b, const Prob& P, int force) {
   const int bk = bucket_of(P.nEl);
-  int e = forceEpb > 0 ? forceEpb : (b->epb[P.N][bk] > 0 ? b->epb[P.N][bk] : max_epb_rt(P.N));
-  return std::max(1, std::min(e, max_epb_rt(P.N)));
+  const int r = max_epb_rt(P.N);
+  int e = force > 0 ? force : (b->epb[P.N][bk] > 0 ? b->epb[P.N][bk] : default_tile_elems(P.N));
+  return std::max(r, (e / r) * r);
 }
 
 // Upload the compacted tile tables of the problems in `members` (ascending slots) into view v.  With onlyN >= 0
@@ -657,19 +734,16 @@ int upload_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& 
     ++m;
     const Prob& P = b->hp[p];
     const bool sel = (onlyN < 0 || P.N == onlyN) && (onlyBucket < 0 || bucket_of(P.nEl) == onlyBucket);
-    const int e = tile_epb(b, P, forceEpb);
-    const int nn = (P.N + 1) * (P.N + 1);
-    const int rounds = std::max(1, kElemTileNodes / (e * nn));
+    const int e = tile_elems(b, P, forceEpb);
     if (sel)
-      for (int e0 = 0; e0 < P.nEl; e0 += e * rounds)
-        et.push_back(ETile{p, P.N, e0, std::min(e * rounds, P.nEl - e0), e});
+      for (int e0 = 0; e0 < P.nEl; e0 += e) et.push_back(ETile{p, P.N, e0, std::min(e, P.nEl - e0), max_epb_rt(P.N)});
     for (int g0 = 0; g0 < P.ngroups; g0 += kThreads) gt.push_back(GTile{p, g0, std::min(kThreads, P.ngroups - g0)});
     for (long long s0 = 0; s0 < P.nl; s0 += kVecChunk)
       vt.push_back(VTile{p, s0, std::min<long long>(P.nl, s0 + kVecChunk)});
   }
   eptr[b->cap] = (int)et.size();
   vptr[b->cap] = (int)vt.size();
-  if (et.size() > b->cap_et || gt.size() > b->cap_gt || vt.size() > b->cap_vt)
+  if (et.size() > v.cap_e || gt.size() > v.cap_g || vt.size() > v.cap_v)
     return set_error(b->ctx, SELF_ERR_INVALID, "batch: tile tables exceed their capacity");
   const int cnt[3] = {(int)et.size(), (int)gt.size(), (int)vt.size()};
   cudaStream_t st = b->ctx->stream;
@@ -684,17 +758,24 @@ int upload_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& 
   SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(st));  // host vectors go out of scope
   v.members = members;
   v.valid = onlyN < 0;
+  v.n_e = cnt[0];
+  v.n_g = cnt[1];
+  v.n_v = cnt[2];
   return SELF_OK;
 }
 
-int alloc_view(self_cgbatch* b, self_cgbatch::View& v) {
+int alloc_view(self_cgbatch* b, self_cgbatch::View& v, size_t ce, size_t cg, size_t cv) {
   int rc;
-  if ((rc = zeros(b->ctx, v.et, std::max<size_t>(1, b->cap_et))) || (rc = zeros(b->ctx, v.gt, std::max<size_t>(1, b->cap_gt))) ||
-      (rc = zeros(b->ctx, v.vt, std::max<size_t>(1, b->cap_vt))) || (rc = zeros(b->ctx, v.cnt, 3)) ||
-      (rc = zeros(b->ctx, v.eptr, (size_t)b->cap + 1)) || (rc = zeros(b->ctx, v.vptr, (size_t)b->cap + 1)))
+  v.cap_e = std::max<size_t>(1, ce);
+  v.cap_g = std::max<size_t>(1, cg);
+  v.cap_v = std::max<size_t>(1, cv);
+  if ((rc = zeros(b->ctx, v.et, v.cap_e)) || (rc = zeros(b->ctx, v.gt, v.cap_g)) || (rc = zeros(b->ctx, v.vt, v.cap_v)) ||
+      (rc = zeros(b->ctx, v.cnt, 3)) || (rc = zeros(b->ctx, v.eptr, (size_t)b->cap + 1)) ||
+      (rc = zeros(b->ctx, v.vptr, (size_t)b->cap + 1)))
     return rc;
   v.members.clear();
   v.valid = false;
+  v.n_e = v.n_g = v.n_v = 0;
   return SELF_OK;
 }
 
@@ -710,25 +791,34 @@ int refresh(self_cgbatch* b) {
   } else {
     SELF_CUDA_TRY(b->ctx, cudaMemcpy(b->DT.p, &b->hDT, sizeof(DTable), cudaMemcpyHostToDevice));
   }
-  size_t ne = 0, ng = 0, nv = 0;
+  size_t ne = 0, ng = 0, nv = 0, ne1 = 0;
   for (int p = 0; p < b->cap; ++p) {
     if (!b->slots[p].used) continue;
     const Prob& P = b->hp[p];
-    ne += (size_t)P.nEl;  // one element per tile is the most tiles any choice gives
+    const size_t te = (size_t)tile_elems(b, P, 0), r = (size_t)max_epb_rt(P.N);
+    ne += ((size_t)P.nEl + te - 1) / te;
+    ne1 += ((size_t)P.nEl + r - 1) / r;  // one round per tile: the most tiles the autotuner lists
     ng += ((size_t)P.ngroups + kThreads - 1) / kThreads;
     nv += ((size_t)P.nl + kVecChunk - 1) / kVecChunk;
   }
   if (ne > b->cap_et || ng > b->cap_gt || nv > b->cap_vt || !b->inner.et.p) {
-    b->cap_et = std::max(ne, 2 * b->cap_et);
-    b->cap_gt = std::max(ng, 2 * b->cap_gt);
-    b->cap_vt = std::max(nv, 2 * b->cap_vt);
-    if ((rc = alloc_view(b, b->inner)) || (rc = alloc_view(b, b->outer)) || (rc = alloc_view(b, b->tune))) return rc;
-    if ((rc = zeros(b->ctx, b->partial, std::max(b->cap_et, 2 * b->cap_vt)))) return rc;
+    // the inner iteration graph launches one block per table slot, so the capacity is its grid
+    b->cap_et = std::max(ne, b->cap_et + b->cap_et / 4);
+    b->cap_gt = std::max(ng, b->cap_gt + b->cap_gt / 4);
+    b->cap_vt = std::max(nv, b->cap_vt + b->cap_vt / 4);
+    if ((rc = alloc_view(b, b->inner, b->cap_et, b->cap_gt, b->cap_vt)) ||
+        (rc = alloc_view(b, b->outer, b->cap_et, b->cap_gt, b->cap_vt)))
+      return rc;
     drop_graphs(b);
   } else {
     b->inner.valid = b->outer.valid = false;  // same buffers, new contents on the next use
   }
-  if (b->grid == 0) b->grid = std::max(1, b->ctx->num_sms) * 8;
+  if (ne1 > b->tune.cap_e || !b->tune.et.p)
+    if ((rc = alloc_view(b, b->tune, ne1, ng, nv))) return rc;
+  const size_t np = std::max({b->cap_et, 2 * b->cap_vt, b->tune.cap_e});
+  if (b->partial.n < np && (rc = zeros(b->ctx, b->partial, np))) return rc;
+  if (b->partial_graph != b->partial.p) drop_graphs(b);
+  b->partial_graph = b->partial.p;
   b->dirty = false;
   return SELF_OK;
 }
@@ -738,16 +828,21 @@ int ensure_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& 
   return upload_view(b, v, members);
 }
 
+// grids: one block per tile; launches inside the captured inner graph use the table capacity (the tile count
+// changes between ticks), direct launches use the count of the last upload
 template <typename R>
 int k_apply_plain(self_cgbatch* b, const self_cgbatch::View& v, int vin, int vout, int residual, int gate) {
-  bk_apply_plain<R><<<b->grid, kThreads, 0, b->ctx->stream>>>(v.dev(), b->probs.p, b->S.p, b->DT.p, vin, vout,
-                                                              residual, gate);
+  if (v.n_e == 0) return SELF_OK;
+  bk_apply_plain<R><<<v.n_e, kThreads, 0, b->ctx->stream>>>(v.dev(), b->probs.p, b->S.p, b->DT.p, vin, vout,
+                                                            residual, gate);
   SELF_LAUNCHED(b->ctx);
   return SELF_OK;
 }
 template <typename R>
-int k_dss(self_cgbatch* b, const self_cgbatch::View& v, int vsel, int gate) {
-  bk_dss<R><<<b->grid, kThreads, 0, b->ctx->stream>>>(v.dev(), b->probs.p, b->S.p, vsel, gate);
+int k_dss(self_cgbatch* b, const self_cgbatch::View& v, int vsel, int gate, bool in_graph) {
+  const int grid = in_graph ? (int)v.cap_g : v.n_g;
+  if (grid == 0) return SELF_OK;
+  bk_dss<R><<<grid, kThreads, 0, b->ctx->stream>>>(v.dev(), b->probs.p, b->S.p, vsel, gate);
   SELF_LAUNCHED(b->ctx);
   return SELF_OK;
 }
@@ -757,14 +852,15 @@ template <typename R>
 int enqueue_inner(self_cgbatch* b) {
   cudaStream_t st = b->ctx->stream;
   const TileView V = b->inner.dev();
-  bk_start<R><<<b->grid, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p);
+  const int ge = (int)b->inner.cap_e, gv = (int)b->inner.cap_v;
+  bk_start<R><<<gv, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p);
   SELF_LAUNCHED(b->ctx);
   for (int k = 0; k < b->graph_k; ++k) {
-    bk_apply<R><<<b->grid, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->DT.p, b->partial.p, b->ticket.p);
+    bk_apply<R><<<ge, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->DT.p, b->partial.p, b->ticket.p);
     SELF_LAUNCHED(b->ctx);
     int rc;
-    if ((rc = k_dss<R>(b, b->inner, V_Z, 0))) return rc;
-    bk_update<R><<<b->grid, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->cap_vt, b->ticket.p);
+    if ((rc = k_dss<R>(b, b->inner, V_Z, 0, true))) return rc;
+    bk_update<R><<<gv, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->inner.cap_v, b->ticket.p);
     SELF_LAUNCHED(b->ctx);
   }
   return SELF_OK;
@@ -788,12 +884,14 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
   if (!outer_set.empty()) {
     if ((rc = ensure_view(b, b->outer, outer_set))) return rc;
     const TileView V = b->outer.dev();
+    const int gv = std::max(1, b->outer.n_v);
     if (fp32) {  // x += u32 for problems whose inner solve ended
-      bk_correct<<<b->grid, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p);
+      bk_correct<<<gv, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p);
       SELF_LAUNCHED(ctx);
     }
-    if ((rc = k_apply_plain<double>(b, b->outer, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, b->outer, V_R, 1))) return rc;
-    bk_rr<<<b->grid, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p, b->red.p);
+    if ((rc = k_apply_plain<double>(b, b->outer, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, b->outer, V_R, 1, false)))
+      return rc;
+    bk_rr<<<gv, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p, b->red.p);
     SELF_LAUNCHED(ctx);
     std::vector<double> rr(b->cap);
     SELF_CUDA_TRY(ctx, cudaMemcpyAsync(rr.data(), b->red.p, b->cap * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1125,10 +1223,10 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
   for (int N = 2; N <= 9; ++N)
     for (int bk = 0; bk < 4; ++bk) {
       if (!present[N][bk] || b->epb[N][bk] > 0) continue;
-      const int mx = max_epb_rt(N);
-      int best = mx;
+      const int r = max_epb_rt(N);
+      int best = default_tile_elems(N);
       double best_ms = 1e30;
-      for (int e = mx;; e = std::max(1, e / 2)) {
+      for (int e = r; e <= 32 * r; e *= 2) {  // element tiles of 1, 2, 4, ... 32 rounds
         if ((rc = upload_view(b, b->tune, used, N, bk, e))) return rc;
         for (int w = 0; w < 2; ++w)
           if ((rc = k_apply_plain<float>(b, b->tune, V_V, V_Z, 0, 0))) return rc;
@@ -1141,7 +1239,6 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
           best_ms = ms;
           best = e;
         }
-        if (e == 1) break;
       }
       b->epb[N][bk] = best;
     }
@@ -1168,7 +1265,7 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
 
 int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* epb) {
   if (!b || N < 2 || N > 9 || bucket < 0 || bucket > 3 || !epb) return SELF_ERR_INVALID;
-  *epb = b->epb[N][bucket] > 0 ? b->epb[N][bucket] : max_epb_rt(N);
+  *epb = b->epb[N][bucket] > 0 ? b->epb[N][bucket] : default_tile_elems(N);
   return SELF_OK;
 }
 

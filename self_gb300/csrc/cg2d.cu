@@ -240,8 +240,9 @@ __device__ __forceinline__ bool grid_sums_last(const R (&v)[NS], double* __restr
   return true;
 }
 
-// Element groups of EPB elements per pass, grid-stride over the groups (1-D blocks of 256 threads: thread t works
-// on node t % NN of element t / NN of the group; threads beyond EPB * NN only join the reductions).
+// Element groups of EPB elements, grid-stride over the groups, P groups per pass (1-D blocks of 256 threads:
+// thread t works on node t % NN of element t / NN of each group; threads beyond EPB * NN only join the
+// reductions).  With P = 2 (FP32) every thread has two independent chains of loads in flight.
 template <int N1, typename R, int NF>
 __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restrict__ w, const R* __restrict__ vold,
                                                                R* __restrict__ vnew, const int* __restrict__ src,
@@ -252,11 +253,12 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
   if (S->done) return;
   constexpr int NN = N1 * N1;
   constexpr int EPB = cg_epb<N1>();
+  constexpr int P = sizeof(R) == 4 ? 2 : 1;
   static_assert(EPB * NN <= kRedThreads, "one element group per block pass");
   __shared__ R D[N1 * N1];
-  __shared__ R su[EPB][NN];
-  __shared__ R s1[EPB][NN];
-  __shared__ R s2[EPB][NN];
+  __shared__ R su[P][EPB][NN];
+  __shared__ R s1[P][EPB][NN];
+  __shared__ R s2[P][EPB][NN];
   const int tid = threadIdx.x % NN, le = threadIdx.x / NN;
   for (int t = threadIdx.x; t < N1 * N1; t += kRedThreads) D[t] = Cg.D[t];
   const bool first = S->iter == 0;
@@ -264,53 +266,76 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
   const int i = tid % N1, j = tid / N1;
   const int ngroups = (nEl + EPB - 1) / EPB;
   R pa = 0;
-  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-    const int e = grp * EPB + le;
-    const bool active = le < EPB && e < nEl;
-    const size_t l = (size_t)e * NN + tid;
-    // every independent load of the node first (index, own w and v, folded factors), then the gathers
-    R u = 0, G11 = 0, G12 = 0, G22 = 0, M = 0, B1 = 0, B2 = 0;
-    if (active) {
-      const int sl = src[l];
-      const R wl = w[l], vl = first ? R(0) : vold[l];
-      const R* fe = fac + (size_t)e * NF * NN;
-      G11 = fe[tid];
-      G12 = fe[NN + tid];
-      G22 = fe[2 * NN + tid];
-      M = fe[3 * NN + tid];
+  for (int g0 = blockIdx.x * P; g0 < ngroups; g0 += gridDim.x * P) {
+    // every independent load of the P nodes first (index, own w and v, folded factors), then the gathers
+    bool active[P];
+    size_t l[P];
+    int e[P];
+    R u[P], G11[P], G12[P], G22[P], M[P], B1[P], B2[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      e[q] = (g0 + q) * EPB + le;
+      active[q] = le < EPB && g0 + q < ngroups && e[q] < nEl;
+      l[q] = (size_t)e[q] * NN + tid;
+      u[q] = G11[q] = G12[q] = G22[q] = M[q] = B1[q] = B2[q] = R(0);
+    }
+    int sl[P];
+    R wl[P], vl[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      if (!active[q]) continue;
+      sl[q] = src[l[q]];
+      wl[q] = w[l[q]];
+      vl[q] = first ? R(0) : vold[l[q]];
+      const R* fe = fac + (size_t)e[q] * NF * NN;
+      G11[q] = fe[tid];
+      G12[q] = fe[NN + tid];
+      G22[q] = fe[2 * NN + tid];
+      M[q] = fe[3 * NN + tid];
       if (NF == 6) {
-        B1 = fe[4 * NN + tid];
-        B2 = fe[5 * NN + tid];
+        B1[q] = fe[4 * NN + tid];
+        B2[q] = fe[5 * NN + tid];
       }
-      const R ws = w[sl], vs = first ? R(0) : vold[sl];
-      u = first ? ws : ws + beta * vs;
-      vnew[l] = first ? wl : wl + beta * vl;
+    }
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      if (!active[q]) continue;
+      const R ws = w[sl[q]], vs = first ? R(0) : vold[sl[q]];
+      u[q] = first ? ws : ws + beta * vs;
+      vnew[l[q]] = first ? wl[q] : wl[q] + beta * vl[q];
     }
     __syncthreads();  // D loaded / previous pass done with the scratch arrays
-    if (active) su[le][tid] = u;
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+      if (active[q]) su[q][le][tid] = u[q];
     __syncthreads();
-    R us = 0, up = 0;
-    if (active) {
+    R us[P], up[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      us[q] = up[q] = R(0);
+      if (!active[q]) continue;
 #pragma unroll
       for (int m = 0; m < N1; ++m) {
-        us += D[i + N1 * m] * su[le][m + N1 * j];
-        up += D[j + N1 * m] * su[le][i + N1 * m];
+        us[q] += D[i + N1 * m] * su[q][le][m + N1 * j];
+        up[q] += D[j + N1 * m] * su[q][le][i + N1 * m];
       }
-      s1[le][tid] = G11 * us + G12 * up;
-      s2[le][tid] = G12 * us + G22 * up;
+      s1[q][le][tid] = G11[q] * us[q] + G12[q] * up[q];
+      s2[q][le][tid] = G12[q] * us[q] + G22[q] * up[q];
     }
     __syncthreads();
-    if (active) {
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      if (!active[q]) continue;
       R a = 0, b = 0;
 #pragma unroll
       for (int m = 0; m < N1; ++m) {
-        a += D[m + N1 * i] * s1[le][m + N1 * j];
-        b += D[m + N1 * j] * s2[le][i + N1 * m];
+        a += D[m + N1 * i] * s1[q][le][m + N1 * j];
+        b += D[m + N1 * j] * s2[q][le][i + N1 * m];
       }
-      R Lu = -(a + b) - M * u;
-      if (NF == 6) Lu -= B1 * us + B2 * up;
-      z[l] = Lu;
-      pa += u * Lu;
+      R Lu = -(a + b) - M[q] * u[q];
+      if (NF == 6) Lu -= B1[q] * us[q] + B2[q] * up[q];
+      z[l[q]] = Lu;
+      pa += u[q] * Lu;
     }
   }
   const R acc[1] = {pa};
@@ -599,7 +624,19 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
                           const std::vector<R>& D) {
   CGConst<N1, R> C;
   for (int k = 0; k < N1 * N1; ++k) C.D[k] = D[k];
-  pcg_apply_fused<N1, R, NF><<<h->apply_grid, kRedThreads, 0, h->ctx->stream>>>(
+  // one wave of resident blocks (at most apply_grid, for which the partial sums are sized)
+  static int resident[2][11][2] = {};  // per precision, degree and operator: blocks per SM (0 = not queried)
+  int& nb = resident[sizeof(R) == 4][N1][NF == 6];
+  if (nb == 0) {
+    int q = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused<N1, R, NF>, kRedThreads, 0) != cudaSuccess)
+      q = 4;
+    nb = std::max(1, q);
+  }
+  constexpr int P = sizeof(R) == 4 ? 2 : 1;
+  const int groups = (h->nEl + cg_epb<N1>() - 1) / cg_epb<N1>();
+  const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), (groups + P - 1) / P}));
+  pcg_apply_fused<N1, R, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
       w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
 }
 
