@@ -261,7 +261,7 @@ def _e2e(nat, L, ctx, sw, dof, steps, dist):
 
 # DRAM bytes (read + write) of one launch from the ncu --set full captures summarised in
 # profiles/sw32_fused_sw128_n7.md (launch 0) and profiles/dg_volume_fp64_sw128_n7.md (launch 1)
-NCU_TRAFFIC_BYTES = {"sw32_fused": 85.29e6, "dg_volume": 128.2e6}
+NCU_TRAFFIC_BYTES = {"sw32_fused": 85.59e6, "dg_volume": 128.2e6}
 
 FLOPS_PER_EL_STAGE_N7 = 14.0e3  # algorithmic FP64 flops of one element-stage at N=7 (traces, fluxes, contractions,
 #                                 lift, 1/J, sources, RK update, Riemann), the count of the design notes

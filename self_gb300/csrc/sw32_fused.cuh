@@ -313,26 +313,26 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       const int flags = es.b_flags & 0xff, bb = es.b_flags >> 8;
       const float* egs = &B.eg[side * 5 * N1];
       const float nx = egs[k], ny = egs[N1 + k], len = egs[2 * N1 + k], hP = egs[3 * N1 + k], hS = egs[4 * N1 + k];
-      float own[3], oth[3], f[3];
+      float own[3], oth[3], in[3], ex[3], f[3];
 #pragma unroll
       for (int v = 0; v < 3; ++v) own[v] = ws.sT[k + N1 * v + 3 * N1 * side];
-      float sgn = 1.f;
-      if (es.nbr >= 0) {
-        const int kn = es.a + bb * k;
+      // one flux evaluation for every lane (no divergence between the interior-primary, interior-secondary and
+      // wall sides of the warp): the external state and the orientation are selected, hS = hP on walls.
+      // A wall side has a = 0, b = 1, so kn stays a valid index; its neighbour slot is not read into the flux.
+      const bool interior = es.nbr >= 0;
+      const bool primary = !interior || (flags & 1);
+      const int kn = es.a + bb * k;
+      const float mirror0 = (ny * ny - nx * nx) * own[0] - 2.0f * nx * ny * own[1];  // NO_NORMAL_FLOW
+      const float mirror1 = (nx * nx - ny * ny) * own[1] - 2.0f * nx * ny * own[0];
 #pragma unroll
-        for (int v = 0; v < 3; ++v) oth[v] = B.nb[side * 3 * N1 + v * N1 + kn];
-        if (flags & 1) {
-          riemann_pert(own, oth, hP, hS, nx, ny, A.g, f);
-        } else {
-          riemann_pert(oth, own, hP, hS, nx, ny, A.g, f);
-          sgn = -1.f;
-        }
-      } else {
-        oth[0] = (ny * ny - nx * nx) * own[0] - 2.0f * nx * ny * own[1];  // mirror (NO_NORMAL_FLOW)
-        oth[1] = (nx * nx - ny * ny) * own[1] - 2.0f * nx * ny * own[0];
-        oth[2] = own[2];
-        riemann_pert(own, oth, hP, hP, nx, ny, A.g, f);
+      for (int v = 0; v < 3; ++v) {
+        const float nbv = B.nb[side * 3 * N1 + v * N1 + kn];
+        oth[v] = interior ? nbv : (v == 0 ? mirror0 : v == 1 ? mirror1 : own[2]);
+        in[v] = primary ? own[v] : oth[v];
+        ex[v] = primary ? oth[v] : own[v];
       }
+      riemann_pert(in, ex, hP, hS, nx, ny, A.g, f);
+      const float sgn = primary ? 1.f : -1.f;
 #pragma unroll
       for (int v = 0; v < 3; ++v) ws.sB[k + N1 * v + 3 * N1 * side] = sgn * (f[v] * len);
     }
