@@ -128,9 +128,9 @@ def bytes_per_volume_launch(nEl, n, prec_bytes):
 def bytes_per_fused_launch(nEl, n):
     """Algorithmic HBM bytes of one fused FP32 stage (edge fluxes inside): q r/w, G r/w, 5 metric fields,
     4 aux fields, 3 lake-at-rest tendency fields, per-side edge data (nx, ny, |n|, hP, hS per side node),
-    the 4 neighbours' traces read and the element's new traces written."""
+    the element's own and its 4 neighbours' traces read and the element's new traces written."""
     nn = n * n
-    return 4 * (4 * 3 * nn + 5 * nn + 4 * nn + 3 * nn + 4 * 5 * n + 2 * 4 * 3 * n) * nEl
+    return 4 * (4 * 3 * nn + 5 * nn + 4 * nn + 3 * nn + 4 * 5 * n + 3 * 4 * 3 * n) * nEl
 
 
 def cpu_baseline(oracle, nod, mesh, q, h, fcor, dhdx, dhdy, dt, budget_s=12.0, max_steps=5000):

@@ -4,10 +4,11 @@
 // worker that owns one element at a time (N = 7: 64 nodes, two per lane) and walks over the elements
 // e = warp, warp + total warps, ... with its own NBUF-deep pipeline: lanes of the warp issue 1-D TMA bulk
 // copies (cp.async.bulk ... mbarrier::complete_tx) of the element blocks of a later element -- state q, RK
-// register G, metrics, aux fields, lake-at-rest tendency, per-side edge data and the neighbours' boundary
-// traces -- into the warp's shared-memory buffers while the warp computes the current one.  No block-wide
+// register G, metrics, aux fields, lake-at-rest tendency, per-side edge data, its own and the neighbours'
+// boundary traces -- into the warp's shared-memory buffers while the warp computes the current one.  No block-wide
 // barrier is used after set-up; phases inside an element synchronise with __syncwarp.  Per element:
-//   1. traces of the element's own state (warp shuffles over the registers of the node pairs);
+//   1. traces of the element's own state: staged with the element (the previous stage wrote them, by warp
+//      shuffles over the registers of its node pairs, together with the new state);
 //   2. LLF flux at the 32 side nodes (one per lane), evaluated exactly as the edge's primary element sees it
 //      (primary trace "in", secondary trace "ex", primary normal and length), +flux on the primary side and
 //      -flux on the secondary side, so both elements use bitwise-identical values as in EdgeFlux
@@ -134,13 +135,13 @@ struct alignas(16) WarpBuf {
   float R0[S::R];
   float eg[S::EG];
   float nb[S::NB];  // neighbour traces per side (the neighbour's side, neighbour node order)
+  float own[S::NB];  // the element's own traces (written by the previous stage), t = k + N1 v + 3 N1 side
 };
 
 template <int N1, int NBUF>
 struct alignas(16) WarpSmem {
   WarpBuf<N1> buf[NBUF];
   ESide es[NBUF][4];
-  float sT[4 * 3 * N1];  // own traces, t = k + N1 * v + 3 * N1 * side
   float sB[4 * 3 * N1];  // side fluxes, same order
   uint64_t bar[NBUF];
   uint64_t pad[NBUF & 1];
@@ -229,10 +230,11 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   const int nwarps = gridDim.x * W;
   const int gw = blockIdx.x * W + wid;
   const long long kMaxSpin = 1LL << 20;  // try_wait polls; normal waits end within microseconds
-  const uint32_t base_bytes = 4u * (S::Q + S::M + (uint32_t)A.naux * NN + S::R + S::EG) + (MODE == 2 ? 4u * S::G : 0u);
+  const uint32_t base_bytes =
+      4u * (S::Q + S::M + (uint32_t)A.naux * NN + S::R + S::EG + S::NB) + (MODE == 2 ? 4u * S::G : 0u);
 
   // issue the bulk copies of element e into buffer b: lanes 0-3 the neighbour traces of side = lane, lanes
-  // 4-9 the element blocks; the byte count is posted before any copy is issued
+  // 4-10 the element blocks; the byte count is posted before any copy is issued
   // side records of element e (lanes 0-3), loaded one iteration before the element's copies are issued
   auto load_es = [&](int e) {
     ESide es;
@@ -262,6 +264,8 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       bulk_g2s(B.R0, A.R0 + e * S::R, 4u * S::R, &ws.bar[b]);
     else if (lane == 8)
       bulk_g2s(B.eg, A.eg + e * S::EG, 4u * S::EG, &ws.bar[b]);
+    else if (lane == 10)
+      bulk_g2s(B.own, A.bs_in + e * S::NB, 4u * S::NB, &ws.bar[b]);
     else if (MODE == 2 && lane == 9)
       bulk_g2s(B.G, A.G + e * S::G, 4u * S::G, &ws.bar[b]);
   };
@@ -301,9 +305,8 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
 #pragma unroll
     for (int c = 0; c < 5; ++c) m2[c] = *reinterpret_cast<const float2*>(&B.met[c * NN + node]);
     const float2 h2 = *reinterpret_cast<const float2*>(&B.aux[3 * NN + node]);
-    // 1. own traces
-    traces_shfl(q2, lSj, lNj, lEa, lEb, lWa, lWb, lane, i, j, ws.sT);
-    __syncwarp();  // q and met are free (scratch) and the own traces are visible
+    // 1. own traces: the previous stage wrote them with the new state (staged with the element)
+    __syncwarp();  // q and met are free (scratch)
     float* sF = B.q;            // [3][NN], natural order
     float* sGt = B.q + 3 * NN;  // [3][N1 rows of 12]: sGt[v][m + 12 i] = G_v(i, m)
     // 2. side fluxes: lane = (side, k)
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       const float nx = egs[k], ny = egs[N1 + k], len = egs[2 * N1 + k], hP = egs[3 * N1 + k], hS = egs[4 * N1 + k];
       float own[3], oth[3], in[3], ex[3], f[3];
 #pragma unroll
-      for (int v = 0; v < 3; ++v) own[v] = ws.sT[k + N1 * v + 3 * N1 * side];
+      for (int v = 0; v < 3; ++v) own[v] = B.own[k + N1 * v + 3 * N1 * side];
       // one flux evaluation for every lane (no divergence between the interior-primary, interior-secondary and
       // wall sides of the warp): the external state and the orientation are selected, hS = hP on walls.
       // A wall side has a = 0, b = 1, so kn stays a valid index; its neighbour slot is not read into the flux.
