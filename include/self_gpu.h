@@ -75,7 +75,8 @@ int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
 /* Measured fused-multiply-add rate of the device (TFLOP/s, FP64 when fp64 != 0 else FP32): the compute
  * roofline used for kernels bound by the FP64 pipe. */
 int self_probe_fma_peak(self_ctx* ctx, int fp64, double* tflops);
-/* Page-locked host memory for host<->device copies at full link speed. */
+/* Page-locked, device-mapped host memory for host<->device transfers at full link speed.  State arrays in such a
+ * block are read and written by the conversion kernels directly (no staging copy). */
 int self_host_alloc(size_t bytes, void** ptr);
 int self_host_free(void* ptr);
 

@@ -713,9 +713,14 @@ int set_state(self_dg2d* hd, State* s, const double* q) {
   self_ctx* ctx = handle_ctx(hd);
   int rc = ensure_staging(ctx, s);
   if (rc) return rc;
-  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->stage64.p, q, s->stage64.bytes(), cudaMemcpyHostToDevice, ctx->stream));
+  // a block from self_host_alloc is read by the conversion kernel directly; other memory goes through staging
+  const double* src = static_cast<const double*>(selfgpu::mapped_host(q, s->q.n * sizeof(double)));
+  if (!src) {
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(s->stage64.p, q, s->stage64.bytes(), cudaMemcpyHostToDevice, ctx->stream));
+    src = s->stage64.p;
+  }
   const size_t NN = (size_t)s->n * s->n;
-  to_pert<<<2 * ctx->num_sms * 4, 256, 0, ctx->stream>>>(s->q.p, s->stage64.p, s->h64.p, NN, s->nEq, s->sw, s->q.n);
+  to_pert<<<2 * ctx->num_sms * 4, 256, 0, ctx->stream>>>(s->q.p, src, s->h64.p, NN, s->nEq, s->sw, s->q.n);
   SELF_LAUNCHED(ctx);
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->traces_valid = false;
@@ -727,9 +732,12 @@ int get_state(self_dg2d* hd, State* s, double* q) {
   int rc = ensure_staging(ctx, s);
   if (rc) return rc;
   const size_t NN = (size_t)s->n * s->n;
-  from_pert<<<2 * ctx->num_sms * 4, 256, 0, ctx->stream>>>(s->stage64.p, s->q.p, s->h64.p, NN, s->nEq, s->sw, s->q.n);
+  double* dst = static_cast<double*>(selfgpu::mapped_host(q, s->q.n * sizeof(double)));
+  from_pert<<<2 * ctx->num_sms * 4, 256, 0, ctx->stream>>>(dst ? dst : s->stage64.p, s->q.p, s->h64.p, NN, s->nEq,
+                                                           s->sw, s->q.n);
   SELF_LAUNCHED(ctx);
-  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(q, s->stage64.p, s->stage64.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dst)
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(q, s->stage64.p, s->stage64.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return SELF_OK;
 }

@@ -69,4 +69,10 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
 };
 
+// Device-visible address of the host range [p, p + bytes) when it lies inside one block returned by
+// self_host_alloc (page-locked and mapped), else null: such buffers are read and written by kernels directly.
+void host_blocks_add(const void* p, size_t bytes);
+void host_blocks_remove(const void* p);
+void* mapped_host(const void* p, size_t bytes);
+
 }  // namespace selfgpu

@@ -10,6 +10,45 @@
 
 #include "internal.hpp"
 
+#include <map>
+
+namespace selfgpu {
+
+// Page-locked, mapped host blocks handed out by self_host_alloc (start -> size).
+namespace {
+std::mutex g_host_mu;
+std::map<uintptr_t, size_t> g_host_blocks;
+}  // namespace
+
+void host_blocks_add(const void* p, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  g_host_blocks[reinterpret_cast<uintptr_t>(p)] = bytes;
+}
+
+void host_blocks_remove(const void* p) {
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  g_host_blocks.erase(reinterpret_cast<uintptr_t>(p));
+}
+
+void* mapped_host(const void* p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = g_host_blocks.upper_bound(a);
+    if (it == g_host_blocks.begin()) return nullptr;
+    --it;
+    if (a < it->first || a + bytes > it->first + it->second) return nullptr;
+  }
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, const_cast<void*>(p), 0) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return d;
+}
+
+}  // namespace selfgpu
+
 namespace selfgpu {
 
 static std::mutex g_err_mu;
@@ -294,13 +333,17 @@ int self_ctx_flush_l2(self_ctx* ctx, size_t bytes) {
 
 int self_host_alloc(size_t bytes, void** ptr) {
   if (!ptr) return SELF_ERR_INVALID;
-  cudaError_t e = cudaMallocHost(ptr, bytes);
-  if (e != cudaSuccess) return set_error(nullptr, SELF_ERR_ALLOC, "cudaMallocHost: %s", cudaGetErrorString(e));
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e != cudaSuccess) return set_error(nullptr, SELF_ERR_ALLOC, "cudaHostAlloc: %s", cudaGetErrorString(e));
+  selfgpu::host_blocks_add(*ptr, bytes);
   return SELF_OK;
 }
 
 int self_host_free(void* ptr) {
-  if (ptr) cudaFreeHost(ptr);
+  if (ptr) {
+    selfgpu::host_blocks_remove(ptr);
+    cudaFreeHost(ptr);
+  }
   return SELF_OK;
 }
 

@@ -223,10 +223,9 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   const float lNj = C.lN[j], lSj = C.lS[j], qwj = C.qwinv[j];
 
   // Programmatic dependent launch: the next stage's CTAs may be scheduled as this grid's CTAs retire, and this
-  // grid's set-up above overlaps the previous stage's tail; every read or write of data the previous stage
-  // touches (state, RK register, traces) comes after the wait for that stage's completion.
+  // grid's set-up overlaps the previous stage's tail; every read or write of data the previous stage touches
+  // (state, RK register, traces) comes after the wait for that stage's completion (griddepcontrol.wait below).
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int nwarps = gridDim.x * W;
   const int gw = blockIdx.x * W + wid;
   const long long kMaxSpin = 1LL << 20;  // try_wait polls; normal waits end within microseconds
@@ -234,7 +233,9 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
       4u * (S::Q + S::M + (uint32_t)A.naux * NN + S::R + S::EG + S::NB) + (MODE == 2 ? 4u * S::G : 0u);
 
   // issue the bulk copies of element e into buffer b: lanes 0-3 the neighbour traces of side = lane, lanes
-  // 4-10 the element blocks; the byte count is posted before any copy is issued
+  // 4-10 the element blocks; the byte count is posted before any copy is issued.  part 1 posts the count and
+  // copies only the blocks no stage writes (metrics, aux, R0, side geometry), part 2 the rest (state, RK
+  // register, traces), part 0 everything.
   // side records of element e (lanes 0-3), loaded one iteration before the element's copies are issued
   auto load_es = [&](int e) {
     ESide es;
@@ -242,39 +243,52 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
     if (lane < 4 && e < A.nEl) es = A.es[e * 4 + lane];
     return es;
   };
-  auto issue = [&](int e, int b, const ESide& es) {
-    if (lane < 4) ws.es[b][lane] = es;
+  auto issue = [&](int e, int b, const ESide& es, int part) {
     const bool hasnb = lane < 4 && es.nbr >= 0;
-    const unsigned nbm = __ballot_sync(0xffffffffu, hasnb);
-    fence_proxy_async();  // earlier generic accesses of this buffer before the async-proxy writes
-    __syncwarp();
-    if (lane == 0) mbar_expect_tx(&ws.bar[b], base_bytes + (uint32_t)__popc(nbm) * 4u * 3u * N1);
-    __syncwarp();
+    if (part != 2) {
+      if (lane < 4) ws.es[b][lane] = es;
+      const unsigned nbm = __ballot_sync(0xffffffffu, hasnb);
+      fence_proxy_async();  // earlier generic accesses of this buffer before the async-proxy writes
+      __syncwarp();
+      if (lane == 0) mbar_expect_tx(&ws.bar[b], base_bytes + (uint32_t)__popc(nbm) * 4u * 3u * N1);
+      __syncwarp();
+    }
     WarpBuf<N1>& B = ws.buf[b];
-    if (hasnb)
-      bulk_g2s(&B.nb[lane * 3 * N1], A.bs_in + 3 * N1 * (es.nside + 4 * es.nbr), 4u * 3u * N1,
-               &ws.bar[b]);
-    else if (lane == 4)
-      bulk_g2s(B.q, A.q + e * S::Q, 4u * S::Q, &ws.bar[b]);
-    else if (lane == 5)
-      bulk_g2s(B.met, A.met + e * S::M, 4u * S::M, &ws.bar[b]);
-    else if (lane == 6)
-      bulk_g2s(B.aux, A.aux + e * A.naux * NN, 4u * A.naux * NN, &ws.bar[b]);
-    else if (lane == 7)
-      bulk_g2s(B.R0, A.R0 + e * S::R, 4u * S::R, &ws.bar[b]);
-    else if (lane == 8)
-      bulk_g2s(B.eg, A.eg + e * S::EG, 4u * S::EG, &ws.bar[b]);
-    else if (lane == 10)
-      bulk_g2s(B.own, A.bs_in + e * S::NB, 4u * S::NB, &ws.bar[b]);
-    else if (MODE == 2 && lane == 9)
-      bulk_g2s(B.G, A.G + e * S::G, 4u * S::G, &ws.bar[b]);
+    const bool stat = part != 2, dyn = part != 1;
+    if (hasnb) {
+      if (dyn)
+        bulk_g2s(&B.nb[lane * 3 * N1], A.bs_in + 3 * N1 * (es.nside + 4 * es.nbr), 4u * 3u * N1, &ws.bar[b]);
+    } else if (lane == 4) {
+      if (dyn) bulk_g2s(B.q, A.q + e * S::Q, 4u * S::Q, &ws.bar[b]);
+    } else if (lane == 5) {
+      if (stat) bulk_g2s(B.met, A.met + e * S::M, 4u * S::M, &ws.bar[b]);
+    } else if (lane == 6) {
+      if (stat) bulk_g2s(B.aux, A.aux + e * A.naux * NN, 4u * A.naux * NN, &ws.bar[b]);
+    } else if (lane == 7) {
+      if (stat) bulk_g2s(B.R0, A.R0 + e * S::R, 4u * S::R, &ws.bar[b]);
+    } else if (lane == 8) {
+      if (stat) bulk_g2s(B.eg, A.eg + e * S::EG, 4u * S::EG, &ws.bar[b]);
+    } else if (lane == 10) {
+      if (dyn) bulk_g2s(B.own, A.bs_in + e * S::NB, 4u * S::NB, &ws.bar[b]);
+    } else if (MODE == 2 && lane == 9) {
+      if (dyn) bulk_g2s(B.G, A.G + e * S::G, 4u * S::G, &ws.bar[b]);
+    }
   };
 
-  // prologue: elements of iterations 0 .. NBUF-2
+  // prologue: elements of iterations 0 .. NBUF-2; their blocks that no stage writes are requested before the
+  // wait for the previous stage (they overlap its tail), the others after it
+  ESide es_pro[NBUF > 1 ? NBUF - 1 : 1];
 #pragma unroll
   for (int k = 0; k < NBUF - 1; ++k) {
     const int e = gw + k * nwarps;
-    if (e < A.nEl) issue(e, k, load_es(e));
+    es_pro[k] = load_es(e);
+    if (e < A.nEl) issue(e, k, es_pro[k], 1);
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < NBUF - 1; ++k) {
+    const int e = gw + k * nwarps;
+    if (e < A.nEl) issue(e, k, es_pro[k], 2);
   }
   ESide es_next = load_es(gw + (NBUF - 1) * nwarps);
   int it = 0;
@@ -283,7 +297,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
     {
       const int ef = e + (NBUF - 1) * nwarps;  // buffer (b + NBUF - 1) % NBUF was released by iteration it - 1
       if (ef < A.nEl) {
-        issue(ef, (b + NBUF - 1) % NBUF, es_next);
+        issue(ef, (b + NBUF - 1) % NBUF, es_next, 0);
         es_next = load_es(ef + nwarps);
       }
     }

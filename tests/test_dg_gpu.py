@@ -249,3 +249,35 @@ def test_fp32_sw_rk3_close_to_oracle(oracle, gpu_ctx):
     hh = h.reshape(mesh.nEl, -1)
     assert rel_inf(got[:, 0], ref[:, 0]) < 1e-5 and rel_inf(got[:, 1], ref[:, 1]) < 1e-5
     assert rel_inf(got[:, 2] - hh, ref[:, 2] - hh) < 1e-5
+
+
+def test_fp32_state_through_mapped_host_buffer_matches_staged_path(oracle, gpu_ctx):
+    """A state in a self_host_alloc block is converted on the device straight from / into host memory; the
+    result of set -> 5 steps -> get is bit-identical to the staged path with ordinary host arrays."""
+    import ctypes as C
+    import self_gb300 as sg
+    nat = sg._native
+    N, nx = 7, 6
+    nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, _, _ = _sw_problem(oracle, N, nx, flow=True)
+    sw = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy, precision=nat.PREC_FP32)
+    sw.SetSolution(q)
+    sw.ForwardStepRK3(0.0, 5)
+    staged = sw.GetSolution()
+    L = nat.lib()
+    ptrs = []
+    try:
+        for _ in range(2):
+            p = C.c_void_p()
+            nat.check(L.self_host_alloc(C.c_size_t(q.size * 8), C.byref(p)))
+            ptrs.append(p)
+        hin = np.ctypeslib.as_array((C.c_double * q.size).from_address(ptrs[0].value))
+        hout = np.ctypeslib.as_array((C.c_double * q.size).from_address(ptrs[1].value))
+        hin[:] = q
+        hout[:] = np.nan
+        nat.check(L.self_dg2d_set_state(sw.ptr, C.cast(ptrs[0], nat.dp)), gpu_ctx.ptr)
+        nat.check(L.self_dg2d_rk3(sw.ptr, C.c_double(0.0), 5), gpu_ctx.ptr)
+        nat.check(L.self_dg2d_get_state(sw.ptr, C.cast(ptrs[1], nat.dp)), gpu_ctx.ptr)
+        assert np.array_equal(hout, staged)
+    finally:
+        for p in ptrs:
+            L.self_host_free(p)
