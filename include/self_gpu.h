@@ -58,6 +58,7 @@ typedef struct self_ctx self_ctx;
 /* One context per (process, device).  Replaces nothing in the reference (its drivers run on the
  * host); it carries the CUDA device, stream and the last error text. */
 int self_ctx_create(int device, self_ctx** out);
+/* Destroy every handle created on a context before the context itself. */
 int self_ctx_destroy(self_ctx* ctx);
 int self_last_error(const self_ctx* ctx, char* buf, size_t len);
 const char* self_status_string(int status);
@@ -141,11 +142,31 @@ int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* m
 
 /* Known answer helpers for the shallow-water set-up (host, FP64):
  * CalculateBathymetryGradient (ConservativeShallowWaterClass.f90:1733-1868). */
+/* ReadSpecMeshFile_QuadMesh (QuadMeshClass.f90:2100-2475): an ISM-V2 (SpecMesh) file.  counts first, then
+ * build into arrays of the sizes self_mesh_build uses; corner nodes, transfinite element geometry from the
+ * file's side curves, edges rebuilt from the elements (first-appearance order), boundary flags from the side
+ * names (unnamed boundary sides are SELF_NO_NORMAL_FLOW). */
+int self_mesh_ism_counts(const char* path, int* nEl, int* nEdges, int* nNodes, int* geomDegree);
+int self_mesh_ism_build(const char* path, int N, int quadrature, int* edges, int* elemNodes, int* nodeType,
+                        int* n2e_ptr, int* n2e_elem, int* n2e_local, double* x, double* y, double* dxds,
+                        double* dxdp, double* dyds, double* dydp, double* J, double* nhx, double* nhy,
+                        double* nlen, double* bx, double* by);
+
 int self_sw_bathymetry_gradient(int N, int nEl, const double* dmatS, const double* dmatP, const double* qweight,
                                 const double* lagW, const double* lagE, const double* lagS, const double* lagN,
                                 const double* dxds, const double* dxdp, const double* dyds, const double* dydp,
                                 const double* J, const double* nhx, const double* nhy, const double* nlen,
                                 const double* h, double* dhdx, double* dhdy);
+
+/* ---------------------------------------------------------------- pickup (checkpoint) files
+ * The reference's restart format (WritePickup/ReadPickup_ShallowWater, ConservativeShallowWaterClass.f90:
+ * 2013-2130; _Advection, AdvectionClass.f90:2040-2171): direct-access, big-endian, unformatted records of
+ * (N+1)^2 doubles, no record markers.  For every element, for every field f in order, recs[f] records come
+ * from fields[f] + (e * recs[f] + r) * (N+1)^2.  Shallow water: {state (3), bathymetry h (1), f (1)};
+ * advection: {state (nEq), relaxation field (nEq), relaxation factor (nEq), u (1), v (1)}.  On read a null
+ * field is skipped. */
+int self_pickup_write(const char* path, int N, int nEl, int nfields, const double* const* fields, const int* recs);
+int self_pickup_read(const char* path, int N, int nEl, int nfields, double* const* fields, const int* recs);
 
 /* ---------------------------------------------------------------- CGSEM 2-D
  * Replaces CGsemElliptic_2D (CGsemElliptic_2D_Class.f90:57-93) compute procedures on element-local
@@ -173,6 +194,7 @@ typedef struct {
 #define SELF_SOLVE_CG 0           /* conjugate gradient, no preconditioner */
 #define SELF_SOLVE_PCG_JACOBI 1   /* conjugate gradient, assembled-diagonal (Jacobi) preconditioner */
 #define SELF_SOLVE_GMRES 2        /* GMRES(m), modified Gram-Schmidt + Givens */
+#define SELF_SOLVE_PGMRES_JACOBI 3 /* flexible right-preconditioned GMRES(m) (Solve_PCGMRES), Jacobi */
 
 typedef struct {
   int method;             /* SELF_SOLVE_* */

@@ -2,9 +2,9 @@
 // Restates src/cgsem/CGsemElliptic_2D_Class.f90 (SetDirichletBoundaryCondition :234-301, Mask :350-430,
 // MaskSide :434-466, UnMask :470-542, UnMaskSide :546-613, GlobalSum :617-702, SumSide :706-787,
 // CalculateGradient :791-850, FluxDivergence :854-926, MatrixAction :930-976, Residual :980-1068,
-// DotProduct :1072-1110, Solve_PCConjugateGradient :1114-1207) and the GMRES(m) of
+// DotProduct :1072-1110, Solve_PCConjugateGradient :1114-1207), the GMRES(m) of
 // src/highend/Stommel/Stommel_Class.f90 :1161-1322 (= IterativeSolvers_Class.f90 :493-652 on
-// element-local vectors).
+// element-local vectors) and Solve_PCGMRES (IterativeSolvers_Class.f90 :656-822) with Jacobi.
 // Documented decisions (not restatements):
 //  * Mask_CGsemElliptic_2D tests an uninitialised eID (:385-391); the secondary side of every
 //    interior edge is masked, the evident intent;
@@ -461,6 +461,94 @@ int orc_cg_solve_gmres(const orc_cg_problem* p, const double* source, double* so
     for (size_t q = 0; q < nl; ++q) {
       double dd = 0.0;
       for (int k = 1; k <= nr; ++k) dd = dd + V[q + nl * (k - 1)] * y[k - 1];
+      solution[q] = solution[q] + dd;
+    }
+    *iters = l;
+    if (rcur / r0 <= tol) {
+      ioerr = 0;
+      break;
+    }
+    rc = orc_cg_residual(p, source, solution, dir, r.data());
+    if (rc) return rc;
+  }
+  if (rcur / r0 > tol) ioerr = -1;
+  orc_cg_unmask(p, solution);
+  set_dirichlet(p, solution, dir);
+  return ioerr;
+}
+
+// Solve_PCGMRES (IterativeSolvers_Class.f90:656-822): flexible GMRES(m) with variable right preconditioning;
+// PreconditionInvert = Jacobi (z = v / assembled diagonal, 1 on masked nodes).  The preconditioned basis Z is
+// kept and the update is sol += Z y.
+int orc_cg_solve_pgmres(const orc_cg_problem* p, const double* source, double* solution, const double* dir, int m,
+                        int maxIters, double tol, double* resi, int* iters) {
+  const int n = p->N + 1;
+  const size_t nl = (size_t)n * n * p->nEl;
+  std::vector<double> r(nl, 0.0), w(nl), V(nl * (m + 1), 0.0), Z(nl * (m + 1), 0.0), diag(nl);
+  std::vector<double> rho(m * m, 0.0), h((m + 1) * m, 0.0), c(m, 0.0), s(m, 0.0), bhat(m + 1, 0.0), y(m + 1, 0.0);
+  auto RHO = [&](int i, int j) -> double& { return rho[(i - 1) + m * (j - 1)]; };
+  auto H = [&](int i, int j) -> double& { return h[(i - 1) + (m + 1) * (j - 1)]; };
+  orc_cg_jacobi_diagonal(p, diag.data());
+  if (dir) set_dirichlet(p, solution, dir);
+  int ioerr = -2;
+  int rc = orc_cg_residual(p, source, solution, dir, r.data());
+  if (rc) return rc;
+  double r0 = std::sqrt(orc_cg_dot(p, r.data(), r.data()));
+  int l = 0;
+  for (int k = 0; k <= maxIters; ++k) resi[k] = 0.0;
+  resi[0] = r0;
+  double rcur = r0;
+  *iters = 0;
+  if (r0 == 0.0) return 0;
+  for (int j = 1; j <= maxIters; ++j) {
+    double b = std::sqrt(orc_cg_dot(p, r.data(), r.data()));
+    for (size_t k = 0; k < nl; ++k) V[k] = r[k] / b;
+    bhat[0] = b;
+    int nr = 0;
+    for (int i = 1; i <= m; ++i) {
+      l = l + 1;
+      nr = i;
+      double* vi = &V[nl * (i - 1)];
+      double* zi = &Z[nl * (i - 1)];
+      for (size_t q = 0; q < nl; ++q) zi[q] = vi[q] / diag[q];  // PreconditionInvert
+      orc_cg_matrix_action(p, zi, w.data());
+      for (int k = 1; k <= i; ++k) {
+        double* vk = &V[nl * (k - 1)];
+        H(k, i) = orc_cg_dot(p, vk, w.data());
+        double hk = H(k, i);
+        for (size_t q = 0; q < nl; ++q) w[q] = w[q] - hk * vk[q];
+      }
+      H(i + 1, i) = std::sqrt(orc_cg_dot(p, w.data(), w.data()));
+      if (orc::almost_equal(H(i + 1, i), 0.0)) break;
+      double* vn = &V[nl * i];
+      double hn = H(i + 1, i);
+      for (size_t q = 0; q < nl; ++q) vn[q] = w[q] / hn;
+      RHO(1, i) = H(1, i);
+      for (int k = 2; k <= i; ++k) {
+        double g = c[k - 2] * RHO(k - 1, i) + s[k - 2] * H(k, i);
+        RHO(k, i) = -s[k - 2] * RHO(k - 1, i) + c[k - 2] * H(k, i);
+        RHO(k - 1, i) = g;
+      }
+      double d = std::sqrt(std::pow(RHO(i, i), 2) + std::pow(H(i + 1, i), 2));
+      c[i - 1] = RHO(i, i) / d;
+      s[i - 1] = H(i + 1, i) / d;
+      RHO(i, i) = c[i - 1] * RHO(i, i) + s[i - 1] * H(i + 1, i);
+      bhat[i] = -s[i - 1] * bhat[i - 1];
+      bhat[i - 1] = c[i - 1] * bhat[i - 1];
+      rcur = std::fabs(bhat[i]);
+      if (l <= maxIters) resi[l] = rcur;
+      if (rcur / r0 <= tol) break;
+    }
+    if (rcur / r0 > tol) nr = m;
+    y[nr - 1] = bhat[nr - 1] / RHO(nr, nr);
+    for (int k = nr - 1; k >= 1; --k) {
+      y[k - 1] = bhat[k - 1];
+      for (int i = k + 1; i <= nr; ++i) y[k - 1] = y[k - 1] - RHO(k, i) * y[i - 1];
+      y[k - 1] = y[k - 1] / RHO(k, k);
+    }
+    for (size_t q = 0; q < nl; ++q) {
+      double dd = 0.0;
+      for (int k = 1; k <= nr; ++k) dd = dd + Z[q + nl * (k - 1)] * y[k - 1];
       solution[q] = solution[q] + dd;
     }
     *iters = l;

@@ -69,6 +69,13 @@ int orc_mesh_build(int nx, int ny, int periodic_x, int periodic_y, int N, int qu
                    double* x, double* y, double* dxds, double* dxdp, double* dyds, double* dydp, double* J,
                    double* nhx, double* nhy, double* nlen, double* bx, double* by);
 
+/* ---------------- ISM-V2 (SpecMesh) mesh files: ReadSpecMeshFile_QuadMesh (QuadMeshClass.f90:2100-2475) with
+ * transfinite element geometry; the same output arrays as orc_mesh_build. */
+int orc_ism_counts(const char* path, int* nEl, int* nEdges, int* nNodes, int* geomDegree);
+int orc_ism_build(const char* path, int N, int quad, int* edges, int* elemNodes, int* nodeType, int* n2e_ptr,
+                  int* n2e_elem, int* n2e_local, double* x, double* y, double* dxds, double* dxdp, double* dyds,
+                  double* dydp, double* J, double* nhx, double* nhy, double* nlen, double* bx, double* by);
+
 /* ---------------- DGSEM 2-D (ConservativeShallowWaterClass.f90, AdvectionClass.f90) */
 typedef struct {
   int N, nEl, nEdges, nEq;
@@ -120,6 +127,9 @@ int orc_cg_solve_pcg(const orc_cg_problem* p, const double* source, double* solu
                      int maxIters, double tol, int precond, double* resi, int* iters);
 int orc_cg_solve_gmres(const orc_cg_problem* p, const double* source, double* solution, const double* dirichlet,
                        int m, int maxIters, double tol, double* resi, int* iters);
+/* Solve_PCGMRES (IterativeSolvers_Class.f90:656-822): flexible GMRES(m), right preconditioning by Jacobi. */
+int orc_cg_solve_pgmres(const orc_cg_problem* p, const double* source, double* solution, const double* dirichlet,
+                        int m, int maxIters, double tol, double* resi, int* iters);
 
 /* ---------------- 1-D CGSEM elliptic example (examples/elliptic1d/parabola/localmods/Elliptic1D_Class.f90) */
 int orc_elliptic1d_solve(int N, int nEl, int maxIters, double tol, int cg_quirk, double* x, double* u,

@@ -128,6 +128,34 @@ class Mesh:
         assert rc == 0, rc
 
 
+class IsmMesh:
+    """Mesh read from an ISM-V2 file (ReadSpecMeshFile_QuadMesh): same attributes as Mesh."""
+
+    def __init__(self, path, N, quad):
+        nEl, nEd, nNo, g = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        rc = lib().orc_ism_counts(str(path).encode(), C.byref(nEl), C.byref(nEd), C.byref(nNo), C.byref(g))
+        assert rc == 0, "unreadable mesh file"
+        self.nEl, self.nEdges, self.nNodes, self.geomDegree = nEl.value, nEd.value, nNo.value, g.value
+        n = N + 1
+        self.N, self.n = N, n
+        ne = self.nEl
+        self.edges = np.zeros(6 * self.nEdges, np.int32)
+        self.elemNodes = np.zeros(4 * ne, np.int32)
+        self.nodeType = np.zeros(self.nNodes, np.int32)
+        self.n2e_ptr = np.zeros(self.nNodes + 1, np.int32)
+        self.n2e_elem = np.zeros(4 * ne, np.int32)
+        self.n2e_local = np.zeros(4 * ne, np.int32)
+        f = lambda: np.zeros(n * n * ne)
+        self.x, self.y, self.dxds, self.dxdp, self.dyds, self.dydp, self.J = (f() for _ in range(7))
+        b = lambda: np.zeros(n * 4 * ne)
+        self.nhx, self.nhy, self.nlen, self.bx, self.by = (b() for _ in range(5))
+        rc = lib().orc_ism_build(str(path).encode(), N, quad, _i(self.edges), _i(self.elemNodes),
+                                 _i(self.nodeType), _i(self.n2e_ptr), _i(self.n2e_elem), _i(self.n2e_local),
+                                 _d(self.x), _d(self.y), _d(self.dxds), _d(self.dxdp), _d(self.dyds), _d(self.dydp),
+                                 _d(self.J), _d(self.nhx), _d(self.nhy), _d(self.nlen), _d(self.bx), _d(self.by))
+        assert rc == 0, rc
+
+
 # --------------------------------------------------------------------------- DG
 class _DGProblem(C.Structure):
     _fields_ = [("N", C.c_int), ("nEl", C.c_int), ("nEdges", C.c_int), ("nEq", C.c_int), ("model", C.c_int),
@@ -263,6 +291,15 @@ class CGProblem:
                                        C.c_double(tol), precond, _d(resi), C.byref(it))
         return sol, ioerr, it.value, resi[: it.value + 1]
 
+    def solve_pgmres(self, source, solution=None, m=30, maxIters=2000, tol=1e-10, dirichlet=None):
+        """Solve_PCGMRES with the Jacobi preconditioner."""
+        sol = np.zeros(self.nl) if solution is None else np.array(solution, dtype=np.float64, copy=True)
+        resi = np.zeros(maxIters + 1)
+        it = C.c_int()
+        ioerr = lib().orc_cg_solve_pgmres(C.byref(self.s), _d(source), _d(sol), _d(dirichlet), m, maxIters,
+                                          C.c_double(tol), _d(resi), C.byref(it))
+        return sol, ioerr, it.value, resi[: min(it.value, maxIters) + 1]
+
     def solve_gmres(self, source, solution=None, m=30, maxIters=2000, tol=1e-10, dirichlet=None):
         sol = np.zeros(self.nl) if solution is None else np.array(solution, dtype=np.float64, copy=True)
         resi = np.zeros(maxIters + 1)
@@ -281,3 +318,18 @@ def elliptic1d(N=5, nEl=10, maxIters=1000, tol=1e-8, cg_quirk=1):
     ioerr = lib().orc_elliptic1d_solve(N, nEl, maxIters, C.c_double(tol), cg_quirk, _d(x), _d(u), _d(resi),
                                        C.byref(it))
     return x, u, resi, it.value, ioerr
+
+
+def pickup_bytes(N, nEl, fields):
+    """Bytes of a pickup file as WritePickup_ShallowWater / WritePickup_Advection write it
+    (ConservativeShallowWaterClass.f90:2013-2064, AdvectionClass.f90:2040-2098): ACCESS='direct',
+    CONVERT='big_endian', RECL = 8 (N+1)^2 bytes, records in the order element -> field -> record, each record
+    the (N+1)^2 values of sol(:,:,iEq) with iS fastest.  fields: [(array, records per element), ...]."""
+    nn = (N + 1) ** 2
+    out = []
+    for e in range(nEl):
+        for a, r in fields:
+            a = np.asarray(a, dtype=np.float64).reshape(nEl, r, nn)
+            for k in range(r):
+                out.append(a[e, k].astype(">f8").tobytes())
+    return b"".join(out)

@@ -30,6 +30,7 @@ class CGBatch:
         p = C.c_void_p()
         nat.check(nat.lib().self_cgbatch_create(ctx.ptr, n, descs, C.byref(p)), ctx.ptr)
         self.ptr = p
+        ctx.adopt(self)
         self.n = n
         self.sizes = []
         for i, pr in enumerate(problems):

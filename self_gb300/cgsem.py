@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _native as nat
 
-SOLVE_CG, SOLVE_PCG_JACOBI, SOLVE_GMRES = 0, 1, 2
+SOLVE_CG, SOLVE_PCG_JACOBI, SOLVE_GMRES, SOLVE_PGMRES_JACOBI = 0, 1, 2, 3
 
 
 class CG2DDesc(C.Structure):
@@ -40,7 +40,8 @@ class SolveReport(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-_METHODS = {"cg": SOLVE_CG, "pcg": SOLVE_PCG_JACOBI, "pcg_jacobi": SOLVE_PCG_JACOBI, "gmres": SOLVE_GMRES}
+_METHODS = {"cg": SOLVE_CG, "pcg": SOLVE_PCG_JACOBI, "pcg_jacobi": SOLVE_PCG_JACOBI, "gmres": SOLVE_GMRES,
+            "pgmres": SOLVE_PGMRES_JACOBI}
 
 
 class CGsemElliptic_2D:
@@ -62,6 +63,7 @@ class CGsemElliptic_2D:
         p = C.c_void_p()
         nat.check(nat.lib().self_cg2d_create(ctx.ptr, C.byref(s), C.byref(p)), ctx.ptr)
         self.ptr = p
+        ctx.adopt(self)
 
     def _chk(self, st):
         return nat.check(st, self.ctx.ptr)

@@ -447,32 +447,43 @@ __global__ void scale_copy(R* __restrict__ y, const R* __restrict__ x, const dou
     y[k] = (R)(f * (double)x[k]);
 }
 
-// y -= h * x where h = red[0]; and partial <x_next, y> when x_next != NULL (MGS fused step)
+// MGS step: y -= h * x (h = hk[0]) and out = <x_next, y> (or <y, y> when x_next is null), the grid-wide sum
+// closed by the last block (ticket)
 template <typename R>
-__global__ void __launch_bounds__(kRedThreads) mgs_axpy_dot(R* __restrict__ y, const R* __restrict__ x,
-                                                            const double* __restrict__ red, const R* __restrict__ xn,
-                                                            size_t n, double* __restrict__ partial) {
-  const R h = (R)red[0];
-  double s0 = 0;
+__global__ void __launch_bounds__(kRedThreads) mgs_axpy_dot_fused(R* __restrict__ y, const R* __restrict__ x,
+                                                                  const double* __restrict__ hk,
+                                                                  const R* __restrict__ xn, size_t n,
+                                                                  double* __restrict__ partial,
+                                                                  unsigned int* __restrict__ ticket,
+                                                                  double* __restrict__ out) {
+  const R h = (R)hk[0];
+  R s0 = 0;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-    R yk = y[k] - h * x[k];
+    const R yk = y[k] - h * x[k];
     y[k] = yk;
-    if (xn) s0 += (double)xn[k] * (double)yk;
-    else s0 += (double)yk * (double)yk;
+    s0 += xn ? xn[k] * yk : yk * yk;
   }
-  s0 = block_sum(s0);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s0;
+  const R acc[1] = {s0};
+  double tot[1];
+  if (grid_sums_last<1, R>(acc, partial, ticket, tot) && threadIdx.x == 0) out[0] = tot[0];
 }
 
 // x += sum_k V_k y_k
 template <typename R>
 __global__ void gmres_update(R* __restrict__ x, const R* __restrict__ V, const double* __restrict__ y, int nr,
-                             size_t n) {
+                             size_t n, const R* __restrict__ dinv) {
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
     double s = 0;
     for (int j = 0; j < nr; ++j) s += (double)V[(size_t)j * n + k] * y[j];
-    x[k] += (R)s;
+    x[k] += dinv ? (R)(s * (double)dinv[k]) : (R)s;
   }
+}
+
+// y = x * d elementwise
+template <typename R>
+__global__ void scale_by(R* __restrict__ y, const R* __restrict__ x, const R* __restrict__ d, size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    y[k] = x[k] * d[k];
 }
 
 template <typename R, typename S>
@@ -1158,8 +1169,11 @@ double read1(self_cg2d* h, const double* dptr, int* rc) {
 
 // GMRES(m) (IterativeSolvers_Class.f90:493-652) on the device, FP64.  x, r are device vectors; r holds the
 // initial residual.  Returns ioerr; iters = total Arnoldi steps (the reference's l).
+// GMRES(m) of IterativeSolvers_Class.f90:493-652, or with dinv the flexible right-preconditioned GMRES of
+// Solve_PCGMRES (:656-822) with Jacobi: z_i = dinv v_i, w = A z_i, and x += Z y = dinv (V y) at the end of a
+// cycle (the preconditioner is fixed, so the basis Z is not stored).
 int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int maxIters, double tol,
-                 double* resi_host, int* iters, double* rel, double* r0_out) {
+                 double* resi_host, int* iters, double* rel, double* r0_out, const double* dinv) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
   const size_t nl = h->nl;
@@ -1212,15 +1226,20 @@ int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int
       l += 1;
       nr = i + 1;
       double* vi = h->gm_V.p + (size_t)i * nl;
-      if ((rc = matrix_action<double>(h, vi, h->w.p, h->op64))) return rc;
+      if (dinv) {  // z_i = PreconditionInvert(v_i)
+        scale_by<double><<<h->nblk, kRedThreads, 0, st>>>(h->t.p, vi, dinv, nl);
+        SELF_LAUNCHED(ctx);
+        if ((rc = matrix_action<double>(h, h->t.p, h->w.p, h->op64))) return rc;
+      } else if ((rc = matrix_action<double>(h, vi, h->w.p, h->op64))) {
+        return rc;
+      }
       // MGS: h(k,i) = <v_k, w>; w -= h(k,i) v_k, the axpy of step k fused with the dot of step k+1
       if ((rc = dots<double>(h, h->gm_V.p, h->w.p, nullptr, nullptr, h->gm_H.p))) return rc;
       for (int k = 0; k <= i; ++k) {
         const double* vk = h->gm_V.p + (size_t)k * nl;
         const double* vn = (k < i) ? h->gm_V.p + (size_t)(k + 1) * nl : nullptr;
-        mgs_axpy_dot<double><<<h->nblk, kRedThreads, 0, st>>>(h->w.p, vk, h->gm_H.p + k, vn, nl, h->partial.p);
-        SELF_LAUNCHED(ctx);
-        reduce_partials<<<1, kRedThreads, 0, st>>>(h->partial.p, h->nblk, 1, h->gm_H.p + k + 1);
+        mgs_axpy_dot_fused<double><<<h->nblk, kRedThreads, 0, st>>>(h->w.p, vk, h->gm_H.p + k, vn, nl,
+                                                                     h->partial.p, h->ticket.p, h->gm_H.p + k + 1);
         SELF_LAUNCHED(ctx);
       }
       // gm_H[i+1] = <w,w>; Givens on the device
@@ -1252,7 +1271,7 @@ int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int
     SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
     gmres_backsolve<<<1, 1, 0, st>>>(h->gm_rho.p, h->gm_bhat.p, m, h->GS.p, h->gm_y.p);
     SELF_LAUNCHED(ctx);
-    gmres_update<double><<<h->nblk, kRedThreads, 0, st>>>(x, h->gm_V.p, h->gm_y.p, nr, nl);
+    gmres_update<double><<<h->nblk, kRedThreads, 0, st>>>(x, h->gm_V.p, h->gm_y.p, nr, nl, dinv);
     SELF_LAUNCHED(ctx);
     *iters = l;
     if (rcur / r0 <= tol) {
@@ -1324,9 +1343,12 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   self_ctx* ctx = h->ctx;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   if (o->maxIters < 0 || !(o->tolerance > 0)) return set_error(ctx, SELF_ERR_INVALID, "bad solver options");
-  if (o->method == SELF_SOLVE_GMRES && (o->m < 1 || o->m > 512))
+  if (o->method < SELF_SOLVE_CG || o->method > SELF_SOLVE_PGMRES_JACOBI)
+    return set_error(ctx, SELF_ERR_INVALID, "solver method %d", o->method);
+  const bool gm = o->method == SELF_SOLVE_GMRES || o->method == SELF_SOLVE_PGMRES_JACOBI;
+  if (gm && (o->m < 1 || o->m > 512))
     return set_error(ctx, SELF_ERR_INVALID, "GMRES restart length %d", o->m);
-  if (o->method == SELF_SOLVE_GMRES && o->precision != SELF_PREC_FP64)
+  if (gm && o->precision != SELF_PREC_FP64)
     return set_error(ctx, SELF_ERR_UNSUPPORTED, "GMRES runs in FP64");
   const size_t nl = h->nl;
   int rc;
@@ -1335,15 +1357,16 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   std::vector<double> load = make_load(h, source);
   if ((rc = upload_vec(h, h->f, load.data())) || (rc = upload_vec(h, h->u, x0.data())) ||
       (rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->v, nl)) || (rc = ensure(ctx, h->w, nl)) ||
-      (rc = ensure(ctx, h->z, nl)) || (o->method != SELF_SOLVE_GMRES && (rc = ensure(ctx, h->v2, nl))))
+      (rc = ensure(ctx, h->z, nl)) || (!gm && (rc = ensure(ctx, h->v2, nl))))
     return rc;
   if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
   self_solve_report R{};
   R.ioerr = -2;
   int iters = 0;
   double rel = 0, r0 = 0;
-  if (o->method == SELF_SOLVE_GMRES) {
-    R.ioerr = gmres_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, resi, &iters, &rel, &r0);
+  if (gm) {
+    R.ioerr = gmres_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, resi, &iters, &rel, &r0,
+                           o->method == SELF_SOLVE_PGMRES_JACOBI ? h->op64.dinv.p : nullptr);
     R.outer_iterations = 1;
   } else {
     const bool jac = o->method == SELF_SOLVE_PCG_JACOBI;

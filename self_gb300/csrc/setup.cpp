@@ -5,7 +5,13 @@
 // GPU path consumes.  They run once, on the host, in FP64.
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
 #include <mutex>
+#include <unordered_map>
+#include <string>
+#include <sstream>
 #include <vector>
 
 #include "internal.hpp"
@@ -577,6 +583,309 @@ int self_mesh_build(int nx, int ny, int px, int py, int N, int quad, double warp
   return SELF_OK;
 }
 
+// ------------------------------------------------------------------------------------------------ ISM-V2 meshes
+// SpecMesh ISM-V2 files (ReadSpecMeshFile_QuadMesh, QuadMeshClass.f90:2100-2475): corner nodes, an edge list
+// (not used: the edges are rebuilt from the elements as ConstructEdges does), and per element 4 corner node IDs,
+// 4 side kinds (0 straight interior side, 1 boundary curve given by its points at the Chebyshev-Gauss-Lobatto
+// nodes of the file's geometry degree) and 4 side names (boundary condition).  The element geometry is the
+// transfinite (Coons) blend of the 4 side curves with its analytic covariant metrics (Build_MappedGeometry_2D,
+// MappedGeometryClass_2D.f90:105-144, 536-710).
+namespace {
+
+struct IsmMesh {
+  int nNodes = 0, nEdges = 0, nElems = 0, gdeg = 1;
+  std::vector<double> px, py;           // corner nodes
+  std::vector<int> corner;              // 4 per element, 1-based
+  std::vector<int> kind;                // 4 per element
+  std::vector<std::vector<double>> cx, cy;
+  std::vector<int> bc;                  // boundary flag per element side (1 = interior / unnamed)
+};
+
+int ism_flag(const std::string& w) {
+  static const std::pair<const char*, int> names[] = {
+      {"NO_NORMAL_FLOW", -100}, {"NEUMANN", -100},  {"RADIATION", -101},          {"PRESCRIBED", -102},
+      {"InflowOne", -103},      {"InflowTwo", -104}, {"DIRICHLET", -200},          {"HOMOGENEOUS_NEUMANN", -201},
+      {"ROBIN", -202},          {"ROBIN_FORCED", -204}, {"NEUMANN_WALL", -206}};
+  for (const auto& nm : names)
+    if (w == nm.first) return nm.second;
+  return 1;
+}
+
+int ism_read(const char* path, IsmMesh& m, bool header_only) {
+  FILE* fp = fopen(path, "r");
+  if (!fp) return set_error(nullptr, SELF_ERR_INVALID, "cannot open mesh file %s", path);
+  std::string text;
+  char chunk[65536];
+  size_t got;
+  while ((got = fread(chunk, 1, sizeof(chunk), fp)) > 0) text.append(chunk, got);
+  fclose(fp);
+  // line-oriented: the side-name line is read whole, everything else as blank-separated numbers
+  std::vector<std::string> lines;
+  {
+    size_t a = 0;
+    while (a < text.size()) {
+      size_t b = text.find('\n', a);
+      if (b == std::string::npos) b = text.size();
+      lines.emplace_back(text.substr(a, b - a));
+      a = b + 1;
+    }
+  }
+  size_t li = 1;  // line 0: version tag
+  auto numbers = [&](size_t k, std::vector<double>& out) {
+    out.clear();
+    if (k >= lines.size()) return false;
+    const char* c = lines[k].c_str();
+    char* end;
+    for (;;) {
+      while (*c == ' ' || *c == '\t' || *c == '\r') ++c;
+      if (!*c) break;
+      const double v = strtod(c, &end);
+      if (end == c) return false;
+      out.push_back(v);
+      c = end;
+    }
+    return true;
+  };
+  std::vector<double> v;
+  if (!numbers(li++, v) || v.size() < 4) return set_error(nullptr, SELF_ERR_INVALID, "%s: bad ISM header", path);
+  m.nNodes = (int)v[0];
+  m.nEdges = (int)v[1];
+  m.nElems = (int)v[2];
+  m.gdeg = (int)v[3];
+  if (m.nNodes < 4 || m.nElems < 1 || m.nEdges < 4 || m.gdeg < 1)
+    return set_error(nullptr, SELF_ERR_INVALID, "%s: bad ISM counts", path);
+  if (header_only) return SELF_OK;
+  auto fail = [&](const char* what) { return set_error(nullptr, SELF_ERR_INVALID, "%s: %s", path, what); };
+  m.px.resize(m.nNodes);
+  m.py.resize(m.nNodes);
+  for (int k = 0; k < m.nNodes; ++k) {
+    if (!numbers(li++, v) || v.size() < 2) return fail("bad node record");
+    m.px[k] = v[0];
+    m.py[k] = v[1];
+  }
+  li += (size_t)m.nEdges;  // edge records
+  m.corner.resize(4 * (size_t)m.nElems);
+  m.kind.resize(4 * (size_t)m.nElems);
+  m.cx.assign(4 * (size_t)m.nElems, {});
+  m.cy.assign(4 * (size_t)m.nElems, {});
+  m.bc.assign(4 * (size_t)m.nElems, 1);
+  for (int e = 0; e < m.nElems; ++e) {
+    if (!numbers(li++, v) || v.size() < 4) return fail("bad element node record");
+    for (int k = 0; k < 4; ++k) {
+      m.corner[4 * e + k] = (int)v[k];
+      if (m.corner[4 * e + k] < 1 || m.corner[4 * e + k] > m.nNodes) return fail("element node out of range");
+    }
+    if (!numbers(li++, v) || v.size() < 4) return fail("bad side-kind record");
+    for (int k = 0; k < 4; ++k) m.kind[4 * e + k] = (int)v[k];
+    for (int k = 0; k < 4; ++k) {
+      if (m.kind[4 * e + k] == 0) continue;
+      if (m.kind[4 * e + k] != 1) return fail("side kind other than 0 or 1");
+      auto& X = m.cx[4 * e + k];
+      auto& Y = m.cy[4 * e + k];
+      for (int j = 0; j <= m.gdeg; ++j) {
+        if (!numbers(li++, v) || v.size() < 2) return fail("bad curve point");
+        X.push_back(v[0]);
+        Y.push_back(v[1]);
+      }
+    }
+    if (li >= lines.size()) return fail("missing side names");
+    std::istringstream names(lines[li++]);
+    for (int k = 0; k < 4; ++k) {
+      std::string w;
+      if (!(names >> w)) return fail("fewer than 4 side names");
+      m.bc[4 * e + k] = ism_flag(w);
+    }
+  }
+  return SELF_OK;
+}
+
+// a side curve: interpolant of degree g through points at the Chebyshev-Gauss-Lobatto nodes
+struct SideCurve {
+  Interp1D I;
+  std::vector<double> x, y;
+  void at(double s, double& ox, double& oy) const {
+    std::vector<double> l(x.size());
+    I.basis(s, l.data());
+    ox = oy = 0.0;
+    for (size_t j = 0; j < x.size(); ++j) ox += l[j] * x[j], oy += l[j] * y[j];
+  }
+  void slope(double s, double& ox, double& oy) const {
+    std::vector<double> l(x.size());
+    I.dbasis(s, l.data());
+    ox = oy = 0.0;
+    for (size_t j = 0; j < x.size(); ++j) ox += l[j] * x[j], oy += l[j] * y[j];
+  }
+};
+
+// Coons patch of the S, E, N, W curves (S, N parametrised by s; W, E by p) and its covariant metrics
+void coons(const SideCurve* c, double s, double p, double* P, double* cov) {
+  double sw[2], se[2], nw[2], ne[2], S[2], E[2], Nn[2], W[2], dS[2], dE[2], dN[2], dW[2];
+  c[0].at(-1.0, sw[0], sw[1]);
+  c[0].at(1.0, se[0], se[1]);
+  c[2].at(-1.0, nw[0], nw[1]);
+  c[2].at(1.0, ne[0], ne[1]);
+  c[0].at(s, S[0], S[1]);
+  c[2].at(s, Nn[0], Nn[1]);
+  c[3].at(p, W[0], W[1]);
+  c[1].at(p, E[0], E[1]);
+  c[0].slope(s, dS[0], dS[1]);
+  c[2].slope(s, dN[0], dN[1]);
+  c[3].slope(p, dW[0], dW[1]);
+  c[1].slope(p, dE[0], dE[1]);
+  const double am = 0.5 * (1.0 - s), ap = 0.5 * (1.0 + s), bm = 0.5 * (1.0 - p), bp = 0.5 * (1.0 + p);
+  for (int d = 0; d < 2; ++d) {
+    const double bil = bm * (am * sw[d] + ap * se[d]) + bp * (am * nw[d] + ap * ne[d]);
+    P[d] = am * W[d] + ap * E[d] + bm * S[d] + bp * Nn[d] - bil;
+    // d/ds and d/dp of the blend
+    const double ds = 0.5 * (E[d] - W[d]) + bm * (dS[d] - 0.5 * (se[d] - sw[d])) + bp * (dN[d] - 0.5 * (ne[d] - nw[d]));
+    const double dp = 0.5 * (Nn[d] - S[d]) + am * (dW[d] - 0.5 * (nw[d] - sw[d])) + ap * (dE[d] - 0.5 * (ne[d] - se[d]));
+    cov[2 * d] = ds;      // dxds, dyds
+    cov[2 * d + 1] = dp;  // dxdp, dydp
+  }
+}
+
+}  // namespace
+
+int self_mesh_ism_counts(const char* path, int* nEl, int* nEdges, int* nNodes, int* geomDegree) {
+  if (!path || !nEl || !nEdges || !nNodes) return SELF_ERR_INVALID;
+  IsmMesh m;
+  int rc = ism_read(path, m, true);
+  if (rc) return rc;
+  *nEl = m.nElems;
+  *nEdges = m.nEdges;
+  *nNodes = m.nNodes;
+  if (geomDegree) *geomDegree = m.gdeg;
+  return SELF_OK;
+}
+
+int self_mesh_ism_build(const char* path, int N, int quad, int* edges, int* elemNodes, int* nodeType, int* n2e_ptr,
+                        int* n2e_elem, int* n2e_local, double* X, double* Y, double* dxds, double* dxdp,
+                        double* dyds, double* dydp, double* J, double* nhx, double* nhy, double* nlen, double* bx,
+                        double* by) {
+  if (!path) return SELF_ERR_INVALID;
+  if (N < 1 || N > 15) return set_error(nullptr, SELF_ERR_INVALID, "polynomial degree %d outside 1..15", N);
+  IsmMesh m;
+  int rc = ism_read(path, m, false);
+  if (rc) return rc;
+  const int n = N + 1, nEl = m.nElems;
+  std::vector<double> xq, wq;
+  quadrature(N, quad, xq, wq);
+  std::vector<double> cgl(m.gdeg + 1);
+  for (int j = 0; j <= m.gdeg; ++j) cgl[j] = -std::cos(j * (kPi / m.gdeg));
+  static const int corner_of[4][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}};  // S, E, N, W: first and last corner
+  for (int k = 0; k < m.nNodes; ++k) nodeType[k] = 0;
+  for (int e = 0; e < nEl; ++e) {
+    for (int k = 0; k < 4; ++k) elemNodes[4 * e + k] = m.corner[4 * e + k];
+    SideCurve c[4];
+    for (int side = 0; side < 4; ++side) {
+      c[side].I.build(cgl);
+      if (m.kind[4 * e + side] == 0) {
+        const int a = m.corner[4 * e + corner_of[side][0]] - 1, b = m.corner[4 * e + corner_of[side][1]] - 1;
+        c[side].x.resize(m.gdeg + 1);
+        c[side].y.resize(m.gdeg + 1);
+        for (int j = 0; j <= m.gdeg; ++j) {
+          const double t = 0.5 * (cgl[j] + 1.0);
+          c[side].x[j] = m.px[a] + (m.px[b] - m.px[a]) * t;
+          c[side].y[j] = m.py[a] + (m.py[b] - m.py[a]) * t;
+        }
+      } else {
+        c[side].x = m.cx[4 * e + side];
+        c[side].y = m.cy[4 * e + side];
+      }
+    }
+    const size_t o = (size_t)n * n * e;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double P[2], cov[4];
+        coons(c, xq[i], xq[j], P, cov);
+        const size_t id = o + i + (size_t)n * j;
+        X[id] = P[0];
+        Y[id] = P[1];
+        dxds[id] = cov[0];
+        dxdp[id] = cov[1];
+        dyds[id] = cov[2];
+        dydp[id] = cov[3];
+        J[id] = cov[0] * cov[3] - cov[1] * cov[2];
+      }
+    for (int side = 0; side < 4; ++side)
+      for (int k = 0; k < n; ++k) {
+        const double s = (side == 1) ? 1.0 : (side == 3) ? -1.0 : xq[k];
+        const double p = (side == 0) ? -1.0 : (side == 2) ? 1.0 : xq[k];
+        double P[2], cov[4];
+        coons(c, s, p, P, cov);
+        const double Jb = cov[0] * cov[3] - cov[1] * cov[2];
+        const double sg = Jb > 0 ? 1.0 : -1.0;
+        double d0, d1;  // outward normal scaled by the side's length element
+        switch (side) {
+          case 0: d0 = sg * cov[2]; d1 = -sg * cov[0]; break;
+          case 2: d0 = -sg * cov[2]; d1 = sg * cov[0]; break;
+          case 3: d0 = -sg * cov[3]; d1 = sg * cov[1]; break;
+          default: d0 = sg * cov[3]; d1 = -sg * cov[1]; break;
+        }
+        const size_t ib = (size_t)k + n * (side + 4 * (size_t)e);
+        const double len = std::sqrt(d0 * d0 + d1 * d1);
+        nhx[ib] = d0 / len;
+        nhy[ib] = d1 / len;
+        nlen[ib] = len;
+        bx[ib] = P[0];
+        by[ib] = P[1];
+      }
+  }
+  // edges in order of first appearance; keyed by the corner-node pair
+  std::unordered_map<unsigned long long, int> seen;
+  seen.reserve(2 * (size_t)m.nEdges);
+  std::vector<int> first_node, last_node;
+  int ne = 0;
+  for (int e = 0; e < nEl; ++e)
+    for (int side = 0; side < 4; ++side) {
+      const int a = m.corner[4 * e + corner_of[side][0]], b = m.corner[4 * e + corner_of[side][1]];
+      const unsigned long long key = ((unsigned long long)std::min(a, b) << 32) | (unsigned)std::max(a, b);
+      auto it = seen.find(key);
+      if (it == seen.end()) {
+        if (ne >= m.nEdges) return set_error(nullptr, SELF_ERR_INVALID, "%s: more sides than edges", path);
+        seen.emplace(key, ne);
+        int* E = edges + 6 * ne;
+        E[0] = e + 1;
+        E[1] = side + 1;
+        E[2] = SELF_NO_NORMAL_FLOW;  // default boundary kind until a second element claims the edge
+        E[3] = 0;
+        first_node.push_back(a);
+        last_node.push_back(b);
+        ++ne;
+      } else {
+        int* E = edges + 6 * it->second;
+        E[2] = e + 1;
+        E[3] = (a == first_node[it->second]) ? side + 1 : -(side + 1);
+      }
+    }
+  if (ne != m.nEdges) return set_error(nullptr, SELF_ERR_INVALID, "%s: %d edges built, %d in the file", path, ne, m.nEdges);
+  for (int k = 0; k < ne; ++k) {
+    int* E = edges + 6 * k;
+    const int fl = m.bc[4 * (E[0] - 1) + E[1] - 1];
+    if (fl < 0) {  // a named boundary condition on the primary side
+      E[2] = fl;
+      nodeType[first_node[k] - 1] = fl;
+      nodeType[last_node[k] - 1] = fl;
+    }
+    E[4] = (E[3] < 0) ? N - 1 : 1;
+    E[5] = (E[3] < 0) ? -1 : 1;
+  }
+  std::vector<int> cnt(m.nNodes + 1, 0);
+  for (int e = 0; e < nEl; ++e)
+    for (int c = 0; c < 4; ++c) cnt[elemNodes[4 * e + c]]++;
+  n2e_ptr[0] = 0;
+  for (int i = 0; i < m.nNodes; ++i) n2e_ptr[i + 1] = n2e_ptr[i] + cnt[i + 1];
+  std::vector<int> pos(n2e_ptr, n2e_ptr + m.nNodes);
+  for (int e = 0; e < nEl; ++e)
+    for (int c = 0; c < 4; ++c) {
+      const int nd = elemNodes[4 * e + c] - 1;
+      n2e_elem[pos[nd]] = e + 1;
+      n2e_local[pos[nd]] = c + 1;
+      pos[nd]++;
+    }
+  return SELF_OK;
+}
+
 // CalculateBathymetryGradient: the DG weak derivative of h with the element's own boundary values.
 int self_sw_bathymetry_gradient(int N, int nEl, const double* dS, const double* dP, const double* qw,
                                 const double* lW, const double* lE, const double* lS, const double* lN,
@@ -640,6 +949,75 @@ int self_sw_bathymetry_gradient(int N, int nEl, const double* dS, const double* 
       dhdy[o + k] = out[k + n * n];
     }
   }
+  return SELF_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ pickup files
+// Direct-access, big-endian, unformatted records of (N+1)^2 doubles (i fastest) without record markers, as the
+// reference writes them (WritePickup_ShallowWater / ReadPickup_ShallowWater, ConservativeShallowWaterClass.f90:
+// 2013-2130; WritePickup_Advection / ReadPickup_Advection, AdvectionClass.f90:2040-2171): for every element, for
+// every field in order, recs[f] records taken from fields[f] at element offset (e * recs[f] + r) * (N+1)^2.
+namespace {
+inline uint64_t swap64(uint64_t v) {
+  uint64_t r = 0;
+  for (int b = 0; b < 8; ++b) r |= ((v >> (8 * b)) & 0xffULL) << (8 * (7 - b));
+  return r;
+}
+int pickup_args(int N, int nEl, int nfields, const void* fields, const int* recs) {
+  if (N < 1 || nEl < 1 || nfields < 1 || !fields || !recs) return SELF_ERR_INVALID;
+  for (int f = 0; f < nfields; ++f)
+    if (recs[f] < 1) return SELF_ERR_INVALID;
+  return SELF_OK;
+}
+}  // namespace
+
+int self_pickup_write(const char* path, int N, int nEl, int nfields, const double* const* fields, const int* recs) {
+  if (!path || pickup_args(N, nEl, nfields, fields, recs)) return set_error(nullptr, SELF_ERR_INVALID, "pickup arguments");
+  for (int f = 0; f < nfields; ++f)
+    if (!fields[f]) return set_error(nullptr, SELF_ERR_INVALID, "pickup field %d is null", f);
+  FILE* fp = fopen(path, "wb");
+  if (!fp) return set_error(nullptr, SELF_ERR_INVALID, "cannot open %s for writing", path);
+  const size_t nn = (size_t)(N + 1) * (N + 1);
+  std::vector<uint64_t> rec(nn);
+  for (int e = 0; e < nEl; ++e)
+    for (int f = 0; f < nfields; ++f)
+      for (int r = 0; r < recs[f]; ++r) {
+        const double* src = fields[f] + ((size_t)e * recs[f] + r) * nn;
+        for (size_t k = 0; k < nn; ++k) {
+          uint64_t v;
+          std::memcpy(&v, &src[k], 8);
+          rec[k] = swap64(v);
+        }
+        if (fwrite(rec.data(), 8, nn, fp) != nn) {
+          fclose(fp);
+          return set_error(nullptr, SELF_ERR_INVALID, "short write to %s", path);
+        }
+      }
+  if (fclose(fp) != 0) return set_error(nullptr, SELF_ERR_INVALID, "closing %s failed", path);
+  return SELF_OK;
+}
+
+int self_pickup_read(const char* path, int N, int nEl, int nfields, double* const* fields, const int* recs) {
+  if (!path || pickup_args(N, nEl, nfields, fields, recs)) return set_error(nullptr, SELF_ERR_INVALID, "pickup arguments");
+  FILE* fp = fopen(path, "rb");
+  if (!fp) return set_error(nullptr, SELF_ERR_INVALID, "cannot open %s", path);
+  const size_t nn = (size_t)(N + 1) * (N + 1);
+  std::vector<uint64_t> rec(nn);
+  for (int e = 0; e < nEl; ++e)
+    for (int f = 0; f < nfields; ++f)
+      for (int r = 0; r < recs[f]; ++r) {
+        if (fread(rec.data(), 8, nn, fp) != nn) {
+          fclose(fp);
+          return set_error(nullptr, SELF_ERR_INVALID, "%s ends before element %d, field %d", path, e + 1, f);
+        }
+        if (!fields[f]) continue;  // a field the caller does not want
+        double* dst = fields[f] + ((size_t)e * recs[f] + r) * nn;
+        for (size_t k = 0; k < nn; ++k) {
+          const uint64_t v = swap64(rec[k]);
+          std::memcpy(&dst[k], &v, 8);
+        }
+      }
+  fclose(fp);
   return SELF_OK;
 }
 

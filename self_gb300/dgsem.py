@@ -13,6 +13,8 @@ against the Fortran types reads the same:
 Arrays are numpy float64 in the Fortran storage order (element-contiguous, i fastest).
 """
 import ctypes as C
+import os
+import weakref
 
 import numpy as np
 
@@ -26,6 +28,10 @@ class Context:
         p = C.c_void_p()
         nat.check(nat.lib().self_ctx_create(int(device), C.byref(p)))
         self.ptr = p
+        self._handles = weakref.WeakSet()  # handles created on this context, released before it
+
+    def adopt(self, handle):
+        self._handles.add(handle)
 
     def synchronize(self):
         nat.check(nat.lib().self_ctx_synchronize(self.ptr), self.ptr)
@@ -35,6 +41,8 @@ class Context:
 
     def close(self):
         if self.ptr:
+            for h in list(getattr(self, "_handles", ())):
+                h.Trash()
             nat.lib().self_ctx_destroy(self.ptr)
             self.ptr = None
 
@@ -87,6 +95,31 @@ class QuadMesh:
             nat.d(self.nhy), nat.d(self.nlen), nat.d(self.bx), nat.d(self.by)))
 
 
+def read_ism_mesh(path, N, quadrature=nat.GAUSS):
+    """QuadMesh%ReadSpecMeshFile (QuadMeshClass.f90:2100-2475): a QuadMesh from an ISM-V2 (SpecMesh) file."""
+    nEl, nEd, nNo, g = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    bpath = str(path).encode()
+    nat.check(nat.lib().self_mesh_ism_counts(bpath, C.byref(nEl), C.byref(nEd), C.byref(nNo), C.byref(g)))
+    m = QuadMesh.__new__(QuadMesh)
+    m.nx = m.ny = None
+    m.N, m.n = N, N + 1
+    m.nEl, m.nEdges, m.nNodes, m.geomDegree = nEl.value, nEd.value, nNo.value, g.value
+    n, ne = N + 1, m.nEl
+    m.edges = np.zeros(6 * m.nEdges, np.int32)
+    m.elemNodes = np.zeros(4 * ne, np.int32)
+    m.nodeType = np.zeros(m.nNodes, np.int32)
+    m.n2e_ptr = np.zeros(m.nNodes + 1, np.int32)
+    m.n2e_elem = np.zeros(4 * ne, np.int32)
+    m.n2e_local = np.zeros(4 * ne, np.int32)
+    m.x, m.y, m.dxds, m.dxdp, m.dyds, m.dydp, m.J = (np.zeros(n * n * ne) for _ in range(7))
+    m.nhx, m.nhy, m.nlen, m.bx, m.by = (np.zeros(n * 4 * ne) for _ in range(5))
+    nat.check(nat.lib().self_mesh_ism_build(
+        bpath, N, quadrature, nat.i(m.edges), nat.i(m.elemNodes), nat.i(m.nodeType), nat.i(m.n2e_ptr),
+        nat.i(m.n2e_elem), nat.i(m.n2e_local), nat.d(m.x), nat.d(m.y), nat.d(m.dxds), nat.d(m.dxdp), nat.d(m.dyds),
+        nat.d(m.dydp), nat.d(m.J), nat.d(m.nhx), nat.d(m.nhy), nat.d(m.nlen), nat.d(m.bx), nat.d(m.by)))
+    return m
+
+
 def bathymetry_gradient(nodal, mesh, h):
     """CalculateBathymetryGradient for every element (host, FP64)."""
     dhdx, dhdy = np.zeros_like(h), np.zeros_like(h)
@@ -118,6 +151,7 @@ class _DG2D:
         p = C.c_void_p()
         nat.check(nat.lib().self_dg2d_create(ctx.ptr, C.byref(s), C.byref(p)), ctx.ptr)
         self.ptr = p
+        ctx.adopt(self)
 
     def _chk(self, st):
         return nat.check(st, self.ctx.ptr)
@@ -169,7 +203,42 @@ class ShallowWater(_DG2D):
             dhdx, dhdy = bathymetry_gradient(nodal, mesh, h)
         super().__init__(ctx, nodal, mesh, nat.MODEL_SW_CONSERVATIVE, 3, dt, precision, g=g, linear_drag=linear_drag,
                          h=h, dhdx=dhdx, dhdy=dhdy, fcor=fcor, relax=relax, rfac=timescale)
-        self.h, self.dhdx, self.dhdy = h, dhdx, dhdy
+        self.h, self.dhdx, self.dhdy, self.fcor = h, dhdx, dhdy, fcor
+
+    def WritePickup(self, iteration, directory="."):
+        """WritePickup_ShallowWater (ConservativeShallowWaterClass.f90:2013-2064): ShallowWater.<iter>.pickup
+        with, per element, the 3 state records, the bathymetry and the planetary vorticity."""
+        path = os.path.join(directory, "ShallowWater.%010d.pickup" % iteration)
+        q = self.GetSolution()
+        h = np.ascontiguousarray(self.h, dtype=np.float64).ravel()
+        f = np.ascontiguousarray(self.fcor, dtype=np.float64).ravel()
+        write_pickup(path, self.nodal.N, self.mesh.nEl, [(q, 3), (h, 1), (f, 1)])
+        return path
+
+    def ReadPickup(self, iteration, directory="."):
+        """ReadPickup_ShallowWater (:2068-2126): sets the state from the file and returns (state, h, f).  The
+        bathymetry and vorticity define the handle, so a file with other fields needs a new handle."""
+        path = os.path.join(directory, "ShallowWater.%010d.pickup" % iteration)
+        n2, ne = self.nodal.n * self.nodal.n, self.mesh.nEl
+        q, h, f = np.zeros(3 * n2 * ne), np.zeros(n2 * ne), np.zeros(n2 * ne)
+        read_pickup(path, self.nodal.N, ne, [(q, 3), (h, 1), (f, 1)])
+        self.SetSolution(q)
+        return q, h, f
+
+
+def write_pickup(path, N, nEl, fields):
+    """Direct-access big-endian records of (N+1)^2 doubles; fields: [(array, records per element), ...]."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a, _ in fields]
+    recs = (C.c_int * len(fields))(*[r for _, r in fields])
+    ptrs = (nat.dp * len(fields))(*[nat.d(a) for a in arrs])
+    nat.check(nat.lib().self_pickup_write(path.encode(), N, nEl, len(fields), ptrs, recs))
+
+
+def read_pickup(path, N, nEl, fields):
+    """Fill the given arrays (float64, contiguous; None skips a field) from a pickup file."""
+    recs = (C.c_int * len(fields))(*[r for _, r in fields])
+    ptrs = (nat.dp * len(fields))(*[nat.d(a) if a is not None else None for a, _ in fields])
+    nat.check(nat.lib().self_pickup_read(path.encode(), N, nEl, len(fields), ptrs, recs))
 
 
 class Advection(_DG2D):
@@ -178,3 +247,17 @@ class Advection(_DG2D):
     def __init__(self, ctx, nodal, mesh, u, v, dt, nTracers=1, precision=nat.PREC_FP64, relax=None, rfac=None):
         super().__init__(ctx, nodal, mesh, nat.MODEL_ADVECTION, nTracers, dt, precision, u=u, v=v, relax=relax,
                          rfac=rfac)
+        self.u, self.v, self.relax, self.rfac = u, v, relax, rfac
+
+    def WritePickup(self, iteration, directory="."):
+        """WritePickup_Advection (AdvectionClass.f90:2040-2098): per element the nEq state records, the nEq
+        relaxation-field and nEq relaxation-factor records, then u and v."""
+        path = os.path.join(directory, "Advection.%010d.pickup" % iteration)
+        nq = self.nq
+        zero = np.zeros(nq)
+        fields = [(self.GetSolution(), self.nEq),
+                  (zero if self.relax is None else self.relax, self.nEq),
+                  (zero if self.rfac is None else self.rfac, self.nEq),
+                  (self.u, 1), (self.v, 1)]
+        write_pickup(path, self.nodal.N, self.mesh.nEl, fields)
+        return path

@@ -109,6 +109,21 @@ def test_gmres_advection_diffusion_parity(oracle, gpu_ctx):
     assert rel_inf(sol, osol) <= 1e-8
 
 
+def test_pgmres_jacobi_advection_diffusion_parity(oracle, gpu_ctx):
+    """Solve_PCGMRES with the Jacobi preconditioner: same residual history (first 20 Arnoldi steps), iteration
+    count and solution as the oracle."""
+    import self_gb300 as sg
+    N, nx = 4, 6
+    nod, mesh, k, source, P = _problem(oracle, N, nx, warp=0.03, lam=0.0, op=1, vel=(1.0, 0.5), kappa=1e-2)
+    cg = sg.CGsemElliptic_2D(gpu_ctx, nod, mesh, k, lam=0.0, op=1, vel=(1.0, 0.5))
+    sol, rep = cg.Solve(source, method="pgmres", m=30, tolerance=1e-10, maxIters=2000, return_resi=True)
+    osol, ioerr, oit, oresi = P.solve_pgmres(source, m=30, maxIters=2000, tol=1e-10)
+    assert rep["ioerr"] == 0 and ioerr == 0
+    assert abs(rep["iterations"] - oit) <= max(2, 0.02 * oit)
+    assert rel_inf(rep["resi"][:20], oresi[:20]) <= 1e-9
+    assert rel_inf(sol, osol) <= 1e-8
+
+
 def test_manufactured_solution_converges(gpu_ctx):
     """u = sin(pi x) sin(pi y), k = 1, lam = 0.1: spectral accuracy of the solved field."""
     import self_gb300 as sg

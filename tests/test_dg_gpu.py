@@ -281,3 +281,24 @@ def test_fp32_state_through_mapped_host_buffer_matches_staged_path(oracle, gpu_c
     finally:
         for p in ptrs:
             L.self_host_free(p)
+
+
+def test_pickup_restart_continues_bit_identically(oracle, gpu_ctx, tmp_path):
+    """10 RK3 steps in one go equal 5 steps, WritePickup, a fresh handle's ReadPickup and 5 more steps (FP64
+    form): the pickup carries the state exactly."""
+    import self_gb300 as sg
+    N, nx = 5, 6
+    nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, _, _ = _sw_problem(oracle, N, nx, flow=True)
+    a = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy)
+    a.SetSolution(q)
+    a.ForwardStepRK3(0.0, 10)
+    ref = a.GetSolution()
+    b = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy)
+    b.SetSolution(q)
+    b.ForwardStepRK3(0.0, 5)
+    b.WritePickup(5, directory=str(tmp_path))
+    c = sg.ShallowWater(gpu_ctx, nod, mesh, h, fcor, dt, dhdx=dhdx, dhdy=dhdy)
+    q5, h5, f5 = c.ReadPickup(5, directory=str(tmp_path))
+    assert np.array_equal(h5, np.ravel(h)) and np.array_equal(f5, np.ravel(fcor))
+    c.ForwardStepRK3(0.0, 5)
+    assert np.array_equal(c.GetSolution(), ref)

@@ -105,3 +105,20 @@ def test_lake_at_rest_flat_bottom_is_steady(oracle):
     scale = 9.81 * 1000.0 ** 2 / (2e6 / 4)  # g H^2 / dx
     assert np.abs(td[:, :2]).max() < 1e-9 * scale
     assert np.abs(td[:, 2]).max() == 0.0
+
+
+def test_oracle_pgmres_solves_what_gmres_solves(oracle):
+    """The restated Solve_PCGMRES (Jacobi) reaches the same solution as the restated GMRES on a small
+    advection-diffusion problem (both to 1e-10)."""
+    import numpy as np
+    import self_gb300 as sg
+    N, nx = 3, 4
+    nod = sg.NodalStorage_2D(N, sg._native.GAUSS_LOBATTO, sg._native.CG)
+    mesh = sg.QuadMesh(nx, nx, N, sg._native.GAUSS_LOBATTO, warp=0.03, boundary_flag=sg._native.DIRICHLET)
+    from self_gb300 import workloads as W
+    _, f, source = W.helmholtz(mesh, N)
+    P = oracle.CGProblem(nod, mesh, np.full(mesh.x.shape, 1e-2), lam=0.0, op=1, vel=(1.0, 0.5))
+    s1, e1, it1, _ = P.solve_gmres(source, m=20, maxIters=500, tol=1e-10)
+    s2, e2, it2, _ = P.solve_pgmres(source, m=20, maxIters=500, tol=1e-10)
+    assert e1 == 0 and e2 == 0
+    assert np.abs(s1 - s2).max() <= 1e-7 * np.abs(s1).max()
