@@ -467,15 +467,27 @@ def run_gpu(args):
     nat.check(L.self_probe_fma_peak(ctx.ptr, 1, C.byref(f64peak)), ctx.ptr)
 
     def roof(prec):
+        """Dominant kernel: algorithmic bytes per launch / average launch duration over the timed region.  For
+        the FP32 form every launch of the timed step is one sw32_fused stage (3 per step), so the average
+        duration is the timed step time / 3; cold_launch is the same kernel timed alone after an L2 flush."""
         pb = 8 if prec == nat.PREC_FP64 else 4
         fused = prec == nat.PREC_FP32 and out[prec]["edge_ms"] == 0.0
         vb = bytes_per_fused_launch(mesh.nEl, n) if fused else bytes_per_volume_launch(mesh.nEl, n, pb)
-        ach = vb / (out[prec]["volume_ms"] * 1e-3) / 1e9
+        cold = vb / (out[prec]["volume_ms"] * 1e-3) / 1e9
+        if fused:
+            launch_ms = out[prec]["ms"] / 3.0
+            ach = vb / (launch_ms * 1e-3) / 1e9
+        else:  # the FP64 step also holds the edge-flux kernels: keep the kernel-alone timing
+            launch_ms, ach = out[prec]["volume_ms"], cold
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": NCU_TRAFFIC_BYTES["sw32_fused" if fused else "dg_volume"], "traffic_unit": "B",
                 "kernel": ("sw32_fused (TMA-staged edge fluxes + volume + RK update + traces)" if fused
                            else "dg_volume (volume + RK update + next-stage traces)"),
-                "launch_ms": out[prec]["volume_ms"], "bytes_per_launch": vb, "peak_source": peak_kind,
+                "launch_ms": launch_ms, "launch_ms_source": ("timed step / 3 launches" if fused
+                                                             else "kernel alone, L2 flushed"),
+                "bytes_per_launch": vb, "peak_source": peak_kind,
+                "cold_launch": {"launch_ms": out[prec]["volume_ms"], "achieved": cold, "frac": cold / peak,
+                                "note": "one launch alone after a 512 MiB L2 flush (no reuse between stages)"},
                 "edge_kernel_ms": out[prec]["edge_ms"]}
 
     e2e_steps = max(3, min(args.steps, 50))
