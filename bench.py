@@ -409,6 +409,28 @@ def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, fp64_sample=60):
             "throughput_ratio": st["throughput_req_s"] / base["throughput_req_s"]}
 
 
+def run_cg_profile(args):
+    """Bounded CGSEM workload for profilers (no JSON line): the 256x256 N=7 Helmholtz problem of the elliptic
+    leg, `--profile-cg K` FP32 PCG iterations after a 32-iteration warm-up solve."""
+    import self_gb300 as sg
+    from self_gb300 import _native as nat
+    from self_gb300 import workloads as W
+    ctx = sg.Context(0)
+    N, nx = 7, 256
+    nod = sg.NodalStorage_2D(N, nat.GAUSS_LOBATTO, nat.CG)
+    mesh = sg.QuadMesh(nx, nx, N, nat.GAUSS_LOBATTO, boundary_flag=nat.DIRICHLET)
+    k, f, source = W.helmholtz(mesh, N, seed=3)
+    cg = sg.CGsemElliptic_2D(ctx, nod, mesh, k, lam=0.1)
+    cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-10, maxIters=32)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    _, rep = cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-30, maxIters=args.profile_cg, max_outer=1)
+    el = time.perf_counter() - t0
+    print(f"profile-cg: {rep['iterations']} FP32 PCG iterations in {el:.4f} s", flush=True)
+    cg.Trash()
+    ctx.close()
+
+
 def run_gpu(args):
     dist, rank, ws, local = dist_init()
     import ctypes as C
@@ -566,9 +588,13 @@ def main():
     ap.add_argument("--no-elliptic", dest="elliptic", action="store_false", help="skip the CGSEM solve leg")
     ap.add_argument("--batched-n", type=int, default=512, help="problems of the batched leg (0 skips it)")
     ap.add_argument("--serve-n", type=int, default=300, help="requests of the serving leg (0 skips it)")
+    ap.add_argument("--profile-cg", type=int, default=0,
+                    help="run only K FP32 PCG iterations of the elliptic workload (for profilers) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
+    if args.profile_cg > 0:
+        run_cg_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

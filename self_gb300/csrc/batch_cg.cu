@@ -642,14 +642,18 @@ struct self_cgbatch {
   size_t cap_et = 0, cap_gt = 0, cap_vt = 0;  // table capacities (tiles of every problem in the pool)
   bool dirty = true;
   int epb[10][4];
-  cudaGraphExec_t inner32 = nullptr, inner64 = nullptr;
-  long long inner32_launches = 0, inner64_launches = 0;  // kernels per captured graph
+  // inner-iteration graphs per precision and grid level: level L launches capacity >> (2 L) blocks per kernel,
+  // the smallest level that covers the current tile counts is replayed (blocks past the count exit at once)
+  static constexpr int kLevels = 4;
+  cudaGraphExec_t graphs[2][kLevels] = {};
+  long long graph_launches[2][kLevels] = {};
   const double* partial_graph = nullptr;                 // partial-sum array the graphs were captured with
   int graph_k = 8;
   long long bytes_in_use = 0;
   ~self_cgbatch() {
-    if (inner32) cudaGraphExecDestroy(inner32);
-    if (inner64) cudaGraphExecDestroy(inner64);
+    for (auto& row : graphs)
+      for (auto& g : row)
+        if (g) cudaGraphExecDestroy(g);
   }
 };
 
@@ -677,9 +681,11 @@ int zeros(self_ctx* ctx, DevBuf<T>& b, size_t n) {
 }
 
 void drop_graphs(self_cgbatch* b) {
-  if (b->inner32) cudaGraphExecDestroy(b->inner32);
-  if (b->inner64) cudaGraphExecDestroy(b->inner64);
-  b->inner32 = b->inner64 = nullptr;
+  for (auto& row : b->graphs)
+    for (auto& g : row) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
 }
 
 // grow the slot arrays (host and device) to hold at least `want` problems
@@ -847,19 +853,24 @@ int k_dss(self_cgbatch* b, const self_cgbatch::View& v, int vsel, int gate, bool
   return SELF_OK;
 }
 
+// grid of a table with capacity cap at level L (at least one block)
+inline int level_grid(size_t cap, int L) { return (int)std::max<size_t>(1, cap >> (2 * L)); }
+
 // inner iterations: graph = start (problems entering an inner solve) + graph_k x (apply, dss, update)
 template <typename R>
-int enqueue_inner(self_cgbatch* b) {
+int enqueue_inner(self_cgbatch* b, int L) {
   cudaStream_t st = b->ctx->stream;
   const TileView V = b->inner.dev();
-  const int ge = (int)b->inner.cap_e, gv = (int)b->inner.cap_v;
+  const int ge = level_grid(b->inner.cap_e, L), gv = level_grid(b->inner.cap_v, L);
   bk_start<R><<<gv, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p);
   SELF_LAUNCHED(b->ctx);
   for (int k = 0; k < b->graph_k; ++k) {
     bk_apply<R><<<ge, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->DT.p, b->partial.p, b->ticket.p);
     SELF_LAUNCHED(b->ctx);
-    int rc;
-    if ((rc = k_dss<R>(b, b->inner, V_Z, 0, true))) return rc;
+    if (b->inner.cap_g > 0) {
+      bk_dss<R><<<level_grid(b->inner.cap_g, L), kThreads, 0, st>>>(V, b->probs.p, b->S.p, V_Z, 0);
+      SELF_LAUNCHED(b->ctx);
+    }
     bk_update<R><<<gv, kThreads, 0, st>>>(V, b->probs.p, b->S.p, b->partial.p, b->inner.cap_v, b->ticket.p);
     SELF_LAUNCHED(b->ctx);
   }
@@ -923,13 +934,18 @@ int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
     if (b->slots[p].used && b->hs[p].phase == 0) inner_set.push_back(p);
   if (!inner_set.empty()) {
     if ((rc = ensure_view(b, b->inner, inner_set))) return rc;
-    cudaGraphExec_t& G = fp32 ? b->inner32 : b->inner64;
-    long long& nk = fp32 ? b->inner32_launches : b->inner64_launches;
+    int L = self_cgbatch::kLevels - 1;  // smallest grid level covering the current tiles
+    while (L > 0 && ((size_t)b->inner.n_e > (size_t)level_grid(b->inner.cap_e, L) ||
+                     (size_t)b->inner.n_g > (size_t)level_grid(b->inner.cap_g, L) ||
+                     (size_t)b->inner.n_v > (size_t)level_grid(b->inner.cap_v, L)))
+      --L;
+    cudaGraphExec_t& G = b->graphs[fp32 ? 1 : 0][L];
+    long long& nk = b->graph_launches[fp32 ? 1 : 0][L];
     if (!G) {
       cudaGraph_t g;
       const long long l0 = ctx->launches.load();
       SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      rc = fp32 ? enqueue_inner<float>(b) : enqueue_inner<double>(b);
+      rc = fp32 ? enqueue_inner<float>(b, L) : enqueue_inner<double>(b, L);
       cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
       if (rc) return rc;
       if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
