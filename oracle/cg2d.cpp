@@ -236,7 +236,10 @@ int orc_cg_matrix_action(const orc_cg_problem* p, double* u, double* Au) {
   return 0;
 }
 
-static void set_dirichlet(const orc_cg_problem* p, double* sol, const double* dir) {
+}  // extern "C"
+
+namespace orc {
+void cg_set_dirichlet(const orc_cg_problem* p, double* sol, const double* dir) {
   CGIdx I{p->N + 1};
   const int N = p->N;
   for (int k = 0; k < p->nEdges; ++k) {
@@ -259,6 +262,9 @@ static void set_dirichlet(const orc_cg_problem* p, double* sol, const double* di
     }
   }
 }
+}  // namespace orc
+
+extern "C" {
 
 int orc_cg_residual(const orc_cg_problem* p, const double* source, double* solution, const double* dir,
                     double* r) {
@@ -276,7 +282,7 @@ int orc_cg_residual(const orc_cg_problem* p, const double* source, double* solut
   orc_cg_global_sum(p, r);
   orc_cg_mask(p, r);
   orc_cg_mask(p, solution);
-  set_dirichlet(p, solution, dir);
+  orc::cg_set_dirichlet(p, solution, dir);
   return 0;
 }
 
@@ -350,7 +356,7 @@ int orc_cg_solve_pcg(const orc_cg_problem* p, const double* source, double* solu
     diag.resize(nl);
     orc_cg_jacobi_diagonal(p, diag.data());
   }
-  if (dir) set_dirichlet(p, solution, dir);
+  if (dir) orc::cg_set_dirichlet(p, solution, dir);
   int ioerr = -2;
   std::memcpy(u.data(), solution, nl * sizeof(double));
   int rc = orc_cg_residual(p, source, solution, dir, r.data());
@@ -391,7 +397,7 @@ int orc_cg_solve_pcg(const orc_cg_problem* p, const double* source, double* solu
   if (rNorm / r0 > tol) ioerr = -1;
   orc_cg_unmask(p, u.data());
   std::memcpy(solution, u.data(), nl * sizeof(double));
-  set_dirichlet(p, solution, dir);
+  orc::cg_set_dirichlet(p, solution, dir);
   return ioerr;
 }
 
@@ -403,7 +409,7 @@ int orc_cg_solve_gmres(const orc_cg_problem* p, const double* source, double* so
   std::vector<double> rho(m * m, 0.0), h((m + 1) * m, 0.0), c(m, 0.0), s(m, 0.0), bhat(m + 1, 0.0), y(m + 1, 0.0);
   auto RHO = [&](int i, int j) -> double& { return rho[(i - 1) + m * (j - 1)]; };
   auto H = [&](int i, int j) -> double& { return h[(i - 1) + (m + 1) * (j - 1)]; };
-  if (dir) set_dirichlet(p, solution, dir);
+  if (dir) orc::cg_set_dirichlet(p, solution, dir);
   int ioerr = -2;
   int rc = orc_cg_residual(p, source, solution, dir, r.data());
   if (rc) return rc;
@@ -473,7 +479,7 @@ int orc_cg_solve_gmres(const orc_cg_problem* p, const double* source, double* so
   }
   if (rcur / r0 > tol) ioerr = -1;
   orc_cg_unmask(p, solution);
-  set_dirichlet(p, solution, dir);
+  orc::cg_set_dirichlet(p, solution, dir);
   return ioerr;
 }
 
@@ -489,7 +495,7 @@ int orc_cg_solve_pgmres(const orc_cg_problem* p, const double* source, double* s
   auto RHO = [&](int i, int j) -> double& { return rho[(i - 1) + m * (j - 1)]; };
   auto H = [&](int i, int j) -> double& { return h[(i - 1) + (m + 1) * (j - 1)]; };
   orc_cg_jacobi_diagonal(p, diag.data());
-  if (dir) set_dirichlet(p, solution, dir);
+  if (dir) orc::cg_set_dirichlet(p, solution, dir);
   int ioerr = -2;
   int rc = orc_cg_residual(p, source, solution, dir, r.data());
   if (rc) return rc;
@@ -561,7 +567,7 @@ int orc_cg_solve_pgmres(const orc_cg_problem* p, const double* source, double* s
   }
   if (rcur / r0 > tol) ioerr = -1;
   orc_cg_unmask(p, solution);
-  set_dirichlet(p, solution, dir);
+  orc::cg_set_dirichlet(p, solution, dir);
   return ioerr;
 }
 

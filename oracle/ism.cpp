@@ -41,27 +41,9 @@ int flag_of(const std::string& s) {
   return 1;  // INTERIOR (unrecognised names keep the default)
 }
 
-struct CurveG {  // CurveClass_2D of degree g on Chebyshev-Gauss-Lobatto nodes
-  int g = 1;
-  std::vector<double> s, bw, x, y;
-  void nodes(int deg) {
-    g = deg;
-    s.assign(g + 1, 0.0);
-    bw.assign(g + 1, 0.0);
-    for (int j = 0; j <= g; ++j) s[j] = -std::cos((double)j * (kPiI / (double)g));
-    orc::barycentric(g, s.data(), bw.data());
-    x.assign(g + 1, 0.0);
-    y.assign(g + 1, 0.0);
-  }
-  void eval(double a, double& ox, double& oy) const {
-    ox = orc::lagrange_eval(g, s.data(), bw.data(), a, x.data());
-    oy = orc::lagrange_eval(g, s.data(), bw.data(), a, y.data());
-  }
-  void slope(double a, double& ox, double& oy) const {
-    ox = orc::lagrange_deriv(g, s.data(), bw.data(), a, x.data());
-    oy = orc::lagrange_deriv(g, s.data(), bw.data(), a, y.data());
-  }
-};
+}  // namespace
+
+namespace orc {
 
 inline void uni(const double* l, const double* r, double a, double* p) {
   p[0] = 0.5 * ((1.0 - a) * l[0] + (1.0 + a) * r[0]);
@@ -127,6 +109,14 @@ void tfi_metrics(const CurveG* c, double a, double b, double* cov) {  // dxds dx
   cov[1] = P2[0] + U[0];
   cov[3] = P2[1] + U[1];
 }
+
+}  // namespace orc
+
+namespace {
+
+using orc::CurveG;
+using orc::tfi;
+using orc::tfi_metrics;
 
 struct IsmFile {
   int nNodes = 0, nEdges = 0, nElems = 0, gdeg = 1;
