@@ -176,6 +176,7 @@ int self_pickup_read(const char* path, int N, int nEl, int nfields, double* cons
  *   self_cg2d_dot           == %DotProduct(u, v)       (:1072-1110)
  *   self_cg2d_mask/unmask   == %Mask / %UnMask         (:350-542)
  *   self_cg2d_solve         == %Solve (PCG, :1114-1207) and IterativeSolver GMRES (IterativeSolvers_Class.f90:493-652)
+ *   self_cg2d_precondition  == %preconditioner%Solve (CGsemPreconditioner_2D_Class.f90:646-746)
  * Operator: op 0 = FluxDivergence - lambda*J*w_i*w_j (weak form of div(k grad u) - lambda u, the reference's
  * sign); op 1 adds the advection term -J*w_i*w_j*(vx du/dx + vy du/dy) (nonsymmetric; use GMRES). */
 typedef struct {
@@ -189,12 +190,22 @@ typedef struct {
   double lambda;
   int op;
   double vx, vy;
+  /* GLL node positions x(i,j,e), y(i,j,e): only SELF_SOLVE_PCG_LINEAR needs them (NULL otherwise), to build the
+   * bilinear sub-quads of the reference's preconditioner mesh (QuadMeshClass.f90 ConstructLinearMeshFromOther
+   * :1863-2092). */
+  const double *x, *y;
 } self_cg2d_desc;
 
 #define SELF_SOLVE_CG 0           /* conjugate gradient, no preconditioner */
 #define SELF_SOLVE_PCG_JACOBI 1   /* conjugate gradient, assembled-diagonal (Jacobi) preconditioner */
 #define SELF_SOLVE_GMRES 2        /* GMRES(m), modified Gram-Schmidt + Givens */
 #define SELF_SOLVE_PGMRES_JACOBI 3 /* flexible right-preconditioned GMRES(m) (Solve_PCGMRES), Jacobi */
+/* conjugate gradient preconditioned by the reference's linear-FEM inner CG (CGsemElliptic_2D %Solve =
+ * Solve_PCConjugateGradient :1114-1207 with CGsemPreconditioner_2D %Solve :646-746): w = pc_iterations CG steps
+ * (or fewer, to ||r||/||r0|| < pc_tolerance) on the N = 1 mesh of the GLL nodes (nodes identified by position as
+ * the reference does), k = 1, the nodes of unshared sub-quad sides Dirichlet; pc_iterations = 0 makes w = r.
+ * Needs desc x, y. */
+#define SELF_SOLVE_PCG_LINEAR 4
 
 typedef struct {
   int method;             /* SELF_SOLVE_* */
@@ -204,7 +215,16 @@ typedef struct {
   double tolerance;       /* stop at ||r|| / ||r0|| < tolerance (FP64 residual) */
   double inner_tolerance; /* FP32 inner solve: relative reduction per refinement step (default 1e-4) */
   int max_outer;          /* refinement steps cap (default 30) */
+  int pc_iterations;      /* SELF_SOLVE_PCG_LINEAR: inner CG steps per application (CGsemParams pcIterates, 50) */
+  double pc_tolerance;    /* SELF_SOLVE_PCG_LINEAR: inner stop ||r||/||r0|| < pc_tolerance (pcTolerance, 1e-4) */
+  int pc_nodes;           /* SELF_SOLVE_PCG_LINEAR: SELF_PC_NODES_POSITION or SELF_PC_NODES_CONNECTIVITY */
 } self_solve_opts;
+/* How the preconditioner mesh identifies shared GLL nodes.  POSITION is the reference (AlmostEqual positions,
+ * ~1 ulp): where positions of one node computed in different elements differ by more (transfinite elements, e.g.
+ * SpecMesh files), the node stays split, the split sub-quad sides become Dirichlet and the PCG can stall, as the
+ * reference's does.  CONNECTIVITY takes the spectral mesh's own shared copies (no split nodes). */
+#define SELF_PC_NODES_POSITION 0
+#define SELF_PC_NODES_CONNECTIVITY 1
 
 typedef struct {
   int ioerr;            /* 0 converged, -1 not converged (reference meanings), -2 other */
@@ -226,6 +246,10 @@ int self_cg2d_unmask(self_cg2d* h, double* u);
  * resi: NULL or maxIters+1 doubles (||r|| per iteration; per refinement step for the FP32 form). */
 int self_cg2d_solve(self_cg2d* h, const self_solve_opts* opts, const double* source, const double* dirichlet,
                     double* solution, double* resi, self_solve_report* report);
+/* == preconditioner%Solve(w, UnMask(r)) of Solve_PCConjugateGradient (CGsemPreconditioner_2D_Class.f90:646-746):
+ * one application of the linear-FEM preconditioner in FP64 with opts.pc_iterations / opts.pc_tolerance.
+ * r: residual L-vector (masked or unmasked); w: result, unmasked; iterations: inner CG steps run (may be NULL). */
+int self_cg2d_precondition(self_cg2d* h, const self_solve_opts* opts, const double* r, double* w, int* iterations);
 
 /* ---------------------------------------------------------------- batched uneven CGSEM solves
  * Many independent Helmholtz problems (op 0; different meshes and degrees N = 2..9) solved together: one

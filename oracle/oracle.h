@@ -132,16 +132,18 @@ int orc_cg_solve_pgmres(const orc_cg_problem* p, const double* source, double* s
                         int m, int maxIters, double tol, double* resi, int* iters);
 
 /* The reference's linear-FEM preconditioner (CGsemPreconditioner_2D_Class.f90 on the mesh of
- * QuadMeshClass.f90 ConstructLinearMeshFromOther :1863-2092); x, y = GLL node positions of the problem.
+ * QuadMeshClass.f90 ConstructLinearMeshFromOther :1863-2092); x, y = GLL node positions of the problem; ids =
+ * NULL (nodes identified by position, as the reference) or one node id per local node (equal ids = one node).
  * info: unique corner nodes of the linear mesh and how many of them are DIRICHLET.
  * apply: out (unmasked, original layout) = preconditioner%Solve(b) with pcIters / pcTol, iters = CG steps run.
  * solve: Solve_PCConjugateGradient (CGsemElliptic_2D_Class.f90:1114-1207) with that preconditioner. */
-int orc_pc_linear_info(const orc_cg_problem* p, const double* x, const double* y, int* nUnique, int* nDirichlet);
-int orc_pc_linear_apply(const orc_cg_problem* p, const double* x, const double* y, int pcIters, double pcTol,
-                        const double* b, double* out, int* iters);
-int orc_cg_solve_pcg_linear(const orc_cg_problem* p, const double* x, const double* y, const double* source,
-                            double* solution, const double* dirichlet, int maxIters, double tol, int pcIters,
-                            double pcTol, double* resi, int* iters);
+int orc_pc_linear_info(const orc_cg_problem* p, const double* x, const double* y, const int* ids, int* nUnique,
+                       int* nDirichlet);
+int orc_pc_linear_apply(const orc_cg_problem* p, const double* x, const double* y, const int* ids, int pcIters,
+                        double pcTol, const double* b, double* out, int* iters);
+int orc_cg_solve_pcg_linear(const orc_cg_problem* p, const double* x, const double* y, const int* ids,
+                            const double* source, double* solution, const double* dirichlet, int maxIters, double tol,
+                            int pcIters, double pcTol, double* resi, int* iters);
 
 /* ---------------- 1-D CGSEM elliptic example (examples/elliptic1d/parabola/localmods/Elliptic1D_Class.f90) */
 int orc_elliptic1d_solve(int N, int nEl, int maxIters, double tol, int cg_quirk, double* x, double* u,

@@ -304,32 +304,41 @@ class CGProblem:
         mesh = self.keep[1]
         return _d(mesh.x), _d(mesh.y)
 
-    def pc_linear_info(self):
-        """(unique corner nodes, DIRICHLET nodes) of the reference's linear preconditioner mesh."""
+    @staticmethod
+    def _ids(ids):
+        return None if ids is None else _i(np.ascontiguousarray(ids, dtype=np.int32))
+
+    def pc_linear_info(self, ids=None):
+        """(unique corner nodes, DIRICHLET nodes) of the reference's linear preconditioner mesh (nodes by position,
+        or by the given per-node ids)."""
         nu, nd = C.c_int(), C.c_int()
         x, y = self._xy()
-        assert lib().orc_pc_linear_info(C.byref(self.s), x, y, C.byref(nu), C.byref(nd)) == 0
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
+        assert lib().orc_pc_linear_info(C.byref(self.s), x, y, self._ids(ids), C.byref(nu), C.byref(nd)) == 0
         return nu.value, nd.value
 
-    def pc_linear_apply(self, b, pcIters=50, pcTol=1e-4):
+    def pc_linear_apply(self, b, pcIters=50, pcTol=1e-4, ids=None):
         """preconditioner%Solve(b): the linear-FEM inner CG, output unmasked on the original nodes."""
         out = np.zeros(self.nl)
         it = C.c_int()
         x, y = self._xy()
         b = np.ascontiguousarray(b, dtype=np.float64)
-        assert lib().orc_pc_linear_apply(C.byref(self.s), x, y, pcIters, C.c_double(pcTol), _d(b), _d(out),
-                                         C.byref(it)) == 0
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
+        assert lib().orc_pc_linear_apply(C.byref(self.s), x, y, self._ids(ids), pcIters, C.c_double(pcTol), _d(b),
+                                         _d(out), C.byref(it)) == 0
         return out, it.value
 
     def solve_pcg_linear(self, source, solution=None, maxIters=2000, tol=1e-10, pcIters=50, pcTol=1e-4,
-                         dirichlet=None):
+                         dirichlet=None, ids=None):
         """Solve_PCConjugateGradient with the reference's linear-FEM preconditioner."""
         sol = np.zeros(self.nl) if solution is None else np.array(solution, dtype=np.float64, copy=True)
         resi = np.zeros(maxIters + 1)
         it = C.c_int()
         x, y = self._xy()
-        ioerr = lib().orc_cg_solve_pcg_linear(C.byref(self.s), x, y, _d(source), _d(sol), _d(dirichlet), maxIters,
-                                              C.c_double(tol), pcIters, C.c_double(pcTol), _d(resi), C.byref(it))
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
+        ioerr = lib().orc_cg_solve_pcg_linear(C.byref(self.s), x, y, self._ids(ids), _d(source), _d(sol),
+                                              _d(dirichlet), maxIters, C.c_double(tol), pcIters, C.c_double(pcTol),
+                                              _d(resi), C.byref(it))
         return sol, ioerr, it.value, resi[: it.value + 1]
 
     def solve_gmres(self, source, solution=None, m=30, maxIters=2000, tol=1e-10, dirichlet=None):

@@ -16,7 +16,9 @@
 //    solver's own fluxCoeff still holds ONE, so the linear operator always has k = 1).
 // Decisions: the unique-node search uses a hash grid of cell size 1e-9 x the mesh extent, which finds the same
 // first earlier AlmostEqual match as the reference's all-pairs loop (AlmostEqual's tolerance is ~1e-16
-// relative); ioerr = 0 on convergence as in the other oracle solvers.
+// relative); ioerr = 0 on convergence as in the other oracle solvers.  Extension: with `ids` (one node id per
+// local node, equal ids = one node) the nodes are identified by those ids instead of by position, numbered in
+// the same first-appearance order.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -83,11 +85,23 @@ int unique_ids(const double* x, const double* y, size_t n, std::vector<int>& uid
   return nUnique;
 }
 
-void build(const orc_cg_problem* p, const double* x, const double* y, LinearPC& L) {
+int ids_in_order(const int* ids, size_t n, std::vector<int>& uid) {
+  std::unordered_map<int, int> seen;
+  uid.assign(n, 0);
+  int nUnique = 0;
+  for (size_t i = 0; i < n; ++i) {
+    auto it = seen.find(ids[i]);
+    if (it == seen.end()) it = seen.emplace(ids[i], ++nUnique).first;
+    uid[i] = it->second;
+  }
+  return nUnique;
+}
+
+void build(const orc_cg_problem* p, const double* x, const double* y, const int* ids, LinearPC& L) {
   const int N = p->N, n = N + 1;
   const size_t nl = (size_t)n * n * p->nEl;
   std::vector<int> uid;
-  L.nNodes = unique_ids(x, y, nl, uid);
+  L.nNodes = ids ? ids_in_order(ids, nl, uid) : unique_ids(x, y, nl, uid);
   L.nEl = p->nEl * N * N;
   // node positions: every original node writes its position to its unique ID (the last write stays)
   std::vector<double> nx(L.nNodes + 1), ny(L.nNodes + 1);
@@ -256,11 +270,11 @@ int pc_solve(const LinearPC& L, const double* b, double* x, int* iters_out) {
 
 extern "C" {
 
-int orc_pc_linear_info(const orc_cg_problem* p, const double* x, const double* y, int* nUnique,
+int orc_pc_linear_info(const orc_cg_problem* p, const double* x, const double* y, const int* ids, int* nUnique,
                        int* nDirichlet) {
   if (p->N < 1) return -1;
   LinearPC L;
-  build(p, x, y, L);
+  build(p, x, y, ids, L);
   *nUnique = L.nNodes;
   int nd = 0;
   for (int t : L.nodeType) nd += t == ORC_DIRICHLET;
@@ -268,22 +282,22 @@ int orc_pc_linear_info(const orc_cg_problem* p, const double* x, const double* y
   return 0;
 }
 
-int orc_pc_linear_apply(const orc_cg_problem* p, const double* x, const double* y, int pcIters, double pcTol,
-                        const double* b, double* out, int* iters) {
+int orc_pc_linear_apply(const orc_cg_problem* p, const double* x, const double* y, const int* ids, int pcIters,
+                        double pcTol, const double* b, double* out, int* iters) {
   if (p->N < 1 || pcIters < 0) return -1;
   LinearPC L;
-  build(p, x, y, L);
+  build(p, x, y, ids, L);
   L.maxIters = pcIters;
   L.tol = pcTol;
   return pc_solve(L, b, out, iters);
 }
 
-int orc_cg_solve_pcg_linear(const orc_cg_problem* p, const double* x, const double* y, const double* source,
-                            double* solution, const double* dir, int maxIters, double tol, int pcIters, double pcTol,
-                            double* resi, int* iters) {
+int orc_cg_solve_pcg_linear(const orc_cg_problem* p, const double* x, const double* y, const int* ids,
+                            const double* source, double* solution, const double* dir, int maxIters, double tol,
+                            int pcIters, double pcTol, double* resi, int* iters) {
   if (p->N < 1 || pcIters < 0) return -1;
   LinearPC L;
-  build(p, x, y, L);
+  build(p, x, y, ids, L);
   L.maxIters = pcIters;
   L.tol = pcTol;
   const int n = p->N + 1;

@@ -6,7 +6,10 @@ Method names follow CGsemElliptic_2D_Class.f90:57-93 and IterativeSolvers_Class.
     Au = cg.MatrixAction(u)                                       # %MatrixAction
     r = cg.Residual(source, solution)                             # %Residual
     d = cg.DotProduct(u, v)                                       # %DotProduct
-    sol, rep = cg.Solve(source, method="pcg")                     # %Solve  (or "cg", "gmres")
+    sol, rep = cg.Solve(source, method="pcg")                     # %Solve  (or "cg", "gmres", "pgmres")
+    sol, rep = cg.Solve(source, method="pcg_linear")              # %Solve with the reference's linear-FEM
+                                                                  # preconditioner (pcIterates / pcTolerance)
+    w, its = cg.Precondition(r)                                   # %preconditioner%Solve
 
 Arrays are element-local float64 vectors u(0:N,0:N,1:nEl) flattened in Fortran order.
 """
@@ -16,7 +19,8 @@ import numpy as np
 
 from . import _native as nat
 
-SOLVE_CG, SOLVE_PCG_JACOBI, SOLVE_GMRES, SOLVE_PGMRES_JACOBI = 0, 1, 2, 3
+SOLVE_CG, SOLVE_PCG_JACOBI, SOLVE_GMRES, SOLVE_PGMRES_JACOBI, SOLVE_PCG_LINEAR = 0, 1, 2, 3, 4
+PC_NODES = {"position": 0, "connectivity": 1}  # how the linear-FEM preconditioner mesh finds shared nodes
 
 
 class CG2DDesc(C.Structure):
@@ -24,12 +28,19 @@ class CG2DDesc(C.Structure):
                 ("dmat", nat.dp), ("qweight", nat.dp), ("edges", nat.ip), ("nodeType", nat.ip),
                 ("n2e_ptr", nat.ip), ("n2e_elem", nat.ip), ("n2e_local", nat.ip),
                 ("dxds", nat.dp), ("dxdp", nat.dp), ("dyds", nat.dp), ("dydp", nat.dp), ("J", nat.dp),
-                ("fluxCoeff", nat.dp), ("lam", C.c_double), ("op", C.c_int), ("vx", C.c_double), ("vy", C.c_double)]
+                ("fluxCoeff", nat.dp), ("lam", C.c_double), ("op", C.c_int), ("vx", C.c_double), ("vy", C.c_double),
+                ("x", nat.dp), ("y", nat.dp)]
 
 
 class SolveOpts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("maxIters", C.c_int), ("m", C.c_int),
-                ("tolerance", C.c_double), ("inner_tolerance", C.c_double), ("max_outer", C.c_int)]
+                ("tolerance", C.c_double), ("inner_tolerance", C.c_double), ("max_outer", C.c_int),
+                ("pc_iterations", C.c_int), ("pc_tolerance", C.c_double), ("pc_nodes", C.c_int)]
+
+    def __init__(self, *a, **kw):
+        super().__init__(*a, **kw)
+        if "pc_iterations" not in kw:  # CGsemParams defaults (pcIterates = 50, pcTolerance = 1e-4)
+            self.pc_iterations, self.pc_tolerance = 50, 1e-4
 
 
 class SolveReport(C.Structure):
@@ -41,7 +52,7 @@ class SolveReport(C.Structure):
 
 
 _METHODS = {"cg": SOLVE_CG, "pcg": SOLVE_PCG_JACOBI, "pcg_jacobi": SOLVE_PCG_JACOBI, "gmres": SOLVE_GMRES,
-            "pgmres": SOLVE_PGMRES_JACOBI}
+            "pgmres": SOLVE_PGMRES_JACOBI, "pcg_linear": SOLVE_PCG_LINEAR}
 
 
 class CGsemElliptic_2D:
@@ -58,6 +69,7 @@ class CGsemElliptic_2D:
         fluxCoeff = np.ascontiguousarray(fluxCoeff, dtype=np.float64)
         s.fluxCoeff = nat.d(fluxCoeff)
         s.lam, s.op, s.vx, s.vy = lam, op, vel[0], vel[1]
+        s.x, s.y = nat.d(mesh.x), nat.d(mesh.y)  # node positions: the linear-FEM preconditioner's mesh
         self.ctx, self.nodal, self.mesh = ctx, nodal, mesh
         self.nl = nodal.n * nodal.n * mesh.nEl
         p = C.c_void_p()
@@ -100,12 +112,14 @@ class CGsemElliptic_2D:
         return u
 
     def Solve(self, source, solution=None, method="pcg", precision="fp64", maxIters=20000, tolerance=1e-10, m=30,
-              inner_tolerance=1e-4, max_outer=30, dirichlet=None, return_resi=False):
+              inner_tolerance=1e-4, max_outer=30, dirichlet=None, return_resi=False, pc_iterations=50,
+              pc_tolerance=1e-4, pc_nodes="position"):
         o = SolveOpts()
         o.method = _METHODS[method]
         o.precision = nat.PREC_FP32 if precision == "fp32" else nat.PREC_FP64
         o.maxIters, o.m, o.tolerance = maxIters, m, tolerance
         o.inner_tolerance, o.max_outer = inner_tolerance, max_outer
+        o.pc_iterations, o.pc_tolerance, o.pc_nodes = pc_iterations, pc_tolerance, PC_NODES[pc_nodes]
         sol = np.zeros(self.nl) if solution is None else self._vec(solution).copy()
         resi = np.zeros(maxIters + 1) if return_resi else None
         rep = SolveReport()
@@ -116,6 +130,17 @@ class CGsemElliptic_2D:
         if return_resi:
             out["resi"] = resi
         return sol, out
+
+    def Precondition(self, r, pc_iterations=50, pc_tolerance=1e-4, pc_nodes="position"):
+        """preconditioner%Solve(w, UnMask(r)): the linear-FEM inner CG (FP64).  Returns (w unmasked, CG steps).
+        pc_nodes "position" finds shared nodes by position as the reference does, "connectivity" by the mesh's
+        own shared copies."""
+        o = SolveOpts()
+        o.pc_iterations, o.pc_tolerance, o.pc_nodes = pc_iterations, pc_tolerance, PC_NODES[pc_nodes]
+        w = np.zeros(self.nl)
+        its = C.c_int()
+        self._chk(nat.lib().self_cg2d_precondition(self.ptr, C.byref(o), nat.d(self._vec(r)), nat.d(w), C.byref(its)))
+        return w, its.value
 
     def Trash(self):
         if getattr(self, "ptr", None):

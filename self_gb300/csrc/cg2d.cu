@@ -25,6 +25,8 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <limits>
+#include <unordered_map>
 #include <vector>
 
 #include "cg2d_api.hpp"
@@ -377,7 +379,7 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ 
       const R rk = rr[q] - a * zz[q];
       r[x] = rk;
       const R wk = dinv ? rk * dd[q] : rk;
-      w[x] = wk;
+      if (w) w[x] = wk;
       prw += rk * wk;
       prr += rk * rk;
     }
@@ -387,7 +389,7 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ 
     const R rk = r[k] - a * z[k];
     r[k] = rk;
     const R wk = dinv ? rk * dinv[k] : rk;
-    w[k] = wk;
+    if (w) w[k] = wk;
     prw += rk * wk;
     prr += rk * rk;
   }
@@ -431,6 +433,8 @@ __global__ void __launch_bounds__(kRedThreads) pcg_start_fused(const R* __restri
   double tot[1];
   if (grid_sums_last<1, R>(acc, partial, ticket, tot) && threadIdx.x == 0) S->num = tot[0];
 }
+
+#include "pc_linear.cuh"
 
 // ---------------------------------------------------------------------------------- generic vector ops
 template <typename R>
@@ -574,10 +578,30 @@ struct self_cg2d {
   selfgpu::cg::PcgGraphKey pcg_key[2][2] = {};
   long long pcg_graph_launches = 0;  // kernels in a captured PCG graph
   int apply_grid = 0;                // blocks of the fused apply (grid-stride over element groups)
+  // linear-FEM preconditioner (SELF_SOLVE_PCG_LINEAR): node positions kept from create; the linear mesh's topology,
+  // sub-quad factors and work vectors are built on first use
+  struct PcLinear {
+    std::vector<double> x, y;
+    bool built = false;
+    int ngroups = 0, nUnique = 0, nDirichlet = 0;
+    bool lift = false;  // the linear mesh has Dirichlet nodes the spectral mesh does not
+    int nodes_mode = -1;  // SELF_PC_NODES_* the operands were built for
+    DevBuf<int> src, gptr, gidx;
+    DevBuf<unsigned char> gdir, lprim, dlift;
+    DevBuf<double> fac64, rl, ul, vl, vl2, zl, rd;
+    DevBuf<float> fac32, rl32, ul32, vl32, vl2_32, zl32, rd32;
+    DevBuf<selfgpu::cg::CGScalars> SL;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    selfgpu::cg::PcgGraphKey key[2] = {};
+    int key_iters[2] = {-1, -1};
+    long long graph_launches = 0;
+  } pcl;
   ~self_cg2d() {
     for (auto& row : pcg_graph)
       for (auto& g : row)
         if (g) cudaGraphExecDestroy(g);
+    for (auto& g : pcl.graph)
+      if (g) cudaGraphExecDestroy(g);
   }
 };
 
@@ -679,6 +703,76 @@ int launch_apply_fused(self_cg2d* h, const R* w, const R* vold, R* vnew, R* z, c
   return SELF_OK;
 }
 
+// Linear-FEM preconditioner operator: one wave of resident blocks, grid-stride over element groups.
+template <int N1, typename R>
+void launch_q1_t(self_cg2d* h, const R* w, const R* vold, R* vnew, const int* src, const R* rd, const R* fac, R* z,
+                 CGScalars* SL) {
+  static int resident[2][11] = {};  // per precision and degree: blocks per SM (0 = not queried)
+  int& nb = resident[sizeof(R) == 4][N1];
+  if (nb == 0) {
+    int q = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, q1_apply_fused<N1, R>, kRedThreads, 0) != cudaSuccess) q = 4;
+    nb = std::max(1, q);
+  }
+  const int groups = (h->nEl + cg_epb<N1>() - 1) / cg_epb<N1>();
+  const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
+  q1_apply_fused<N1, R><<<grid, kRedThreads, 0, h->ctx->stream>>>(w, vold, vnew, src, rd, fac, z, h->nEl, h->S.p,
+                                                                 SL, h->partial.p, h->ticket.p);
+}
+
+template <typename R>
+int launch_q1(self_cg2d* h, const R* w, const R* vold, R* vnew, const int* src, const R* rd, const R* fac, R* z,
+              CGScalars* SL) {
+  switch (h->n) {
+    case 3: launch_q1_t<3, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 4: launch_q1_t<4, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 5: launch_q1_t<5, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 6: launch_q1_t<6, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 7: launch_q1_t<7, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 8: launch_q1_t<8, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 9: launch_q1_t<9, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    case 10: launch_q1_t<10, R>(h, w, vold, vnew, src, rd, fac, z, SL); break;
+    default:
+      return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "CG degree %d", h->N);
+  }
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+// Operands of one application of the linear-FEM preconditioner in precision R.
+template <typename R>
+struct PcRun {
+  const R* fac;
+  const int *src, *gptr, *gidx;  // the linear mesh's primary-copy gather and groups
+  const unsigned char *gdir, *lprim, *dlift;
+  int ngroups, iters;
+  R *rl, *ul, *vl, *vl2, *zl, *rd;  // rd: Dirichlet lift, null when the linear mesh needs none
+  CGScalars* SL;
+};
+
+// preconditioner%Solve on the device: u_l from r (spectral masked L-vector), `iters` inner CG iterations at most
+template <typename R>
+int pc_linear_apply(self_cg2d* h, const R* r, const PcRun<R>& pc) {
+  cudaStream_t st = h->ctx->stream;
+  pcl_start<R><<<h->nblk, kRedThreads, 0, st>>>(r, h->src.p, pc.lprim, pc.dlift, pc.rl, pc.ul, pc.rd, h->nl, h->S.p,
+                                                pc.SL, h->partial.p, h->ticket.p);
+  SELF_LAUNCHED(h->ctx);
+  for (int it = 0; it < pc.iters; ++it) {
+    R* lo = (it % 2 == 0) ? pc.vl : pc.vl2;
+    R* ln = (it % 2 == 0) ? pc.vl2 : pc.vl;
+    int rc = launch_q1<R>(h, pc.rl, lo, ln, pc.src, pc.rd, pc.fac, pc.zl, pc.SL);
+    if (rc) return rc;
+    if (pc.ngroups > 0) {
+      cg_dss_mask<R><<<(pc.ngroups + 255) / 256, 256, 0, st>>>(pc.zl, pc.gptr, pc.gidx, pc.gdir, pc.ngroups);
+      SELF_LAUNCHED(h->ctx);
+    }
+    pcl_update<R><<<h->nblk, kRedThreads, 0, st>>>(pc.ul, pc.rl, ln, pc.zl, h->nl, h->S.p, pc.SL, h->partial.p,
+                                                   h->ticket.p);
+    SELF_LAUNCHED(h->ctx);
+  }
+  return SELF_OK;
+}
+
 // MatrixAction: out = Mask(GlobalSum(L(UnMask(x))))
 template <typename R>
 int matrix_action(self_cg2d* h, const R* x, R* out, const selfgpu::cg::OpData<R>& od) {
@@ -724,9 +818,14 @@ namespace cg {
 // buffers alternating); the host reads the scalar block after each graph launch.
 constexpr int kGraphIters = 16;  // even: the current direction is back in `v` after every graph launch
 
+// With pc (linear-FEM preconditioner) every outer iteration starts with the inner solve u_l = M^-1 r and
+// w, num = <r, w> (pc_num); the graph then holds kGraphItersPC outer iterations of 3 * pc->iters + 5 launches.
+constexpr int kGraphItersPC = 2;
+
 template <typename R>
 int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int maxIters, double tol, double r0,
-               double* resi_dev, int* iters, double* rel, const OpData<R>& od, bool abs_stop = true) {
+               double* resi_dev, int* iters, double* rel, const OpData<R>& od, bool abs_stop = true,
+               const PcRun<R>* pc = nullptr) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
   R* v2 = (sizeof(R) == 4) ? reinterpret_cast<R*>(h->v2_32.p) : reinterpret_cast<R*>(h->v2.p);
@@ -741,12 +840,18 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
   hs.resi = resi_dev;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
   if (!hs.done) {
-    pcg_start_fused<R><<<h->nblk, kRedThreads, 0, st>>>(r, dinv, w, h->nl, h->S.p, h->partial.p, h->ticket.p);
-    SELF_LAUNCHED(ctx);
+    if (!pc) {
+      pcg_start_fused<R><<<h->nblk, kRedThreads, 0, st>>>(r, dinv, w, h->nl, h->S.p, h->partial.p, h->ticket.p);
+      SELF_LAUNCHED(ctx);
+    }
+    const int prec = sizeof(R) == 4 ? 1 : 0;
     PcgGraphKey key{u, r, v, v2, w, z, dinv, od.fac.p};
-    cudaGraphExec_t& G = h->pcg_graph[sizeof(R) == 4 ? 1 : 0][dinv ? 1 : 0];
-    PcgGraphKey& gk = h->pcg_key[sizeof(R) == 4 ? 1 : 0][dinv ? 1 : 0];
-    if (G && !(gk == key)) {
+    if (pc) key = PcgGraphKey{u, r, v, v2, w, z, pc->ul, pc->fac};
+    cudaGraphExec_t& G = pc ? h->pcl.graph[prec] : h->pcg_graph[prec][dinv ? 1 : 0];
+    PcgGraphKey& gk = pc ? h->pcl.key[prec] : h->pcg_key[prec][dinv ? 1 : 0];
+    long long& glaunches = pc ? h->pcl.graph_launches : h->pcg_graph_launches;
+    const int per_graph = pc ? kGraphItersPC : kGraphIters;
+    if (G && (!(gk == key) || (pc && h->pcl.key_iters[prec] != pc->iters))) {
       cudaGraphExecDestroy(G);
       G = nullptr;
     }
@@ -755,14 +860,22 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
       int rc = SELF_OK;
       const long long l0 = ctx->launches.load();
       SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < kGraphIters && !rc; ++k) {
+      for (int k = 0; k < per_graph && !rc; ++k) {
         R* vold = (k % 2 == 0) ? v : v2;
         R* vnew = (k % 2 == 0) ? v2 : v;
+        if (pc) {
+          rc = pc_linear_apply<R>(h, r, *pc);
+          if (!rc) {
+            pc_num<R><<<h->nblk, kRedThreads, 0, st>>>(r, pc->ul, h->src.p, pc->src, w, h->nl, h->S.p,
+                                                       h->partial.p, h->ticket.p);
+            SELF_LAUNCHED(ctx);
+          }
+        }
         if (!rc) rc = launch_apply_fused<R>(h, w, vold, vnew, z, od);
         if (!rc) rc = launch_dss<R>(h, z);
         if (!rc) {
-          pcg_update_fused<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, w, vnew, z, dinv, h->nl, h->S.p, h->partial.p,
-                                                              h->ticket.p);
+          pcg_update_fused<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, pc ? nullptr : w, vnew, z, pc ? nullptr : dinv,
+                                                              h->nl, h->S.p, h->partial.p, h->ticket.p);
           SELF_LAUNCHED(ctx);
         }
       }
@@ -773,13 +886,14 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
       gk = key;
-      h->pcg_graph_launches = ctx->launches.load() - l0;
-      ctx->launches.fetch_sub(h->pcg_graph_launches);
+      if (pc) h->pcl.key_iters[prec] = pc->iters;
+      glaunches = ctx->launches.load() - l0;
+      ctx->launches.fetch_sub(glaunches);
     }
-    const long long max_launches = (long long)maxIters / kGraphIters + 2;
+    const long long max_launches = (long long)maxIters / per_graph + 2;
     for (long long gl = 0; gl < max_launches; ++gl) {
       SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
-      ctx->launches.fetch_add(h->pcg_graph_launches);
+      ctx->launches.fetch_add(glaunches);
       SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
       SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (hs.done) break;
@@ -1042,6 +1156,10 @@ int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* d, self_cg2d** out) {
   h->nl = (size_t)h->n * h->n * h->nEl;
   int rc = compile_topology(h.get(), d);
   if (rc) return rc;
+  if (d->x && d->y) {  // kept for the linear-FEM preconditioner, built on first use
+    h->pcl.x.assign(d->x, d->x + h->nl);
+    h->pcl.y.assign(d->y, d->y + h->nl);
+  }
   std::vector<double> Jww;
   if ((rc = build_factors(h.get(), d, Jww))) return rc;
   h->h_J.assign(d->J, d->J + h->nl);
@@ -1147,6 +1265,245 @@ template <typename R>
 int unmask_dev(self_cg2d* h, R* out, const R* in) {
   cg_unmask<R><<<h->nblk, kRedThreads, 0, h->ctx->stream>>>(out, in, h->src.p, h->nl);
   SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+// AlmostEqual (CommonRoutines.f90:58-96): |a-b| <= eps, or eps relative to either value when neither is 0.
+bool almost_equal(double a, double b) {
+  const double eps = std::numeric_limits<double>::epsilon();
+  if (a == 0.0 || b == 0.0) return std::fabs(a - b) <= eps;
+  return std::fabs(a - b) <= eps * std::fabs(a) || std::fabs(a - b) <= eps * std::fabs(b);
+}
+
+// Node identification of ConstructLinearMeshFromOther (QuadMeshClass.f90:1899-1952): local node l takes the ID of
+// the first earlier local node at the same position (AlmostEqual in x and y), else a new ID.  A hash grid of cell
+// size 1e-9 x the mesh extent (far above AlmostEqual's ~1e-16 relative tolerance) limits the search to the 3 x 3
+// neighbouring cells; the result is that of the reference's all-pairs search.
+int linear_node_ids(const std::vector<double>& x, const std::vector<double>& y, std::vector<int>& uid) {
+  const size_t n = x.size();
+  double x0 = x[0], x1 = x[0], y0 = y[0], y1 = y[0];
+  for (size_t k = 1; k < n; ++k) {
+    x0 = std::min(x0, x[k]);
+    x1 = std::max(x1, x[k]);
+    y0 = std::min(y0, y[k]);
+    y1 = std::max(y1, y[k]);
+  }
+  const double h = std::max({x1 - x0, y1 - y0, 1e-300}) * 1e-9;
+  auto cell = [&](double v, double o) { return (long long)std::floor((v - o) / h); };
+  auto key = [](long long a, long long b) {
+    return (unsigned long long)a * 0x9E3779B97F4A7C15ull ^ (unsigned long long)b;
+  };
+  std::unordered_map<unsigned long long, int> head;  // cell -> latest node in it (list through `next`)
+  head.reserve(n);
+  std::vector<int> next(n, -1);
+  uid.assign(n, -1);
+  int nu = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const long long cx = cell(x[i], x0), cy = cell(y[i], y0);
+    int best = -1;
+    for (long long dx = -1; dx <= 1; ++dx)
+      for (long long dy = -1; dy <= 1; ++dy) {
+        auto it = head.find(key(cx + dx, cy + dy));
+        if (it == head.end()) continue;
+        for (int j = it->second; j >= 0; j = next[j])
+          if ((best < 0 || j < best) && almost_equal(x[i], x[j]) && almost_equal(y[i], y[j])) best = j;
+      }
+    uid[i] = best >= 0 ? uid[best] : nu++;
+    auto it = head.find(key(cx, cy));
+    if (it == head.end()) {
+      head.emplace(key(cx, cy), (int)i);
+    } else {
+      next[i] = it->second;
+      it->second = (int)i;
+    }
+  }
+  return nu;
+}
+
+// Linear-FEM preconditioner operands, built on first use:
+//  * the linear mesh's topology in the L-vector layout: node IDs by position (above); its Dirichlet set = the
+//    nodes of sub-quad sides no other sub-quad shares (ConstructEdges gives them NO_NORMAL_FLOW, which
+//    CGsemPreconditioner_2D Build turns into DIRICHLET), plus the spectral mesh's own Dirichlet nodes; src (copy
+//    -> primary copy, the lowest local index, i.e. the first linear element of the node's list), groups (all
+//    copies of a shared or Dirichlet node in element order), lprim (primary copies of non-Dirichlet nodes) and
+//    dlift (copies Dirichlet here but not in the spectral mesh: the Dirichlet lift);
+//  * the folded metric factors of every GLL sub-quad (bilinear element through its four corner nodes,
+//    CGsemPreconditioner_2D's fluxCoeff = 1, Gauss-Lobatto weights 1), corner (a, b) of sub-quad (si, pj) at
+//    4 (si + N pj) + a + 2 b:
+//      dx/ds = (x(si+1, pj+b) - x(si, pj+b)) / 2,  dx/dp = (x(si+a, pj+1) - x(si+a, pj)) / 2  (and y alike),
+//      G11 = (yp^2 + xp^2) / J,  G12 = -(ys yp + xs xp) / J,  G22 = (xs^2 + ys^2) / J,  J = xs yp - xp ys,
+//    the transfinite metrics of a straight-sided element at its corners (MappedGeometryClass_2D GenerateMetrics
+//    :611-710 on ConstructLinearMeshFromOther's straight side curves);
+//  * work vectors in the precision asked for.
+int pcl_ensure(self_cg2d* h, bool fp32, int nodes_mode) {
+  auto& P = h->pcl;
+  self_ctx* ctx = h->ctx;
+  if (P.x.empty())
+    return set_error(ctx, SELF_ERR_INVALID, "linear-FEM preconditioner: the descriptor gave no node positions (x, y)");
+  if (nodes_mode != SELF_PC_NODES_POSITION && nodes_mode != SELF_PC_NODES_CONNECTIVITY)
+    return set_error(ctx, SELF_ERR_INVALID, "preconditioner node identification %d", nodes_mode);
+  int rc;
+  const int N = h->N, n = h->n, NQ = 4 * N * N;
+  const size_t NN = (size_t)n * n, nl = h->nl;
+  if (P.built && P.nodes_mode != nodes_mode) {  // rebuild the topology; graphs hold the old group count
+    P.built = false;
+    for (auto& g : P.graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
+  if (!P.built) {
+    std::vector<int> uid;
+    int nu = 0;
+    if (nodes_mode == SELF_PC_NODES_POSITION) {
+      nu = linear_node_ids(P.x, P.y, uid);
+    } else {  // the spectral mesh's groups, numbered in first-appearance order
+      std::vector<int> rep(nl);
+      for (size_t l = 0; l < nl; ++l) rep[l] = (int)l;
+      for (int g = 0; g < h->ngroups; ++g)
+        for (int k = h->h_gptr[g]; k < h->h_gptr[g + 1]; ++k) rep[h->h_gidx[k]] = h->h_gidx[h->h_gptr[g]];
+      std::vector<int> id_of(nl, -1);
+      uid.assign(nl, 0);
+      for (size_t l = 0; l < nl; ++l) {
+        int& v = id_of[rep[l]];
+        if (v < 0) v = nu++;
+        uid[l] = v;
+      }
+    }
+    std::vector<unsigned char> dir(nu, 0);
+    for (int g = 0; g < h->ngroups; ++g)
+      if (h->h_gdir[g])
+        for (int k = h->h_gptr[g]; k < h->h_gptr[g + 1]; ++k) dir[uid[h->h_gidx[k]]] = 1;
+    // sub-quad sides on the spectral elements' sides (sub-quad sides inside an element are always shared)
+    std::unordered_map<unsigned long long, int> sides;
+    sides.reserve((size_t)h->nEl * 4 * N);
+    auto side_key = [](int a, int b) {
+      return ((unsigned long long)std::min(a, b) << 32) | (unsigned long long)std::max(a, b);
+    };
+    auto side_node = [&](int side, int k, int& i, int& j) {
+      switch (side) {
+        case 0: i = k; j = 0; break;
+        case 1: i = N; j = k; break;
+        case 2: i = k; j = N; break;
+        default: i = 0; j = k; break;
+      }
+    };
+    for (int pass = 0; pass < 2; ++pass)
+      for (int e = 0; e < h->nEl; ++e)
+        for (int side = 0; side < 4; ++side)
+          for (int m = 0; m < N; ++m) {
+            int i0, j0, i1, j1;
+            side_node(side, m, i0, j0);
+            side_node(side, m + 1, i1, j1);
+            const int a = uid[(size_t)e * NN + i0 + (size_t)n * j0], b = uid[(size_t)e * NN + i1 + (size_t)n * j1];
+            if (pass == 0) {
+              sides[side_key(a, b)] += 1;
+            } else if (sides[side_key(a, b)] == 1) {
+              dir[a] = 1;
+              dir[b] = 1;
+            }
+          }
+    // copies of every node, in local-index (= element) order
+    std::vector<int> first(nu, -1), ptr(nu + 1, 0);
+    for (size_t l = 0; l < nl; ++l) {
+      ptr[uid[l] + 1]++;
+      if (first[uid[l]] < 0) first[uid[l]] = (int)l;
+    }
+    for (int u = 0; u < nu; ++u) ptr[u + 1] += ptr[u];
+    std::vector<int> lst(nl), pos(ptr.begin(), ptr.end() - 1);
+    for (size_t l = 0; l < nl; ++l) lst[pos[uid[l]]++] = (int)l;
+    std::vector<int> src(nl), gptr(1, 0), gidx;
+    std::vector<unsigned char> gdir, lprim(nl, 0), sdir(nl, 0), dlift(nl, 0);
+    for (int g = 0; g < h->ngroups; ++g)
+      if (h->h_gdir[g])
+        for (int k = h->h_gptr[g]; k < h->h_gptr[g + 1]; ++k) sdir[h->h_gidx[k]] = 1;
+    P.lift = false;
+    for (size_t l = 0; l < nl; ++l) {
+      const int u = uid[l];
+      src[l] = dir[u] ? (int)l : first[u];
+      lprim[l] = (!dir[u] && first[u] == (int)l) ? 1 : 0;
+      dlift[l] = (dir[u] && !sdir[l]) ? 1 : 0;
+      P.lift = P.lift || dlift[l];
+    }
+    int nd = 0;
+    for (int u = 0; u < nu; ++u) {
+      nd += dir[u];
+      if (ptr[u + 1] - ptr[u] < 2 && !dir[u]) continue;
+      for (int k = ptr[u]; k < ptr[u + 1]; ++k) gidx.push_back(lst[k]);
+      gptr.push_back((int)gidx.size());
+      gdir.push_back(dir[u]);
+    }
+    P.ngroups = (int)gdir.size();
+    P.nodes_mode = nodes_mode;
+    P.nUnique = nu;
+    P.nDirichlet = nd;
+    std::vector<double> fac((size_t)3 * NQ * h->nEl);
+    for (int e = 0; e < h->nEl; ++e) {
+      const double* X = &P.x[(size_t)e * NN];
+      const double* Y = &P.y[(size_t)e * NN];
+      double* fe = &fac[(size_t)e * 3 * NQ];
+      for (int pj = 0; pj < N; ++pj)
+        for (int si = 0; si < N; ++si)
+          for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) {
+              const double xs = 0.5 * (X[(si + 1) + n * (pj + b)] - X[si + n * (pj + b)]);
+              const double ys = 0.5 * (Y[(si + 1) + n * (pj + b)] - Y[si + n * (pj + b)]);
+              const double xp = 0.5 * (X[(si + a) + n * (pj + 1)] - X[(si + a) + n * pj]);
+              const double yp = 0.5 * (Y[(si + a) + n * (pj + 1)] - Y[(si + a) + n * pj]);
+              const double J = xs * yp - xp * ys;
+              if (!(J != 0.0) || !std::isfinite(J))
+                return set_error(ctx, SELF_ERR_INVALID, "degenerate GLL sub-quad in element %d", e + 1);
+              const int c = 4 * (si + N * pj) + a + 2 * b;
+              fe[c] = (yp * yp + xp * xp) / J;
+              fe[NQ + c] = -(ys * yp + xs * xp) / J;
+              fe[2 * NQ + c] = (xs * xs + ys * ys) / J;
+            }
+    }
+    if ((rc = upload(ctx, P.fac64, fac))) return rc;
+    std::vector<float> f32(fac.begin(), fac.end());
+    if ((rc = upload(ctx, P.fac32, f32))) return rc;
+    if ((rc = upload(ctx, P.src, src)) || (rc = upload(ctx, P.lprim, lprim))) return rc;
+    if (P.lift && (rc = upload(ctx, P.dlift, dlift))) return rc;
+    if (P.ngroups > 0 &&
+        ((rc = upload(ctx, P.gptr, gptr)) || (rc = upload(ctx, P.gidx, gidx)) || (rc = upload(ctx, P.gdir, gdir))))
+      return rc;
+    if (P.SL.n == 0 && P.SL.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "allocation failed");
+    P.built = true;
+  }
+  if (fp32) {
+    if ((rc = ensuref(ctx, P.rl32, nl)) || (rc = ensuref(ctx, P.ul32, nl)) || (rc = ensuref(ctx, P.vl32, nl)) ||
+        (rc = ensuref(ctx, P.vl2_32, nl)) || (rc = ensuref(ctx, P.zl32, nl)) ||
+        (P.lift && (rc = ensuref(ctx, P.rd32, nl))))
+      return rc;
+  } else if ((rc = ensure(ctx, P.rl, nl)) || (rc = ensure(ctx, P.ul, nl)) || (rc = ensure(ctx, P.vl, nl)) ||
+             (rc = ensure(ctx, P.vl2, nl)) || (rc = ensure(ctx, P.zl, nl)) || (P.lift && (rc = ensure(ctx, P.rd, nl)))) {
+    return rc;
+  }
+  return SELF_OK;
+}
+
+template <typename R>
+PcRun<R> pcl_run(self_cg2d* h, int iters);
+template <>
+PcRun<double> pcl_run<double>(self_cg2d* h, int iters) {
+  auto& P = h->pcl;
+  return PcRun<double>{P.fac64.p, P.src.p, P.gptr.p, P.gidx.p, P.gdir.p, P.lprim.p, P.dlift.p, P.ngroups, iters,
+                       P.rl.p, P.ul.p, P.vl.p, P.vl2.p, P.zl.p, P.lift ? P.rd.p : nullptr, P.SL.p};
+}
+template <>
+PcRun<float> pcl_run<float>(self_cg2d* h, int iters) {
+  auto& P = h->pcl;
+  return PcRun<float>{P.fac32.p, P.src.p, P.gptr.p, P.gidx.p, P.gdir.p, P.lprim.p, P.dlift.p, P.ngroups, iters,
+                      P.rl32.p, P.ul32.p, P.vl32.p, P.vl2_32.p, P.zl32.p, P.lift ? P.rd32.p : nullptr, P.SL.p};
+}
+
+// inner CG limits of the preconditioner (pcl_start resets the other scalars and keeps these)
+int pcl_limits(self_cg2d* h, int iters, double tol) {
+  CGScalars sl{};
+  sl.maxIters = iters;
+  sl.tol = tol;
+  SELF_CUDA_TRY(h->ctx, cudaMemcpyAsync(h->pcl.SL.p, &sl, sizeof(sl), cudaMemcpyHostToDevice, h->ctx->stream));
   return SELF_OK;
 }
 
@@ -1343,8 +1700,12 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   self_ctx* ctx = h->ctx;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   if (o->maxIters < 0 || !(o->tolerance > 0)) return set_error(ctx, SELF_ERR_INVALID, "bad solver options");
-  if (o->method < SELF_SOLVE_CG || o->method > SELF_SOLVE_PGMRES_JACOBI)
+  if (o->method < SELF_SOLVE_CG || o->method > SELF_SOLVE_PCG_LINEAR)
     return set_error(ctx, SELF_ERR_INVALID, "solver method %d", o->method);
+  const bool lin = o->method == SELF_SOLVE_PCG_LINEAR;
+  if (lin && (o->pc_iterations < 0 || !(o->pc_tolerance >= 0)))
+    return set_error(ctx, SELF_ERR_INVALID, "preconditioner iterations %d / tolerance %g", o->pc_iterations,
+                     o->pc_tolerance);
   const bool gm = o->method == SELF_SOLVE_GMRES || o->method == SELF_SOLVE_PGMRES_JACOBI;
   if (gm && (o->m < 1 || o->m > 512))
     return set_error(ctx, SELF_ERR_INVALID, "GMRES restart length %d", o->m);
@@ -1359,6 +1720,12 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
       (rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->v, nl)) || (rc = ensure(ctx, h->w, nl)) ||
       (rc = ensure(ctx, h->z, nl)) || (!gm && (rc = ensure(ctx, h->v2, nl))))
     return rc;
+  // the linear-FEM preconditioner with pc_iterations = 0 is the identity (w = r): plain CG
+  const bool use_pcl = lin && o->pc_iterations > 0;
+  if (use_pcl) {
+    if ((rc = pcl_ensure(h, o->precision != SELF_PREC_FP64, o->pc_nodes))) return rc;
+    if ((rc = pcl_limits(h, o->pc_iterations, o->pc_tolerance))) return rc;
+  }
   if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
   self_solve_report R{};
   R.ioerr = -2;
@@ -1379,8 +1746,10 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         if ((rc = ensure(ctx, resi_dev, (size_t)o->maxIters + 1))) return rc;
         SELF_CUDA_TRY(ctx, cudaMemsetAsync(resi_dev.p, 0, ((size_t)o->maxIters + 1) * sizeof(double), ctx->stream));
       }
+      const PcRun<double> pc = use_pcl ? pcl_run<double>(h, o->pc_iterations) : PcRun<double>{};
       R.ioerr = pcg_device<double>(h, h->u.p, h->r.p, h->v.p, h->w.p, h->z.p, jac ? h->op64.dinv.p : nullptr,
-                                   o->maxIters, o->tolerance, r0, resi ? resi_dev.p : nullptr, &iters, &rel, h->op64);
+                                   o->maxIters, o->tolerance, r0, resi ? resi_dev.p : nullptr, &iters, &rel, h->op64,
+                                   true, use_pcl ? &pc : nullptr);
       if (resi) {
         SELF_CUDA_TRY(ctx, cudaMemcpyAsync(resi, resi_dev.p, ((size_t)o->maxIters + 1) * sizeof(double),
                                            cudaMemcpyDeviceToHost, ctx->stream));
@@ -1406,8 +1775,10 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->u32.p, 0, nl * sizeof(float), ctx->stream));
         int it_in = 0;
         double rel_in = 0;
+        const PcRun<float> pc = use_pcl ? pcl_run<float>(h, o->pc_iterations) : PcRun<float>{};
         pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p, jac ? h->op32.dinv.p : nullptr,
-                          o->maxIters - total, inner_tol, rn, nullptr, &it_in, &rel_in, h->op32, false);
+                          o->maxIters - total, inner_tol, rn, nullptr, &it_in, &rel_in, h->op32, false,
+                          use_pcl ? &pc : nullptr);
         total += it_in;
         // x += d (FP64), r = b - A x in FP64
         convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->u32.p, nl);
@@ -1440,6 +1811,38 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   R.rel_residual = rel;
   if (rep) *rep = R;
   if (R.ioerr == SELF_ERR_NONFINITE) return set_error(ctx, SELF_ERR_NONFINITE, "non-finite residual");
+  return SELF_OK;
+}
+
+int self_cg2d_precondition(self_cg2d* h, const self_solve_opts* o, const double* r, double* w, int* iterations) {
+  if (!h || !o || !r || !w) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (o->pc_iterations < 0 || !(o->pc_tolerance >= 0))
+    return set_error(ctx, SELF_ERR_INVALID, "preconditioner iterations %d / tolerance %g", o->pc_iterations,
+                     o->pc_tolerance);
+  int rc;
+  if ((rc = upload_vec(h, h->r, r)) || (rc = ensure(ctx, h->w, h->nl))) return rc;
+  if ((rc = mask_dev<double>(h, h->r.p))) return rc;
+  int its = 0;
+  if (o->pc_iterations == 0) {  // u = r
+    if ((rc = unmask_dev<double>(h, h->w.p, h->r.p))) return rc;
+  } else {
+    if ((rc = pcl_ensure(h, false, o->pc_nodes)) || (rc = pcl_limits(h, o->pc_iterations, o->pc_tolerance)))
+      return rc;
+    CGScalars hs{};  // outer scalars: not done, so the preconditioner kernels run
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
+    const PcRun<double> pc = pcl_run<double>(h, o->pc_iterations);
+    if ((rc = pc_linear_apply<double>(h, h->r.p, pc))) return rc;
+    cg_unmask<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->w.p, pc.ul, pc.src, h->nl);  // linear UnMask
+    SELF_LAUNCHED(ctx);
+    CGScalars sl{};
+    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&sl, h->pcl.SL.p, sizeof(sl), cudaMemcpyDeviceToHost, ctx->stream));
+    SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    its = sl.iter;
+  }
+  if ((rc = download_vec(h, w, h->w.p))) return rc;
+  if (iterations) *iterations = its;
   return SELF_OK;
 }
 

@@ -8,6 +8,8 @@ import os
 
 import numpy as np
 
+from helpers import connectivity_ids
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -89,3 +91,35 @@ def test_preconditioner_application_properties(oracle):
     w0, it0 = P.pc_linear_apply(b, pcIters=0, pcTol=1e-4)
     assert it0 == 0
     np.testing.assert_array_equal(w0, b)
+
+
+def test_connectivity_ids_give_the_topological_linear_mesh(oracle):
+    """Identified by the mesh's own shared copies, the SpecMesh square's linear mesh has the topology's node count
+    and only its physical boundary Dirichlet; the preconditioned solve then converges where the position search
+    (the reference) stalls."""
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    nat = sg._native
+    N = 4
+    mesh = sg.read_ism_mesh(os.path.join(ROOT, "tests", "golden", "square.mesh"), N, nat.GAUSS_LOBATTO)
+    nod = sg.NodalStorage_2D(N, nat.GAUSS_LOBATTO, nat.CG)
+    k, f, source = W.helmholtz(mesh, N)
+    P = oracle.CGProblem(nod, mesh, k, lam=0.1)
+    ids = connectivity_ids(mesh, N)
+    topo = mesh.nNodes + mesh.nEdges * (N - 1) + mesh.nEl * (N - 1) ** 2
+    nb = int((mesh.edges.reshape(-1, 6)[:, 2] < 0).sum()) * N
+    assert P.pc_linear_info(ids) == (topo, nb)
+    s1, e1, it1, r1 = P.solve_pcg_linear(source, maxIters=400, tol=1e-10, pcIters=12, ids=ids)
+    s0, e0, it0, r0 = P.solve_pcg_linear(source, maxIters=100, tol=1e-10, pcIters=12)
+    s2, e2, it2, _ = P.solve_pcg(source, maxIters=3000, tol=1e-10, precond=1)
+    assert e1 == 0 and e2 == 0 and it1 < it2
+    assert np.abs(s1 - s2).max() <= 1e-8 * np.abs(s2).max()
+    assert e0 == -1 and r0[-1] / r0[0] > 1e-2
+    # on a structured mesh both identifications give the same linear mesh and the same iterates
+    _, _, src2, Q = _square(oracle, 4, 5, 0.02)
+    import self_gb300 as sg2  # noqa: F401
+    m2 = Q.keep[1]
+    a = Q.solve_pcg_linear(src2, maxIters=300, tol=1e-10, pcIters=10)
+    b = Q.solve_pcg_linear(src2, maxIters=300, tol=1e-10, pcIters=10, ids=connectivity_ids(m2, 4))
+    assert a[2] == b[2]
+    np.testing.assert_array_equal(a[3], b[3])
