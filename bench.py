@@ -294,6 +294,25 @@ def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=3000):
         else:
             out["pcg_fp32"]["max_rel_diff_vs_fp64"] = float(np.abs(sol - s64).max() / np.abs(s64).max())
     out["speedup_fp32_ir_vs_fp64"] = out["pcg_fp64"]["seconds"] / out["pcg_fp32"]["seconds"]
+    # the reference's own %Solve: PCG with the linear-FEM preconditioner (pcIterates = 20, pcTolerance = 1e-4 as in
+    # its paraboloid example); the first call builds the preconditioner mesh (host) and captures the graphs
+    t0 = time.perf_counter()
+    cg.Solve(source, method="pcg_linear", tolerance=1e-10, maxIters=4, pc_iterations=20)
+    ctx.synchronize()
+    setup = time.perf_counter() - t0
+    for prec in ("fp64", "fp32"):
+        cg.Solve(source, method="pcg_linear", precision=prec, tolerance=1e-10, maxIters=4, pc_iterations=20)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        sol, rep = cg.Solve(source, method="pcg_linear", precision=prec, tolerance=1e-10, maxIters=20000,
+                            pc_iterations=20, pc_tolerance=1e-4)
+        el = time.perf_counter() - t0
+        out["pcg_linear_" + prec] = {"seconds": el, "solves_per_s": 1.0 / el, "iterations": rep["iterations"],
+                                     "ms_per_iteration": 1e3 * el / max(1, rep["iterations"]),
+                                     "inner_iterations_max": 20, "outer": rep["outer_iterations"],
+                                     "rel_residual": rep["rel_residual"], "ioerr": rep["ioerr"],
+                                     "max_rel_diff_vs_pcg_fp64": float(np.abs(sol - s64).max() / np.abs(s64).max())}
+    out["pcg_linear_fp64"]["preconditioner_setup_seconds"] = setup
     cg.Trash()
     ad = sg.CGsemElliptic_2D(ctx, nod, mesh, np.full_like(k, 1e-3), lam=0.0, op=1, vel=(1.0, 0.5))
     for method, key in (("gmres", "gmres30_fp64"), ("pgmres", "pgmres30_jacobi_fp64")):
@@ -411,7 +430,8 @@ def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, fp64_sample=60):
 
 def run_cg_profile(args):
     """Bounded CGSEM workload for profilers (no JSON line): the 256x256 N=7 Helmholtz problem of the elliptic
-    leg, `--profile-cg K` FP32 PCG iterations after a 32-iteration warm-up solve."""
+    leg, `--profile-cg K` PCG iterations (`--profile-method`: pcg = Jacobi, pcg_linear = the linear-FEM
+    preconditioner with 20 inner iterations; `--profile-precision`) after a short warm-up solve."""
     import self_gb300 as sg
     from self_gb300 import _native as nat
     from self_gb300 import workloads as W
@@ -421,12 +441,15 @@ def run_cg_profile(args):
     mesh = sg.QuadMesh(nx, nx, N, nat.GAUSS_LOBATTO, boundary_flag=nat.DIRICHLET)
     k, f, source = W.helmholtz(mesh, N, seed=3)
     cg = sg.CGsemElliptic_2D(ctx, nod, mesh, k, lam=0.1)
-    cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-10, maxIters=32)
+    method, prec = args.profile_method, args.profile_precision
+    warm = 32 if method == "pcg" else 4
+    cg.Solve(source, method=method, precision=prec, tolerance=1e-10, maxIters=warm, pc_iterations=20)
     ctx.synchronize()
     t0 = time.perf_counter()
-    _, rep = cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-30, maxIters=args.profile_cg, max_outer=1)
+    _, rep = cg.Solve(source, method=method, precision=prec, tolerance=1e-30, maxIters=args.profile_cg, max_outer=1,
+                      pc_iterations=20, pc_tolerance=0.0)
     el = time.perf_counter() - t0
-    print(f"profile-cg: {rep['iterations']} FP32 PCG iterations in {el:.4f} s", flush=True)
+    print(f"profile-cg: {rep['iterations']} {prec.upper()} {method} iterations in {el:.4f} s", flush=True)
     cg.Trash()
     ctx.close()
 
@@ -589,7 +612,9 @@ def main():
     ap.add_argument("--batched-n", type=int, default=512, help="problems of the batched leg (0 skips it)")
     ap.add_argument("--serve-n", type=int, default=300, help="requests of the serving leg (0 skips it)")
     ap.add_argument("--profile-cg", type=int, default=0,
-                    help="run only K FP32 PCG iterations of the elliptic workload (for profilers) and exit")
+                    help="run only K PCG iterations of the elliptic workload (for profilers) and exit")
+    ap.add_argument("--profile-method", default="pcg", choices=["pcg", "pcg_linear"])
+    ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_cg > 0:
