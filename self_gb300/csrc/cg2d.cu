@@ -1327,13 +1327,13 @@ int linear_node_ids(const std::vector<double>& x, const std::vector<double>& y, 
 //    -> primary copy, the lowest local index, i.e. the first linear element of the node's list), groups (all
 //    copies of a shared or Dirichlet node in element order), lprim (primary copies of non-Dirichlet nodes) and
 //    dlift (copies Dirichlet here but not in the spectral mesh: the Dirichlet lift);
-//  * the folded metric factors of every GLL sub-quad (bilinear element through its four corner nodes,
-//    CGsemPreconditioner_2D's fluxCoeff = 1, Gauss-Lobatto weights 1), corner (a, b) of sub-quad (si, pj) at
-//    4 (si + N pj) + a + 2 b:
+//  * the element stencils: per GLL sub-quad (bilinear element through its four corner nodes,
+//    CGsemPreconditioner_2D's fluxCoeff = 1, Gauss-Lobatto weights 1) the folded metric factors at corner (a, b)
 //      dx/ds = (x(si+1, pj+b) - x(si, pj+b)) / 2,  dx/dp = (x(si+a, pj+1) - x(si+a, pj)) / 2  (and y alike),
 //      G11 = (yp^2 + xp^2) / J,  G12 = -(ys yp + xs xp) / J,  G22 = (xs^2 + ys^2) / J,  J = xs yp - xp ys,
-//    the transfinite metrics of a straight-sided element at its corners (MappedGeometryClass_2D GenerateMetrics
-//    :611-710 on ConstructLinearMeshFromOther's straight side curves);
+//    (the transfinite metrics of a straight-sided element at its corners, MappedGeometryClass_2D GenerateMetrics
+//    :611-710 on ConstructLinearMeshFromOther's straight side curves), the sub-quad operator formed from them
+//    and summed into the element's 9-point stencil;
 //  * work vectors in the precision asked for.
 int pcl_ensure(self_cg2d* h, bool fp32, int nodes_mode) {
   auto& P = h->pcl;
@@ -1343,7 +1343,7 @@ int pcl_ensure(self_cg2d* h, bool fp32, int nodes_mode) {
   if (nodes_mode != SELF_PC_NODES_POSITION && nodes_mode != SELF_PC_NODES_CONNECTIVITY)
     return set_error(ctx, SELF_ERR_INVALID, "preconditioner node identification %d", nodes_mode);
   int rc;
-  const int N = h->N, n = h->n, NQ = 4 * N * N;
+  const int N = h->N, n = h->n;
   const size_t NN = (size_t)n * n, nl = h->nl;
   if (P.built && P.nodes_mode != nodes_mode) {  // rebuild the topology; graphs hold the old group count
     P.built = false;
@@ -1438,13 +1438,17 @@ int pcl_ensure(self_cg2d* h, bool fp32, int nodes_mode) {
     P.nodes_mode = nodes_mode;
     P.nUnique = nu;
     P.nDirichlet = nd;
-    std::vector<double> fac((size_t)3 * NQ * h->nEl);
+    // the element's 9-point stencil: every sub-quad's 4 x 4 operator (FluxDivergence on the sub-quad applied to
+    // its 4 unit corner vectors) added into the rows of its corner nodes; kept: self, E, N, NE, NW per node
+    std::vector<double> fac((size_t)kQ1Slots * NN * h->nEl, 0.0);
+    std::vector<double> st(NN * 9);
     for (int e = 0; e < h->nEl; ++e) {
       const double* X = &P.x[(size_t)e * NN];
       const double* Y = &P.y[(size_t)e * NN];
-      double* fe = &fac[(size_t)e * 3 * NQ];
+      std::fill(st.begin(), st.end(), 0.0);
       for (int pj = 0; pj < N; ++pj)
-        for (int si = 0; si < N; ++si)
+        for (int si = 0; si < N; ++si) {
+          double G11[4], G12[4], G22[4];
           for (int b = 0; b < 2; ++b)
             for (int a = 0; a < 2; ++a) {
               const double xs = 0.5 * (X[(si + 1) + n * (pj + b)] - X[si + n * (pj + b)]);
@@ -1454,11 +1458,39 @@ int pcl_ensure(self_cg2d* h, bool fp32, int nodes_mode) {
               const double J = xs * yp - xp * ys;
               if (!(J != 0.0) || !std::isfinite(J))
                 return set_error(ctx, SELF_ERR_INVALID, "degenerate GLL sub-quad in element %d", e + 1);
-              const int c = 4 * (si + N * pj) + a + 2 * b;
-              fe[c] = (yp * yp + xp * xp) / J;
-              fe[NQ + c] = -(ys * yp + xs * xp) / J;
-              fe[2 * NQ + c] = (xs * xs + ys * ys) / J;
+              const int c = a + 2 * b;
+              G11[c] = (yp * yp + xp * xp) / J;
+              G12[c] = -(ys * yp + xs * xp) / J;
+              G22[c] = (xs * xs + ys * ys) / J;
             }
+          for (int beta = 0; beta < 4; ++beta) {
+            double u[4] = {0, 0, 0, 0}, F1[4], F2[4];
+            u[beta] = 1.0;
+            for (int c = 0; c < 4; ++c) {
+              const int a = c & 1, b = c >> 1;
+              const double us = 0.5 * (u[1 + 2 * b] - u[2 * b]);
+              const double up = 0.5 * (u[a + 2] - u[a]);
+              F1[c] = G11[c] * us + G12[c] * up;
+              F2[c] = G12[c] * us + G22[c] * up;
+            }
+            for (int al = 0; al < 4; ++al) {
+              const int a = al & 1, b = al >> 1;
+              const double d1 = (a ? 0.5 : -0.5) * (F1[2 * b] + F1[1 + 2 * b]);
+              const double d2 = (b ? 0.5 : -0.5) * (F2[a] + F2[a + 2]);
+              const int di = (beta & 1) - a, dj = (beta >> 1) - b;
+              st[(size_t)((si + a) + n * (pj + b)) * 9 + (di + 1) + 3 * (dj + 1)] += -(d1 + d2);
+            }
+          }
+        }
+      double* fe = &fac[(size_t)e * kQ1Slots * NN];
+      for (size_t t = 0; t < NN; ++t) {
+        const double* c9 = &st[t * 9];
+        fe[kQ1Self * NN + t] = c9[4];  // (0, 0)
+        fe[kQ1E * NN + t] = c9[5];     // (1, 0)
+        fe[kQ1N * NN + t] = c9[7];     // (0, 1)
+        fe[kQ1NE * NN + t] = c9[8];    // (1, 1)
+        fe[kQ1NW * NN + t] = c9[6];    // (-1, 1)
+      }
     }
     if ((rc = upload(ctx, P.fac64, fac))) return rc;
     std::vector<float> f32(fac.begin(), fac.end());

@@ -8,13 +8,14 @@
 // its 1-4 sub-quad copies, which always share one position), with the linear mesh's own primary-copy gather
 // (UnMask), direct-stiffness groups (GlobalSum + Mask) and Dirichlet set, compiled on the host from the
 // reference's position-based node identification; the inner CG uses the element-local <v, Lv> trick of the
-// fused PCG.  The N^2 sub-quads of one element are applied together from shared memory:
-//   corner (a, b) of sub-quad (si, pj):  us = (u(si+1, pj+b) - u(si, pj+b)) / 2,  up = (u(si+a, pj+1) - u(si+a, pj)) / 2
-//     F1 = G11 us + G12 up,  F2 = G12 us + G22 up  (G = folded metric factors of the bilinear sub-quad, k = 1)
-//   node (i, j) sums, over the sub-quads (i-1, j-1), (i, j-1), (i-1, j), (i, j) that contain it (the reference's
-//   linear element order), -( +-(F1(0, b) + F1(1, b)) / 2 + +-(F2(a, 0) + F2(a, 1)) / 2 )
-// which is FluxDivergence_CGsemPreconditioner_2D (:480-555) with the N = 1 Gauss-Lobatto derivative matrix
-// (entries -1/2, 1/2) and weights (1, 1).
+// fused PCG.
+// Operator: FluxDivergence_CGsemPreconditioner_2D (:480-555) on one bilinear sub-quad, with the N = 1
+// Gauss-Lobatto derivative matrix (entries -1/2, 1/2) and weights (1, 1), is a symmetric 4 x 4 matrix; summed over
+// the sub-quads of a spectral element it is a symmetric 9-point stencil on the element's GLL grid.  The host
+// assembles it once (k = 1, the preconditioner's fluxCoeff) and stores, per node, the coefficients of itself and
+// of its E, N, NE and NW neighbours; the W, S, SW and SE coefficients are those of the neighbour in the opposite
+// direction (symmetry).  Per node this is 9 multiply-adds: the FP64 pipe, far narrower than the FP32 one on this
+// part, bounds the FP64 form, so the fluxes are not recomputed at every sub-quad corner.
 // One inner CG iteration is three launches (q1_apply_fused, cg_dss_mask with the linear groups, pcl_update);
 // pcl_start maps the outer residual in and pc_num forms w, <r, w> and the outer beta from the inner solution.
 // Dirichlet lift: the reference's inner CG keeps the mapped residual's values on the linear mesh's Dirichlet nodes
@@ -22,6 +23,9 @@
 // there.  They are zero when the spectral residual is (its own Dirichlet nodes); where the linear mesh has Dirichlet
 // nodes the spectral mesh does not (a Neumann boundary, nodes its position search left split) rd holds them and
 // the operator adds them to the gathered direction, outside the masked <v, Lv>.
+
+// stencil coefficient slots per node
+constexpr int kQ1Self = 0, kQ1E = 1, kQ1N = 2, kQ1NE = 3, kQ1NW = 4, kQ1Slots = 5;
 
 template <int N1, typename R>
 __global__ void __launch_bounds__(kRedThreads) q1_apply_fused(const R* __restrict__ w, const R* __restrict__ vold,
@@ -34,12 +38,10 @@ __global__ void __launch_bounds__(kRedThreads) q1_apply_fused(const R* __restric
   if (S->done || SL->done) return;
   constexpr int N = N1 - 1;
   constexpr int NN = N1 * N1;
-  constexpr int NQ = 4 * N * N;  // sub-quad corners per element
   constexpr int EPB = cg_epb<N1>();
   static_assert(EPB * NN <= kRedThreads, "one element group per block pass");
   __shared__ R su[EPB][NN];
-  __shared__ R sF1[EPB][NQ];
-  __shared__ R sF2[EPB][NQ];
+  __shared__ R sc[EPB][kQ1Slots - 1][NN];  // E, N, NE, NW coefficients (read by the neighbours)
   const int tid = threadIdx.x % NN, le = threadIdx.x / NN;
   const bool first = SL->iter == 0;
   const R beta = first ? R(0) : (sizeof(R) == 4 ? (R)SL->beta32 : (R)SL->beta);
@@ -50,45 +52,37 @@ __global__ void __launch_bounds__(kRedThreads) q1_apply_fused(const R* __restric
     const int e = g * EPB + le;
     const bool active = le < EPB && e < nEl;
     const size_t l = (size_t)e * NN + tid;
-    R u = 0, ud = 0;
+    R u = 0, c0 = 0, cE = 0, cN = 0, cNE = 0, cNW = 0;
     if (active) {
+      const R* fe = fac + (size_t)e * kQ1Slots * NN;
+      c0 = fe[kQ1Self * NN + tid];
+      cE = fe[kQ1E * NN + tid];
+      cN = fe[kQ1N * NN + tid];
+      cNE = fe[kQ1NE * NN + tid];
+      cNW = fe[kQ1NW * NN + tid];
       const int sl = src[l];
-      const R ws = w[sl];
-      u = first ? ws : ws + beta * vold[sl];
-      vnew[l] = first ? w[l] : w[l] + beta * vold[l];
-      if (rd) ud = rd[l];
-      su[le][tid] = u + ud;
-    }
-    __syncthreads();
-    // sub-quad corners: fluxes F1, F2
-    for (int c = threadIdx.x; c < EPB * NQ; c += kRedThreads) {
-      const int ee = c / NQ, cc = c - ee * NQ;
-      const int e2 = g * EPB + ee;
-      if (e2 >= nEl) continue;
-      const int q = cc >> 2, a = cc & 1, b = (cc >> 1) & 1;
-      const int si = q % N, pj = q / N;
-      const R* U = su[ee];
-      const R us = R(0.5) * (U[(si + 1) + N1 * (pj + b)] - U[si + N1 * (pj + b)]);
-      const R up = R(0.5) * (U[(si + a) + N1 * (pj + 1)] - U[(si + a) + N1 * pj]);
-      const R* fe = fac + (size_t)e2 * 3 * NQ;
-      const R G11 = fe[cc], G12 = fe[NQ + cc], G22 = fe[2 * NQ + cc];
-      sF1[ee][cc] = G11 * us + G12 * up;
-      sF2[ee][cc] = G12 * us + G22 * up;
+      const R wl = w[l];
+      const R vn = first ? wl : wl + beta * vold[l];
+      vnew[l] = vn;
+      u = sl == (int)l ? vn : (first ? w[sl] : w[sl] + beta * vold[sl]);
+      su[le][tid] = rd ? u + rd[l] : u;
+      sc[le][kQ1E - 1][tid] = cE;
+      sc[le][kQ1N - 1][tid] = cN;
+      sc[le][kQ1NE - 1][tid] = cNE;
+      sc[le][kQ1NW - 1][tid] = cNW;
     }
     __syncthreads();
     if (active) {
-      R Lu = 0;
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int si = i - 1 + (t & 1), pj = j - 1 + (t >> 1);
-        if (si < 0 || si >= N || pj < 0 || pj >= N) continue;
-        const int a = i - si, b = j - pj;
-        const R* F1 = &sF1[le][4 * (si + N * pj)];
-        const R* F2 = &sF2[le][4 * (si + N * pj)];
-        const R d1 = (a ? R(0.5) : R(-0.5)) * (F1[2 * b] + F1[1 + 2 * b]);
-        const R d2 = (b ? R(0.5) : R(-0.5)) * (F2[a] + F2[a + 2]);
-        Lu += -(d1 + d2);
-      }
+      const R* U = su[le];
+      R Lu = c0 * U[tid];
+      if (i < N) Lu += cE * U[tid + 1];
+      if (j < N) Lu += cN * U[tid + N1];
+      if (i < N && j < N) Lu += cNE * U[tid + N1 + 1];
+      if (i > 0 && j < N) Lu += cNW * U[tid + N1 - 1];
+      if (i > 0) Lu += sc[le][kQ1E - 1][tid - 1] * U[tid - 1];
+      if (j > 0) Lu += sc[le][kQ1N - 1][tid - N1] * U[tid - N1];
+      if (i > 0 && j > 0) Lu += sc[le][kQ1NE - 1][tid - N1 - 1] * U[tid - N1 - 1];
+      if (i < N && j > 0) Lu += sc[le][kQ1NW - 1][tid - N1 + 1] * U[tid - N1 + 1];
       z[l] = Lu;
       pa += u * Lu;
     }
