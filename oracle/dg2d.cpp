@@ -5,6 +5,11 @@
 // GetExternalState :1698-1729, CalculateBathymetryGradient :1733-1868), the matching routines of
 // src/highend/advection-diffusion2d/AdvectionClass.f90 (:1268-1886) and
 // src/dgsem/DGSEMSolutionStorageClass_2D.f90 CalculateSolutionAtBoundaries (:749-802).
+// Model 3 restates the LINEAR formulation of src/highend/shallowwater/ShallowWaterClass.f90 (state u, v, eta):
+// EdgeFlux :1530-1624 (depth HALF*(inBathy + exBathy) at interior edges, inBathy on the boundary, the bathymetry
+// traces of CalculateBathymetryAtBoundaries :1357-1368), RiemannSolver :2072-2161 (LINEAR branch), XFlux/YFlux
+// :2165-2256, Source :2260-2294 (vorticity = f, relativeFactor = 0), GetExternalState :2298-2325 (NO_NORMAL_FLOW
+// mirror, other flags zero) and MappedTimeDerivative :1728-1887 (same DG structure).
 // Decision: the Riemann solver's undeclared "g" (:1589-1592) is the parameter g (locG).
 // OpenMP over elements and edges follows the reference's !$OMP DO placement.
 #include <cmath>
@@ -55,6 +60,33 @@ void sw_riemann(const double* in, const double* out, const double* nH, double g,
   aS[1] = (uOut / pR) * vR + 0.5 * g * pR * pR * nH[1] + (uIn / pL) * vL + 0.5 * g * pL * pL * nH[1];
   aS[2] = uOut + uIn;
   for (int k = 0; k < 3; ++k) flux[k] = 0.5 * (aS[k] - fac * jump[k]);
+}
+
+// RiemannSolver, LINEAR branch (ShallowWaterClass.f90:2106-2113), depth h at the edge node
+void swl_riemann(const double* in, const double* out, const double* nH, double h, double g, double* flux) {
+  double uL = in[0], vL = in[1], pL = in[2];
+  double uR = out[0], vR = out[1], pR = out[2];
+  double uOut = uR * nH[0] + vR * nH[1];
+  double uIn = uL * nH[0] + vL * nH[1];
+  double fac = std::sqrt(g * h);
+  flux[0] = 0.5 * (g * (pR + pL) + fac * (uIn - uOut)) * nH[0];
+  flux[1] = 0.5 * (g * (pR + pL) + fac * (uIn - uOut)) * nH[1];
+  flux[2] = 0.5 * (h * (uIn + uOut) + fac * (pL - pR));
+}
+
+// trace of a nodal field on side s of element e at side node i (CalculateSolutionAtBoundaries order)
+double field_trace(const orc_dg_problem* p, const double* fld, int s, int i, int e) {
+  const int n = p->N + 1;
+  Idx I{n, 1};
+  double acc = 0.0;
+  if (s == 0 || s == 2) {
+    const double* L = s == 0 ? p->lS : p->lN;
+    for (int j = 0; j < n; ++j) acc = acc + L[j] * fld[I.f(i, j, e)];
+  } else {
+    const double* L = s == 1 ? p->lE : p->lW;
+    for (int m = 0; m < n; ++m) acc = acc + L[m] * fld[I.f(m, i, e)];
+  }
+  return acc;
 }
 
 void sw_external(const double* nH, const double* in, double* ex) {  // NO_NORMAL_FLOW mirror
@@ -126,6 +158,9 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
         }
         if (p->model == 1) {
           sw_riemann(in, ex, nH, p->g, fl);
+        } else if (p->model == 3) {
+          const double hd = 0.5 * (field_trace(p, p->h, s1, i, e1) + field_trace(p, p->h, s2, kk, e2));
+          swl_riemann(in, ex, nH, hd, p->g, fl);
         } else {
           // advection (AdvectionClass.f90:1756-1787) with the primary element's boundary velocity
           // (CalculateVelocityAtBoundaries: Lagrange traces of u and v)
@@ -155,13 +190,16 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
         nH[1] = p->nhy[I.nh(i, s1, e1)];
         double len = p->nlen[I.nh(i, s1, e1)];
         for (int v = 0; v < nEq; ++v) in[v] = bs[I.b(i, v, s1, e1)];
-        if (p->model == 1) {
+        if (p->model == 1 || p->model == 3) {
           if (e2 == ORC_NO_NORMAL_FLOW) {
             sw_external(nH, in, ex);
           } else {
             ex[0] = ex[1] = ex[2] = 0.0;
           }
-          sw_riemann(in, ex, nH, p->g, fl);
+          if (p->model == 1)
+            sw_riemann(in, ex, nH, p->g, fl);
+          else
+            swl_riemann(in, ex, nH, field_trace(p, p->h, s1, i, e1), p->g, fl);
         } else {
           for (int v = 0; v < nEq; ++v) ex[v] = 0.0;
           if (e2 == ORC_INFLOW_ONE) ex[0] = std::tanh(t);
@@ -203,6 +241,15 @@ static void mapped_time_derivative(const orc_dg_problem* p, double t, const doub
       yF[0] = sol[1] * sol[0] / (sol[2]);
       yF[1] = sol[1] * sol[1] / (sol[2]) + g * 0.5 * sol[2] * sol[2];
       yF[2] = sol[1];
+    } else if (p->model == 3) {
+      // XFlux / YFlux, LINEAR (ShallowWaterClass.f90:2171-2177, 2218-2224)
+      double g = p->g, h = p->h[I.f(i, j, e)];
+      xF[0] = g * sol[2];
+      xF[1] = 0.0;
+      xF[2] = h * sol[0];
+      yF[0] = 0.0;
+      yF[1] = g * sol[2];
+      yF[2] = h * sol[1];
     } else {
       double u = p->u[I.f(i, j, e)], v = p->v[I.f(i, j, e)];
       for (int k = 0; k < nEq; ++k) {
@@ -257,6 +304,20 @@ static void mapped_time_derivative(const orc_dg_problem* p, double t, const doub
         double g = p->g, lD = p->drag;
         double s0 = plv * sol[1] + g * sol[2] * dhdx - lD * sol[0] / h - (sol[0] - relax[0]) * ts;
         double s1 = -plv * sol[0] + g * sol[2] * dhdy - lD * sol[1] / h - (sol[1] - relax[1]) * ts;
+        double s2 = -(sol[2] - relax[2]) * ts;
+        tend[I.q(i, j, 0, e)] = tend[I.q(i, j, 0, e)] + s0;
+        tend[I.q(i, j, 1, e)] = tend[I.q(i, j, 1, e)] + s1;
+        tend[I.q(i, j, 2, e)] = tend[I.q(i, j, 2, e)] + s2;
+      } else if (p->model == 3) {
+        // Source, LINEAR (ShallowWaterClass.f90:2272-2281): vorticity = f (relativeFactor = 0)
+        double relax[3] = {0, 0, 0}, ts = 0.0;
+        if (p->relax) {
+          for (int v = 0; v < 3; ++v) relax[v] = p->relax[I.q(i, j, v, e)];
+        }
+        if (p->rfac) ts = p->rfac[id];
+        double vort = p->fcor[id], lD = p->drag;
+        double s0 = vort * sol[1] - lD * sol[0] - (sol[0] - relax[0]) * ts;
+        double s1 = -vort * sol[0] - lD * sol[1] - (sol[1] - relax[1]) * ts;
         double s2 = -(sol[2] - relax[2]) * ts;
         tend[I.q(i, j, 0, e)] = tend[I.q(i, j, 0, e)] + s0;
         tend[I.q(i, j, 1, e)] = tend[I.q(i, j, 1, e)] + s1;

@@ -130,6 +130,29 @@ struct SWFlux {
   }
 };
 
+// LINEAR formulation of ShallowWaterClass (state u, v, eta); `depth` is the edge depth HALF*(inBathy + exBathy)
+// (interior) or inBathy (boundary), precomputed per edge node from the bathymetry traces.
+struct SWLinFlux {
+  template <int NEQ, bool EX>
+  static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
+                                                 double depth, double g, double* f) {
+    // RiemannSolver, LINEAR branch (ShallowWaterClass.f90:2106-2113)
+    using A = Ar<EX>;
+    const double uOut = A::add(A::mul(ex[0], nx), A::mul(ex[1], ny));
+    const double uIn = A::add(A::mul(in[0], nx), A::mul(in[1], ny));
+    const double fac = sqrt(A::mul(g, depth));
+    const double m = A::mul(0.5, A::add(A::mul(g, A::add(ex[2], in[2])), A::mul(fac, A::sub(uIn, uOut))));
+    f[0] = A::mul(m, nx);
+    f[1] = A::mul(m, ny);
+    f[2] = A::mul(0.5, A::add(A::mul(depth, A::add(uIn, uOut)), A::mul(fac, A::sub(in[2], ex[2]))));
+  }
+  template <int NEQ, bool EX>
+  static __device__ __forceinline__ void external(int bc, double nx, double ny, double t, const double* in,
+                                                  double* ex) {
+    SWFlux::external<NEQ, EX>(bc, nx, ny, t, in, ex);  // GetExternalState (:2298-2325): the same mirror
+  }
+};
+
 struct AdvFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
@@ -226,8 +249,10 @@ __device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const doub
   }
 }
 
-template <int N1, int NEQ, bool SW, bool EX>
+// PH: 0 advection, 1 conservative shallow water, 2 linear shallow water
+template <int N1, int NEQ, int PH, bool EX>
 __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
+  constexpr bool SW = PH == 1;
   using X = Ar<EX>;
   constexpr int NN = N1 * N1;
   constexpr int EPB = elems_per_block<N1>();
@@ -265,7 +290,17 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
     double* sb = &sB[le][0][0][0];
     for (int t = tid; t < 4 * NEQ * N1; t += NN) sb[t] = be[t];
     double xF[NEQ], yF[NEQ];
-    if (SW) {
+    if (PH == 2) {
+      // XFlux / YFlux, LINEAR (ShallowWaterClass.f90:2171-2177, 2218-2224): aux = (h, f, ...)
+      const double hh = A.aux[(size_t)e * A.naux * NN + tid];
+      const double gp = X::mul(A.g, qv[2]);
+      xF[0] = gp;
+      xF[1] = 0.0;
+      xF[2] = X::mul(hh, qv[0]);
+      yF[0] = 0.0;
+      yF[1] = gp;
+      yF[2] = X::mul(hh, qv[1]);
+    } else if (SW) {
       // XFlux / YFlux (:1608-1658)
       if (EX) {
         const double p = X::mul(X::mul(X::mul(A.g, 0.5), qv[2]), qv[2]);
@@ -346,6 +381,23 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
         s0 = X::sub(s0, X::mul(X::sub(qv[0], ae[o * NN + tid]), ts));
         s1 = X::sub(s1, X::mul(X::sub(qv[1], ae[(o + 1) * NN + tid]), ts));
         s2 = -X::mul(X::sub(qv[2], ae[(o + 2) * NN + tid]), ts);
+      }
+      tend[0] = X::add(tend[0], s0);
+      tend[1] = X::add(tend[1], s1);
+      if (NEQ > 2 && A.has_relax) tend[NEQ > 2 ? 2 : 0] = X::add(tend[NEQ > 2 ? 2 : 0], s2);
+    } else if (PH == 2) {
+      // Source, LINEAR (ShallowWaterClass.f90:2272-2281): (f v - drag u) - (u - relax) ts; aux = (h, f, relax..)
+      const double f = ae[NN + tid];
+      double s0 = X::mul(f, qv[1]), s1 = X::mul(-f, qv[0]), s2 = 0.0;
+      if (A.has_drag) {
+        s0 = X::sub(s0, X::mul(A.drag, qv[0]));
+        s1 = X::sub(s1, X::mul(A.drag, qv[1]));
+      }
+      if (A.has_relax) {
+        const double ts = ae[5 * NN + tid];
+        s0 = X::sub(s0, X::mul(X::sub(qv[0], ae[2 * NN + tid]), ts));
+        s1 = X::sub(s1, X::mul(X::sub(qv[1], ae[3 * NN + tid]), ts));
+        s2 = -X::mul(X::sub(qv[2], ae[4 * NN + tid]), ts);
       }
       tend[0] = X::add(tend[0], s0);
       tend[1] = X::add(tend[1], s1);
@@ -450,7 +502,7 @@ NodalConst<N1> make_const(const self_dg2d* h) {
   return C;
 }
 
-template <int N1, int NEQ, bool SW, bool EX>
+template <int N1, int NEQ, int PH, bool EX>
 int launch_edge_t(self_dg2d* h, double t) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
@@ -463,15 +515,17 @@ int launch_edge_t(self_dg2d* h, double t) {
   EA.g = h->g;
   EA.t = t;
   const int nthr = h->nEdges * N1;
-  if (SW)
+  if (PH == 1)
     dg_edge_flux<N1, NEQ, SWFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
+  else if (PH == 2)
+    dg_edge_flux<N1, NEQ, SWLinFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   else
     dg_edge_flux<N1, NEQ, AdvFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   SELF_LAUNCHED(ctx);
   return SELF_OK;
 }
 
-template <int N1, int NEQ, bool SW, bool EX>
+template <int N1, int NEQ, int PH, bool EX>
 int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend,
                     int write_traces) {
   self_ctx* ctx = h->ctx;
@@ -497,17 +551,17 @@ int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* 
   VA.write_traces = write_traces;
   constexpr int EPB = elems_per_block<N1>();
   dim3 blk(N1 * N1, EPB);
-  dg_volume<N1, NEQ, SW, EX><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(VA, make_const<N1>(h));
+  dg_volume<N1, NEQ, PH, EX><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(VA, make_const<N1>(h));
   SELF_LAUNCHED(ctx);
   return SELF_OK;
 }
 
-template <int N1, int NEQ, bool SW, bool EX>
+template <int N1, int NEQ, int PH, bool EX>
 int launch_stage_t(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout,
                    double* tend, int write_traces) {
-  int rc = launch_edge_t<N1, NEQ, SW, EX>(h, t);
+  int rc = launch_edge_t<N1, NEQ, PH, EX>(h, t);
   if (rc) return rc;
-  return launch_volume_t<N1, NEQ, SW, EX>(h, mode, a, gdt, qin, qout, tend, write_traces);
+  return launch_volume_t<N1, NEQ, PH, EX>(h, mode, a, gdt, qin, qout, tend, write_traces);
 }
 
 template <int N1, int NEQ, bool EX>
@@ -524,12 +578,13 @@ template <int N1, bool EX>
 int stage_nx(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout, double* tend,
              int wt) {
   if (h->model == SELF_MODEL_SW_CONSERVATIVE)
-    return launch_stage_t<N1, 3, true, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    return launch_stage_t<N1, 3, 1, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  if (h->model == SELF_MODEL_SW_LINEAR) return launch_stage_t<N1, 3, 2, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
   switch (h->nEq) {
-    case 1: return launch_stage_t<N1, 1, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
-    case 2: return launch_stage_t<N1, 2, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
-    case 3: return launch_stage_t<N1, 3, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
-    case 4: return launch_stage_t<N1, 4, false, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 1: return launch_stage_t<N1, 1, 0, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 2: return launch_stage_t<N1, 2, 0, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 3: return launch_stage_t<N1, 3, 0, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+    case 4: return launch_stage_t<N1, 4, 0, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
   }
   return SELF_ERR_UNSUPPORTED;
 }
@@ -541,12 +596,13 @@ int stage_n(self_dg2d* h, int mode, double a, double gdt, double t, const double
 }
 template <int N1, bool EX>
 int edge_nx(self_dg2d* h, double t) {
-  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_edge_t<N1, 3, true, EX>(h, t);
+  if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_edge_t<N1, 3, 1, EX>(h, t);
+  if (h->model == SELF_MODEL_SW_LINEAR) return launch_edge_t<N1, 3, 2, EX>(h, t);
   switch (h->nEq) {
-    case 1: return launch_edge_t<N1, 1, false, EX>(h, t);
-    case 2: return launch_edge_t<N1, 2, false, EX>(h, t);
-    case 3: return launch_edge_t<N1, 3, false, EX>(h, t);
-    case 4: return launch_edge_t<N1, 4, false, EX>(h, t);
+    case 1: return launch_edge_t<N1, 1, 0, EX>(h, t);
+    case 2: return launch_edge_t<N1, 2, 0, EX>(h, t);
+    case 3: return launch_edge_t<N1, 3, 0, EX>(h, t);
+    case 4: return launch_edge_t<N1, 4, 0, EX>(h, t);
   }
   return SELF_ERR_UNSUPPORTED;
 }
@@ -557,12 +613,13 @@ int edge_n(self_dg2d* h, double t) {
 template <int N1, bool EX>
 int volume_nx(self_dg2d* h, int mode, double a, double gdt, const double* qin, double* qout, double* tend, int wt) {
   if (h->model == SELF_MODEL_SW_CONSERVATIVE)
-    return launch_volume_t<N1, 3, true, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    return launch_volume_t<N1, 3, 1, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+  if (h->model == SELF_MODEL_SW_LINEAR) return launch_volume_t<N1, 3, 2, EX>(h, mode, a, gdt, qin, qout, tend, wt);
   switch (h->nEq) {
-    case 1: return launch_volume_t<N1, 1, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
-    case 2: return launch_volume_t<N1, 2, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
-    case 3: return launch_volume_t<N1, 3, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
-    case 4: return launch_volume_t<N1, 4, false, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 1: return launch_volume_t<N1, 1, 0, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 2: return launch_volume_t<N1, 2, 0, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 3: return launch_volume_t<N1, 3, 0, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+    case 4: return launch_volume_t<N1, 4, 0, EX>(h, mode, a, gdt, qin, qout, tend, wt);
   }
   return SELF_ERR_UNSUPPORTED;
 }
@@ -667,6 +724,9 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
     if (d->nEq != 3) return set_error(ctx, SELF_ERR_INVALID, "shallow water needs nEq = 3");
     if (!d->h || !d->dhdx || !d->dhdy || !d->fcor) return set_error(ctx, SELF_ERR_INVALID, "missing bathymetry");
+  } else if (d->model == SELF_MODEL_SW_LINEAR) {
+    if (d->nEq != 3) return set_error(ctx, SELF_ERR_INVALID, "shallow water needs nEq = 3");
+    if (!d->h || !d->fcor) return set_error(ctx, SELF_ERR_INVALID, "missing bathymetry or planetary vorticity");
   } else if (d->model == SELF_MODEL_ADVECTION) {
     if (d->nEq < 1 || d->nEq > 4) return set_error(ctx, SELF_ERR_UNSUPPORTED, "advection nEq must be 1..4");
     if (!d->u || !d->v) return set_error(ctx, SELF_ERR_INVALID, "missing velocity");
@@ -728,16 +788,20 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   // aux block
   std::vector<const double*> fields;
   h->has_relax = (d->relax && d->rfac) ? 1 : 0;
+  const bool swl = d->model == SELF_MODEL_SW_LINEAR;
   if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
     h->has_drag = d->linear_drag != 0.0 ? 1 : 0;
     fields = {d->dhdx, d->dhdy, d->fcor};
     if (h->has_drag) fields.push_back(d->h);
+  } else if (swl) {
+    h->has_drag = d->linear_drag != 0.0 ? 1 : 0;
+    fields = {d->h, d->fcor};
   } else {
     fields = {d->u, d->v};
   }
   h->naux = (int)fields.size();
   int nrelax = 0;
-  if (h->has_relax) nrelax = (d->model == SELF_MODEL_SW_CONSERVATIVE) ? 4 : 2 * d->nEq;
+  if (h->has_relax) nrelax = (d->model == SELF_MODEL_SW_CONSERVATIVE || swl) ? 4 : 2 * d->nEq;
   h->naux += nrelax;
   std::vector<double> aux((size_t)h->naux * NN * nEl);
   for (size_t e = 0; e < nEl; ++e) {
@@ -749,7 +813,7 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
     if (h->has_relax) {
       for (int v = 0; v < d->nEq; ++v, ++f)
         for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->relax[(e * d->nEq + v) * NN + k];
-      if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
+      if (d->model == SELF_MODEL_SW_CONSERVATIVE || swl) {
         for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->rfac[e * NN + k];
       } else {
         for (int v = 0; v < d->nEq; ++v, ++f)
@@ -757,7 +821,20 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
       }
     }
   }
-  // per-edge geometry: primary side normals, lengths and (advection) normal velocity
+  // per-edge geometry: primary side normals, lengths and (advection) normal velocity or (linear shallow water)
+  // the edge depth HALF*(inBathy + exBathy), inBathy on the boundary (ShallowWaterClass.f90 EdgeFlux :1530-1624)
+  // from the bathymetry traces (CalculateBathymetryAtBoundaries :1357-1368, CalculateSolutionAtBoundaries order)
+  auto h_trace = [&](int e, int s, int i) {
+    double acc = 0.0;
+    if (s == 0 || s == 2) {
+      const double* L = s == 0 ? d->lagS : d->lagN;
+      for (int m = 0; m < n; ++m) acc = acc + L[m] * d->h[(size_t)e * NN + i + (size_t)n * m];
+    } else {
+      const double* L = s == 1 ? d->lagE : d->lagW;
+      for (int m = 0; m < n; ++m) acc = acc + L[m] * d->h[(size_t)e * NN + m + (size_t)n * i];
+    }
+    return acc;
+  };
   std::vector<double> eg((size_t)4 * n * d->nEdges, 0.0);
   for (int k = 0; k < d->nEdges; ++k) {
     const int e1 = ed[6 * k] - 1, s1 = ed[6 * k + 1] - 1;
@@ -777,6 +854,14 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
           vb += L[m] * d->v[id];
         }
         eg[(size_t)k * 4 * n + 3 * n + i] = ub * nx + vb * ny;
+      } else if (swl) {
+        double dep = h_trace(e1, s1, i);
+        if (ed[6 * k + 2] > 0) {
+          const int e2 = ed[6 * k + 2] - 1, s2 = std::abs(ed[6 * k + 3]) - 1;
+          const int kk = ed[6 * k + 4] - ed[6 * k + 5] + i * ed[6 * k + 5];
+          dep = 0.5 * (dep + h_trace(e2, s2, kk));
+        }
+        eg[(size_t)k * 4 * n + 3 * n + i] = dep;
       }
     }
   }
