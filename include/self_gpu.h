@@ -48,6 +48,10 @@ extern "C" {
 #define SELF_MODEL_SW_CONSERVATIVE 1 /* ConservativeShallowWaterClass.f90 */
 #define SELF_MODEL_ADVECTION 2       /* AdvectionClass.f90 (kappa = 0) */
 #define SELF_MODEL_SW_LINEAR 3       /* ShallowWaterClass.f90, ModelFormulation LINEAR: state (u, v, eta) */
+/* ShallowWaterClass.f90, ModelFormulation SKEW_SYMMETRIC: nEq = 4, state (u, v, eta, zeta) with the relative
+ * vorticity zeta (the reference's vorticity(:)%solution(:,:,2)) advanced by RelativeVorticityEdgeFlux and
+ * VorticityTimeDerivative in the same RK3 steps */
+#define SELF_MODEL_SW_SKEW 4
 
 #define SELF_PREC_FP64 0 /* plain FP64 drop-in */
 #define SELF_PREC_FP32 1 /* FP32 arithmetic; shallow water in perturbation form about the lake at rest */

@@ -10,6 +10,14 @@
 // traces of CalculateBathymetryAtBoundaries :1357-1368), RiemannSolver :2072-2161 (LINEAR branch), XFlux/YFlux
 // :2165-2256, Source :2260-2294 (vorticity = f, relativeFactor = 0), GetExternalState :2298-2325 (NO_NORMAL_FLOW
 // mirror, other flags zero) and MappedTimeDerivative :1728-1887 (same DG structure).
+// Model 4 restates its SKEW_SYMMETRIC formulation with the relative vorticity as a 4th state variable (the
+// reference keeps it in vorticity(:)%solution(:,:,2) and advances it with the same RK3 coefficients,
+// ForwardStepRK3 :1372-1432): RiemannSolver SKEW_SYMMETRIC branch, XFlux/YFlux with the kinetic energy, Source with
+// vorticity = f + zeta (relativeFactor = 1), RelativeVorticityEdgeFlux :1628-1724 (VorticityFluxSolver
+// :2041-2068, GetExternalVorticity :2329-2356: NO_NORMAL_FLOW copies the interior value, other flags zero; the
+// boundary's outer planetary vorticity is the inner one) and VorticityTimeDerivative :1891-2008.
+// Decision: V2D, never initialised in ForwardStepRK3, is taken as zero (its first use multiplies it by
+// rk3_a(1) = 0).
 // Decision: the Riemann solver's undeclared "g" (:1589-1592) is the parameter g (locG).
 // OpenMP over elements and edges follows the reference's !$OMP DO placement.
 #include <cmath>
@@ -72,6 +80,30 @@ void swl_riemann(const double* in, const double* out, const double* nH, double h
   flux[0] = 0.5 * (g * (pR + pL) + fac * (uIn - uOut)) * nH[0];
   flux[1] = 0.5 * (g * (pR + pL) + fac * (uIn - uOut)) * nH[1];
   flux[2] = 0.5 * (h * (uIn + uOut) + fac * (pL - pR));
+}
+
+// RiemannSolver, SKEW_SYMMETRIC branch (ShallowWaterClass.f90:2114-2133), depth h at the edge node
+void sws_riemann(const double* in, const double* out, const double* nH, double h, double g, double* flux) {
+  double jump[3] = {out[0] - in[0], out[1] - in[1], out[2] - in[2]};
+  double uL = in[0], vL = in[1], pL = in[2];
+  double uR = out[0], vR = out[1], pR = out[2];
+  double uOut = uR * nH[0] + vR * nH[1];
+  double uIn = uL * nH[0] + vL * nH[1];
+  double c1 = std::fabs(0.25 * (uOut + std::sqrt(uOut * uOut + 16.0 * g * (pR + h))));
+  double c2 = std::fabs(0.25 * (uOut - std::sqrt(uOut * uOut + 16.0 * g * (pR + h))));
+  double c3 = std::fabs(0.25 * (uIn + std::sqrt(uIn * uIn + 16.0 * g * (pL + h))));
+  double c4 = std::fabs(0.25 * (uIn - std::sqrt(uIn * uIn + 16.0 * g * (pL + h))));
+  double fac = std::fmax(std::fmax(std::fmax(c1, c2), c3), c4);
+  double e = 0.5 * (uR * uR + vR * vR) + g * pR + 0.5 * (uL * uL + vL * vL) + g * pL;
+  double aS[3] = {e * nH[0], e * nH[1], uIn * (pL + h) + uOut * (pR + h)};
+  for (int k = 0; k < 3; ++k) flux[k] = 0.5 * (aS[k] - fac * jump[k]);
+}
+
+// VorticityFluxSolver (ShallowWaterClass.f90:2041-2068)
+double vort_flux(const double* in, const double* out, double zIn, double zOut, const double* nH) {
+  double uOut = out[0] * nH[0] + out[1] * nH[1];
+  double uIn = in[0] * nH[0] + in[1] * nH[1];
+  return 0.5 * (uOut * zOut + uIn * zIn - std::fmax(std::fabs(uOut), std::fabs(uIn)) * (zOut - zIn));
 }
 
 // trace of a nodal field on side s of element e at side node i (CalculateSolutionAtBoundaries order)
@@ -161,6 +193,12 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
         } else if (p->model == 3) {
           const double hd = 0.5 * (field_trace(p, p->h, s1, i, e1) + field_trace(p, p->h, s2, kk, e2));
           swl_riemann(in, ex, nH, hd, p->g, fl);
+        } else if (p->model == 4) {
+          const double hd = 0.5 * (field_trace(p, p->h, s1, i, e1) + field_trace(p, p->h, s2, kk, e2));
+          sws_riemann(in, ex, nH, hd, p->g, fl);
+          const double zIn = in[3] + field_trace(p, p->fcor, s1, i, e1);
+          const double zOut = ex[3] + field_trace(p, p->fcor, s2, kk, e2);
+          fl[3] = vort_flux(in, ex, zIn, zOut, nH);
         } else {
           // advection (AdvectionClass.f90:1756-1787) with the primary element's boundary velocity
           // (CalculateVelocityAtBoundaries: Lagrange traces of u and v)
@@ -190,16 +228,22 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
         nH[1] = p->nhy[I.nh(i, s1, e1)];
         double len = p->nlen[I.nh(i, s1, e1)];
         for (int v = 0; v < nEq; ++v) in[v] = bs[I.b(i, v, s1, e1)];
-        if (p->model == 1 || p->model == 3) {
+        if (p->model == 1 || p->model == 3 || p->model == 4) {
           if (e2 == ORC_NO_NORMAL_FLOW) {
             sw_external(nH, in, ex);
           } else {
             ex[0] = ex[1] = ex[2] = 0.0;
           }
-          if (p->model == 1)
+          if (p->model == 1) {
             sw_riemann(in, ex, nH, p->g, fl);
-          else
+          } else if (p->model == 3) {
             swl_riemann(in, ex, nH, field_trace(p, p->h, s1, i, e1), p->g, fl);
+          } else {
+            sws_riemann(in, ex, nH, field_trace(p, p->h, s1, i, e1), p->g, fl);
+            const double relOut = e2 == ORC_NO_NORMAL_FLOW ? in[3] : 0.0;
+            const double fIn = field_trace(p, p->fcor, s1, i, e1);
+            fl[3] = vort_flux(in, ex, in[3] + fIn, relOut + fIn, nH);
+          }
         } else {
           for (int v = 0; v < nEq; ++v) ex[v] = 0.0;
           if (e2 == ORC_INFLOW_ONE) ex[0] = std::tanh(t);
@@ -241,6 +285,19 @@ static void mapped_time_derivative(const orc_dg_problem* p, double t, const doub
       yF[0] = sol[1] * sol[0] / (sol[2]);
       yF[1] = sol[1] * sol[1] / (sol[2]) + g * 0.5 * sol[2] * sol[2];
       yF[2] = sol[1];
+    } else if (p->model == 4) {
+      // XFlux / YFlux, SKEW_SYMMETRIC (ShallowWaterClass.f90:2179-2187, 2226-2234), and the vorticity fluxes
+      // u (zeta + f), v (zeta + f) of VorticityTimeDerivative (:1934-1936)
+      double g = p->g, h = p->h[I.f(i, j, e)], f = p->fcor[I.f(i, j, e)];
+      double KE = (sol[0] * sol[0] + sol[1] * sol[1]) * 0.5;
+      xF[0] = g * sol[2] + KE;
+      xF[1] = 0.0;
+      xF[2] = (h + sol[2]) * sol[0];
+      yF[0] = 0.0;
+      yF[1] = g * sol[2] + KE;
+      yF[2] = (h + sol[2]) * sol[1];
+      xF[3] = sol[0] * (sol[3] + f);
+      yF[3] = sol[1] * (sol[3] + f);
     } else if (p->model == 3) {
       // XFlux / YFlux, LINEAR (ShallowWaterClass.f90:2171-2177, 2218-2224)
       double g = p->g, h = p->h[I.f(i, j, e)];
@@ -308,14 +365,15 @@ static void mapped_time_derivative(const orc_dg_problem* p, double t, const doub
         tend[I.q(i, j, 0, e)] = tend[I.q(i, j, 0, e)] + s0;
         tend[I.q(i, j, 1, e)] = tend[I.q(i, j, 1, e)] + s1;
         tend[I.q(i, j, 2, e)] = tend[I.q(i, j, 2, e)] + s2;
-      } else if (p->model == 3) {
-        // Source, LINEAR (ShallowWaterClass.f90:2272-2281): vorticity = f (relativeFactor = 0)
+      } else if (p->model == 3 || p->model == 4) {
+        // Source, LINEAR / SKEW_SYMMETRIC (ShallowWaterClass.f90:2272-2281): vorticity = f + relativeFactor zeta
+        // (relativeFactor 0 / 1, :1876); the vorticity equation has no source
         double relax[3] = {0, 0, 0}, ts = 0.0;
         if (p->relax) {
           for (int v = 0; v < 3; ++v) relax[v] = p->relax[I.q(i, j, v, e)];
         }
         if (p->rfac) ts = p->rfac[id];
-        double vort = p->fcor[id], lD = p->drag;
+        double vort = p->model == 4 ? p->fcor[id] + 1.0 * sol[3] : p->fcor[id], lD = p->drag;
         double s0 = vort * sol[1] - lD * sol[0] - (sol[0] - relax[0]) * ts;
         double s1 = -vort * sol[0] - lD * sol[1] - (sol[1] - relax[1]) * ts;
         double s2 = -(sol[2] - relax[2]) * ts;

@@ -79,7 +79,7 @@ int orc_ism_build(const char* path, int N, int quad, int* edges, int* elemNodes,
 /* ---------------- DGSEM 2-D (ConservativeShallowWaterClass.f90, AdvectionClass.f90) */
 typedef struct {
   int N, nEl, nEdges, nEq;
-  int model;                  /* 1 = conservative shallow water, 2 = linear advection, 3 = linear shallow water */
+  int model;                  /* 1 = conservative SW, 2 = advection, 3 = linear SW, 4 = skew-symmetric SW (nEq 4) */
   const double *dmatS, *dmatP, *qw, *lW, *lE, *lS, *lN;
   const int* edges;
   const double *dxds, *dxdp, *dyds, *dydp, *J;

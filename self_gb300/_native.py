@@ -23,6 +23,7 @@ CG = 2001
 MODEL_SW_CONSERVATIVE = 1
 MODEL_ADVECTION = 2
 MODEL_SW_LINEAR = 3
+MODEL_SW_SKEW = 4
 PREC_FP64 = 0
 PREC_FP32 = 1
 PREC_FP64_EXACT = 2

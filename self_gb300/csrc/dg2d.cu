@@ -61,7 +61,8 @@ struct EdgeArgs {
   const double* bs;
   double* bf;
   const int* edges;     // 6 per edge
-  const double* egeo;   // 4 n per edge: nx, ny, |n|, u.n (advection)
+  const double* egeo;   // 4 n per edge: nx, ny, |n|, u.n (advection) or the edge depth (linear / skew SW)
+  const double* eplan;  // skew SW: 2 n per edge, planetary vorticity traces of the primary and secondary side
   int nEdges;
   double g, t;
 };
@@ -81,7 +82,9 @@ struct Ar {
 struct SWFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double un_adv, double g, double* f) {
+                                                 double un_adv, double fin, double fout, double g, double* f) {
+    (void)fin;
+    (void)fout;
     (void)un_adv;
     // RiemannSolver (ConservativeShallowWaterClass.f90:1555-1604), g taken from the parameters
     using A = Ar<EX>;
@@ -135,7 +138,9 @@ struct SWFlux {
 struct SWLinFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double depth, double g, double* f) {
+                                                 double depth, double fin, double fout, double g, double* f) {
+    (void)fin;
+    (void)fout;
     // RiemannSolver, LINEAR branch (ShallowWaterClass.f90:2106-2113)
     using A = Ar<EX>;
     const double uOut = A::add(A::mul(ex[0], nx), A::mul(ex[1], ny));
@@ -153,10 +158,50 @@ struct SWLinFlux {
   }
 };
 
+// SKEW_SYMMETRIC formulation of ShallowWaterClass with the relative vorticity as the 4th variable (u, v, eta,
+// zeta): the skew-symmetric flux for the first three and VorticityFluxSolver for zeta, with zIn = zeta_in + f_in,
+// zOut = zeta_out + f_out (f_out = f_in on the boundary, RelativeVorticityEdgeFlux :1628-1724).
+struct SWSkewFlux {
+  template <int NEQ, bool EX>
+  static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
+                                                 double depth, double fin, double fout, double g, double* f) {
+    // RiemannSolver, SKEW_SYMMETRIC branch (ShallowWaterClass.f90:2114-2133)
+    using A = Ar<EX>;
+    const double uL = in[0], vL = in[1], pL = in[2], uR = ex[0], vR = ex[1], pR = ex[2];
+    const double uOut = A::add(A::mul(uR, nx), A::mul(vR, ny));
+    const double uIn = A::add(A::mul(uL, nx), A::mul(vL, ny));
+    const double g16 = A::mul(16.0, g);
+    const double sR = sqrt(A::add(A::mul(uOut, uOut), A::mul(g16, A::add(pR, depth))));
+    const double sL = sqrt(A::add(A::mul(uIn, uIn), A::mul(g16, A::add(pL, depth))));
+    const double fac = fmax(fmax(fmax(fabs(A::mul(0.25, A::add(uOut, sR))), fabs(A::mul(0.25, A::sub(uOut, sR)))),
+                                 fabs(A::mul(0.25, A::add(uIn, sL)))),
+                            fabs(A::mul(0.25, A::sub(uIn, sL))));
+    const double e = A::add(A::add(A::add(A::mul(0.5, A::add(A::mul(uR, uR), A::mul(vR, vR))), A::mul(g, pR)),
+                                   A::mul(0.5, A::add(A::mul(uL, uL), A::mul(vL, vL)))),
+                            A::mul(g, pL));
+    const double a2 = A::add(A::mul(uIn, A::add(pL, depth)), A::mul(uOut, A::add(pR, depth)));
+    f[0] = A::mul(0.5, A::sub(A::mul(e, nx), A::mul(fac, A::sub(uR, uL))));
+    f[1] = A::mul(0.5, A::sub(A::mul(e, ny), A::mul(fac, A::sub(vR, vL))));
+    f[2] = A::mul(0.5, A::sub(a2, A::mul(fac, A::sub(pR, pL))));
+    // VorticityFluxSolver (:2041-2068)
+    const double zIn = A::add(in[3], fin), zOut = A::add(ex[3], fout);
+    f[3] = A::mul(0.5, A::sub(A::add(A::mul(uOut, zOut), A::mul(uIn, zIn)),
+                              A::mul(fmax(fabs(uOut), fabs(uIn)), A::sub(zOut, zIn))));
+  }
+  template <int NEQ, bool EX>
+  static __device__ __forceinline__ void external(int bc, double nx, double ny, double t, const double* in,
+                                                  double* ex) {
+    SWFlux::external<NEQ, EX>(bc, nx, ny, t, in, ex);
+    ex[3] = bc == SELF_NO_NORMAL_FLOW ? in[3] : 0.0;  // GetExternalVorticity (:2329-2356)
+  }
+};
+
 struct AdvFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double un, double g, double* f) {
+                                                 double un, double fin, double fout, double g, double* f) {
+    (void)fin;
+    (void)fout;
     (void)nx;
     (void)ny;
     (void)g;
@@ -190,6 +235,8 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
   const int e1 = E[0] - 1, s1 = E[1] - 1, e2f = E[2];
   const double* eg = A.egeo + (size_t)k * 4 * N1;
   const double nx = eg[i], ny = eg[N1 + i], len = eg[2 * N1 + i], un = eg[3 * N1 + i];
+  const double fin = A.eplan ? A.eplan[(size_t)k * 2 * N1 + i] : 0.0;
+  const double fout = A.eplan ? A.eplan[(size_t)k * 2 * N1 + N1 + i] : 0.0;
   double in[NEQ], ex[NEQ], f[NEQ];
   const double* b1 = A.bs + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
 #pragma unroll
@@ -200,7 +247,7 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
     const double* b2 = A.bs + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
-    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, A.g, f);
+    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, f);
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
     double* o2 = A.bf + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
@@ -211,7 +258,7 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
     }
   } else {
     Phys::template external<NEQ, EX>(e2f, nx, ny, A.t, in, ex);
-    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, A.g, f);
+    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, f);
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = Ar<EX>::mul(f[v], len);
@@ -249,7 +296,7 @@ __device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const doub
   }
 }
 
-// PH: 0 advection, 1 conservative shallow water, 2 linear shallow water
+// PH: 0 advection, 1 conservative shallow water, 2 linear shallow water, 3 skew-symmetric shallow water (NEQ 4)
 template <int N1, int NEQ, int PH, bool EX>
 __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
   constexpr bool SW = PH == 1;
@@ -290,7 +337,24 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
     double* sb = &sB[le][0][0][0];
     for (int t = tid; t < 4 * NEQ * N1; t += NN) sb[t] = be[t];
     double xF[NEQ], yF[NEQ];
-    if (PH == 2) {
+    if (PH == 3) {
+      // XFlux / YFlux, SKEW_SYMMETRIC (ShallowWaterClass.f90:2179-2187, 2226-2234) and the vorticity fluxes
+      // u (zeta + f), v (zeta + f) of VorticityTimeDerivative (:1934-1936); aux = (h, f, ...)
+      const double* ae = A.aux + (size_t)e * A.naux * NN;
+      const double hh = ae[tid], fc = ae[NN + tid];
+      const double KE = X::mul(X::add(X::mul(qv[0], qv[0]), X::mul(qv[1], qv[1])), 0.5);
+      const double gp = X::add(X::mul(A.g, qv[2]), KE);
+      const double H = X::add(hh, qv[2]);
+      xF[0] = gp;
+      xF[1] = 0.0;
+      xF[2] = X::mul(H, qv[0]);
+      yF[0] = 0.0;
+      yF[1] = gp;
+      yF[2] = X::mul(H, qv[1]);
+      const double za = X::add(qv[NEQ > 3 ? 3 : 0], fc);
+      xF[NEQ > 3 ? 3 : 0] = X::mul(qv[0], za);
+      yF[NEQ > 3 ? 3 : 0] = X::mul(qv[1], za);
+    } else if (PH == 2) {
       // XFlux / YFlux, LINEAR (ShallowWaterClass.f90:2171-2177, 2218-2224): aux = (h, f, ...)
       const double hh = A.aux[(size_t)e * A.naux * NN + tid];
       const double gp = X::mul(A.g, qv[2]);
@@ -385,9 +449,10 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
       tend[0] = X::add(tend[0], s0);
       tend[1] = X::add(tend[1], s1);
       if (NEQ > 2 && A.has_relax) tend[NEQ > 2 ? 2 : 0] = X::add(tend[NEQ > 2 ? 2 : 0], s2);
-    } else if (PH == 2) {
-      // Source, LINEAR (ShallowWaterClass.f90:2272-2281): (f v - drag u) - (u - relax) ts; aux = (h, f, relax..)
-      const double f = ae[NN + tid];
+    } else if (PH == 2 || PH == 3) {
+      // Source, LINEAR / SKEW_SYMMETRIC (ShallowWaterClass.f90:2272-2281): (w v - drag u) - (u - relax) ts with
+      // w = f + relativeFactor zeta (0 / 1); aux = (h, f, relax u, v, eta, timescale); no vorticity source
+      const double f = PH == 3 ? X::add(ae[NN + tid], X::mul(1.0, qv[NEQ > 3 ? 3 : 0])) : ae[NN + tid];
       double s0 = X::mul(f, qv[1]), s1 = X::mul(-f, qv[0]), s2 = 0.0;
       if (A.has_drag) {
         s0 = X::sub(s0, X::mul(A.drag, qv[0]));
@@ -468,7 +533,7 @@ struct self_dg2d {
   int naux = 0, has_drag = 0, has_relax = 0, has_inflow = 0;
   double g = 9.81, drag = 0.0, dt = 0.0;
   std::vector<double> dS, dP, lW, lE, lS, lN, qw;
-  DevBuf<double> q, G, bs, bf, metrics, aux, egeo, tend;
+  DevBuf<double> q, G, bs, bf, metrics, aux, egeo, eplan, tend;
   DevBuf<int> edges;
   bool traces_valid = false;
   cudaGraphExec_t step_graph = nullptr;
@@ -511,6 +576,7 @@ int launch_edge_t(self_dg2d* h, double t) {
   EA.bf = h->bf.p;
   EA.edges = h->edges.p;
   EA.egeo = h->egeo.p;
+  EA.eplan = h->eplan.p;
   EA.nEdges = h->nEdges;
   EA.g = h->g;
   EA.t = t;
@@ -519,6 +585,8 @@ int launch_edge_t(self_dg2d* h, double t) {
     dg_edge_flux<N1, NEQ, SWFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   else if (PH == 2)
     dg_edge_flux<N1, NEQ, SWLinFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
+  else if (PH == 3)
+    dg_edge_flux<N1, NEQ, SWSkewFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   else
     dg_edge_flux<N1, NEQ, AdvFlux, EX><<<(nthr + 255) / 256, 256, 0, st>>>(EA);
   SELF_LAUNCHED(ctx);
@@ -580,6 +648,7 @@ int stage_nx(self_dg2d* h, int mode, double a, double gdt, double t, const doubl
   if (h->model == SELF_MODEL_SW_CONSERVATIVE)
     return launch_stage_t<N1, 3, 1, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
   if (h->model == SELF_MODEL_SW_LINEAR) return launch_stage_t<N1, 3, 2, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
+  if (h->model == SELF_MODEL_SW_SKEW) return launch_stage_t<N1, 4, 3, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
   switch (h->nEq) {
     case 1: return launch_stage_t<N1, 1, 0, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
     case 2: return launch_stage_t<N1, 2, 0, EX>(h, mode, a, gdt, t, qin, qout, tend, wt);
@@ -598,6 +667,7 @@ template <int N1, bool EX>
 int edge_nx(self_dg2d* h, double t) {
   if (h->model == SELF_MODEL_SW_CONSERVATIVE) return launch_edge_t<N1, 3, 1, EX>(h, t);
   if (h->model == SELF_MODEL_SW_LINEAR) return launch_edge_t<N1, 3, 2, EX>(h, t);
+  if (h->model == SELF_MODEL_SW_SKEW) return launch_edge_t<N1, 4, 3, EX>(h, t);
   switch (h->nEq) {
     case 1: return launch_edge_t<N1, 1, 0, EX>(h, t);
     case 2: return launch_edge_t<N1, 2, 0, EX>(h, t);
@@ -615,6 +685,7 @@ int volume_nx(self_dg2d* h, int mode, double a, double gdt, const double* qin, d
   if (h->model == SELF_MODEL_SW_CONSERVATIVE)
     return launch_volume_t<N1, 3, 1, EX>(h, mode, a, gdt, qin, qout, tend, wt);
   if (h->model == SELF_MODEL_SW_LINEAR) return launch_volume_t<N1, 3, 2, EX>(h, mode, a, gdt, qin, qout, tend, wt);
+  if (h->model == SELF_MODEL_SW_SKEW) return launch_volume_t<N1, 4, 3, EX>(h, mode, a, gdt, qin, qout, tend, wt);
   switch (h->nEq) {
     case 1: return launch_volume_t<N1, 1, 0, EX>(h, mode, a, gdt, qin, qout, tend, wt);
     case 2: return launch_volume_t<N1, 2, 0, EX>(h, mode, a, gdt, qin, qout, tend, wt);
@@ -724,8 +795,9 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
     if (d->nEq != 3) return set_error(ctx, SELF_ERR_INVALID, "shallow water needs nEq = 3");
     if (!d->h || !d->dhdx || !d->dhdy || !d->fcor) return set_error(ctx, SELF_ERR_INVALID, "missing bathymetry");
-  } else if (d->model == SELF_MODEL_SW_LINEAR) {
-    if (d->nEq != 3) return set_error(ctx, SELF_ERR_INVALID, "shallow water needs nEq = 3");
+  } else if (d->model == SELF_MODEL_SW_LINEAR || d->model == SELF_MODEL_SW_SKEW) {
+    if (d->nEq != (d->model == SELF_MODEL_SW_SKEW ? 4 : 3))
+      return set_error(ctx, SELF_ERR_INVALID, "linear shallow water needs nEq = 3, skew-symmetric nEq = 4");
     if (!d->h || !d->fcor) return set_error(ctx, SELF_ERR_INVALID, "missing bathymetry or planetary vorticity");
   } else if (d->model == SELF_MODEL_ADVECTION) {
     if (d->nEq < 1 || d->nEq > 4) return set_error(ctx, SELF_ERR_UNSUPPORTED, "advection nEq must be 1..4");
@@ -788,7 +860,8 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   // aux block
   std::vector<const double*> fields;
   h->has_relax = (d->relax && d->rfac) ? 1 : 0;
-  const bool swl = d->model == SELF_MODEL_SW_LINEAR;
+  const bool swl = d->model == SELF_MODEL_SW_LINEAR || d->model == SELF_MODEL_SW_SKEW;
+  const bool sws = d->model == SELF_MODEL_SW_SKEW;
   if (d->model == SELF_MODEL_SW_CONSERVATIVE) {
     h->has_drag = d->linear_drag != 0.0 ? 1 : 0;
     fields = {d->dhdx, d->dhdy, d->fcor};
@@ -811,7 +884,7 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
       ++f;
     }
     if (h->has_relax) {
-      for (int v = 0; v < d->nEq; ++v, ++f)
+      for (int v = 0; v < (sws ? 3 : d->nEq); ++v, ++f)
         for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->relax[(e * d->nEq + v) * NN + k];
       if (d->model == SELF_MODEL_SW_CONSERVATIVE || swl) {
         for (size_t k = 0; k < NN; ++k) aux[(e * h->naux + f) * NN + k] = d->rfac[e * NN + k];
@@ -835,7 +908,19 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
     }
     return acc;
   };
-  std::vector<double> eg((size_t)4 * n * d->nEdges, 0.0);
+  std::vector<double> eg((size_t)4 * n * d->nEdges, 0.0), ep;
+  if (sws) ep.assign((size_t)2 * n * d->nEdges, 0.0);
+  auto f_trace = [&](int e, int s, int i) {  // planetary vorticity traces (CalculateVorticityAtBoundaries order)
+    double acc = 0.0;
+    if (s == 0 || s == 2) {
+      const double* L = s == 0 ? d->lagS : d->lagN;
+      for (int m = 0; m < n; ++m) acc = acc + L[m] * d->fcor[(size_t)e * NN + i + (size_t)n * m];
+    } else {
+      const double* L = s == 1 ? d->lagE : d->lagW;
+      for (int m = 0; m < n; ++m) acc = acc + L[m] * d->fcor[(size_t)e * NN + m + (size_t)n * i];
+    }
+    return acc;
+  };
   for (int k = 0; k < d->nEdges; ++k) {
     const int e1 = ed[6 * k] - 1, s1 = ed[6 * k + 1] - 1;
     for (int i = 0; i < n; ++i) {
@@ -862,12 +947,23 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
           dep = 0.5 * (dep + h_trace(e2, s2, kk));
         }
         eg[(size_t)k * 4 * n + 3 * n + i] = dep;
+        if (sws) {
+          const double fi = f_trace(e1, s1, i);
+          double fo = fi;
+          if (ed[6 * k + 2] > 0) {
+            const int e2 = ed[6 * k + 2] - 1, s2 = std::abs(ed[6 * k + 3]) - 1;
+            fo = f_trace(e2, s2, ed[6 * k + 4] - ed[6 * k + 5] + i * ed[6 * k + 5]);
+          }
+          ep[(size_t)k * 2 * n + i] = fi;
+          ep[(size_t)k * 2 * n + n + i] = fo;
+        }
       }
     }
   }
   int rc;
   if ((rc = upload(ctx, h->edges, ed))) return rc;
   if ((rc = upload(ctx, h->egeo, eg))) return rc;
+  if (sws && (rc = upload(ctx, h->eplan, ep))) return rc;
   if (d->precision != SELF_PREC_FP32) {
     if ((rc = upload(ctx, h->metrics, met))) return rc;
     if ((rc = upload(ctx, h->aux, aux))) return rc;

@@ -197,19 +197,24 @@ class _DG2D:
 class ShallowWater(_DG2D):
     """formulation "conservative": ConservativeShallowWater (U=Hu, V=Hv, H) with LLF flux, bathymetry and Coriolis
     sources, mirror walls.  formulation "linear": ShallowWaterClass with ModelFormulation LINEAR (u, v, eta about a
-    resting depth h; linear flux with the edge depth, Coriolis, linear drag and relaxation sources)."""
+    resting depth h; linear flux with the edge depth, Coriolis, linear drag and relaxation sources).
+    formulation "skew_symmetric": ModelFormulation SKEW_SYMMETRIC, 4 state variables (u, v, eta, zeta): the
+    relative vorticity zeta is advanced with the state and enters the Coriolis term as f + zeta."""
 
     def __init__(self, ctx, nodal, mesh, h, fcor, dt, g=9.81, linear_drag=0.0, dhdx=None, dhdy=None,
                  precision=nat.PREC_FP64, relax=None, timescale=None, formulation="conservative"):
+        nEq = 3
         if formulation == "linear":
             model = nat.MODEL_SW_LINEAR
+        elif formulation == "skew_symmetric":
+            model, nEq = nat.MODEL_SW_SKEW, 4
         elif formulation == "conservative":
             model = nat.MODEL_SW_CONSERVATIVE
             if dhdx is None or dhdy is None:
                 dhdx, dhdy = bathymetry_gradient(nodal, mesh, h)
         else:
             raise ValueError(f"formulation {formulation!r}")
-        super().__init__(ctx, nodal, mesh, model, 3, dt, precision, g=g, linear_drag=linear_drag,
+        super().__init__(ctx, nodal, mesh, model, nEq, dt, precision, g=g, linear_drag=linear_drag,
                          h=h, dhdx=dhdx, dhdy=dhdy, fcor=fcor, relax=relax, rfac=timescale)
         self.h, self.dhdx, self.dhdy, self.fcor = h, dhdx, dhdy, fcor
         self.formulation = formulation
