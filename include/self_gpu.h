@@ -125,6 +125,9 @@ typedef struct {
   const double* rfac;                   /* optional: SW relaxation timescale (i,j,e); advection (i,j,v,e) */
   const double *u, *v;                  /* advection velocity (i,j,e) */
   double g, linear_drag, dt;
+  /* advection only: diffusivity kappa >= 0; kappa > 0 adds the BR1 passes of AdvectionClass.f90 (gradient by the
+   * DG weak derivative with central fluxes, :1123-1264 and :1482-1563; flux c u - kappa grad c; FP64 forms) */
+  double kappa;
 } self_dg2d_desc;
 
 typedef struct self_dg2d self_dg2d;

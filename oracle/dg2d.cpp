@@ -16,6 +16,11 @@
 // vorticity = f + zeta (relativeFactor = 1), RelativeVorticityEdgeFlux :1628-1724 (VorticityFluxSolver
 // :2041-2068, GetExternalVorticity :2329-2356: NO_NORMAL_FLOW copies the interior value, other flags zero; the
 // boundary's outer planetary vorticity is the inner one) and VorticityTimeDerivative :1891-2008.
+// Advection with kappa > 0 restates the BR1 passes of AdvectionClass.f90: GlobalTimeDerivative :1316-1378
+// (traces, EdgeGradientFlux :1482-1563 = central flux HALF*(in + ex)*n*|n|, CalculateConcentrationGradient
+// :1123-1264 = DG weak derivative with lift, divided by J, CalculateGradientAtBoundaries :1092-1104, EdgeFlux
+// :1382-1478 with the averaged gradient on interior edges and the inner one on the boundary, RiemannSolver
+// :1756-1787 minus kappa dc/dn, XFlux/YFlux :1790-1825 = c u - kappa dc/dx, c v - kappa dc/dy).
 // Decision: V2D, never initialised in ForwardStepRK3, is taken as zero (its first use multiplies it by
 // rk3_a(1) = 0).
 // Decision: the Riemann solver's undeclared "g" (:1589-1592) is the parameter g (locG).
@@ -164,7 +169,15 @@ int orc_dg_traces(const orc_dg_problem* p, const double* q, double* bs) {
   return 0;
 }
 
+static int edge_flux(const orc_dg_problem* p, double t, const double* bs, const double* gtx, const double* gty,
+                     double* bf);
+
 int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double* bf) {
+  return edge_flux(p, t, bs, nullptr, nullptr, bf);
+}
+
+static int edge_flux(const orc_dg_problem* p, double t, const double* bs, const double* gtx, const double* gty,
+                     double* bf) {
   const int n = p->N + 1, nEq = p->nEq, N = p->N;
   Idx I{n, nEq};
   int err = 0;
@@ -213,6 +226,11 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
           for (int v = 0; v < nEq; ++v) {
             double jump = ex[v] - in[v];
             fl[v] = 0.5 * (un * (ex[v] + in[v]) - std::fabs(un) * jump);
+            if (gtx) {  // - kappa dc/dn with the averaged gradient
+              double gx = (gtx[I.b(i, v, s1, e1)] + gtx[I.b(kk, v, s2, e2)]) * 0.5;
+              double gy = (gty[I.b(i, v, s1, e1)] + gty[I.b(kk, v, s2, e2)]) * 0.5;
+              fl[v] = fl[v] - p->kappa * (gx * nH[0] + gy * nH[1]);
+            }
           }
         }
         for (int v = 0; v < nEq; ++v) {
@@ -259,6 +277,8 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
           for (int v = 0; v < nEq; ++v) {
             double jump = ex[v] - in[v];
             fl[v] = 0.5 * (un * (ex[v] + in[v]) - std::fabs(un) * jump);
+            if (gtx)  // - kappa dc/dn with the inner gradient
+              fl[v] = fl[v] - p->kappa * (gtx[I.b(i, v, s1, e1)] * nH[0] + gty[I.b(i, v, s1, e1)] * nH[1]);
           }
         }
         for (int v = 0; v < nEq; ++v) bf[I.b(i, v, s1, e1)] = fl[v] * len;
@@ -270,7 +290,7 @@ int orc_dg_edge_flux(const orc_dg_problem* p, double t, const double* bs, double
 
 // MappedTimeDerivative for one element
 static void mapped_time_derivative(const orc_dg_problem* p, double t, const double* q, const double* bf,
-                                   double* tend, int e) {
+                                   const double* gx, const double* gy, double* tend, int e) {
   const int n = p->N + 1, nEq = p->nEq;
   Idx I{n, nEq};
   std::vector<double> cf(n * nEq), der(n), xF(nEq), yF(nEq), sol(nEq);
@@ -312,6 +332,10 @@ static void mapped_time_derivative(const orc_dg_problem* p, double t, const doub
       for (int k = 0; k < nEq; ++k) {
         xF[k] = sol[k] * u;
         yF[k] = sol[k] * v;
+        if (gx) {
+          xF[k] = xF[k] - p->kappa * gx[I.q(i, j, k, e)];
+          yF[k] = yF[k] - p->kappa * gy[I.q(i, j, k, e)];
+        }
       }
     }
   };
@@ -390,15 +414,107 @@ static void mapped_time_derivative(const orc_dg_problem* p, double t, const doub
     }
 }
 
+// EdgeGradientFlux: central flux of the traces into the boundary fluxes of dC/dx and dC/dy
+static void edge_gradient_flux(const orc_dg_problem* p, double t, const double* bs, double* bgx, double* bgy) {
+  const int n = p->N + 1, nEq = p->nEq, N = p->N;
+  Idx I{n, nEq};
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < p->nEdges; ++k) {
+    const int* E = p->edges + 6 * k;
+    int e1 = E[0] - 1, s1 = E[1] - 1, e2 = E[2], s2 = std::abs(E[3]) - 1, start = E[4], inc = E[5];
+    int kk = start - inc;
+    for (int i = 0; i <= N; ++i) {
+      double nx = p->nhx[I.nh(i, s1, e1)], ny = p->nhy[I.nh(i, s1, e1)], len = p->nlen[I.nh(i, s1, e1)];
+      for (int v = 0; v < nEq; ++v) {
+        double in = bs[I.b(i, v, s1, e1)], ex;
+        if (e2 > 0) {
+          ex = bs[I.b(kk, v, s2, e2 - 1)];
+        } else {
+          ex = 0.0;  // GetExternalState (:1851-1886)
+          if (e2 == ORC_INFLOW_ONE && v == 0) ex = std::tanh(t);
+          if (e2 == ORC_INFLOW_TWO && v == 1) ex = std::tanh(t);
+        }
+        double fx = 0.5 * (in + ex) * nx * len, fy = 0.5 * (in + ex) * ny * len;
+        bgx[I.b(i, v, s1, e1)] = fx;
+        bgy[I.b(i, v, s1, e1)] = fy;
+        if (e2 > 0) {
+          bgx[I.b(kk, v, s2, e2 - 1)] = -fx;
+          bgy[I.b(kk, v, s2, e2 - 1)] = -fy;
+        }
+      }
+      kk = kk + inc;
+    }
+  }
+}
+
+// CalculateConcentrationGradient for one element
+static void concentration_gradient(const orc_dg_problem* p, const double* q, const double* bgx, const double* bgy,
+                                   double* gx, double* gy, int e) {
+  const int n = p->N + 1, nEq = p->nEq;
+  Idx I{n, nEq};
+  std::vector<double> c1(n), c2(n), d1(n), d2(n);
+  for (int v = 0; v < nEq; ++v) {
+    for (int j = 0; j < n; ++j) {
+      for (int i = 0; i < n; ++i) {
+        size_t id = I.f(i, j, e);
+        double sol = q[I.q(i, j, v, e)];
+        c1[i] = p->dydp[id] * sol - p->dxdp[id] * 0.0;
+        c2[i] = p->dydp[id] * 0.0 - p->dxdp[id] * sol;
+      }
+      dg_system_derivative(n, p->dmatS, p->qw, bgx[I.b(j, v, 3, e)], bgx[I.b(j, v, 1, e)], c1.data(), p->lW, p->lE,
+                           d1.data());
+      dg_system_derivative(n, p->dmatS, p->qw, bgy[I.b(j, v, 3, e)], bgy[I.b(j, v, 1, e)], c2.data(), p->lW, p->lE,
+                           d2.data());
+      for (int i = 0; i < n; ++i) {
+        gx[I.q(i, j, v, e)] = d1[i];
+        gy[I.q(i, j, v, e)] = d2[i];
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < n; ++j) {
+        size_t id = I.f(i, j, e);
+        double sol = q[I.q(i, j, v, e)];
+        c1[j] = -p->dyds[id] * sol + p->dxds[id] * 0.0;
+        c2[j] = -p->dyds[id] * 0.0 + p->dxds[id] * sol;
+      }
+      dg_system_derivative(n, p->dmatP, p->qw, bgx[I.b(i, v, 0, e)], bgx[I.b(i, v, 2, e)], c1.data(), p->lS, p->lN,
+                           d1.data());
+      dg_system_derivative(n, p->dmatP, p->qw, bgy[I.b(i, v, 0, e)], bgy[I.b(i, v, 2, e)], c2.data(), p->lS, p->lN,
+                           d2.data());
+      for (int j = 0; j < n; ++j) {
+        double Jn = p->J[I.f(i, j, e)];
+        gx[I.q(i, j, v, e)] = (gx[I.q(i, j, v, e)] + d1[j]) / Jn;
+        gy[I.q(i, j, v, e)] = (gy[I.q(i, j, v, e)] + d2[j]) / Jn;
+      }
+    }
+  }
+}
+
 int orc_dg_tendency(const orc_dg_problem* p, double t, const double* q, double* tend) {
-  if (p->kappa != 0.0) return -5;  // the BR1 diffusion passes are not restated
+  const bool br1 = p->model == 2 && p->kappa != 0.0;
+  if (p->kappa != 0.0 && !br1) return -5;
   const int n = p->N + 1;
-  size_t nb = (size_t)n * p->nEq * 4 * p->nEl;
+  size_t nb = (size_t)n * p->nEq * 4 * p->nEl, nq = (size_t)n * n * p->nEq * p->nEl;
   std::vector<double> bs(nb, 0.0), bf(nb, 0.0);
   orc_dg_traces(p, q, bs.data());
-  if (orc_dg_edge_flux(p, t, bs.data(), bf.data()) != 0) return -1;
+  std::vector<double> bgx, bgy, gx, gy, gtx, gty;
+  if (br1) {
+    bgx.assign(nb, 0.0);
+    bgy.assign(nb, 0.0);
+    gx.assign(nq, 0.0);
+    gy.assign(nq, 0.0);
+    gtx.assign(nb, 0.0);
+    gty.assign(nb, 0.0);
+    edge_gradient_flux(p, t, bs.data(), bgx.data(), bgy.data());
 #pragma omp parallel for schedule(static)
-  for (int e = 0; e < p->nEl; ++e) mapped_time_derivative(p, t, q, bf.data(), tend, e);
+    for (int e = 0; e < p->nEl; ++e) concentration_gradient(p, q, bgx.data(), bgy.data(), gx.data(), gy.data(), e);
+    orc_dg_traces(p, gx.data(), gtx.data());  // CalculateGradientAtBoundaries
+    orc_dg_traces(p, gy.data(), gty.data());
+  }
+  if (edge_flux(p, t, bs.data(), br1 ? gtx.data() : nullptr, br1 ? gty.data() : nullptr, bf.data()) != 0) return -1;
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < p->nEl; ++e)
+    mapped_time_derivative(p, t, q, bf.data(), br1 ? gx.data() : nullptr, br1 ? gy.data() : nullptr, tend, e);
   return 0;
 }
 

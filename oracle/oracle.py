@@ -170,7 +170,7 @@ class DGProblem:
     """Shallow water (model=1, nEq=3) or linear advection (model=2) on a Mesh with a Nodal (DG, GAUSS)."""
 
     def __init__(self, nodal, mesh, model, nEq, dt, g=9.81, drag=0.0, h=None, dhdx=None, dhdy=None, fcor=None,
-                 u=None, v=None, relax=None, rfac=None):
+                 u=None, v=None, relax=None, rfac=None, kappa=0.0):
         self.keep = [nodal, mesh, h, dhdx, dhdy, fcor, u, v, relax, rfac]
         s = _DGProblem()
         s.N, s.nEl, s.nEdges, s.nEq, s.model = nodal.N, mesh.nEl, mesh.nEdges, nEq, model
@@ -182,7 +182,7 @@ class DGProblem:
         s.h, s.dhdx, s.dhdy, s.fcor = _d(h), _d(dhdx), _d(dhdy), _d(fcor)
         s.relax, s.rfac = _d(relax), _d(rfac)
         s.u, s.v = _d(u), _d(v)
-        s.g, s.drag, s.dt, s.kappa = g, drag, dt, 0.0
+        s.g, s.drag, s.dt, s.kappa = g, drag, dt, kappa
         self.s = s
         self.nodal, self.mesh, self.nEq = nodal, mesh, nEq
         self.nq = nodal.n * nodal.n * nEq * mesh.nEl

@@ -94,4 +94,4 @@ class DG2DDesc(C.Structure):
                 ("lagN", dp), ("edges", ip), ("dxds", dp), ("dxdp", dp), ("dyds", dp), ("dydp", dp), ("J", dp),
                 ("nhx", dp), ("nhy", dp), ("nlen", dp), ("h", dp), ("dhdx", dp), ("dhdy", dp), ("fcor", dp),
                 ("relax", dp), ("rfac", dp), ("u", dp), ("v", dp),
-                ("g", C.c_double), ("linear_drag", C.c_double), ("dt", C.c_double)]
+                ("g", C.c_double), ("linear_drag", C.c_double), ("dt", C.c_double), ("kappa", C.c_double)]

@@ -55,6 +55,8 @@ struct VolArgs {
   double g, drag, a, gdt;
   int mode;  // 0 tendency only, 1 RK stage with a = 0 (G not read), 2 RK stage reading G
   int write_traces;
+  const double *gx, *gy;  // advection with kappa > 0: concentration gradient (i, j, v, e), else null
+  double kappa;
 };
 
 struct EdgeArgs {
@@ -63,6 +65,8 @@ struct EdgeArgs {
   const int* edges;     // 6 per edge
   const double* egeo;   // 4 n per edge: nx, ny, |n|, u.n (advection) or the edge depth (linear / skew SW)
   const double* eplan;  // skew SW: 2 n per edge, planetary vorticity traces of the primary and secondary side
+  const double *gtx, *gty;  // advection with kappa > 0: traces of the concentration gradient, else null
+  double kappa;
   int nEdges;
   double g, t;
 };
@@ -248,6 +252,16 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
     Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, f);
+    if (A.gtx) {  // BR1: - kappa dc/dn with the averaged gradient (AdvectionClass.f90 EdgeFlux :1413-1420)
+      using X = Ar<EX>;
+      const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i, o2i = (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2) + kk;
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v) {
+        const double gx = X::mul(X::add(A.gtx[o1i + N1 * v], A.gtx[o2i + N1 * v]), 0.5);
+        const double gy = X::mul(X::add(A.gty[o1i + N1 * v], A.gty[o2i + N1 * v]), 0.5);
+        f[v] = X::sub(f[v], X::mul(A.kappa, X::add(X::mul(gx, nx), X::mul(gy, ny))));
+      }
+    }
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
     double* o2 = A.bf + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
@@ -259,6 +273,13 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
   } else {
     Phys::template external<NEQ, EX>(e2f, nx, ny, A.t, in, ex);
     Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, f);
+    if (A.gtx) {  // BR1: the inner gradient on the boundary
+      using X = Ar<EX>;
+      const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i;
+#pragma unroll
+      for (int v = 0; v < NEQ; ++v)
+        f[v] = X::sub(f[v], X::mul(A.kappa, X::add(X::mul(A.gtx[o1i + N1 * v], nx), X::mul(A.gty[o1i + N1 * v], ny))));
+    }
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = Ar<EX>::mul(f[v], len);
@@ -391,6 +412,10 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
       for (int v = 0; v < NEQ; ++v) {
         xF[v] = X::mul(qv[v], u);
         yF[v] = X::mul(qv[v], vv);
+        if (A.gx) {  // XFlux / YFlux (AdvectionClass.f90:1790-1825): c u - kappa dc/dx, c v - kappa dc/dy
+          xF[v] = X::sub(xF[v], X::mul(A.kappa, A.gx[(size_t)e * NEQ * NN + v * NN + tid]));
+          yF[v] = X::sub(yF[v], X::mul(A.kappa, A.gy[(size_t)e * NEQ * NN + v * NN + tid]));
+        }
       }
     }
 #pragma unroll
@@ -523,6 +548,173 @@ __global__ void __launch_bounds__(256) dg_traces(const double* q, double* bs, in
   if (e < nEl) write_traces<N1, NEQ, EX>(C, &sQ[le][0][0], bs, e, tid);
 }
 
+
+// ------------------------------------------------------------------------------------ BR1 gradient passes
+// Advection-diffusion with kappa > 0 (AdvectionClass.f90 GlobalTimeDerivative :1316-1378): before the edge flux
+// and the volume pass of a stage, the concentration gradient is formed by the DG weak derivative of c with
+// central boundary fluxes (EdgeGradientFlux :1482-1563, CalculateConcentrationGradient :1123-1264) and traced to
+// the element sides (CalculateGradientAtBoundaries :1092-1104).
+struct GradArgs {
+  const double* q;
+  const double* bs;     // traces of c
+  double *bgx, *bgy;    // boundary fluxes of the gradient passes
+  double *gx, *gy;      // gradient (i, j, v, e)
+  double *gtx, *gty;    // its traces
+  const int* edges;
+  const double* egeo;
+  const double* metrics;
+  int nEdges, nEl;
+  double t;
+};
+
+// central flux HALF*(c_in + c_ex)*n*|n| of every edge node, +/- to the two sides; outer state GetExternalState
+template <int N1, int NEQ, bool EX>
+__global__ void __launch_bounds__(256) dg_grad_edge(GradArgs A) {
+  using X = Ar<EX>;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = gid / N1;
+  const int i = gid - k * N1;
+  if (k >= A.nEdges) return;
+  const int* E = A.edges + 6 * k;
+  const int e1 = E[0] - 1, s1 = E[1] - 1, e2f = E[2];
+  const double* eg = A.egeo + (size_t)k * 4 * N1;
+  const double nx = eg[i], ny = eg[N1 + i], len = eg[2 * N1 + i];
+  const size_t b1 = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i;
+  size_t b2 = 0;
+  if (e2f > 0) {
+    const int kk = E[4] - E[5] + i * E[5];
+    b2 = (size_t)N1 * NEQ * (abs(E[3]) - 1 + 4 * (size_t)(e2f - 1)) + kk;
+  }
+#pragma unroll
+  for (int v = 0; v < NEQ; ++v) {
+    const double in = A.bs[b1 + N1 * v];
+    double ex = 0.0;
+    if (e2f > 0) {
+      ex = A.bs[b2 + N1 * v];
+    } else {
+      if (e2f == SELF_INFLOW_ONE && v == 0) ex = tanh(A.t);
+      if (e2f == SELF_INFLOW_TWO && v == 1) ex = tanh(A.t);
+    }
+    const double avg = X::mul(0.5, X::add(in, ex));
+    const double fx = X::mul(X::mul(avg, nx), len), fy = X::mul(X::mul(avg, ny), len);
+    A.bgx[b1 + N1 * v] = fx;
+    A.bgy[b1 + N1 * v] = fy;
+    if (e2f > 0) {
+      A.bgx[b2 + N1 * v] = -fx;
+      A.bgy[b2 + N1 * v] = -fy;
+    }
+  }
+}
+
+// gradient of c per element and variable (s direction with the west/east lifts, p direction with the
+// south/north lifts, divided by J), then its traces
+template <int N1, int NEQ, bool EX>
+__global__ void __launch_bounds__(256) dg_grad_volume(GradArgs A, NodalConst<N1> Cg) {
+  using X = Ar<EX>;
+  constexpr int NN = N1 * N1;
+  constexpr int EPB = elems_per_block<N1>();
+  __shared__ NodalConst<N1> C;
+  __shared__ double s1x[EPB][NN], s1y[EPB][NN], s2x[EPB][NN], s2y[EPB][NN];
+  __shared__ double sBx[EPB][4][N1], sBy[EPB][4][N1];
+  const int tid = threadIdx.x, le = threadIdx.y;
+  const int e = blockIdx.x * EPB + le;
+  const bool active = e < A.nEl;
+  {
+    const int flat = tid + NN * le;
+    constexpr int NC = sizeof(NodalConst<N1>) / sizeof(double);
+    const double* src = reinterpret_cast<const double*>(&Cg);
+    double* dst = reinterpret_cast<double*>(&C);
+    for (int t = flat; t < NC; t += NN * EPB) dst[t] = src[t];
+  }
+  const int i = tid % N1, j = tid / N1;
+  double dxds = 0, dxdp = 0, dyds = 0, dydp = 0, jac = 0;
+  if (active) {
+    const double* me = A.metrics + (size_t)e * 5 * NN;
+    dxds = me[tid];
+    dxdp = me[NN + tid];
+    dyds = me[2 * NN + tid];
+    dydp = me[3 * NN + tid];
+    jac = me[4 * NN + tid];
+  }
+  for (int v = 0; v < NEQ; ++v) {
+    __syncthreads();  // the previous variable is done with the scratch arrays
+    if (active) {
+      const double c = A.q[(size_t)e * NEQ * NN + v * NN + tid];
+      s1x[le][tid] = X::sub(X::mul(dydp, c), X::mul(dxdp, 0.0));
+      s1y[le][tid] = X::sub(X::mul(dydp, 0.0), X::mul(dxdp, c));
+      s2x[le][tid] = X::add(X::mul(-dyds, c), X::mul(dxds, 0.0));
+      s2y[le][tid] = X::add(X::mul(-dyds, 0.0), X::mul(dxds, c));
+      for (int t = tid; t < 4 * N1; t += NN) {
+        const int side = t / N1, kq = t - side * N1;
+        const size_t b = (size_t)N1 * NEQ * (side + 4 * (size_t)e) + kq + N1 * v;
+        sBx[le][side][kq] = A.bgx[b];
+        sBy[le][side][kq] = A.bgy[b];
+      }
+    }
+    __syncthreads();
+    double gx = 0.0, gy = 0.0;
+    if (active) {
+      double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        ax = X::add(ax, X::mul(C.dS[i + N1 * m], s1x[le][m + N1 * j]));
+        ay = X::add(ay, X::mul(C.dS[i + N1 * m], s1y[le][m + N1 * j]));
+      }
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        bx = X::add(bx, X::mul(C.dP[j + N1 * m], s2x[le][i + N1 * m]));
+        by = X::add(by, X::mul(C.dP[j + N1 * m], s2y[le][i + N1 * m]));
+      }
+      if (EX) {
+        ax = X::add(ax, X::add(X::mul(sBx[le][1][j], C.lE[i]), X::mul(sBx[le][3][j], C.lW[i])) / C.qw[i]);
+        ay = X::add(ay, X::add(X::mul(sBy[le][1][j], C.lE[i]), X::mul(sBy[le][3][j], C.lW[i])) / C.qw[i]);
+        bx = X::add(bx, X::add(X::mul(sBx[le][2][i], C.lN[j]), X::mul(sBx[le][0][i], C.lS[j])) / C.qw[j]);
+        by = X::add(by, X::add(X::mul(sBy[le][2][i], C.lN[j]), X::mul(sBy[le][0][i], C.lS[j])) / C.qw[j]);
+        gx = X::add(ax, bx) / jac;
+        gy = X::add(ay, by) / jac;
+      } else {
+        ax += (sBx[le][1][j] * C.lE[i] + sBx[le][3][j] * C.lW[i]) * C.qwinv[i];
+        ay += (sBy[le][1][j] * C.lE[i] + sBy[le][3][j] * C.lW[i]) * C.qwinv[i];
+        bx += (sBx[le][2][i] * C.lN[j] + sBx[le][0][i] * C.lS[j]) * C.qwinv[j];
+        by += (sBy[le][2][i] * C.lN[j] + sBy[le][0][i] * C.lS[j]) * C.qwinv[j];
+        gx = (ax + bx) * jac;
+        gy = (ay + by) * jac;
+      }
+      A.gx[(size_t)e * NEQ * NN + v * NN + tid] = gx;
+      A.gy[(size_t)e * NEQ * NN + v * NN + tid] = gy;
+    }
+    __syncthreads();  // the contravariant arrays are read; they now hold the gradient for the traces
+    if (active) {
+      s1x[le][tid] = gx;
+      s1y[le][tid] = gy;
+    }
+    __syncthreads();
+    if (active) {
+      for (int t = tid; t < 4 * N1; t += NN) {
+        const int side = t / N1, kq = t - side * N1;
+        double accx = 0.0, accy = 0.0;
+        if (side == 0 || side == 2) {
+          const double* L = (side == 0) ? C.lS : C.lN;
+#pragma unroll
+          for (int m = 0; m < N1; ++m) {
+            accx = X::add(accx, X::mul(L[m], s1x[le][kq + N1 * m]));
+            accy = X::add(accy, X::mul(L[m], s1y[le][kq + N1 * m]));
+          }
+        } else {
+          const double* L = (side == 1) ? C.lE : C.lW;
+#pragma unroll
+          for (int m = 0; m < N1; ++m) {
+            accx = X::add(accx, X::mul(L[m], s1x[le][m + N1 * kq]));
+            accy = X::add(accy, X::mul(L[m], s1y[le][m + N1 * kq]));
+          }
+        }
+        const size_t b = (size_t)N1 * NEQ * (side + 4 * (size_t)e) + kq + N1 * v;
+        A.gtx[b] = accx;
+        A.gty[b] = accy;
+      }
+    }
+  }
+}
 }  // namespace dg
 }  // namespace selfgpu
 
@@ -531,9 +723,10 @@ struct self_dg2d {
   self_ctx* ctx = nullptr;
   int N = 0, n = 0, nEl = 0, nEdges = 0, nEq = 0, model = 0, precision = 0;
   int naux = 0, has_drag = 0, has_relax = 0, has_inflow = 0;
-  double g = 9.81, drag = 0.0, dt = 0.0;
+  double g = 9.81, drag = 0.0, dt = 0.0, kappa = 0.0;
   std::vector<double> dS, dP, lW, lE, lS, lN, qw;
   DevBuf<double> q, G, bs, bf, metrics, aux, egeo, eplan, tend;
+  DevBuf<double> gx, gy, gtx, gty, bgx, bgy;  // advection with kappa > 0: BR1 gradient, traces, boundary fluxes
   DevBuf<int> edges;
   bool traces_valid = false;
   cudaGraphExec_t step_graph = nullptr;
@@ -577,6 +770,10 @@ int launch_edge_t(self_dg2d* h, double t) {
   EA.edges = h->edges.p;
   EA.egeo = h->egeo.p;
   EA.eplan = h->eplan.p;
+  const bool br1 = PH == 0 && h->kappa != 0.0;
+  EA.gtx = br1 ? h->gtx.p : nullptr;
+  EA.gty = br1 ? h->gty.p : nullptr;
+  EA.kappa = h->kappa;
   EA.nEdges = h->nEdges;
   EA.g = h->g;
   EA.t = t;
@@ -617,6 +814,10 @@ int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* 
   VA.gdt = gdt;
   VA.mode = mode;
   VA.write_traces = write_traces;
+  const bool br1 = PH == 0 && h->kappa != 0.0;
+  VA.gx = br1 ? h->gx.p : nullptr;
+  VA.gy = br1 ? h->gy.p : nullptr;
+  VA.kappa = h->kappa;
   constexpr int EPB = elems_per_block<N1>();
   dim3 blk(N1 * N1, EPB);
   dg_volume<N1, NEQ, PH, EX><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(VA, make_const<N1>(h));
@@ -624,9 +825,43 @@ int launch_volume_t(self_dg2d* h, int mode, double a, double gdt, const double* 
   return SELF_OK;
 }
 
+// BR1 gradient passes of one stage (advection with kappa > 0): central edge fluxes, then gradient + traces
+template <int N1, int NEQ, bool EX>
+int launch_gradient_t(self_dg2d* h, double t, const double* qin) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  GradArgs GA;
+  GA.q = qin;
+  GA.bs = h->bs.p;
+  GA.bgx = h->bgx.p;
+  GA.bgy = h->bgy.p;
+  GA.gx = h->gx.p;
+  GA.gy = h->gy.p;
+  GA.gtx = h->gtx.p;
+  GA.gty = h->gty.p;
+  GA.edges = h->edges.p;
+  GA.egeo = h->egeo.p;
+  GA.metrics = h->metrics.p;
+  GA.nEdges = h->nEdges;
+  GA.nEl = h->nEl;
+  GA.t = t;
+  const int nthr = h->nEdges * N1;
+  dg_grad_edge<N1, NEQ, EX><<<(nthr + 255) / 256, 256, 0, st>>>(GA);
+  SELF_LAUNCHED(ctx);
+  constexpr int EPB = elems_per_block<N1>();
+  dim3 blk(N1 * N1, EPB);
+  dg_grad_volume<N1, NEQ, EX><<<(h->nEl + EPB - 1) / EPB, blk, 0, st>>>(GA, make_const<N1>(h));
+  SELF_LAUNCHED(ctx);
+  return SELF_OK;
+}
+
 template <int N1, int NEQ, int PH, bool EX>
 int launch_stage_t(self_dg2d* h, int mode, double a, double gdt, double t, const double* qin, double* qout,
                    double* tend, int write_traces) {
+  if (PH == 0 && h->kappa != 0.0) {
+    const int rg = launch_gradient_t<N1, NEQ, EX>(h, t, qin);
+    if (rg) return rg;
+  }
   int rc = launch_edge_t<N1, NEQ, PH, EX>(h, t);
   if (rc) return rc;
   return launch_volume_t<N1, NEQ, PH, EX>(h, mode, a, gdt, qin, qout, tend, write_traces);
@@ -821,6 +1056,10 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
   h->g = d->g;
   h->drag = d->linear_drag;
   h->dt = d->dt;
+  h->kappa = d->kappa;
+  if (d->kappa != 0.0 && (d->model != SELF_MODEL_ADVECTION || d->precision == SELF_PREC_FP32))
+    return set_error(ctx, SELF_ERR_UNSUPPORTED, "kappa > 0 (BR1 diffusion): FP64 advection only");
+  if (!(d->kappa >= 0.0)) return set_error(ctx, SELF_ERR_INVALID, "kappa %g", d->kappa);
   const size_t NN = (size_t)n * n, nEl = d->nEl;
   h->dS.assign(d->dmatS, d->dmatS + NN);
   h->dP.assign(d->dmatP, d->dmatP + NN);
@@ -970,6 +1209,9 @@ int self_dg2d_create(self_ctx* ctx, const self_dg2d_desc* d, self_dg2d** out) {
     const size_t nq = NN * d->nEq * nEl, nb = (size_t)n * d->nEq * 4 * nEl;
     if (h->q.alloc(nq) || h->G.alloc(nq) || h->bs.alloc(nb) || h->bf.alloc(nb))
       return set_error(ctx, SELF_ERR_ALLOC, "device allocation of the state failed");
+    if (h->kappa != 0.0 && (h->gx.alloc(nq) || h->gy.alloc(nq) || h->gtx.alloc(nb) || h->gty.alloc(nb) ||
+                            h->bgx.alloc(nb) || h->bgy.alloc(nb)))
+      return set_error(ctx, SELF_ERR_ALLOC, "device allocation of the gradient fields failed");
     SELF_CUDA_TRY(ctx, cudaMemset(h->q.p, 0, h->q.bytes()));
     SELF_CUDA_TRY(ctx, cudaMemset(h->G.p, 0, h->G.bytes()));
     SELF_CUDA_TRY(ctx, cudaMemset(h->bf.p, 0, h->bf.bytes()));

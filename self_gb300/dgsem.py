@@ -133,7 +133,7 @@ def bathymetry_gradient(nodal, mesh, h):
 
 class _DG2D:
     def __init__(self, ctx, nodal, mesh, model, nEq, dt, precision, g=9.81, linear_drag=0.0, h=None, dhdx=None,
-                 dhdy=None, fcor=None, u=None, v=None, relax=None, rfac=None):
+                 dhdy=None, fcor=None, u=None, v=None, relax=None, rfac=None, kappa=0.0):
         s = nat.DG2DDesc()
         s.N, s.nEl, s.nEdges, s.nEq, s.model, s.precision = nodal.N, mesh.nEl, mesh.nEdges, nEq, model, precision
         s.dmatS, s.dmatP, s.qweight = nat.d(nodal.dmatS), nat.d(nodal.dmatP), nat.d(nodal.w)
@@ -143,7 +143,7 @@ class _DG2D:
         s.nhx, s.nhy, s.nlen = nat.d(mesh.nhx), nat.d(mesh.nhy), nat.d(mesh.nlen)
         s.h, s.dhdx, s.dhdy, s.fcor = nat.d(h), nat.d(dhdx), nat.d(dhdy), nat.d(fcor)
         s.relax, s.rfac, s.u, s.v = nat.d(relax), nat.d(rfac), nat.d(u), nat.d(v)
-        s.g, s.linear_drag, s.dt = g, linear_drag, dt
+        s.g, s.linear_drag, s.dt, s.kappa = g, linear_drag, dt, kappa
         self._keep = (nodal, mesh, h, dhdx, dhdy, fcor, u, v, relax, rfac)
         self.ctx = ctx
         self.nodal, self.mesh, self.nEq, self.dt, self.precision = nodal, mesh, nEq, dt, precision
@@ -256,11 +256,14 @@ def read_pickup(path, N, nEl, fields):
 
 
 class Advection(_DG2D):
-    """Advection of nTracers with the upwind (Rusanov) flux, kappa = 0."""
+    """Advection(-diffusion) of nTracers with the upwind (Rusanov) flux; kappa > 0 adds the BR1 diffusion passes
+    (gradient by the DG weak derivative with central fluxes, flux c u - kappa grad c)."""
 
-    def __init__(self, ctx, nodal, mesh, u, v, dt, nTracers=1, precision=nat.PREC_FP64, relax=None, rfac=None):
+    def __init__(self, ctx, nodal, mesh, u, v, dt, nTracers=1, precision=nat.PREC_FP64, relax=None, rfac=None,
+                 kappa=0.0):
         super().__init__(ctx, nodal, mesh, nat.MODEL_ADVECTION, nTracers, dt, precision, u=u, v=v, relax=relax,
-                         rfac=rfac)
+                         rfac=rfac, kappa=kappa)
+        self.kappa = kappa
         self.u, self.v, self.relax, self.rfac = u, v, relax, rfac
 
     def WritePickup(self, iteration, directory="."):
