@@ -188,7 +188,8 @@ struct CGScalars {
 // One iteration is three launches, captured in a CUDA graph of several iterations:
 //   pcg_apply_fused : v_new = w + beta v_old (beta = num/den, v_new = w on the first iteration), z = L(v_new)
 //                     per element (before the direct-stiffness sum), partial sums of <v_new, z>;
-//   cg_dss_mask     : z = Mask(GlobalSum(z));
+//   cg_dss_mask     : z = Mask(GlobalSum(z)) (one thread per shared-node group; folding the group sums into the
+//                     update kernel, one node per thread, measured slower: dependent scattered loads);
 //   pcg_update_fused: a = num/<v,z>, u += a v, r -= a z, w = dinv r, partial sums of <r,w> and <r,r>, and the
 //                     end-of-iteration scalar update (den = num, num = <r,w>, ||r||, stop tests).
 // <v, Mask(GlobalSum(Lv))> equals the element-local sum of v(src[l]) * (Lv)_l because v is zero on Dirichlet
@@ -343,6 +344,194 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
   const R acc[1] = {pa};
   double tot[1];
   if (grid_sums_last<1, R>(acc, partial, ticket, tot) && threadIdx.x == 0) {
+    S->vz = tot[0];
+    S->alpha = S->num / tot[0];
+    S->alpha32 = (float)S->alpha;
+  }
+}
+
+// FP32 form of pcg_apply_fused, one thread per grid line: thread (e, t) of a block pass holds line t of element e
+// (the N1 nodes u(., t)) in registers and forms
+//   us(., t) = D u(., t)                       row pass, D read by warp-uniform (broadcast) float4 loads;
+//   up(c, .) = D u(c, .)                       column pass: the same thread as column c, u(c, .) read back from a
+//                                              per-line padded buffer (row stride N1 + 1: bank-conflict free for
+//                                              the row-major write and the column read);
+//   F1, F2 at its row nodes, (D^T F1)(., t) in registers, (D^T F2)(c, .) in the column pass, both summed into Lu.
+// Shared memory per node is a handful of accesses instead of reading the four contraction rows node by node; the
+// arithmetic is that of pcg_apply_fused in another summation order.
+template <int N1>
+constexpr int line_epb() {
+  return kRedThreads / N1;  // elements per block pass
+}
+
+template <int N1>
+__device__ __forceinline__ float row_dot(const float* __restrict__ drow, const float (&x)[N1]) {
+  // drow: N1 floats padded to a multiple of 4 (zeros), 16-byte aligned; x: registers
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < (N1 + 3) / 4; ++k) {
+    const float4 d = *reinterpret_cast<const float4*>(drow + 4 * k);
+    if (4 * k + 0 < N1) s = fmaf(d.x, x[4 * k + 0], s);
+    if (4 * k + 1 < N1) s = fmaf(d.y, x[4 * k + 1], s);
+    if (4 * k + 2 < N1) s = fmaf(d.z, x[4 * k + 2], s);
+    if (4 * k + 3 < N1) s = fmaf(d.w, x[4 * k + 3], s);
+  }
+  return s;
+}
+
+// a line of N1 consecutive values: float4 loads when a line is 16-byte aligned (N1 % 4 == 0: the element base is
+// a multiple of NN values), float2 for even N1, scalar otherwise
+template <int N1, typename T>
+__device__ __forceinline__ void load_line(const T* __restrict__ p, T (&x)[N1]) {
+  static_assert(sizeof(T) == 4, "32-bit values");
+  if constexpr (N1 % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < N1 / 4; ++k) {
+      const int4 v = *reinterpret_cast<const int4*>(p + 4 * k);
+      memcpy(&x[4 * k], &v, 16);
+    }
+  } else if constexpr (N1 % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N1 / 2; ++k) {
+      const int2 v = *reinterpret_cast<const int2*>(p + 2 * k);
+      memcpy(&x[2 * k], &v, 8);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N1; ++k) x[k] = p[k];
+  }
+}
+
+template <int N1>
+__device__ __forceinline__ void store_line(float* __restrict__ p, const float (&x)[N1]) {
+  if constexpr (N1 % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < N1 / 4; ++k)
+      *reinterpret_cast<float4*>(p + 4 * k) = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+  } else if constexpr (N1 % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N1 / 2; ++k) *reinterpret_cast<float2*>(p + 2 * k) = make_float2(x[2 * k], x[2 * k + 1]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < N1; ++k) p[k] = x[k];
+  }
+}
+
+template <int N1, int NF>
+__global__ void __launch_bounds__(kRedThreads) pcg_apply_fused_f32(const float* __restrict__ w,
+                                                                   const float* __restrict__ vold,
+                                                                   float* __restrict__ vnew, const int* __restrict__ src,
+                                                                   const float* __restrict__ fac, float* __restrict__ z,
+                                                                   int nEl, CGConst<N1, float> Cg, CGScalars* S,
+                                                                   double* __restrict__ partial,
+                                                                   unsigned int* __restrict__ ticket) {
+  if (S->done) return;
+  constexpr int NN = N1 * N1;
+  constexpr int EPL = line_epb<N1>();
+  constexpr int DS = 4 * ((N1 + 3) / 4);  // padded row of D
+  constexpr int LS = N1 + 1;              // padded line in the transpose buffers
+  __shared__ __align__(16) float Dr[N1][DS];  // Dr[i][m] = D(i, m)
+  __shared__ __align__(16) float Dc[N1][DS];  // Dc[i][m] = D(m, i)
+  __shared__ float X[EPL * N1 * LS];
+  __shared__ float Y[EPL * N1 * LS];
+  for (int t = threadIdx.x; t < N1 * DS; t += kRedThreads) {
+    const int r = t / DS, m = t - r * DS;
+    Dr[r][m] = m < N1 ? Cg.D[r + N1 * m] : 0.f;
+    Dc[r][m] = m < N1 ? Cg.D[m + N1 * r] : 0.f;
+  }
+  const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;  // element in the pass, line index
+  const bool first = S->iter == 0;
+  const float beta = first ? 0.f : S->beta32;
+  const int ngroups = (nEl + EPL - 1) / EPL;
+  const int line = le < EPL ? le * N1 + t : 0;  // this thread's line in the buffers (idle threads: unused)
+  float* Xl = X + (size_t)line * LS;
+  float* Yl = Y + (size_t)line * LS;
+  float pa = 0.f;
+  for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int e = g * EPL + le;
+    const bool active = le < EPL && e < nEl;
+    float u[N1], us[N1], up[N1];
+    const size_t l0 = (size_t)e * NN + (size_t)N1 * t;  // row t: nodes (i, t), i = 0..N1-1
+    if (active) {
+      int sl[N1];
+      float wl[N1], vl[N1], vn[N1];
+      load_line<N1>(src + l0, sl);
+      load_line<N1>(w + l0, wl);
+      if (first) {
+#pragma unroll
+        for (int i = 0; i < N1; ++i) vl[i] = 0.f;
+      } else {
+        load_line<N1>(vold + l0, vl);
+      }
+#pragma unroll
+      for (int i = 0; i < N1; ++i) {
+        vn[i] = first ? wl[i] : wl[i] + beta * vl[i];
+        u[i] = sl[i] == (int)(l0 + i) ? vn[i] : (first ? w[sl[i]] : w[sl[i]] + beta * vold[sl[i]]);
+      }
+      store_line<N1>(vnew + l0, vn);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) {
+        us[i] = row_dot<N1>(Dr[i], u);
+        Xl[i] = u[i];  // u(i, t)
+      }
+    }
+    __syncthreads();  // (first pass: D is in place as well)
+    if (active) {
+      // column pass: this thread is column c = t of element le: u(c, m) = line m, entry c
+      float uc[N1];
+#pragma unroll
+      for (int m = 0; m < N1; ++m) uc[m] = X[(size_t)(le * N1 + m) * LS + t];
+#pragma unroll
+      for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = row_dot<N1>(Dr[j], uc);  // up(c, j)
+    }
+    __syncthreads();
+    float a[N1];
+    if (active) {
+      const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
+      float F1[N1], G11[N1], G12[N1], G22[N1];
+      load_line<N1>(fe, G11);
+      load_line<N1>(fe + NN, G12);
+      load_line<N1>(fe + 2 * NN, G22);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) {
+        up[i] = Yl[i];
+        F1[i] = G11[i] * us[i] + G12[i] * up[i];
+        Xl[i] = G12[i] * us[i] + G22[i] * up[i];  // F2(i, t); X is free: the column pass has read u
+      }
+#pragma unroll
+      for (int i = 0; i < N1; ++i) a[i] = row_dot<N1>(Dc[i], F1);  // (D^T F1)(i, t)
+    }
+    __syncthreads();
+    if (active) {
+      float fc[N1];
+#pragma unroll
+      for (int m = 0; m < N1; ++m) fc[m] = X[(size_t)(le * N1 + m) * LS + t];  // F2(c, m)
+#pragma unroll
+      for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = row_dot<N1>(Dc[j], fc);  // (D^T F2)(c, j)
+    }
+    __syncthreads();
+    if (active) {
+      const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
+      float Mv[N1], Lu[N1];
+      load_line<N1>(fe + 3 * NN, Mv);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) Lu[i] = -(a[i] + Yl[i]) - Mv[i] * u[i];
+      if (NF == 6) {
+        float B1[N1], B2[N1];
+        load_line<N1>(fe + 4 * NN, B1);
+        load_line<N1>(fe + 5 * NN, B2);
+#pragma unroll
+        for (int i = 0; i < N1; ++i) Lu[i] -= B1[i] * us[i] + B2[i] * up[i];
+      }
+      store_line<N1>(z + l0, Lu);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) pa += u[i] * Lu[i];
+    }
+    __syncthreads();  // the next pass reuses X and Y
+  }
+  const float acc[1] = {pa};
+  double tot[1];
+  if (grid_sums_last<1, float>(acc, partial, ticket, tot) && threadIdx.x == 0) {
     S->vz = tot[0];
     S->alpha = S->num / tot[0];
     S->alpha32 = (float)S->alpha;
@@ -664,15 +853,24 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
   int& nb = resident[sizeof(R) == 4][N1][NF == 6];
   if (nb == 0) {
     int q = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused<N1, R, NF>, kRedThreads, 0) != cudaSuccess)
-      q = 4;
+    cudaError_t ce;
+    if constexpr (sizeof(R) == 4)
+      ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused_f32<N1, NF>, kRedThreads, 0);
+    else
+      ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused<N1, R, NF>, kRedThreads, 0);
+    if (ce != cudaSuccess) q = 4;
     nb = std::max(1, q);
   }
-  constexpr int P = sizeof(R) == 4 ? 2 : 1;
-  const int groups = (h->nEl + cg_epb<N1>() - 1) / cg_epb<N1>();
+  constexpr int P = 1;
+  constexpr int epb = sizeof(R) == 4 ? line_epb<N1>() : cg_epb<N1>();
+  const int groups = (h->nEl + epb - 1) / epb;
   const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), (groups + P - 1) / P}));
-  pcg_apply_fused<N1, R, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
-      w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
+  if constexpr (sizeof(R) == 4)
+    pcg_apply_fused_f32<N1, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+        w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
+  else
+    pcg_apply_fused<N1, R, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+        w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
 }
 
 template <typename R>
