@@ -605,6 +605,78 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ 
   }
 }
 
+// FP32 pcg_update_fused over float4 groups of 4 consecutive nodes (the L-vector length is a multiple of 4 when
+// (N+1)^2 nEl is; otherwise the scalar kernel runs): every thread keeps 2 groups = 8 nodes of 5 streams in flight.
+__global__ void __launch_bounds__(kRedThreads) pcg_update_fused_f4(float4* __restrict__ u, float4* __restrict__ r,
+                                                                   float4* __restrict__ w, const float4* __restrict__ v,
+                                                                   const float4* __restrict__ z,
+                                                                   const float4* __restrict__ dinv, size_t n4,
+                                                                   CGScalars* S, double* __restrict__ partial,
+                                                                   unsigned int* __restrict__ ticket) {
+  if (S->done) return;
+  const float a = S->alpha32;
+  float prw = 0.f, prr = 0.f;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int U = 2;
+  auto step = [&](float uu, float vv, float rr, float zz, float dd, float& uo, float& ro, float& wo) {
+    uo = uu + a * vv;
+    ro = rr - a * zz;
+    wo = dinv ? ro * dd : ro;
+    prw += ro * wo;
+    prr += ro * ro;
+  };
+  for (; k < n4; k += U * stride) {
+    float4 uu[U], vv[U], rr[U], zz[U], dd[U];
+    bool ok[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const size_t x = k + q * stride;
+      ok[q] = x < n4;
+      if (!ok[q]) continue;
+      uu[q] = u[x];
+      vv[q] = v[x];
+      rr[q] = r[x];
+      zz[q] = z[x];
+      dd[q] = dinv ? dinv[x] : make_float4(1.f, 1.f, 1.f, 1.f);
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      if (!ok[q]) continue;
+      const size_t x = k + q * stride;
+      float4 uo, ro, wo;
+      step(uu[q].x, vv[q].x, rr[q].x, zz[q].x, dd[q].x, uo.x, ro.x, wo.x);
+      step(uu[q].y, vv[q].y, rr[q].y, zz[q].y, dd[q].y, uo.y, ro.y, wo.y);
+      step(uu[q].z, vv[q].z, rr[q].z, zz[q].z, dd[q].z, uo.z, ro.z, wo.z);
+      step(uu[q].w, vv[q].w, rr[q].w, zz[q].w, dd[q].w, uo.w, ro.w, wo.w);
+      u[x] = uo;
+      r[x] = ro;
+      if (w) w[x] = wo;
+    }
+  }
+  const float acc[2] = {prw, prr};
+  double tot[2];
+  if (!grid_sums_last<2, float>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
+  const double rn = sqrt(tot[1]);
+  S->den = S->num;
+  S->num = tot[0];
+  S->beta = S->num / S->den;
+  S->beta32 = (float)S->beta;
+  S->iter += 1;
+  if (S->resi) S->resi[S->iter] = rn;
+  S->rr = rn;
+  if (!(rn == rn) || isinf(rn)) {  // non-finite residual
+    S->done = 1;
+    S->ioerr = -7;
+  } else if (rn / S->r0 < S->tol) {
+    S->done = 1;
+    S->ioerr = 0;
+  } else if (S->iter >= S->maxIters) {
+    S->done = 1;
+    S->ioerr = -1;
+  }
+}
+
 // w = dinv r and num = <r, w> before the first iteration
 template <typename R>
 __global__ void __launch_bounds__(kRedThreads) pcg_start_fused(const R* __restrict__ r, const R* __restrict__ dinv,
@@ -1016,6 +1088,8 @@ namespace cg {
 // buffers alternating); the host reads the scalar block after each graph launch.
 constexpr int kGraphIters = 16;  // even: the current direction is back in `v` after every graph launch
 
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 // With pc (linear-FEM preconditioner) every outer iteration starts with the inner solve u_l = M^-1 r and
 // w, num = <r, w> (pc_num); the graph then holds kGraphItersPC outer iterations of 3 * pc->iters + 5 launches.
 constexpr int kGraphItersPC = 2;
@@ -1072,8 +1146,18 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
         if (!rc) rc = launch_apply_fused<R>(h, w, vold, vnew, z, od);
         if (!rc) rc = launch_dss<R>(h, z);
         if (!rc) {
-          pcg_update_fused<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, pc ? nullptr : w, vnew, z, pc ? nullptr : dinv,
-                                                              h->nl, h->S.p, h->partial.p, h->ticket.p);
+          R* wo = pc ? nullptr : w;
+          const R* di = pc ? nullptr : dinv;
+          if (sizeof(R) == 4 && h->nl % 4 == 0 && aligned16(u) && aligned16(r) && aligned16(w) && aligned16(vnew) &&
+              aligned16(z) && aligned16(dinv)) {
+            pcg_update_fused_f4<<<h->nblk, kRedThreads, 0, st>>>(
+                reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(r), reinterpret_cast<float4*>(wo),
+                reinterpret_cast<const float4*>(vnew), reinterpret_cast<const float4*>(z),
+                reinterpret_cast<const float4*>(di), h->nl / 4, h->S.p, h->partial.p, h->ticket.p);
+          } else {
+            pcg_update_fused<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, wo, vnew, z, di, h->nl, h->S.p, h->partial.p,
+                                                                h->ticket.p);
+          }
           SELF_LAUNCHED(ctx);
         }
       }
