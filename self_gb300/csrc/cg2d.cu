@@ -120,6 +120,36 @@ __global__ void cg_dss_mask(R* __restrict__ v, const int* __restrict__ gptr, con
   for (int k = a + 1; k < b; ++k) v[gidx[k]] = 0;
 }
 
+// The same GlobalSum + Mask with the two-copy groups (shared edge nodes, the large majority) as a flat pair list
+// -- one thread per pair, no group-pointer indirection -- and the remaining groups (corner nodes, Dirichlet
+// nodes) in CSR form, one thread per group; sums in the same order, so the result equals cg_dss_mask's.
+template <typename R>
+__global__ void cg_dss_mask_pairs(R* __restrict__ v, const int2* __restrict__ pairs, int npairs,
+                                  const int* __restrict__ gptr, const int* __restrict__ gidx,
+                                  const unsigned char* __restrict__ gdir, int ngroups) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < npairs) {
+    const int2 p = pairs[t];
+    R s = 0;
+    s += v[p.x];
+    s += v[p.y];
+    v[p.x] = s;
+    v[p.y] = 0;
+    return;
+  }
+  const int g = t - npairs;
+  if (g >= ngroups) return;
+  const int a = gptr[g], b = gptr[g + 1];
+  if (gdir[g]) {
+    for (int k = a; k < b; ++k) v[gidx[k]] = 0;
+    return;
+  }
+  R s = 0;
+  for (int k = a; k < b; ++k) s += v[gidx[k]];
+  v[gidx[a]] = s;
+  for (int k = a + 1; k < b; ++k) v[gidx[k]] = 0;
+}
+
 // ---------------------------------------------------------------------------------- reductions
 constexpr int kRedThreads = 256;
 
@@ -812,6 +842,10 @@ struct self_cg2d {
   DevBuf<int> src, gptr, gidx;
   DevBuf<unsigned char> gdir;
   int ngroups = 0;
+  DevBuf<int2> dss_pairs;                  // two-copy groups (primary, secondary)
+  DevBuf<int> dss_gptr, dss_gidx;          // the other groups
+  DevBuf<unsigned char> dss_gdir;
+  int dss_npairs = 0, dss_nrest = 0;
   std::vector<int> h_src, h_gptr, h_gidx;
   std::vector<unsigned char> h_gdir;
   selfgpu::cg::OpData<double> op64;
@@ -909,8 +943,10 @@ int launch_apply(self_cg2d* h, const R* x, const R* rhs, R* out, const selfgpu::
 template <typename R>
 int launch_dss(self_cg2d* h, R* v) {
   if (h->ngroups == 0) return SELF_OK;
-  cg_dss_mask<R><<<(h->ngroups + 255) / 256, 256, 0, h->ctx->stream>>>(v, h->gptr.p, h->gidx.p, h->gdir.p,
-                                                                       h->ngroups);
+  const int nt = h->dss_npairs + h->dss_nrest;
+  cg_dss_mask_pairs<R><<<(nt + 255) / 256, 256, 0, h->ctx->stream>>>(v, h->dss_pairs.p, h->dss_npairs,
+                                                                     h->dss_gptr.p, h->dss_gidx.p, h->dss_gdir.p,
+                                                                     h->dss_nrest);
   SELF_LAUNCHED(h->ctx);
   return SELF_OK;
 }
@@ -1329,6 +1365,25 @@ int compile_topology(self_cg2d* h, const self_cg2d_desc* d) {
   if ((rc = upload(h->ctx, h->gptr, h->h_gptr))) return rc;
   if ((rc = upload(h->ctx, h->gidx, h->h_gidx))) return rc;
   if ((rc = upload(h->ctx, h->gdir, h->h_gdir))) return rc;
+  std::vector<int2> pairs;
+  std::vector<int> rptr(1, 0), ridx;
+  std::vector<unsigned char> rdir;
+  for (int g = 0; g < h->ngroups; ++g) {
+    const int a = h->h_gptr[g], b = h->h_gptr[g + 1];
+    if (b - a == 2 && !h->h_gdir[g]) {
+      pairs.push_back(make_int2(h->h_gidx[a], h->h_gidx[a + 1]));
+    } else {
+      for (int k = a; k < b; ++k) ridx.push_back(h->h_gidx[k]);
+      rptr.push_back((int)ridx.size());
+      rdir.push_back(h->h_gdir[g]);
+    }
+  }
+  h->dss_npairs = (int)pairs.size();
+  h->dss_nrest = (int)rdir.size();
+  if (!pairs.empty() && (rc = upload(h->ctx, h->dss_pairs, pairs))) return rc;
+  if ((rc = upload(h->ctx, h->dss_gptr, rptr))) return rc;
+  if (!ridx.empty() && (rc = upload(h->ctx, h->dss_gidx, ridx))) return rc;
+  if (!rdir.empty() && (rc = upload(h->ctx, h->dss_gdir, rdir))) return rc;
   return SELF_OK;
 }
 
