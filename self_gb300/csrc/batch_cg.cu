@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(kThreads) bk_dss(TileView V, const Prob* __res
       const int a = p.gptr[g], b = p.gptr[g + 1];
       if (p.gdir[g]) {
         for (int k = a; k < b; ++k) v[p.gidx[k]] = 0;
-        return;
+        continue;
       }
       R sum = 0;
       for (int k = a; k < b; ++k) sum += v[p.gidx[k]];

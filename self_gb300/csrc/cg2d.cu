@@ -27,6 +27,7 @@
 #include <memory>
 #include <limits>
 #include <unordered_map>
+#include <type_traits>
 #include <vector>
 
 #include "cg2d_api.hpp"
@@ -409,22 +410,24 @@ __device__ __forceinline__ float row_dot(const float* __restrict__ drow, const f
   return s;
 }
 
-// a line of N1 consecutive values: float4 loads when a line is 16-byte aligned (N1 % 4 == 0: the element base is
-// a multiple of NN values), float2 for even N1, scalar otherwise
+// a line of N1 consecutive 4- or 8-byte values: 16-byte loads when a line is a whole number of 16-byte chunks (the
+// line then starts on a 16-byte boundary: the element base is a multiple of NN values and every vector's length a
+// multiple of a line), 8-byte loads for a whole number of 8-byte chunks, single values otherwise
 template <int N1, typename T>
 __device__ __forceinline__ void load_line(const T* __restrict__ p, T (&x)[N1]) {
-  static_assert(sizeof(T) == 4, "32-bit values");
-  if constexpr (N1 % 4 == 0) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "32- or 64-bit values");
+  constexpr int B = N1 * (int)sizeof(T);
+  if constexpr (B % 16 == 0) {
 #pragma unroll
-    for (int k = 0; k < N1 / 4; ++k) {
-      const int4 v = *reinterpret_cast<const int4*>(p + 4 * k);
-      memcpy(&x[4 * k], &v, 16);
+    for (int k = 0; k < B / 16; ++k) {
+      const int4 v = reinterpret_cast<const int4*>(p)[k];
+      memcpy(reinterpret_cast<char*>(x) + 16 * k, &v, 16);
     }
-  } else if constexpr (N1 % 2 == 0) {
+  } else if constexpr (B % 8 == 0) {
 #pragma unroll
-    for (int k = 0; k < N1 / 2; ++k) {
-      const int2 v = *reinterpret_cast<const int2*>(p + 2 * k);
-      memcpy(&x[2 * k], &v, 8);
+    for (int k = 0; k < B / 8; ++k) {
+      const int2 v = reinterpret_cast<const int2*>(p)[k];
+      memcpy(reinterpret_cast<char*>(x) + 8 * k, &v, 8);
     }
   } else {
 #pragma unroll
@@ -432,15 +435,24 @@ __device__ __forceinline__ void load_line(const T* __restrict__ p, T (&x)[N1]) {
   }
 }
 
-template <int N1>
-__device__ __forceinline__ void store_line(float* __restrict__ p, const float (&x)[N1]) {
-  if constexpr (N1 % 4 == 0) {
+template <int N1, typename T>
+__device__ __forceinline__ void store_line(T* __restrict__ p, const T (&x)[N1]) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "32- or 64-bit values");
+  constexpr int B = N1 * (int)sizeof(T);
+  if constexpr (B % 16 == 0) {
 #pragma unroll
-    for (int k = 0; k < N1 / 4; ++k)
-      *reinterpret_cast<float4*>(p + 4 * k) = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
-  } else if constexpr (N1 % 2 == 0) {
+    for (int k = 0; k < B / 16; ++k) {
+      int4 v;
+      memcpy(&v, reinterpret_cast<const char*>(x) + 16 * k, 16);
+      reinterpret_cast<int4*>(p)[k] = v;
+    }
+  } else if constexpr (B % 8 == 0) {
 #pragma unroll
-    for (int k = 0; k < N1 / 2; ++k) *reinterpret_cast<float2*>(p + 2 * k) = make_float2(x[2 * k], x[2 * k + 1]);
+    for (int k = 0; k < B / 8; ++k) {
+      int2 v;
+      memcpy(&v, reinterpret_cast<const char*>(x) + 8 * k, 8);
+      reinterpret_cast<int2*>(p)[k] = v;
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < N1; ++k) p[k] = x[k];
@@ -568,6 +580,254 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused_f32(const float* 
   }
 }
 
+// ---------------------------------------------------------------------------------- FP64 even-odd operator
+// The GLL collocation derivative matrix is centro-antisymmetric, D(N-i, N-m) = -D(i, m) (nodes symmetric about 0),
+// and so is its transpose.  For such a matrix A, with H = N1/2, xe(m) = x(m) + x(N-m) and xo(m) = x(m) - x(N-m)
+// (m < H),
+//   y(i) = ye(i) + yo(i),  y(N-i) = yo(i) - ye(i),  ye(i) = sum_m E(i,m) xe(m) [+ A(i,H) x(H)],  yo(i) = sum_m O(i,m) xo(m),
+// E(i,m) = (A(i,m) + A(i,N-m))/2, O(i,m) = (A(i,m) - A(i,N-m))/2, and for odd N1 the middle row y(H) = sum_m O(H,m) xo(m)
+// (the even-odd decomposition of Solomonoff, 1992).  At N1 = 8 a line costs 48 FP64 operations instead of 64.  The
+// FP64 operator is bound by the FP64 pipe on this part (a few FP64 operations per byte), so the count is the time.
+template <int N1>
+struct EOTable {
+  static constexpr int H = N1 / 2, ODD = N1 & 1;
+  double E[H][H + ODD];  // E(i, m), then A(i, H) for odd N1
+  double O[H + ODD][H];  // O(i, m); for odd N1 row H is the middle row
+};
+
+template <int N1>
+struct EOPair {
+  EOTable<N1> D, Dt;  // D and its transpose
+};
+
+// host: the tables of the column-major N1 x N1 matrix A (A(i, m) = a[i + N1 m]); false when A is not
+// centro-antisymmetric to 1e-13 of its largest entry (a derivative matrix of non-symmetric nodes)
+template <int N1>
+bool eo_table(const double* a, bool transpose, EOTable<N1>& T) {
+  constexpr int N = N1 - 1, H = N1 / 2;
+  auto A = [&](int i, int m) { return transpose ? a[m + N1 * i] : a[i + N1 * m]; };
+  double amax = 0, dev = 0;
+  for (int i = 0; i < N1; ++i)
+    for (int m = 0; m < N1; ++m) {
+      amax = std::max(amax, std::fabs(A(i, m)));
+      dev = std::max(dev, std::fabs(A(N - i, N - m) + A(i, m)));
+    }
+  if (!(dev <= 1e-13 * amax)) return false;
+  for (int i = 0; i < H + (N1 & 1); ++i)
+    for (int m = 0; m < H; ++m) {
+      if (i < H) T.E[i][m] = 0.5 * (A(i, m) + A(i, N - m));
+      T.O[i][m] = 0.5 * (A(i, m) - A(i, N - m));
+    }
+  if (N1 & 1)
+    for (int i = 0; i < H; ++i) T.E[i][H] = A(i, H);
+  return true;
+}
+
+template <int N1>
+__device__ __forceinline__ void eo_matvec(const EOTable<N1>& T, const double (&x)[N1], double (&y)[N1]) {
+  constexpr int N = N1 - 1, H = N1 / 2;
+  double xe[H], xo[H];
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    xe[m] = x[m] + x[N - m];
+    xo[m] = x[m] - x[N - m];
+  }
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    double ye = T.E[i][0] * xe[0], yo = T.O[i][0] * xo[0];
+#pragma unroll
+    for (int m = 1; m < H; ++m) {
+      ye = fma(T.E[i][m], xe[m], ye);
+      yo = fma(T.O[i][m], xo[m], yo);
+    }
+    if constexpr (N1 & 1) ye = fma(T.E[i][H + (N1 & 1) - 1], x[H], ye);
+    y[i] = ye + yo;
+    y[N - i] = yo - ye;
+  }
+  if constexpr (N1 & 1) {
+    double ym = T.O[H + (N1 & 1) - 1][0] * xo[0];
+#pragma unroll
+    for (int m = 1; m < H; ++m) ym = fma(T.O[H + (N1 & 1) - 1][m], xo[m], ym);
+    y[H] = ym;
+  }
+}
+
+// Lu on line t (nodes (i, t), i = 0..N1-1) of element le of a block pass, from u(., t) in registers: the line-
+// oriented operator of pcg_apply_fused_f32 in FP64 with even-odd contractions.  Every thread of the block calls it
+// (threads without a line pass active = false and only join the barriers); fe = the element's factors + N1 t;
+// X, Y = the block's padded transpose buffers (row stride N1 + 1: 64-bit accesses of a half warp fall in distinct
+// bank pairs for the row-major writes and the column reads).  On return X and Y are free.
+template <int N1, int NF>
+__device__ __forceinline__ void line_op_f64(const EOPair<N1>& T, const double* __restrict__ fe, bool active, int le,
+                                            int t, double* X, double* Y, const double (&u)[N1], double (&Lu)[N1]) {
+  constexpr int NN = N1 * N1, LS = N1 + 1;
+  double* Xl = X + (size_t)(le * N1 + t) * LS;
+  double* Yl = Y + (size_t)(le * N1 + t) * LS;
+  double us[N1], up[N1], a[N1];
+  if (active) {
+    eo_matvec<N1>(T.D, u, us);  // (D u)(., t)
+#pragma unroll
+    for (int i = 0; i < N1; ++i) Xl[i] = u[i];
+  }
+  __syncthreads();
+  if (active) {  // column pass: column c = t, up(c, .) = D u(c, .)
+    double uc[N1], yc[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) uc[m] = X[(size_t)(le * N1 + m) * LS + t];
+    eo_matvec<N1>(T.D, uc, yc);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = yc[j];
+  }
+  __syncthreads();
+  if (active) {
+    double G11[N1], G12[N1], G22[N1], F1[N1];
+    load_line<N1>(fe, G11);
+    load_line<N1>(fe + NN, G12);
+    load_line<N1>(fe + 2 * NN, G22);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      up[i] = Yl[i];
+      F1[i] = G11[i] * us[i] + G12[i] * up[i];
+      Xl[i] = G12[i] * us[i] + G22[i] * up[i];  // F2(i, t)
+    }
+    eo_matvec<N1>(T.Dt, F1, a);  // (D^T F1)(., t)
+  }
+  __syncthreads();
+  if (active) {  // column pass: (D^T F2)(c, .)
+    double fc[N1], yc[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) fc[m] = X[(size_t)(le * N1 + m) * LS + t];
+    eo_matvec<N1>(T.Dt, fc, yc);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = yc[j];
+  }
+  __syncthreads();
+  if (active) {
+    double M[N1];
+    load_line<N1>(fe + 3 * NN, M);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) Lu[i] = -(a[i] + Yl[i]) - M[i] * u[i];
+    if constexpr (NF == 6) {
+      double B1[N1], B2[N1];
+      load_line<N1>(fe + 4 * NN, B1);
+      load_line<N1>(fe + 5 * NN, B2);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) Lu[i] -= B1[i] * us[i] + B2[i] * up[i];
+    }
+  }
+}
+
+template <int N1>
+__device__ __forceinline__ void eo_copy_tables(const EOPair<N1>& src, EOPair<N1>& dst) {
+  constexpr int NC = sizeof(EOPair<N1>) / sizeof(double);
+  const double* s = reinterpret_cast<const double*>(&src);
+  double* d = reinterpret_cast<double*>(&dst);
+  for (int k = threadIdx.x; k < NC; k += blockDim.x) d[k] = s[k];
+}
+
+// FP64 fused PCG apply (pcg_apply_fused's work and outputs) with the even-odd line operator.
+template <int N1, int NF>
+__global__ void __launch_bounds__(kRedThreads, 2) pcg_apply_fused_eo(const double* __restrict__ w,
+                                                                     const double* __restrict__ vold,
+                                                                     double* __restrict__ vnew,
+                                                                     const int* __restrict__ src,
+                                                                     const double* __restrict__ fac,
+                                                                     double* __restrict__ z, int nEl, EOPair<N1> Tg,
+                                                                     CGScalars* S, double* __restrict__ partial,
+                                                                     unsigned int* __restrict__ ticket) {
+  if (S->done) return;
+  constexpr int NN = N1 * N1;
+  constexpr int EPL = line_epb<N1>();
+  constexpr int LS = N1 + 1;
+  __shared__ EOPair<N1> T;
+  __shared__ double X[EPL * N1 * LS];
+  __shared__ double Y[EPL * N1 * LS];
+  eo_copy_tables<N1>(Tg, T);
+  __syncthreads();
+  const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;
+  const bool first = S->iter == 0;
+  const double beta = first ? 0.0 : S->beta;
+  const int ngroups = (nEl + EPL - 1) / EPL;
+  double pa = 0.0;
+  for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int e = g * EPL + le;
+    const bool active = le < EPL && e < nEl;
+    const size_t l0 = (size_t)e * NN + (size_t)N1 * t;
+    double u[N1], Lu[N1];
+    if (active) {
+      int sl[N1];
+      double wl[N1], vn[N1];
+      load_line<N1>(src + l0, sl);
+      load_line<N1>(w + l0, wl);
+      if (first) {
+#pragma unroll
+        for (int i = 0; i < N1; ++i) vn[i] = wl[i];
+      } else {
+        double vl[N1];
+        load_line<N1>(vold + l0, vl);
+#pragma unroll
+        for (int i = 0; i < N1; ++i) vn[i] = wl[i] + beta * vl[i];
+      }
+#pragma unroll
+      for (int i = 0; i < N1; ++i)
+        u[i] = sl[i] == (int)(l0 + i) ? vn[i] : (first ? w[sl[i]] : w[sl[i]] + beta * vold[sl[i]]);
+      store_line<N1>(vnew + l0, vn);
+    }
+    line_op_f64<N1, NF>(T, fac + (size_t)(active ? e : 0) * NF * NN + (size_t)N1 * t, active, le, t, X, Y, u, Lu);
+    if (active) {
+      store_line<N1>(z + l0, Lu);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) pa += u[i] * Lu[i];
+    }
+  }
+  const double acc[1] = {pa};
+  double tot[1];
+  if (grid_sums_last<1, double>(acc, partial, ticket, tot) && threadIdx.x == 0) {
+    S->vz = tot[0];
+    S->alpha = S->num / tot[0];
+    S->alpha32 = (float)S->alpha;
+  }
+}
+
+// FP64 local apply (cg_apply_local's work: out = [rhs] - L(x gathered through src)) with the even-odd line operator.
+template <int N1, int NF>
+__global__ void __launch_bounds__(kRedThreads, 2) cg_apply_local_eo(const double* __restrict__ x,
+                                                                    const int* __restrict__ src,
+                                                                    const double* __restrict__ fac,
+                                                                    const double* __restrict__ rhs,
+                                                                    double* __restrict__ out, int nEl,
+                                                                    EOPair<N1> Tg) {
+  constexpr int NN = N1 * N1;
+  constexpr int EPL = line_epb<N1>();
+  constexpr int LS = N1 + 1;
+  __shared__ EOPair<N1> T;
+  __shared__ double X[EPL * N1 * LS];
+  __shared__ double Y[EPL * N1 * LS];
+  eo_copy_tables<N1>(Tg, T);
+  __syncthreads();
+  const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;
+  const int e = blockIdx.x * EPL + le;
+  const bool active = le < EPL && e < nEl;
+  const size_t l0 = (size_t)e * NN + (size_t)N1 * t;
+  double u[N1], Lu[N1];
+  if (active) {
+    int sl[N1];
+    load_line<N1>(src + l0, sl);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) u[i] = x[sl[i]];
+  }
+  line_op_f64<N1, NF>(T, fac + (size_t)(active ? e : 0) * NF * NN + (size_t)N1 * t, active, le, t, X, Y, u, Lu);
+  if (active) {
+    if (rhs) {
+      double rl[N1];
+      load_line<N1>(rhs + l0, rl);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) Lu[i] = rl[i] - Lu[i];
+    }
+    store_line<N1>(out + l0, Lu);
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ u, R* __restrict__ r,
                                                                 R* __restrict__ w, const R* __restrict__ v,
@@ -635,58 +895,70 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ 
   }
 }
 
-// FP32 pcg_update_fused over float4 groups of 4 consecutive nodes (the L-vector length is a multiple of 4 when
-// (N+1)^2 nEl is; otherwise the scalar kernel runs): every thread keeps 2 groups = 8 nodes of 5 streams in flight.
-__global__ void __launch_bounds__(kRedThreads) pcg_update_fused_f4(float4* __restrict__ u, float4* __restrict__ r,
-                                                                   float4* __restrict__ w, const float4* __restrict__ v,
-                                                                   const float4* __restrict__ z,
-                                                                   const float4* __restrict__ dinv, size_t n4,
-                                                                   CGScalars* S, double* __restrict__ partial,
-                                                                   unsigned int* __restrict__ ticket) {
+// pcg_update_fused over 16-byte groups of consecutive nodes (float4: 4 FP32 nodes, double2: 2 FP64 nodes; the
+// L-vector length is a multiple of the group when (N+1)^2 nEl is, otherwise the scalar kernel runs): every thread
+// keeps two groups of 5 streams in flight.
+template <typename R, typename V>
+__global__ void __launch_bounds__(kRedThreads) pcg_update_fused_vec(V* __restrict__ u, V* __restrict__ r,
+                                                                    V* __restrict__ w, const V* __restrict__ v,
+                                                                    const V* __restrict__ z,
+                                                                    const V* __restrict__ dinv, size_t nv,
+                                                                    CGScalars* S, double* __restrict__ partial,
+                                                                    unsigned int* __restrict__ ticket) {
+  static_assert(sizeof(V) == 16 && sizeof(V) % sizeof(R) == 0, "16-byte groups");
+  constexpr int L = sizeof(V) / sizeof(R);
   if (S->done) return;
-  const float a = S->alpha32;
-  float prw = 0.f, prr = 0.f;
+  const R a = sizeof(R) == 4 ? (R)S->alpha32 : (R)S->alpha;
+  R prw = 0, prr = 0;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int U = 2;
-  auto step = [&](float uu, float vv, float rr, float zz, float dd, float& uo, float& ro, float& wo) {
-    uo = uu + a * vv;
-    ro = rr - a * zz;
-    wo = dinv ? ro * dd : ro;
-    prw += ro * wo;
-    prr += ro * ro;
-  };
-  for (; k < n4; k += U * stride) {
-    float4 uu[U], vv[U], rr[U], zz[U], dd[U];
+  for (; k < nv; k += U * stride) {
+    V uu[U], vv[U], rr[U], zz[U], dd[U];
     bool ok[U];
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       const size_t x = k + q * stride;
-      ok[q] = x < n4;
+      ok[q] = x < nv;
       if (!ok[q]) continue;
       uu[q] = u[x];
       vv[q] = v[x];
       rr[q] = r[x];
       zz[q] = z[x];
-      dd[q] = dinv ? dinv[x] : make_float4(1.f, 1.f, 1.f, 1.f);
+      if (dinv) dd[q] = dinv[x];
     }
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       if (!ok[q]) continue;
       const size_t x = k + q * stride;
-      float4 uo, ro, wo;
-      step(uu[q].x, vv[q].x, rr[q].x, zz[q].x, dd[q].x, uo.x, ro.x, wo.x);
-      step(uu[q].y, vv[q].y, rr[q].y, zz[q].y, dd[q].y, uo.y, ro.y, wo.y);
-      step(uu[q].z, vv[q].z, rr[q].z, zz[q].z, dd[q].z, uo.z, ro.z, wo.z);
-      step(uu[q].w, vv[q].w, rr[q].w, zz[q].w, dd[q].w, uo.w, ro.w, wo.w);
-      u[x] = uo;
-      r[x] = ro;
-      if (w) w[x] = wo;
+      R us[L], vs[L], rs[L], zs[L], ds[L], uo[L], ro[L], wo[L];
+      memcpy(us, &uu[q], 16);
+      memcpy(vs, &vv[q], 16);
+      memcpy(rs, &rr[q], 16);
+      memcpy(zs, &zz[q], 16);
+      if (dinv) memcpy(ds, &dd[q], 16);
+#pragma unroll
+      for (int c = 0; c < L; ++c) {
+        uo[c] = us[c] + a * vs[c];
+        ro[c] = rs[c] - a * zs[c];
+        wo[c] = dinv ? ro[c] * ds[c] : ro[c];
+        prw += ro[c] * wo[c];
+        prr += ro[c] * ro[c];
+      }
+      V t;
+      memcpy(&t, uo, 16);
+      u[x] = t;
+      memcpy(&t, ro, 16);
+      r[x] = t;
+      if (w) {
+        memcpy(&t, wo, 16);
+        w[x] = t;
+      }
     }
   }
-  const float acc[2] = {prw, prr};
+  const R acc[2] = {prw, prr};
   double tot[2];
-  if (!grid_sums_last<2, float>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
+  if (!grid_sums_last<2, R>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
   const double rn = sqrt(tot[1]);
   S->den = S->num;
   S->num = tot[0];
@@ -902,8 +1174,29 @@ struct self_cg2d {
 
 namespace {
 
+// the even-odd tables of D and D^T (FP64), or false when D is not centro-antisymmetric or N1 < 6 (where the
+// even-odd form saves no FP64 operation: 16 of 16 per line at N1 = 4, 20 of 25 at N1 = 5, and the node-per-thread
+// kernel keeps more warps resident)
+template <int N1, typename R>
+bool eo_pair(const std::vector<R>& D, EOPair<N1>& T) {
+  if constexpr (sizeof(R) != 8 || N1 < 6) {
+    return false;
+  } else {
+    return eo_table<N1>(D.data(), false, T.D) && eo_table<N1>(D.data(), true, T.Dt);
+  }
+}
+
 template <int N1, typename R, int NF>
 void launch_apply_t(self_cg2d* h, const R* x, const R* fac, const R* rhs, R* out, const std::vector<R>& D) {
+  if constexpr (sizeof(R) == 8 && N1 >= 6) {
+    EOPair<N1> T;
+    if (eo_pair<N1>(D, T)) {
+      constexpr int EPL = line_epb<N1>();
+      cg_apply_local_eo<N1, NF><<<(h->nEl + EPL - 1) / EPL, kRedThreads, 0, h->ctx->stream>>>(x, h->src.p, fac, rhs,
+                                                                                             out, h->nEl, T);
+      return;
+    }
+  }
   CGConst<N1, R> C;
   for (int k = 0; k < N1 * N1; ++k) C.D[k] = D[k];
   constexpr int EPB = cg_epb<N1>();
@@ -956,29 +1249,39 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
                           const std::vector<R>& D) {
   CGConst<N1, R> C;
   for (int k = 0; k < N1 * N1; ++k) C.D[k] = D[k];
+  EOPair<N1> T;
+  const bool eo = eo_pair<N1>(D, T);  // FP64 with a centro-antisymmetric D: the even-odd line kernel
   // one wave of resident blocks (at most apply_grid, for which the partial sums are sized)
-  static int resident[2][11][2] = {};  // per precision, degree and operator: blocks per SM (0 = not queried)
-  int& nb = resident[sizeof(R) == 4][N1][NF == 6];
+  static int resident[3][11][2] = {};  // per kernel, degree and operator: blocks per SM (0 = not queried)
+  const int kind = sizeof(R) == 4 ? 0 : (eo ? 2 : 1);
+  int& nb = resident[kind][N1][NF == 6];
   if (nb == 0) {
     int q = 0;
     cudaError_t ce;
     if constexpr (sizeof(R) == 4)
       ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused_f32<N1, NF>, kRedThreads, 0);
+    else if constexpr (N1 >= 6)
+      ce = eo ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused_eo<N1, NF>, kRedThreads, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused<N1, R, NF>, kRedThreads, 0);
     else
       ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_fused<N1, R, NF>, kRedThreads, 0);
     if (ce != cudaSuccess) q = 4;
     nb = std::max(1, q);
   }
-  constexpr int P = 1;
-  constexpr int epb = sizeof(R) == 4 ? line_epb<N1>() : cg_epb<N1>();
+  const int epb = (sizeof(R) == 4 || eo) ? line_epb<N1>() : cg_epb<N1>();
   const int groups = (h->nEl + epb - 1) / epb;
-  const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), (groups + P - 1) / P}));
-  if constexpr (sizeof(R) == 4)
+  const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
+  if constexpr (sizeof(R) == 4) {
     pcg_apply_fused_f32<N1, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
         w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
-  else
+  } else if (eo) {
+    if constexpr (N1 >= 6)
+      pcg_apply_fused_eo<N1, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+          w, vold, vnew, h->src.p, fac, z, h->nEl, T, h->S.p, h->partial.p, h->ticket.p);
+  } else {
     pcg_apply_fused<N1, R, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
         w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
+  }
 }
 
 template <typename R>
@@ -1184,12 +1487,14 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
         if (!rc) {
           R* wo = pc ? nullptr : w;
           const R* di = pc ? nullptr : dinv;
-          if (sizeof(R) == 4 && h->nl % 4 == 0 && aligned16(u) && aligned16(r) && aligned16(w) && aligned16(vnew) &&
-              aligned16(z) && aligned16(dinv)) {
-            pcg_update_fused_f4<<<h->nblk, kRedThreads, 0, st>>>(
-                reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(r), reinterpret_cast<float4*>(wo),
-                reinterpret_cast<const float4*>(vnew), reinterpret_cast<const float4*>(z),
-                reinterpret_cast<const float4*>(di), h->nl / 4, h->S.p, h->partial.p, h->ticket.p);
+          using V = typename std::conditional<sizeof(R) == 4, float4, double2>::type;
+          constexpr int L = sizeof(V) / sizeof(R);
+          if (h->nl % L == 0 && aligned16(u) && aligned16(r) && aligned16(w) && aligned16(vnew) && aligned16(z) &&
+              aligned16(dinv)) {
+            pcg_update_fused_vec<R, V><<<h->nblk, kRedThreads, 0, st>>>(
+                reinterpret_cast<V*>(u), reinterpret_cast<V*>(r), reinterpret_cast<V*>(wo),
+                reinterpret_cast<const V*>(vnew), reinterpret_cast<const V*>(z), reinterpret_cast<const V*>(di),
+                h->nl / L, h->S.p, h->partial.p, h->ticket.p);
           } else {
             pcg_update_fused<R><<<h->nblk, kRedThreads, 0, st>>>(u, r, wo, vnew, z, di, h->nl, h->S.p, h->partial.p,
                                                                 h->ticket.p);
