@@ -31,6 +31,7 @@
 
 #include "cg2d_api.hpp"
 #include "internal.hpp"
+#include "line_ops.cuh"
 
 using namespace selfgpu;
 
@@ -39,7 +40,6 @@ namespace cgb {
 
 constexpr int kThreads = 256;
 constexpr int kVecChunk = kThreads * 8;  // nodes per vector tile
-constexpr int kElemTileNodes = 1024;      // nodes per element tile (several rounds of one node per thread)
 constexpr int kRoundsInFlight = 1;        // rounds of an element tile processed together (loads in flight)
 
 // Device descriptor of one problem.
@@ -240,13 +240,153 @@ __device__ __forceinline__ bool tile_last(const double (&bv)[NS], double* __rest
   return true;
 }
 
+// ------------------------------------------------------------------ FP32 element operator, one thread per line
+// The FP32 inner iterations run the element operator as one thread per grid line (the form of the single-problem
+// FP32 PCG apply): a round covers up to 256 / N1 elements, thread (le, t) holding line t (nodes (i, t)) of element
+// e0 + le in registers; the two column passes go through padded transpose buffers (row stride N1 + 1) and the
+// derivative rows are read as 16-byte broadcasts from a zero-padded table.
+constexpr int kLineBuf = 256 * 11;  // transpose buffer floats: (256 / N1) * N1 * (N1 + 1) <= 256 * 11 for N1 <= 10
+constexpr int kDRow = 12;           // padded derivative row (floats) for N1 <= 12
+
+template <int N1>
+constexpr int line_round_elems() {
+  return 256 / N1;
+}
+int line_round_elems_rt(int N) { return 256 / (N + 1); }
+
+// Dr(i, m) = D(i, m), Dc(i, m) = D(m, i), rows of 4 ceil(N1 / 4) floats (zero padded), for degree N = N1 - 1
+template <int N1>
+__device__ __forceinline__ void load_line_tables(const DTable* __restrict__ DT, float* Dr, float* Dc) {
+  constexpr int DS = 4 * ((N1 + 3) / 4);
+  for (int k = threadIdx.x; k < N1 * DS; k += blockDim.x) {
+    const int r = k / DS, m = k - r * DS;
+    Dr[k] = m < N1 ? DT->d32[N1 - 1][r + N1 * m] : 0.f;
+    Dc[k] = m < N1 ? DT->d32[N1 - 1][m + N1 * r] : 0.f;
+  }
+}
+
+// One round of ne <= 256 / N1 elements from e0.  FUSED: v_new = w + beta v_old (written), u = v_new gathered through
+// src, z = L(u), returns the thread's sum of u * Lu; otherwise out = L(w gathered through src), or with rhs
+// out = rhs - L in FP64, rounded (the plain apply's result).
+template <int N1, bool FUSED>
+__device__ __noinline__ float line_round(const Prob& p, const float* __restrict__ Dr, const float* __restrict__ Dc,
+                                         int e0, int ne, const float* __restrict__ w, const float* __restrict__ vold,
+                                         float* __restrict__ vnew, float beta, bool first, float* __restrict__ z,
+                                         const double* __restrict__ rhs, float* X, float* Y) {
+  constexpr int NN = N1 * N1, DS = 4 * ((N1 + 3) / 4), LS = N1 + 1, EPL = line_round_elems<N1>();
+  const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;
+  const bool active = le < EPL && le < ne;
+  const int e = e0 + le;
+  const size_t l0 = (size_t)e * NN + (size_t)N1 * t;
+  const int line = le < EPL ? le * N1 + t : 0;
+  float* Xl = X + line * LS;
+  float* Yl = Y + line * LS;
+  float u[N1], us[N1], up[N1], a[N1];
+  if (active) {
+    int sl[N1];
+    load_line<N1>(p.src + l0, sl);
+    if (FUSED) {
+      float wl[N1], vn[N1];
+      load_line<N1>(w + l0, wl);
+      if (first) {
+#pragma unroll
+        for (int i = 0; i < N1; ++i) vn[i] = wl[i];
+      } else {
+        float vl[N1];
+        load_line<N1>(vold + l0, vl);
+#pragma unroll
+        for (int i = 0; i < N1; ++i) vn[i] = wl[i] + beta * vl[i];
+      }
+#pragma unroll
+      for (int i = 0; i < N1; ++i)
+        u[i] = sl[i] == (int)(l0 + i) ? vn[i] : (first ? w[sl[i]] : w[sl[i]] + beta * vold[sl[i]]);
+      store_line<N1>(vnew + l0, vn);
+    } else {
+#pragma unroll
+      for (int i = 0; i < N1; ++i) u[i] = w[sl[i]];
+    }
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      us[i] = row_dot<N1>(Dr + i * DS, u);
+      Xl[i] = u[i];
+    }
+  }
+  __syncthreads();
+  if (active) {  // column pass: up(c, .) = D u(c, .), c = t
+    float uc[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) uc[m] = X[(le * N1 + m) * LS + t];
+#pragma unroll
+    for (int j = 0; j < N1; ++j) Y[(le * N1 + j) * LS + t] = row_dot<N1>(Dr + j * DS, uc);
+  }
+  __syncthreads();
+  if (active) {
+    const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
+    float G11[N1], G12[N1], G22[N1], F1[N1];
+    load_line<N1>(fe, G11);
+    load_line<N1>(fe + NN, G12);
+    load_line<N1>(fe + 2 * NN, G22);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      up[i] = Yl[i];
+      F1[i] = G11[i] * us[i] + G12[i] * up[i];
+      Xl[i] = G12[i] * us[i] + G22[i] * up[i];  // F2(i, t)
+    }
+#pragma unroll
+    for (int i = 0; i < N1; ++i) a[i] = row_dot<N1>(Dc + i * DS, F1);  // (D^T F1)(i, t)
+  }
+  __syncthreads();
+  if (active) {  // column pass: (D^T F2)(c, .)
+    float fc[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) fc[m] = X[(le * N1 + m) * LS + t];
+#pragma unroll
+    for (int j = 0; j < N1; ++j) Y[(le * N1 + j) * LS + t] = row_dot<N1>(Dc + j * DS, fc);
+  }
+  __syncthreads();
+  float prod = 0.f;
+  if (active) {
+    const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
+    float M[N1], Lu[N1];
+    load_line<N1>(fe + 3 * NN, M);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) Lu[i] = -(a[i] + Yl[i]) - M[i] * u[i];
+    if (FUSED) {
+      store_line<N1>(z + l0, Lu);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) prod += u[i] * Lu[i];
+    } else {
+      if (rhs) {
+#pragma unroll
+        for (int i = 0; i < N1; ++i) Lu[i] = (float)(rhs[l0 + i] - (double)Lu[i]);
+      }
+      store_line<N1>(z + l0, Lu);
+    }
+  }
+  return prod;
+}
+
+// all rounds of element tile t in the line form (the tile's table entry and D are loaded by the caller's switch)
+template <int N1, bool FUSED>
+__device__ __forceinline__ float line_tile(const Prob& p, const DTable* __restrict__ DT, float* Dr, float* Dc,
+                                           const ETile& t, const float* w, const float* vold, float* vnew,
+                                           float beta, bool first, float* z, const double* rhs, float* X, float* Y) {
+  constexpr int EPL = line_round_elems<N1>();
+  load_line_tables<N1>(DT, Dr, Dc);
+  __syncthreads();
+  float prod = 0.f;
+  for (int r0 = 0; r0 < t.ne; r0 += EPL) {
+    if (r0 > 0) __syncthreads();
+    prod += line_round<N1, FUSED>(p, Dr, Dc, t.e0 + r0, min(EPL, t.ne - r0), w, vold, vnew, beta, first, z, rhs, X, Y);
+  }
+  return prod;
+}
+
 // out = L(unmask(in)) [or rhs - L(...)] for the view's element tiles (outer residual, autotuning)
 template <typename R>
 __global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Prob* __restrict__ probs,
                                                            const Scal* __restrict__ S, const DTable* __restrict__ DT,
                                                            int vin, int vout, int residual, int gate) {
-  __shared__ R sh[3 * 256];
-  __shared__ R D[100];
   const int nt = V.cnt[0];
   {  // one tile per block
     const int ti = blockIdx.x;
@@ -255,12 +395,36 @@ __global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Pro
     if (skip(S[t.prob], gate)) return;
     const Prob& p = probs[t.prob];
     const int n = t.N + 1;
-    for (int k = threadIdx.x; k < n * n; k += blockDim.x)
-      D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
-    __syncthreads();
     const R* x = vec<R>(p, vin);
     R* out = vec<R>(p, vout);
     const double* rhs = residual ? p.f : nullptr;
+    if constexpr (sizeof(R) == 4) {  // FP32: the line form of the inner iterations (what the autotuner times)
+      __shared__ __align__(16) float X[kLineBuf];
+      __shared__ __align__(16) float Y[kLineBuf];
+      __shared__ __align__(16) float Dr[10 * kDRow];
+      __shared__ __align__(16) float Dc[10 * kDRow];
+#define SELF_BK_LINE(NV)                                                                                         \
+  case NV:                                                                                                       \
+    line_tile<NV, false>(p, DT, Dr, Dc, t, x, nullptr, nullptr, 0.f, true, out, rhs, X, Y);                       \
+    break;
+      switch (n) {
+        SELF_BK_LINE(3)
+        SELF_BK_LINE(4)
+        SELF_BK_LINE(5)
+        SELF_BK_LINE(6)
+        SELF_BK_LINE(7)
+        SELF_BK_LINE(8)
+        SELF_BK_LINE(9)
+        SELF_BK_LINE(10)
+        default: break;
+      }
+#undef SELF_BK_LINE
+      return;
+    } else {
+    __shared__ R sh[3 * 256];
+    __shared__ R D[100];
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) D[k] = (R)DT->d64[t.N][k];
+    __syncthreads();
     for (int r0 = 0; r0 < t.ne; r0 += t.epr) {
       const int ne = min(t.epr, t.ne - r0);
       if (r0 > 0) __syncthreads();
@@ -275,6 +439,7 @@ __global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Pro
         case 10: apply_body<10, R>(p, D, t.e0 + r0, ne, x, rhs, out, sh); break;
         default: break;
       }
+    }
     }
   }
 }
@@ -367,8 +532,6 @@ template <typename R>
 __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __restrict__ probs, Scal* __restrict__ S,
                                                      const DTable* __restrict__ DT, double* __restrict__ partial,
                                                      unsigned int* __restrict__ ticket) {
-  __shared__ R sh[kRoundsInFlight * 3 * 256];
-  __shared__ R D[100];
   const int nt = V.cnt[0];
   {  // one tile per block
     const int ti = blockIdx.x;
@@ -378,9 +541,6 @@ __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __r
     if (skip(s, 0)) return;
     const Prob& p = probs[t.prob];
     const int n = t.N + 1;
-    for (int k = threadIdx.x; k < n * n; k += blockDim.x)
-      D[k] = (sizeof(R) == 4) ? (R)DT->d32[t.N][k] : (R)DT->d64[t.N][k];
-    __syncthreads();
     const bool first = s.iter == 0;
     const R beta = first ? R(0) : (sizeof(R) == 4 ? (R)s.beta32 : (R)s.beta);
     R *vold, *vnew;
@@ -388,6 +548,32 @@ __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __r
     const R* w = vec<R>(p, V_W);
     R* z = vec<R>(p, V_Z);
     R prod = 0;
+    if constexpr (sizeof(R) == 4) {  // FP32: one thread per grid line
+      __shared__ __align__(16) float X[kLineBuf];
+      __shared__ __align__(16) float Y[kLineBuf];
+      __shared__ __align__(16) float Dr[10 * kDRow];
+      __shared__ __align__(16) float Dc[10 * kDRow];
+#define SELF_BK_LINE(NV)                                                                                         \
+  case NV:                                                                                                       \
+    prod = line_tile<NV, true>(p, DT, Dr, Dc, t, w, vold, vnew, beta, first, z, nullptr, X, Y);                  \
+    break;
+      switch (n) {
+        SELF_BK_LINE(3)
+        SELF_BK_LINE(4)
+        SELF_BK_LINE(5)
+        SELF_BK_LINE(6)
+        SELF_BK_LINE(7)
+        SELF_BK_LINE(8)
+        SELF_BK_LINE(9)
+        SELF_BK_LINE(10)
+        default: break;
+      }
+#undef SELF_BK_LINE
+    } else {
+    __shared__ R sh[kRoundsInFlight * 3 * 256];
+    __shared__ R D[100];
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) D[k] = (R)DT->d64[t.N][k];
+    __syncthreads();
     const int epr = t.epr;  // elements per round (one node per thread); the tile holds several rounds
     for (int r0 = 0; r0 < t.ne; r0 += kRoundsInFlight * epr) {
       const int ne = min(kRoundsInFlight * epr, t.ne - r0);
@@ -409,6 +595,7 @@ __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __r
         default: break;
       }
 #undef SELF_BK_CASE
+    }
     }
     const double bv[1] = {block_sum_r<R>(prod)};
     double tot[1];
@@ -711,11 +898,12 @@ int ensure_cap(self_cgbatch* b, int want) {
   return SELF_OK;
 }
 
-// Elements per element tile: a multiple of the round size max_epb_rt(N) (one node per thread); the default gives
-// about kElemTileNodes nodes per tile, the autotuner may choose another multiple.
+// Elements per element tile: a multiple of the round size max_epb_rt(N) (one node per thread, the FP64 body); the
+// default is one round of the FP32 line body (256 / (N + 1) elements) rounded down to that multiple, the
+// autotuner may choose another multiple.
 int default_tile_elems(int N) {
-  const int r = max_epb_rt(N), nn = (N + 1) * (N + 1);
-  return r * std::max(1, kElemTileNodes / (r * nn));
+  const int r = max_epb_rt(N);
+  return std::max(r, (line_round_elems_rt(N) / r) * r);
 }
 int tile_elems(const self_cgbatch* b, const Prob& P, int force) {
   const int bk = bucket_of(P.nEl);
@@ -1242,7 +1430,14 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
       const int r = max_epb_rt(N);
       int best = default_tile_elems(N);
       double best_ms = 1e30;
-      for (int e = r; e <= 32 * r; e *= 2) {  // element tiles of 1, 2, 4, ... 32 rounds
+      // element tiles of 1, 2, 4, ... 32 node rounds (FP64 body) and 1, 2, 4, 8 line rounds (FP32 body), each a
+      // multiple of the node round
+      std::vector<int> cand;
+      for (int e = r; e <= 32 * r; e *= 2) cand.push_back(e);
+      for (int k = 0; k < 4; ++k) cand.push_back(std::max(r, ((line_round_elems_rt(N) << k) / r) * r));
+      std::sort(cand.begin(), cand.end());
+      cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+      for (int e : cand) {
         if ((rc = upload_view(b, b->tune, used, N, bk, e))) return rc;
         for (int w = 0; w < 2; ++w)
           if ((rc = k_apply_plain<float>(b, b->tune, V_V, V_Z, 0, 0))) return rc;
