@@ -517,78 +517,6 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused_f32(const float* 
   }
 }
 
-// ---------------------------------------------------------------------------------- FP64 even-odd operator
-// The GLL collocation derivative matrix is centro-antisymmetric, D(N-i, N-m) = -D(i, m) (nodes symmetric about 0),
-// and so is its transpose.  For such a matrix A, with H = N1/2, xe(m) = x(m) + x(N-m) and xo(m) = x(m) - x(N-m)
-// (m < H),
-//   y(i) = ye(i) + yo(i),  y(N-i) = yo(i) - ye(i),  ye(i) = sum_m E(i,m) xe(m) [+ A(i,H) x(H)],  yo(i) = sum_m O(i,m) xo(m),
-// E(i,m) = (A(i,m) + A(i,N-m))/2, O(i,m) = (A(i,m) - A(i,N-m))/2, and for odd N1 the middle row y(H) = sum_m O(H,m) xo(m)
-// (the even-odd decomposition of Solomonoff, 1992).  At N1 = 8 a line costs 48 FP64 operations instead of 64.  The
-// FP64 operator is bound by the FP64 pipe on this part (a few FP64 operations per byte), so the count is the time.
-template <int N1>
-struct EOTable {
-  static constexpr int H = N1 / 2, ODD = N1 & 1;
-  double E[H][H + ODD];  // E(i, m), then A(i, H) for odd N1
-  double O[H + ODD][H];  // O(i, m); for odd N1 row H is the middle row
-};
-
-template <int N1>
-struct EOPair {
-  EOTable<N1> D, Dt;  // D and its transpose
-};
-
-// host: the tables of the column-major N1 x N1 matrix A (A(i, m) = a[i + N1 m]); false when A is not
-// centro-antisymmetric to 1e-13 of its largest entry (a derivative matrix of non-symmetric nodes)
-template <int N1>
-bool eo_table(const double* a, bool transpose, EOTable<N1>& T) {
-  constexpr int N = N1 - 1, H = N1 / 2;
-  auto A = [&](int i, int m) { return transpose ? a[m + N1 * i] : a[i + N1 * m]; };
-  double amax = 0, dev = 0;
-  for (int i = 0; i < N1; ++i)
-    for (int m = 0; m < N1; ++m) {
-      amax = std::max(amax, std::fabs(A(i, m)));
-      dev = std::max(dev, std::fabs(A(N - i, N - m) + A(i, m)));
-    }
-  if (!(dev <= 1e-13 * amax)) return false;
-  for (int i = 0; i < H + (N1 & 1); ++i)
-    for (int m = 0; m < H; ++m) {
-      if (i < H) T.E[i][m] = 0.5 * (A(i, m) + A(i, N - m));
-      T.O[i][m] = 0.5 * (A(i, m) - A(i, N - m));
-    }
-  if (N1 & 1)
-    for (int i = 0; i < H; ++i) T.E[i][H] = A(i, H);
-  return true;
-}
-
-template <int N1>
-__device__ __forceinline__ void eo_matvec(const EOTable<N1>& T, const double (&x)[N1], double (&y)[N1]) {
-  constexpr int N = N1 - 1, H = N1 / 2;
-  double xe[H], xo[H];
-#pragma unroll
-  for (int m = 0; m < H; ++m) {
-    xe[m] = x[m] + x[N - m];
-    xo[m] = x[m] - x[N - m];
-  }
-#pragma unroll
-  for (int i = 0; i < H; ++i) {
-    double ye = T.E[i][0] * xe[0], yo = T.O[i][0] * xo[0];
-#pragma unroll
-    for (int m = 1; m < H; ++m) {
-      ye = fma(T.E[i][m], xe[m], ye);
-      yo = fma(T.O[i][m], xo[m], yo);
-    }
-    if constexpr (N1 & 1) ye = fma(T.E[i][H + (N1 & 1) - 1], x[H], ye);
-    y[i] = ye + yo;
-    y[N - i] = yo - ye;
-  }
-  if constexpr (N1 & 1) {
-    double ym = T.O[H + (N1 & 1) - 1][0] * xo[0];
-#pragma unroll
-    for (int m = 1; m < H; ++m) ym = fma(T.O[H + (N1 & 1) - 1][m], xo[m], ym);
-    y[H] = ym;
-  }
-}
-
 // Lu on line t (nodes (i, t), i = 0..N1-1) of element le of a block pass, from u(., t) in registers: the line-
 // oriented operator of pcg_apply_fused_f32 in FP64 with even-odd contractions.  Every thread of the block calls it
 // (threads without a line pass active = false and only join the barriers); fe = the element's factors + N1 t;

@@ -25,6 +25,7 @@
 
 #include "dg2d_fp32.cuh"
 #include "internal.hpp"
+#include "line_ops.cuh"
 
 using namespace selfgpu;
 
@@ -40,6 +41,9 @@ struct NodalConst {
   double lW[N1], lE[N1], lS[N1], lN[N1];
   double qwinv[N1];  // 1 / quadrature weight
   double qw[N1];     // quadrature weight (bit-faithful mode divides)
+  double lWq[N1], lEq[N1], lSq[N1], lNq[N1];  // lifts over the weight, lX(k) / w(k) (plain mode)
+  EOTable<N1> eS, eP;  // even-odd tables of dS, dP (plain mode, when eo)
+  int eo;              // both matrices centro-antisymmetric
 };
 
 struct VolArgs {
@@ -317,9 +321,17 @@ __device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const doub
   }
 }
 
+// Resident blocks asked of the compiler for dg_volume: the plain form is bound by the FP64 pipe and ran 11 % faster
+// at N1 = 8 with 3 blocks of 256 threads per SM (80 registers, a few bytes spilled) than with 2 (86 registers); at
+// other degrees that cap spills hundreds of bytes, so the compiler chooses
+template <int N1, bool EX>
+constexpr int vol_min_blocks() {
+  return (!EX && N1 == 8) ? 3 : 1;
+}
+
 // PH: 0 advection, 1 conservative shallow water, 2 linear shallow water, 3 skew-symmetric shallow water (NEQ 4)
 template <int N1, int NEQ, int PH, bool EX>
-__global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
+__global__ void __launch_bounds__(256, vol_min_blocks<N1, EX>()) dg_volume(VolArgs A, NodalConst<N1> Cg) {
   constexpr bool SW = PH == 1;
   using X = Ar<EX>;
   constexpr int NN = N1 * N1;
@@ -425,23 +437,61 @@ __global__ void __launch_bounds__(256) dg_volume(VolArgs A, NodalConst<N1> Cg) {
     }
   }
   __syncthreads();
+  if constexpr (!EX) {
+    // plain mode: the weak-derivative contractions as line tasks, one grid line of one variable per thread, in place
+    // (row j of F becomes (dS F)(., j), column i of G becomes (dP G)(i, .)); with the even-odd form 3/4 of the FP64
+    // operations of the node-by-node sums, the bound of this kernel.  Tasks are ordered direction-major, so a warp
+    // runs one direction.
+    constexpr int NT1 = EPB * NEQ * N1;  // tasks per direction
+    const int flat = tid + NN * le;
+    for (int task = flat; task < 2 * NT1; task += NN * EPB) {
+      const int dir = task / NT1, rest = task - dir * NT1;
+      const int el = rest / (NEQ * N1), v = (rest / N1) % NEQ, k = rest % N1;
+      if (blockIdx.x * EPB + el >= A.nEl) continue;
+      double* base = dir == 0 ? &sF[el][v][N1 * k] : &sG[el][v][k];
+      const int st = dir == 0 ? 1 : N1;
+      double x[N1], y[N1];
+#pragma unroll
+      for (int m = 0; m < N1; ++m) x[m] = base[m * st];
+      if (C.eo) {
+        eo_matvec<N1>(dir == 0 ? C.eS : C.eP, x, y);
+      } else {
+        const double* Dm = dir == 0 ? C.dS : C.dP;
+#pragma unroll
+        for (int r = 0; r < N1; ++r) {
+          double acc = 0.0;
+#pragma unroll
+          for (int m = 0; m < N1; ++m) acc = fma(Dm[r + N1 * m], x[m], acc);
+          y[r] = acc;
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < N1; ++m) base[m * st] = y[m];
+    }
+    __syncthreads();
+  }
   double tend[NEQ];
   if (active) {
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) {
       // s direction: MATMUL(dMatS, F(:,j)) + lift, along the row j; then the p direction and 1/J
       double ds = 0.0, dp = 0.0;
+      if (EX) {
 #pragma unroll
-      for (int m = 0; m < N1; ++m) ds = X::add(ds, X::mul(C.dS[i + N1 * m], sF[le][v][m + N1 * j]));
+        for (int m = 0; m < N1; ++m) ds = X::add(ds, X::mul(C.dS[i + N1 * m], sF[le][v][m + N1 * j]));
 #pragma unroll
-      for (int m = 0; m < N1; ++m) dp = X::add(dp, X::mul(C.dP[j + N1 * m], sG[le][v][i + N1 * m]));
+        for (int m = 0; m < N1; ++m) dp = X::add(dp, X::mul(C.dP[j + N1 * m], sG[le][v][i + N1 * m]));
+      } else {
+        ds = sF[le][v][tid];
+        dp = sG[le][v][tid];
+      }
       if (EX) {
         ds = X::add(ds, X::add(X::mul(sB[le][1][v][j], C.lE[i]), X::mul(sB[le][3][v][j], C.lW[i])) / C.qw[i]);
         dp = X::add(dp, X::add(X::mul(sB[le][2][v][i], C.lN[j]), X::mul(sB[le][0][v][i], C.lS[j])) / C.qw[j]);
         tend[v] = X::sub(-ds, dp) / jac;
       } else {
-        ds += (sB[le][1][v][j] * C.lE[i] + sB[le][3][v][j] * C.lW[i]) * C.qwinv[i];
-        dp += (sB[le][2][v][i] * C.lN[j] + sB[le][0][v][i] * C.lS[j]) * C.qwinv[j];
+        ds = fma(sB[le][1][v][j], C.lEq[i], fma(sB[le][3][v][j], C.lWq[i], ds));
+        dp = fma(sB[le][2][v][i], C.lNq[j], fma(sB[le][0][v][i], C.lSq[j], dp));
         tend[v] = (-ds - dp) * jac;
       }
     }
@@ -756,7 +806,12 @@ NodalConst<N1> make_const(const self_dg2d* h) {
     C.lN[k] = h->lN[k];
     C.qwinv[k] = 1.0 / h->qw[k];
     C.qw[k] = h->qw[k];
+    C.lWq[k] = h->lW[k] / h->qw[k];
+    C.lEq[k] = h->lE[k] / h->qw[k];
+    C.lSq[k] = h->lS[k] / h->qw[k];
+    C.lNq[k] = h->lN[k] / h->qw[k];
   }
+  C.eo = eo_table<N1>(h->dS.data(), false, C.eS) && eo_table<N1>(h->dP.data(), false, C.eP);
   return C;
 }
 
