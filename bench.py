@@ -261,7 +261,7 @@ def _e2e(nat, L, ctx, sw, dof, steps, dist):
 
 # DRAM bytes (read + write) of one launch from the ncu --set full captures summarised in
 # profiles/sw32_fused_sw128_n7.md (launch 0) and profiles/dg_volume_fp64_sw128_n7.md (launch 1)
-NCU_TRAFFIC_BYTES = {"sw32_fused": 84.90e6, "dg_volume": 128.2e6}
+NCU_TRAFFIC_BYTES = {"sw32_fused": 84.90e6, "dg_volume": 129.5e6}
 
 # algorithmic FP64 flops of one element-stage at N=7: traces 1,536, volume fluxes 2,176, contractions 6,144, lift
 # 1,536, 1/J 384, sources 512, RK update 768, Riemann 960 (edge kernel); timed over both kernels of a stage
