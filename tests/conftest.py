@@ -12,6 +12,17 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU and the built libselfgpu.so")
 
 
+@pytest.fixture(scope="session", autouse=True)
+def _native_library():
+    """Builds the product library in-tree once when it is missing (a fresh checkout): the CPU tests use its host-side
+    set-up routines and its export table.  It is the library itself, not a fallback (there is none)."""
+    from self_gb300 import _native as nat
+    if not os.path.exists(nat.LIB_PATH):
+        from self_gb300 import build as B
+        B.build()
+    yield
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as O
