@@ -24,7 +24,8 @@ def _problem(oracle, N, nx, warp=0.0, lam=0.1, op=0, vel=(0.0, 0.0), kappa=None)
     return nod, mesh, k, source, P
 
 
-@pytest.mark.parametrize("N,nx,warp,op", [(3, 4, 0.0, 0), (7, 8, 0.05, 0), (5, 6, 0.03, 1), (9, 3, 0.0, 0)])
+@pytest.mark.parametrize("N,nx,warp,op", [(3, 4, 0.0, 0), (7, 8, 0.05, 0), (5, 6, 0.03, 1), (9, 3, 0.0, 0),
+                                          (6, 5, 0.03, 0), (8, 4, 0.02, 1)])
 def test_matrix_action_residual_dot_parity(oracle, gpu_ctx, N, nx, warp, op):
     import self_gb300 as sg
     vel = (1.0, 0.5) if op == 1 else (0.0, 0.0)
@@ -65,10 +66,10 @@ def test_jacobi_diagonal_matches_unit_vector_application(oracle):
         assert abs(Ae[idx] - d[idx]) <= 1e-12 * abs(d[idx])
 
 
-@pytest.mark.parametrize("method,precond", [("cg", 0), ("pcg", 1)])
-def test_pcg_parity_with_oracle(oracle, gpu_ctx, method, precond):
+@pytest.mark.parametrize("method,precond,N,nx", [("cg", 0, 5, 6), ("pcg", 1, 5, 6), ("pcg", 1, 6, 5), ("pcg", 1, 7, 4),
+                                                 ("pcg", 1, 8, 4)])
+def test_pcg_parity_with_oracle(oracle, gpu_ctx, method, precond, N, nx):
     import self_gb300 as sg
-    N, nx = 5, 6
     nod, mesh, k, source, P = _problem(oracle, N, nx, warp=0.03)
     cg = sg.CGsemElliptic_2D(gpu_ctx, nod, mesh, k, lam=0.1)
     sol, rep = cg.Solve(source, method=method, tolerance=1e-10, maxIters=3000, return_resi=True)

@@ -41,7 +41,8 @@ def _sw_problem(oracle, N, nx, warp=0.05, seed=7, drag=0.0, relax=False, flow=Tr
 
 
 @pytest.mark.parametrize("N,nx,warp,drag,relax", [(3, 4, 0.05, 0.0, False), (7, 16, 0.05, 0.0, False),
-                                                  (5, 6, 0.0, 1e-3, True), (9, 3, 0.05, 0.0, False)])
+                                                  (5, 6, 0.0, 1e-3, True), (9, 3, 0.05, 0.0, False),
+                                                  (6, 5, 0.05, 0.0, False), (8, 4, 0.05, 1e-3, True)])
 def test_sw_tendency_parity(oracle, gpu_ctx, N, nx, warp, drag, relax):
     import self_gb300 as sg
     nod, mesh, q, h, fcor, dhdx, dhdy, dt, P, rl, ts = _sw_problem(oracle, N, nx, warp, drag=drag, relax=relax)
