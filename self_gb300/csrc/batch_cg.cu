@@ -283,6 +283,11 @@ __device__ __noinline__ float line_round(const Prob& p, const float* __restrict_
   float* Yl = Y + line * LS;
   float u[N1], us[N1], up[N1], a[N1];
   if (active) {
+    {  // the factor lines are read two barriers later: request them into L2 with the first loads
+      const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
+#pragma unroll
+      for (int f = 0; f < 4; ++f) prefetch_l2(fe + f * NN);
+    }
     int sl[N1];
     load_line<N1>(p.src + l0, sl);
     if (FUSED) {

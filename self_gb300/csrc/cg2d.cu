@@ -432,6 +432,11 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused_f32(const float* 
     float u[N1], us[N1], up[N1];
     const size_t l0 = (size_t)e * NN + (size_t)N1 * t;  // row t: nodes (i, t), i = 0..N1-1
     if (active) {
+      {  // the factor lines are read two barriers later: request them into L2 with the first loads
+        const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) prefetch_l2(fe + f * NN);
+      }
       int sl[N1];
       float wl[N1], vl[N1], vn[N1];
       load_line<N1>(src + l0, sl);

@@ -9,6 +9,9 @@
 
 namespace selfgpu {
 
+// request the 128-byte line holding p into L2 (no register result; the load that follows later hits L2)
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 template <int N1>
 __device__ __forceinline__ float row_dot(const float* __restrict__ drow, const float (&x)[N1]) {
   // drow: N1 floats padded to a multiple of 4 (zeros), 16-byte aligned; x: registers
