@@ -442,7 +442,8 @@ def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, fp64_sample=60):
 def run_cg_profile(args):
     """Bounded CGSEM workload for profilers (no JSON line): the 256x256 N=7 Helmholtz problem of the elliptic
     leg, `--profile-cg K` PCG iterations (`--profile-method`: pcg = Jacobi, pcg_linear = the linear-FEM
-    preconditioner with 20 inner iterations; `--profile-precision`) after a short warm-up solve."""
+    preconditioner with 20 inner iterations; `--profile-precision`) after a short warm-up solve; gmres = K FP64
+    GMRES(30) Arnoldi steps on the advection-diffusion operator of the leg."""
     import self_gb300 as sg
     from self_gb300 import _native as nat
     from self_gb300 import workloads as W
@@ -451,8 +452,19 @@ def run_cg_profile(args):
     nod = sg.NodalStorage_2D(N, nat.GAUSS_LOBATTO, nat.CG)
     mesh = sg.QuadMesh(nx, nx, N, nat.GAUSS_LOBATTO, boundary_flag=nat.DIRICHLET)
     k, f, source = W.helmholtz(mesh, N, seed=3)
-    cg = sg.CGsemElliptic_2D(ctx, nod, mesh, k, lam=0.1)
     method, prec = args.profile_method, args.profile_precision
+    if method == "gmres":  # the GMRES(30) operator of the elliptic leg, FP64, K Arnoldi steps
+        ad = sg.CGsemElliptic_2D(ctx, nod, mesh, np.full_like(k, 1e-3), lam=0.0, op=1, vel=(1.0, 0.5))
+        ad.Solve(source, method="gmres", m=30, tolerance=1e-10, maxIters=30)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        _, rep = ad.Solve(source, method="gmres", m=30, tolerance=1e-30, maxIters=args.profile_cg)
+        el = time.perf_counter() - t0
+        print(f"profile-cg: {rep['iterations']} FP64 gmres Arnoldi steps in {el:.4f} s", flush=True)
+        ad.Trash()
+        ctx.close()
+        return
+    cg = sg.CGsemElliptic_2D(ctx, nod, mesh, k, lam=0.1)
     warm = 32 if method == "pcg" else 4
     cg.Solve(source, method=method, precision=prec, tolerance=1e-10, maxIters=warm, pc_iterations=20)
     ctx.synchronize()
@@ -625,7 +637,7 @@ def main():
     ap.add_argument("--serve-n", type=int, default=300, help="requests of the serving leg (0 skips it)")
     ap.add_argument("--profile-cg", type=int, default=0,
                     help="run only K PCG iterations of the elliptic workload (for profilers) and exit")
-    ap.add_argument("--profile-method", default="pcg", choices=["pcg", "pcg_linear"])
+    ap.add_argument("--profile-method", default="pcg", choices=["pcg", "pcg_linear", "gmres"])
     ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
