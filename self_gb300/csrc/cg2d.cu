@@ -945,6 +945,8 @@ int upload(self_ctx* ctx, DevBuf<T>& b, const std::vector<T>& host) {
   return SELF_OK;
 }
 
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 inline int grid_for(const self_ctx* ctx, size_t n) {
   size_t want = (n + kRedThreads - 1) / kRedThreads;
   size_t cap = (size_t)std::max(1, ctx->num_sms) * 8;  // 8 CTAs of 256 threads per SM, grid-stride loops
@@ -1245,8 +1247,16 @@ int pc_linear_apply(self_cg2d* h, const R* r, const PcRun<R>& pc) {
       cg_dss_mask<R><<<(pc.ngroups + 255) / 256, 256, 0, st>>>(pc.zl, pc.gptr, pc.gidx, pc.gdir, pc.ngroups);
       SELF_LAUNCHED(h->ctx);
     }
-    pcl_update<R><<<h->nblk, kRedThreads, 0, st>>>(pc.ul, pc.rl, ln, pc.zl, h->nl, h->S.p, pc.SL, h->partial.p,
-                                                   h->ticket.p);
+    using V = typename std::conditional<sizeof(R) == 4, float4, double2>::type;
+    constexpr int L = sizeof(V) / sizeof(R);
+    if (h->nl % L == 0 && aligned16(pc.ul) && aligned16(pc.rl) && aligned16(ln) && aligned16(pc.zl)) {
+      pcl_update_vec<R, V><<<h->nblk, kRedThreads, 0, st>>>(
+          reinterpret_cast<V*>(pc.ul), reinterpret_cast<V*>(pc.rl), reinterpret_cast<const V*>(ln),
+          reinterpret_cast<const V*>(pc.zl), h->nl / L, h->S.p, pc.SL, h->partial.p, h->ticket.p);
+    } else {
+      pcl_update<R><<<h->nblk, kRedThreads, 0, st>>>(pc.ul, pc.rl, ln, pc.zl, h->nl, h->S.p, pc.SL, h->partial.p,
+                                                     h->ticket.p);
+    }
     SELF_LAUNCHED(h->ctx);
   }
   return SELF_OK;
@@ -1297,7 +1307,6 @@ namespace cg {
 // buffers alternating); the host reads the scalar block after each graph launch.
 constexpr int kGraphIters = 16;  // even: the current direction is back in `v` after every graph launch
 
-inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // With pc (linear-FEM preconditioner) every outer iteration starts with the inner solve u_l = M^-1 r and
 // w, num = <r, w> (pc_num); the graph then holds kGraphItersPC outer iterations of 3 * pc->iters + 5 launches.

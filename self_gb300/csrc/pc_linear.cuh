@@ -155,6 +155,67 @@ __global__ void __launch_bounds__(kRedThreads) pcl_update(R* __restrict__ ul, R*
   if (SL->rr / SL->r0 < SL->tol || SL->iter >= SL->maxIters) SL->done = 1;
 }
 
+// pcl_update over 16-byte groups of consecutive nodes (float4 / double2; the L-vector length is a multiple of the
+// group when (N+1)^2 nEl is): each thread keeps two groups of its 4 streams in flight
+template <typename R, typename V>
+__global__ void __launch_bounds__(kRedThreads) pcl_update_vec(V* __restrict__ ul, V* __restrict__ rl,
+                                                              const V* __restrict__ vl, const V* __restrict__ zl,
+                                                              size_t nv, const CGScalars* __restrict__ S, CGScalars* SL,
+                                                              double* __restrict__ partial,
+                                                              unsigned int* __restrict__ ticket) {
+  static_assert(sizeof(V) == 16 && sizeof(V) % sizeof(R) == 0, "16-byte groups");
+  constexpr int L = sizeof(V) / sizeof(R);
+  if (S->done || SL->done) return;
+  const R a = sizeof(R) == 4 ? (R)SL->alpha32 : (R)SL->alpha;
+  R prr = 0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  constexpr int U = 2;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += U * stride) {
+    V uu[U], vv[U], rr[U], zz[U];
+    bool ok[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const size_t x = k + q * stride;
+      ok[q] = x < nv;
+      if (!ok[q]) continue;
+      uu[q] = ul[x];
+      vv[q] = vl[x];
+      rr[q] = rl[x];
+      zz[q] = zl[x];
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      if (!ok[q]) continue;
+      R us[L], vs[L], rs[L], zs[L];
+      memcpy(us, &uu[q], 16);
+      memcpy(vs, &vv[q], 16);
+      memcpy(rs, &rr[q], 16);
+      memcpy(zs, &zz[q], 16);
+#pragma unroll
+      for (int c = 0; c < L; ++c) {
+        us[c] += a * vs[c];
+        rs[c] = rs[c] - a * zs[c];
+        prr += rs[c] * rs[c];
+      }
+      V t;
+      memcpy(&t, us, 16);
+      ul[k + q * stride] = t;
+      memcpy(&t, rs, 16);
+      rl[k + q * stride] = t;
+    }
+  }
+  const R acc[1] = {prr};
+  double tot[1];
+  if (!grid_sums_last<1, R>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
+  SL->den = SL->num;
+  SL->num = tot[0];
+  SL->beta = SL->num / SL->den;
+  SL->beta32 = (float)SL->beta;
+  SL->iter += 1;
+  SL->rr = sqrt(tot[0]);
+  if (SL->rr / SL->r0 < SL->tol || SL->iter >= SL->maxIters) SL->done = 1;
+}
+
 // w = MapFromPCToOrig(UnMask(u_l)) in the spectral mesh's masked form: each spectral primary copy (src[k] == k)
 // takes u_l at its linear primary copy (lsrc[k]), the other copies 0; num = <r, w>, and the outer beta = num / den
 // after the first outer iteration.
