@@ -125,21 +125,42 @@ __global__ void cg_dss_mask(R* __restrict__ v, const int* __restrict__ gptr, con
 // The same GlobalSum + Mask with the two-copy groups (shared edge nodes, the large majority) as a flat pair list
 // -- one thread per pair, no group-pointer indirection -- and the remaining groups (corner nodes, Dirichlet
 // nodes) in CSR form, one thread per group; sums in the same order, so the result equals cg_dss_mask's.
+constexpr int kDssPairsPerThread = 8;
+
 template <typename R>
 __global__ void cg_dss_mask_pairs(R* __restrict__ v, const int2* __restrict__ pairs, int npairs,
                                   const int* __restrict__ gptr, const int* __restrict__ gidx,
                                   const unsigned char* __restrict__ gdir, int ngroups) {
+  // the first ceil(npairs / kDssPairsPerThread) threads sum kDssPairsPerThread pairs each (pairs t, t + P, ...;
+  // all loads before the stores, so each thread keeps several independent loads in flight); the rest take the
+  // CSR groups
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < npairs) {
-    const int2 p = pairs[t];
-    R s = 0;
-    s += v[p.x];
-    s += v[p.y];
-    v[p.x] = s;
-    v[p.y] = 0;
+  const int P = (npairs + kDssPairsPerThread - 1) / kDssPairsPerThread;
+  if (t < P) {
+    int2 p[kDssPairsPerThread];
+    R a[kDssPairsPerThread], b[kDssPairsPerThread];
+#pragma unroll
+    for (int q = 0; q < kDssPairsPerThread; ++q) {
+      const int k = t + q * P;
+      if (k < npairs) {
+        p[q] = pairs[k];
+        a[q] = v[p[q].x];
+        b[q] = v[p[q].y];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kDssPairsPerThread; ++q) {
+      if (t + q * P < npairs) {
+        R s = 0;
+        s += a[q];
+        s += b[q];
+        v[p[q].x] = s;
+        v[p[q].y] = 0;
+      }
+    }
     return;
   }
-  const int g = t - npairs;
+  const int g = t - P;
   if (g >= ngroups) return;
   const int a = gptr[g], b = gptr[g + 1];
   if (gdir[g]) {
@@ -1108,7 +1129,7 @@ int launch_apply(self_cg2d* h, const R* x, const R* rhs, R* out, const selfgpu::
 template <typename R>
 int launch_dss(self_cg2d* h, R* v) {
   if (h->ngroups == 0) return SELF_OK;
-  const int nt = h->dss_npairs + h->dss_nrest;
+  const int nt = (h->dss_npairs + kDssPairsPerThread - 1) / kDssPairsPerThread + h->dss_nrest;
   cg_dss_mask_pairs<R><<<(nt + 255) / 256, 256, 0, h->ctx->stream>>>(v, h->dss_pairs.p, h->dss_npairs,
                                                                      h->dss_gptr.p, h->dss_gidx.p, h->dss_gdir.p,
                                                                      h->dss_nrest);
