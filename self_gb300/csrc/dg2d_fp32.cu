@@ -21,13 +21,14 @@
 
 // warps (independent element workers) per CTA of the fused stage, two element buffers per warp
 constexpr int kFusedWarps = 4;
+constexpr int kFusedBuf = 2;  // element buffers per warp
 
 // the fused stage kernel for an RK mode (1: first stage) and whether drag or relaxation terms are present
 const void* fused_kernel(int mode, bool extra) {
   using namespace selfgpu::sw32;
-  if (mode == 1) return extra ? (const void*)sw32_fused<8, 2, kFusedWarps, 1, true>
-                              : (const void*)sw32_fused<8, 2, kFusedWarps, 1, false>;
-  return extra ? (const void*)sw32_fused<8, 2, kFusedWarps, 2, true> : (const void*)sw32_fused<8, 2, kFusedWarps, 2, false>;
+  if (mode == 1) return extra ? (const void*)sw32_fused<8, kFusedBuf, kFusedWarps, 1, true>
+                              : (const void*)sw32_fused<8, kFusedBuf, kFusedWarps, 1, false>;
+  return extra ? (const void*)sw32_fused<8, kFusedBuf, kFusedWarps, 2, true> : (const void*)sw32_fused<8, kFusedBuf, kFusedWarps, 2, false>;
 }
 
 namespace selfgpu {
@@ -664,7 +665,7 @@ int create(self_dg2d* hd, State* s, const self_dg2d_desc* d, const std::vector<d
       SELF_CUDA_TRY(ctx, cudaMemset(s->err.p, 0, sizeof(int)));
       SELF_CUDA_TRY(ctx, cudaHostAlloc(reinterpret_cast<void**>(&s->err_host), sizeof(int), cudaHostAllocDefault));
       *s->err_host = 0;
-      s->fused_smem = selfgpu::sw32::fused_smem_bytes<8, 2, kFusedWarps>();
+      s->fused_smem = selfgpu::sw32::fused_smem_bytes<8, kFusedBuf, kFusedWarps>();
       int per_sm = 4;
       for (int mode = 1; mode <= 2; ++mode)
         for (int extra = 0; extra <= 1; ++extra) {
