@@ -355,7 +355,7 @@ def batched_leg(sg, ctx, nprob=512, fp64_sample=32):
     probs = [W.batched_problem(sg, nx, N, seed) for nx, N, seed in specs]
     setup = time.perf_counter() - t0
     B = sg.CGBatch(ctx, probs)
-    tune = B.autotune(os.path.join(ROOT, "self_gb300", "_build", "cgbatch_tuning.json"))
+    tune = B.autotune(os.path.join(ROOT, "self_gb300", "_build", "cgbatch_tuning_lines.json"))  # line-form FP32 tiles
     B.Solve(precision="fp32", tolerance=1e-10, maxIters=64)  # warm-up: graphs
     ctx.synchronize()
     t0 = time.perf_counter()
