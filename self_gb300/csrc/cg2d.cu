@@ -105,26 +105,7 @@ __global__ void __launch_bounds__(256) cg_apply_local(const R* __restrict__ x, c
   }
 }
 
-// GlobalSum + Mask over the shared-node groups (one thread per group).
-template <typename R>
-__global__ void cg_dss_mask(R* __restrict__ v, const int* __restrict__ gptr, const int* __restrict__ gidx,
-                            const unsigned char* __restrict__ gdir, int ngroups) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ngroups) return;
-  const int a = gptr[g], b = gptr[g + 1];
-  if (gdir[g]) {
-    for (int k = a; k < b; ++k) v[gidx[k]] = 0;
-    return;
-  }
-  R s = 0;
-  for (int k = a; k < b; ++k) s += v[gidx[k]];
-  v[gidx[a]] = s;
-  for (int k = a + 1; k < b; ++k) v[gidx[k]] = 0;
-}
-
-// The same GlobalSum + Mask with the two-copy groups (shared edge nodes, the large majority) as a flat pair list
-// -- one thread per pair, no group-pointer indirection -- and the remaining groups (corner nodes, Dirichlet
-// nodes) in CSR form, one thread per group; sums in the same order, so the result equals cg_dss_mask's.
+// GlobalSum + Mask over the shared-node groups: the two-copy groups as pairs, the others as CSR groups.
 constexpr int kDssPairsPerThread = 8;
 
 template <typename R>
@@ -1048,6 +1029,10 @@ struct self_cg2d {
     int nodes_mode = -1;  // SELF_PC_NODES_* the operands were built for
     DevBuf<int> src, gptr, gidx;
     DevBuf<unsigned char> gdir, lprim, dlift;
+    DevBuf<int2> dss_pairs;  // the groups in the pair + CSR form of cg_dss_mask_pairs
+    DevBuf<int> dss_gptr, dss_gidx;
+    DevBuf<unsigned char> dss_gdir;
+    int dss_npairs = 0, dss_nrest = 0;
     DevBuf<double> fac64, rl, ul, vl, vl2, zl, rd;
     DevBuf<float> fac32, rl32, ul32, vl32, vl2_32, zl32, rd32;
     DevBuf<selfgpu::cg::CGScalars> SL;
@@ -1248,6 +1233,10 @@ struct PcRun {
   const int *src, *gptr, *gidx;  // the linear mesh's primary-copy gather and groups
   const unsigned char *gdir, *lprim, *dlift;
   int ngroups, iters;
+  const int2* pairs;  // the groups in the pair + CSR form
+  const int *pgptr, *pgidx;
+  const unsigned char* pgdir;
+  int npairs, nrest;
   R *rl, *ul, *vl, *vl2, *zl, *rd;  // rd: Dirichlet lift, null when the linear mesh needs none
   CGScalars* SL;
 };
@@ -1265,7 +1254,9 @@ int pc_linear_apply(self_cg2d* h, const R* r, const PcRun<R>& pc) {
     int rc = launch_q1<R>(h, pc.rl, lo, ln, pc.src, pc.rd, pc.fac, pc.zl, pc.SL);
     if (rc) return rc;
     if (pc.ngroups > 0) {
-      cg_dss_mask<R><<<(pc.ngroups + 255) / 256, 256, 0, st>>>(pc.zl, pc.gptr, pc.gidx, pc.gdir, pc.ngroups);
+      const int nt = (pc.npairs + kDssPairsPerThread - 1) / kDssPairsPerThread + pc.nrest;
+      cg_dss_mask_pairs<R><<<(nt + 255) / 256, 256, 0, st>>>(pc.zl, pc.pairs, pc.npairs, pc.pgptr, pc.pgidx,
+                                                             pc.pgdir, pc.nrest);
       SELF_LAUNCHED(h->ctx);
     }
     using V = typename std::conditional<sizeof(R) == 4, float4, double2>::type;
@@ -1493,6 +1484,34 @@ namespace {
 using namespace selfgpu::cg;
 
 // Shared-node topology: groups and primary-copy gather indices (CGsemElliptic_2D_Class.f90 :350-787)
+// The direct-stiffness groups as cg_dss_mask_pairs reads them: two-copy non-Dirichlet groups as (primary,
+// secondary) pairs, the others as CSR groups (same group order and summation order as the group list).
+int upload_dss(self_ctx* ctx, const std::vector<int>& gptr, const std::vector<int>& gidx,
+               const std::vector<unsigned char>& gdir, int ngroups, DevBuf<int2>& dpairs, DevBuf<int>& dgptr,
+               DevBuf<int>& dgidx, DevBuf<unsigned char>& dgdir, int& npairs, int& nrest) {
+  std::vector<int2> pairs;
+  std::vector<int> rptr(1, 0), ridx;
+  std::vector<unsigned char> rdir;
+  for (int g = 0; g < ngroups; ++g) {
+    const int a = gptr[g], b = gptr[g + 1];
+    if (b - a == 2 && !gdir[g]) {
+      pairs.push_back(make_int2(gidx[a], gidx[a + 1]));
+    } else {
+      for (int k = a; k < b; ++k) ridx.push_back(gidx[k]);
+      rptr.push_back((int)ridx.size());
+      rdir.push_back(gdir[g]);
+    }
+  }
+  npairs = (int)pairs.size();
+  nrest = (int)rdir.size();
+  int rc;
+  if (!pairs.empty() && (rc = upload(ctx, dpairs, pairs))) return rc;
+  if ((rc = upload(ctx, dgptr, rptr))) return rc;
+  if (!ridx.empty() && (rc = upload(ctx, dgidx, ridx))) return rc;
+  if (!rdir.empty() && (rc = upload(ctx, dgdir, rdir))) return rc;
+  return SELF_OK;
+}
+
 int compile_topology(self_cg2d* h, const self_cg2d_desc* d) {
   const int n = h->n, N = h->N;
   const size_t NN = (size_t)n * n;
@@ -1570,26 +1589,8 @@ int compile_topology(self_cg2d* h, const self_cg2d_desc* d) {
   if ((rc = upload(h->ctx, h->gptr, h->h_gptr))) return rc;
   if ((rc = upload(h->ctx, h->gidx, h->h_gidx))) return rc;
   if ((rc = upload(h->ctx, h->gdir, h->h_gdir))) return rc;
-  std::vector<int2> pairs;
-  std::vector<int> rptr(1, 0), ridx;
-  std::vector<unsigned char> rdir;
-  for (int g = 0; g < h->ngroups; ++g) {
-    const int a = h->h_gptr[g], b = h->h_gptr[g + 1];
-    if (b - a == 2 && !h->h_gdir[g]) {
-      pairs.push_back(make_int2(h->h_gidx[a], h->h_gidx[a + 1]));
-    } else {
-      for (int k = a; k < b; ++k) ridx.push_back(h->h_gidx[k]);
-      rptr.push_back((int)ridx.size());
-      rdir.push_back(h->h_gdir[g]);
-    }
-  }
-  h->dss_npairs = (int)pairs.size();
-  h->dss_nrest = (int)rdir.size();
-  if (!pairs.empty() && (rc = upload(h->ctx, h->dss_pairs, pairs))) return rc;
-  if ((rc = upload(h->ctx, h->dss_gptr, rptr))) return rc;
-  if (!ridx.empty() && (rc = upload(h->ctx, h->dss_gidx, ridx))) return rc;
-  if (!rdir.empty() && (rc = upload(h->ctx, h->dss_gdir, rdir))) return rc;
-  return SELF_OK;
+  return upload_dss(h->ctx, h->h_gptr, h->h_gidx, h->h_gdir, h->ngroups, h->dss_pairs, h->dss_gptr, h->dss_gidx,
+                    h->dss_gdir, h->dss_npairs, h->dss_nrest);
 }
 
 // Folded element factors, Jacobi diagonal; FP64 master copy, FP32 copy for the inner solves.
@@ -2040,7 +2041,9 @@ int pcl_ensure(self_cg2d* h, bool fp32, int nodes_mode) {
     if ((rc = upload(ctx, P.src, src)) || (rc = upload(ctx, P.lprim, lprim))) return rc;
     if (P.lift && (rc = upload(ctx, P.dlift, dlift))) return rc;
     if (P.ngroups > 0 &&
-        ((rc = upload(ctx, P.gptr, gptr)) || (rc = upload(ctx, P.gidx, gidx)) || (rc = upload(ctx, P.gdir, gdir))))
+        ((rc = upload(ctx, P.gptr, gptr)) || (rc = upload(ctx, P.gidx, gidx)) || (rc = upload(ctx, P.gdir, gdir)) ||
+         (rc = upload_dss(ctx, gptr, gidx, gdir, P.ngroups, P.dss_pairs, P.dss_gptr, P.dss_gidx, P.dss_gdir,
+                          P.dss_npairs, P.dss_nrest))))
       return rc;
     if (P.SL.n == 0 && P.SL.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "allocation failed");
     P.built = true;
@@ -2063,12 +2066,14 @@ template <>
 PcRun<double> pcl_run<double>(self_cg2d* h, int iters) {
   auto& P = h->pcl;
   return PcRun<double>{P.fac64.p, P.src.p, P.gptr.p, P.gidx.p, P.gdir.p, P.lprim.p, P.dlift.p, P.ngroups, iters,
+                       P.dss_pairs.p, P.dss_gptr.p, P.dss_gidx.p, P.dss_gdir.p, P.dss_npairs, P.dss_nrest,
                        P.rl.p, P.ul.p, P.vl.p, P.vl2.p, P.zl.p, P.lift ? P.rd.p : nullptr, P.SL.p};
 }
 template <>
 PcRun<float> pcl_run<float>(self_cg2d* h, int iters) {
   auto& P = h->pcl;
   return PcRun<float>{P.fac32.p, P.src.p, P.gptr.p, P.gidx.p, P.gdir.p, P.lprim.p, P.dlift.p, P.ngroups, iters,
+                      P.dss_pairs.p, P.dss_gptr.p, P.dss_gidx.p, P.dss_gdir.p, P.dss_npairs, P.dss_nrest,
                       P.rl32.p, P.ul32.p, P.vl32.p, P.vl2_32.p, P.zl32.p, P.lift ? P.rd32.p : nullptr, P.SL.p};
 }
 
