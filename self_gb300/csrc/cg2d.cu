@@ -220,12 +220,14 @@ struct CGScalars {
 
 // ---------------------------------------------------------------------------------- fused (P)CG iteration
 // One iteration is three launches, captured in a CUDA graph of several iterations:
-//   pcg_apply_fused : v_new = w + beta v_old (beta = num/den, v_new = w on the first iteration), z = L(v_new)
-//                     per element (before the direct-stiffness sum), partial sums of <v_new, z>;
-//   cg_dss_mask     : z = Mask(GlobalSum(z)) (one thread per shared-node group; folding the group sums into the
-//                     update kernel, one node per thread, measured slower: dependent scattered loads);
-//   pcg_update_fused: a = num/<v,z>, u += a v, r -= a z, w = dinv r, partial sums of <r,w> and <r,r>, and the
-//                     end-of-iteration scalar update (den = num, num = <r,w>, ||r||, stop tests).
+//   pcg_apply_fused (FP32: _f32, FP64: _eo line forms): v_new = w + beta v_old (beta = num/den, v_new = w on the
+//                     first iteration), z = L(v_new) per element (before the direct-stiffness sum), partial sums
+//                     of <v_new, z>;
+//   cg_dss_mask_pairs: z = Mask(GlobalSum(z)) (pairs of two-copy groups, CSR for the rest; folding the group sums
+//                     into the update kernel, one node per thread, measured slower: dependent scattered loads);
+//   pcg_update_fused (_vec: 16-byte node groups): a = num/<v,z>, u += a v, r -= a z, w = dinv r, partial sums of
+//                     <r,w> and <r,r>, and the end-of-iteration scalar update (den = num, num = <r,w>, ||r||, stop
+//                     tests).
 // <v, Mask(GlobalSum(Lv))> equals the element-local sum of v(src[l]) * (Lv)_l because v is zero on Dirichlet
 // nodes and on non-primary copies.  The grid-wide sums are deterministic: every block writes its partial, and the
 // last block to finish (atomic ticket) adds the partials in block order and updates the scalars.

@@ -16,7 +16,7 @@
 // of its E, N, NE and NW neighbours; the W, S, SW and SE coefficients are those of the neighbour in the opposite
 // direction (symmetry).  Per node this is 9 multiply-adds: the FP64 pipe, far narrower than the FP32 one on this
 // part, bounds the FP64 form, so the fluxes are not recomputed at every sub-quad corner.
-// One inner CG iteration is three launches (q1_apply_fused, cg_dss_mask with the linear groups, pcl_update);
+// One inner CG iteration is three launches (q1_apply_fused, cg_dss_mask_pairs with the linear groups, pcl_update);
 // pcl_start maps the outer residual in and pc_num forms w, <r, w> and the outer beta from the inner solution.
 // Dirichlet lift: the reference's inner CG keeps the mapped residual's values on the linear mesh's Dirichlet nodes
 // (w = r, v = w + c v, and MatrixAction's UnMask skips Dirichlet nodes), so every matrix action sees those values
