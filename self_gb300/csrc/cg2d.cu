@@ -1263,7 +1263,9 @@ int pc_linear_apply(self_cg2d* h, const R* r, const PcRun<R>& pc) {
     }
     using V = typename std::conditional<sizeof(R) == 4, float4, double2>::type;
     constexpr int L = sizeof(V) / sizeof(R);
-    if (h->nl % L == 0 && aligned16(pc.ul) && aligned16(pc.rl) && aligned16(ln) && aligned16(pc.zl)) {
+    // FP32 only: the double2 form measured 39.6 against 36.8 us per launch for the scalar FP64 kernel
+    if (sizeof(R) == 4 && h->nl % L == 0 && aligned16(pc.ul) && aligned16(pc.rl) && aligned16(ln) &&
+        aligned16(pc.zl)) {
       pcl_update_vec<R, V><<<h->nblk, kRedThreads, 0, st>>>(
           reinterpret_cast<V*>(pc.ul), reinterpret_cast<V*>(pc.rl), reinterpret_cast<const V*>(ln),
           reinterpret_cast<const V*>(pc.zl), h->nl / L, h->S.p, pc.SL, h->partial.p, h->ticket.p);
