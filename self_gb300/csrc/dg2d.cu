@@ -113,8 +113,10 @@ struct SWFlux {
       f[1] = A::mul(0.5, A::sub(a1, A::mul(fac, A::sub(vR, vL))));
       f[2] = A::mul(0.5, A::sub(a2, A::mul(fac, A::sub(pR, pL))));
     } else {
-      const double ipR = 1.0 / pR, ipL = 1.0 / pL;
-      const double cR = sqrt(g * pR), cL = sqrt(g * pL);
+      // depths are positive: one reciprocal square root per side gives 1/H and sqrt(g H) = sqrt(g) H / sqrt(H)
+      const double rR = rsqrt(pR), rL = rsqrt(pL), sg = sqrt(g);
+      const double ipR = rR * rR, ipL = rL * rL;
+      const double cR = sg * (pR * rR), cL = sg * (pL * rL);
       const double wR = uOut * ipR, wL = uIn * ipL;
       const double fac = fmax(fmax(fabs(wR + cR), fabs(wR - cR)), fmax(fabs(wL + cL), fabs(wL - cL)));
       const double a0 = wR * uR + 0.5 * g * pR * pR * nx + wL * uL + 0.5 * g * pL * pL * nx;
