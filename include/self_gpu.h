@@ -4,7 +4,7 @@
  * It replaces the compute procedures of SELF's Fortran types (lileipku00/SELF) on the
  * spectral-element hot path.  Every entry point is extern "C", takes plain pointers and sizes,
  * and returns an int status (SELF_OK = 0, negative = error; self_last_error() gives the text).
- * A Fortran ISO_C_BINDING interface to these functions is listed in INTEGRATION.md.
+ * A Fortran ISO_C_BINDING module binds these functions one to one.
  *
  * Array conventions are the Fortran ones, so arrays pass without reordering:
  *   matrices     D(i,j) at D[i + j*n], n = N+1 (column major, as DOUBLE D(0:N,0:N))
@@ -68,19 +68,8 @@ int self_ctx_destroy(self_ctx* ctx);
 int self_last_error(const self_ctx* ctx, char* buf, size_t len);
 const char* self_status_string(int status);
 int self_ctx_synchronize(self_ctx* ctx);
-/* number of kernels this context launched so far (for launch accounting) */
-long long self_ctx_kernel_launches(const self_ctx* ctx);
-/* CUDA-event timer on the context's stream: start records an event, stop records a second one,
- * synchronises and returns the elapsed milliseconds between them. */
-int self_ctx_timer_start(self_ctx* ctx);
-int self_ctx_timer_stop(self_ctx* ctx, double* ms);
 /* 1 when all work enqueued on the context's stream has completed, 0 otherwise (cudaStreamQuery). */
 int self_ctx_query(self_ctx* ctx);
-/* Overwrite a scratch buffer of `bytes` on the context's stream (evicts L2 between timed steps). */
-int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
-/* Measured fused-multiply-add rate of the device (TFLOP/s, FP64 when fp64 != 0 else FP32): the compute
- * roofline used for kernels bound by the FP64 pipe. */
-int self_probe_fma_peak(self_ctx* ctx, int fp64, double* tflops);
 /* Page-locked, device-mapped host memory for host<->device transfers at full link speed.  State arrays in such a
  * block are read and written by the conversion kernels directly (no staging copy). */
 int self_host_alloc(size_t bytes, void** ptr);
@@ -143,10 +132,6 @@ int self_dg2d_rk3_async(self_dg2d* h, double tn, int nsteps);
 long long self_dg2d_bytes(const self_dg2d* h);
 /* Device address of the resident state (FP64: double, FP32: float perturbation form). */
 int self_dg2d_state_device(self_dg2d* h, void** dptr, size_t* bytes);
-/* Measurement helper: average CUDA-event time (ms) of one launch of each kernel of an RK stage, each launch
- * preceded by an L2 flush of flush_bytes; the resident state is restored afterwards.
- * ms[0] = edge-flux kernel, ms[1] = volume + RK-update kernel. */
-int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* ms);
 
 /* Known answer helpers for the shallow-water set-up (host, FP64):
  * CalculateBathymetryGradient (ConservativeShallowWaterClass.f90:1733-1868). */
@@ -292,15 +277,35 @@ int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* elements_per_ti
 /* ---------------------------------------------------------------- dot product without allocation
  * No counterpart in the reference.  For callers that cannot allocate device memory where they need an inner
  * product -- Fortran codes whose device arrays live in their own OpenACC / CUDA Fortran data regions and forbid
- * allocation inside the time loop, code running while a stream is captured into a CUDA graph, latency-bound
- * loops -- this computes result = sum_k x[k]*y[k] in FP64 on the current device with the same two-pass tile
- * reduction as self_cg2d_dot, keeping its partial sums in a fixed static device array (32 KiB, held by every
- * GPU that loads the library until exit) instead of cudaMalloc'd memory.  x, y (n doubles) and result (one
- * double) are device pointers; stream may be NULL.  n <= 67,108,864 (4096 partials x 16384 elements), larger n
- * returns SELF_ERR_INVALID.  The call allocates nothing; its first call on a device looks up the array's
- * address and should come before any stream capture.  Calls that overlap on the GPU share the array and race;
- * serialise them.  Errors: self_last_error(NULL, ...). */
+ * allocation inside the time loop, latency-bound loops that cannot take an allocation stall -- this computes
+ * result = sum_k x[k]*y[k] in FP64 on the current device: a two-pass reduction over contiguous tiles of 16384
+ * elements, deterministic for a given n and equal to self_cg2d_dot up to rounding, whose partial sums live in a
+ * fixed static device array (32 KiB, held by every GPU that loads the library until exit) instead of
+ * cudaMalloc'd memory.  x, y (n doubles) and result (one double) are device pointers; stream may be NULL.
+ * n <= 67,108,864 (4096 partials x 16384 elements); larger n returns SELF_ERR_INVALID.  The call allocates
+ * nothing; its first call in a CUDA context looks up the array's address there (a new context, e.g. after
+ * cudaDeviceReset, looks it up again).  Calls that overlap on the GPU share the array and race; serialise them.
+ * An error left pending by earlier work is reported, not cleared.  Errors: self_last_error(NULL, ...). */
 int self_dot_noalloc(const double* x, const double* y, long long n, double* result, void* stream);
+
+/* ---------------------------------------------------------------- measurement helpers
+ * Not part of the drop-in (no reference counterpart): launch accounting, timers, L2 eviction and peak probes used
+ * to measure the entry points above. */
+/* number of kernels this context launched so far (for launch accounting) */
+long long self_ctx_kernel_launches(const self_ctx* ctx);
+/* CUDA-event timer on the context's stream: start records an event, stop records a second one,
+ * synchronises and returns the elapsed milliseconds between them. */
+int self_ctx_timer_start(self_ctx* ctx);
+int self_ctx_timer_stop(self_ctx* ctx, double* ms);
+/* Overwrite a scratch buffer of `bytes` on the context's stream (evicts L2 between timed steps). */
+int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
+/* Measured fused-multiply-add rate of the device (TFLOP/s, FP64 when fp64 != 0 else FP32): the compute
+ * roofline used for kernels bound by the FP64 pipe. */
+int self_probe_fma_peak(self_ctx* ctx, int fp64, double* tflops);
+/* Average CUDA-event time (ms) of one launch of each kernel of an RK stage, each launch preceded by an L2 flush
+ * of flush_bytes; the resident state is restored afterwards.  ms[0] = edge-flux kernel, ms[1] = volume +
+ * RK-update kernel. */
+int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* ms);
 
 #ifdef __cplusplus
 }

@@ -1,11 +1,14 @@
-// Dot product that allocates nothing: the FP64 two-pass reduction of self_cg2d_dot, with its per-tile
-// partial sums kept in a fixed device array of this file instead of memory obtained from cudaMalloc.
+// Dot product that allocates nothing: an FP64 two-pass reduction over contiguous tiles whose per-tile partial
+// sums live in a fixed device array of this file instead of memory obtained from cudaMalloc.
 //
 // Some callers cannot allocate device memory at the point where they need a norm or an inner product:
 // Fortran codes whose device arrays live in their own OpenACC / CUDA Fortran data regions and that forbid
-// allocation inside the time loop, code that runs while a stream is being captured into a CUDA graph (where
-// cudaMalloc is not permitted), and latency-bound loops where an allocation stall is not acceptable.  They pass
-// device pointers for the inputs and the output; the scratch is this file's array.
+// allocation inside the time loop, and latency-bound loops where an allocation stall is not acceptable.  They
+// pass device pointers for the inputs and the output; the scratch is this file's array.
+//
+// Result: sum over tiles (in tile order per thread, then a fixed tree) of the tile sums; deterministic for a
+// given n, and equal to self_cg2d_dot on the same vectors up to rounding (that entry point sums in a different
+// order, grid-stride per block).
 //
 // Limits and sharing:
 //  * the array holds kMaxTiles = 4096 partial sums (32 KiB); each tile covers kTile = 16384 elements, so
@@ -15,8 +18,10 @@
 //  * the array is shared by every call on a device: two calls whose kernels overlap on the GPU (different
 //    streams, or different host threads) race on it, so the caller serialises them;
 //  * every GPU that loads the library holds the array until the process exits;
-//  * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
-//    current; make that first call before any stream capture.
+//  * the first call in a CUDA context looks up the array's device address (cudaGetSymbolAddress) with that
+//    context's device current; the address is kept per context (keyed by the driver's context ID), so a new
+//    context on the same device -- after cudaDeviceReset, say -- looks it up again on its first call.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -66,26 +71,81 @@ __global__ void __launch_bounds__(kThreads) dot_finish(const double* __restrict_
   }
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_scratch[kMaxDevices] = {};
+// Driver entry points for the current context's ID, fetched through the runtime (no link against libcuda).
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
 
-// Device address of g_dot_partials on the current device (looked up once per device).
-int scratch_address(int dev, double** out) {
+constexpr int kMaxContexts = 64;
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
+std::mutex g_mu;
+ScratchEntry g_scratch[kMaxContexts];
+int g_nscratch = 0;
+PfnCtxGetCurrent g_get_current = nullptr;
+PfnCtxGetId g_get_id = nullptr;
+
+void fail(const char* what, cudaError_t e) {
+  char msg[320];
+  snprintf(msg, sizeof(msg), "self_dot_noalloc: %s: %s", what, cudaGetErrorString(e));
+  selfgpu::set_global_error(msg);
+}
+
+// Device address of g_dot_partials in the current context (looked up once per context).
+int scratch_address(double** out) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_dot_partials);
-    if (e != cudaSuccess || !p) {
-      char msg[256];
-      snprintf(msg, sizeof(msg), "self_dot_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-               cudaGetErrorString(e));
-      selfgpu::set_global_error(msg);
+  if (!g_get_current || !g_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&g_get_current, 12000,
+                                                      cudaEnableDefault, &q1);
+    cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&g_get_id, 12000, cudaEnableDefault,
+                                                      &q2);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !g_get_current || !g_get_id) {
+      g_get_current = nullptr;
+      g_get_id = nullptr;
+      fail("driver entry points for the context ID are unavailable", e1 != cudaSuccess ? e1 : e2);
       return SELF_ERR_CUDA;
     }
-    g_scratch[dev] = static_cast<double*>(p);
   }
-  *out = g_scratch[dev];
+  // the current context: the caller's, or (none current yet) the primary context of the current device, which
+  // the runtime makes current on its first call (here the symbol lookup)
+  CUcontext cu = nullptr;
+  void* p = nullptr;
+  if (g_get_current(&cu) != CUDA_SUCCESS) cu = nullptr;
+  if (!cu) {
+    cudaError_t e = cudaGetSymbolAddress(&p, g_dot_partials);
+    if (e != cudaSuccess || !p) {
+      fail("cudaGetSymbolAddress of the scratch array failed", e);
+      return SELF_ERR_CUDA;
+    }
+    if (g_get_current(&cu) != CUDA_SUCCESS) cu = nullptr;
+  }
+  unsigned long long id = 0;
+  if (!cu || g_get_id(cu, &id) != CUDA_SUCCESS) {
+    selfgpu::set_global_error("self_dot_noalloc: cannot read the current CUDA context's ID");
+    return SELF_ERR_CUDA;
+  }
+  for (int k = 0; k < g_nscratch; ++k)
+    if (g_scratch[k].ctx_id == id) {
+      *out = g_scratch[k].addr;
+      return SELF_OK;
+    }
+  if (!p) {
+    cudaError_t e = cudaGetSymbolAddress(&p, g_dot_partials);
+    if (e != cudaSuccess || !p) {
+      fail("cudaGetSymbolAddress of the scratch array failed", e);
+      return SELF_ERR_CUDA;
+    }
+  }
+  // a full table drops its oldest entry (contexts that long outlived are the likeliest to be gone)
+  if (g_nscratch == kMaxContexts) {
+    for (int k = 1; k < kMaxContexts; ++k) g_scratch[k - 1] = g_scratch[k];
+    --g_nscratch;
+  }
+  g_scratch[g_nscratch++] = {id, static_cast<double*>(p)};
+  *out = static_cast<double*>(p);
   return SELF_OK;
 }
 
@@ -105,14 +165,14 @@ extern "C" int self_dot_noalloc(const double* x, const double* y, long long n, d
     selfgpu::set_global_error(msg);
     return SELF_ERR_INVALID;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    selfgpu::set_global_error("self_dot_noalloc: no current CUDA device");
+  // an error left pending by earlier, unrelated work is reported as such and not blamed on this call
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    fail("an earlier CUDA error is pending (not from this call); nothing was launched", e);
     return SELF_ERR_CUDA;
   }
   double* partials = nullptr;
-  int rc = scratch_address(dev, &partials);
+  int rc = scratch_address(&partials);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int ntiles = (int)((n + kTile - 1) / kTile);
@@ -120,9 +180,7 @@ extern "C" int self_dot_noalloc(const double* x, const double* y, long long n, d
   dot_finish<<<1, kThreads, 0, st>>>(partials, ntiles, result);
   e = cudaGetLastError();
   if (e != cudaSuccess) {
-    char msg[256];
-    snprintf(msg, sizeof(msg), "self_dot_noalloc: launch failed: %s", cudaGetErrorString(e));
-    selfgpu::set_global_error(msg);
+    fail("launch failed", e);
     return SELF_ERR_CUDA;
   }
   return SELF_OK;

@@ -5,11 +5,15 @@ Source (reference output files, read as text, run in the build container where t
   examples/elliptic1d/parabola/run/elliptic.curve  -- solution x, u at the GLL nodes
   examples/elliptic1d/parabola/run/runtime.params  -- the namelist that produced them
 The fixtures keep the numbers verbatim (residual lines up to the first zero entry after convergence).
+
+    python tests/golden/extract_reference_curves.py /path/to/reference
 """
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/extract_reference_curves.py /path/to/reference")
+REF = sys.argv[1]
 OUT = os.path.dirname(os.path.abspath(__file__))
 run = os.path.join(REF, "examples", "elliptic1d", "parabola", "run")
 

@@ -13,7 +13,9 @@ FILES = {"square.mesh": "examples/cgsem-elliptic2d/paraboloid/run/square.mesh",
          "box.mesh": "examples/shallowwater/dipole/run/box.mesh"}
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/extract_reference_meshes.py /path/to/reference")
+    ref = sys.argv[1]
     for name, rel in FILES.items():
         shutil.copyfile(os.path.join(ref, rel), os.path.join(HERE, name))
         print(name, os.path.getsize(os.path.join(HERE, name)), "bytes")

@@ -1,7 +1,8 @@
-"""self_dot_noalloc: the dot product for callers that cannot allocate device memory (their arrays live in
-their own device data regions, or they run inside a CUDA graph capture).  It must give the same inner product
-as the existing DotProduct entry point (self_cg2d_dot) on the same masked vectors, on two calls in a row that
-share its static scratch array, and reject lengths beyond its scratch limit.  Collected last on purpose."""
+"""self_dot_noalloc: the dot product for callers that cannot allocate device memory where they need it (their
+device arrays live in their own OpenACC / CUDA Fortran data regions that forbid allocation in the time loop).
+It must give the same inner product as the existing DotProduct entry point (self_cg2d_dot) on the same masked
+vectors, on two calls in a row that share its static scratch array; sum many tiles with a partial last tile as
+an FP64 dot does; and reject lengths beyond its scratch limit.  Collected last on purpose."""
 import ctypes as C
 
 import numpy as np
@@ -45,6 +46,25 @@ def test_dot_noalloc_matches_dotproduct_two_calls(gpu_ctx):
         torch.cuda.synchronize()
         got = res.item()
         assert abs(got - expected) <= 1e-12 * np.sum(np.abs(um * vm)), (call, got, expected)
+
+
+def test_dot_noalloc_many_tiles_partial_tail(gpu_ctx):
+    """n spans several 16384-element tiles plus a partial one, so the partials of many blocks are indexed and
+    summed; two calls in a row with different data and lengths reuse the scratch."""
+    torch = pytest.importorskip("torch")
+    from self_gb300 import _native as nat
+    dot = _fn()
+    rng = np.random.default_rng(7)
+    res = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for n in (3 * 16384 + 17, 37 * 16384 + 1):
+        x, y = rng.normal(size=n), rng.normal(size=n)
+        xd, yd = torch.from_numpy(x).to("cuda"), torch.from_numpy(y).to("cuda")
+        torch.cuda.synchronize()
+        rc = dot(xd.data_ptr(), yd.data_ptr(), n, res.data_ptr(), None)
+        assert rc == 0, nat.last_error()
+        torch.cuda.synchronize()
+        expected = float(np.dot(x, y))
+        assert abs(res.item() - expected) <= 1e-12 * float(np.sum(np.abs(x * y))), (n, res.item(), expected)
 
 
 def test_dot_noalloc_rejects_length_beyond_scratch(gpu_ctx):
