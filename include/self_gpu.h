@@ -306,6 +306,12 @@ int self_probe_fma_peak(self_ctx* ctx, int fp64, double* tflops);
  * of flush_bytes; the resident state is restored afterwards.  ms[0] = edge-flux kernel, ms[1] = volume +
  * RK-update kernel. */
 int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* ms);
+/* Failure-detection test hook (no reference counterpart): arms the bounded bulk-copy waits of the fused FP32
+ * shallow-water stage (N = 7) for the next self_dg2d_rk3 call only.  In that call the first wait of every warp
+ * polls a shared-memory barrier that nothing arrives on, gives up after `polls` polls, drains the warp's copies in
+ * flight with the normal limit and returns without writing; self_dg2d_rk3 then returns SELF_ERR_TIMEOUT and the
+ * handle's state is unchanged.  Other handles: SELF_ERR_UNSUPPORTED. */
+int self_dg2d_test_wait_timeout(self_dg2d* h, int polls);
 
 #ifdef __cplusplus
 }

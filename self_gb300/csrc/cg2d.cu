@@ -2193,6 +2193,11 @@ int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int
         break;
       }
       rcur = G.rc;
+      if (!std::isfinite(rcur)) {  // NaN / Inf in the Arnoldi recurrence: stop with the non-finite status
+        *iters = l;
+        *rel = rcur;
+        return SELF_ERR_NONFINITE;
+      }
       // v_{i+1} = w / h(i+1, i)
       sqrt_scalar<<<1, 1, 0, st>>>(h->gm_H.p + i + 1, h->red.p + 5);
       SELF_LAUNCHED(ctx);
@@ -2313,15 +2318,24 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   R.ioerr = -2;
   int iters = 0;
   double rel = 0, r0 = 0;
+  // a NaN or Inf in the source, the initial guess or the Dirichlet data shows in ||r0||: stop before iterating
+  if ((rc = dots<double>(h, h->r.p, h->r.p, nullptr, nullptr, h->red.p))) return rc;
+  r0 = std::sqrt(read1(h, h->red.p, &rc));
+  if (rc) return rc;
+  if (!std::isfinite(r0)) {
+    R.ioerr = SELF_ERR_NONFINITE;
+    R.r0 = r0;
+    R.rel_residual = r0;
+    if (rep) *rep = R;
+    return set_error(ctx, SELF_ERR_NONFINITE, "non-finite initial residual (NaN or Inf in the source, initial guess "
+                     "or Dirichlet data)");
+  }
   if (gm) {
     R.ioerr = gmres_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, resi, &iters, &rel, &r0,
                            o->method == SELF_SOLVE_PGMRES_JACOBI ? h->op64.dinv.p : nullptr);
     R.outer_iterations = 1;
   } else {
     const bool jac = o->method == SELF_SOLVE_PCG_JACOBI;
-    if ((rc = dots<double>(h, h->r.p, h->r.p, nullptr, nullptr, h->red.p))) return rc;
-    r0 = std::sqrt(read1(h, h->red.p, &rc));
-    if (rc) return rc;
     if (o->precision == SELF_PREC_FP64) {
       DevBuf<double> resi_dev;
       if (resi) {

@@ -1416,6 +1416,14 @@ int self_dg2d_time_kernels(self_dg2d* h, int reps, size_t flush_bytes, double* m
   return SELF_OK;
 }
 
+int self_dg2d_test_wait_timeout(self_dg2d* h, int polls) {
+  if (!h) return SELF_ERR_INVALID;
+  SELF_CUDA_TRY(h->ctx, cudaSetDevice(h->ctx->device));
+  if (h->precision != SELF_PREC_FP32)
+    return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "time-out test hook: fused FP32 stage only");
+  return selfgpu::dg32::arm_wait_timeout(h, h->f32, polls);
+}
+
 int self_dg2d_rk3(self_dg2d* h, double tn, int nsteps) {
   int rc = self_dg2d_rk3_async(h, tn, nsteps);
   if (rc) return rc;

@@ -23,6 +23,8 @@ int rk3(self_dg2d* h, State* s, double tn, int nsteps);
 int time_kernels(self_dg2d* h, State* s, int reps, size_t flush_bytes, double* ms);
 // reports a bounded-wait time-out recorded by the fused stage kernel (after synchronisation)
 int sync_and_check(self_dg2d* h, State* s);
+// time-out test hook of the fused stage: the next call's first bulk-copy wait of every warp runs out after `polls`
+int arm_wait_timeout(self_dg2d* h, State* s, int polls);
 // 1 when the fused TMA-pipelined stage is in use
 int is_fused(State* s);
 long long bytes(const State* s);

@@ -46,6 +46,7 @@ struct FusedArgs {
   float* bs_out;         // traces of the new state
   int* err;              // error flag (time-out)
   int nEl, naux, has_drag, has_relax, mode;  // mode 1: G = tend, 2: G = a G + tend
+  int probe_polls;       // time-out test hook: polls of the first wait on a barrier nothing arrives on (0 = off)
   float g, drag, a, gdt;
 };
 
@@ -144,7 +145,8 @@ struct alignas(16) WarpSmem {
   ESide es[NBUF][4];
   float sB[4 * 3 * N1];  // side fluxes, same order
   uint64_t bar[NBUF];
-  uint64_t pad[NBUF & 1];
+  uint64_t probe;  // initialised, never arrived on: the wait of the time-out test hook runs out on it
+  uint64_t pad[(NBUF + 1) & 1];
 };
 
 template <int N1, int NBUF, int W>
@@ -206,6 +208,7 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
   }
   if (lane == 0) {
     for (int b = 0; b < NBUF; ++b) mbar_init(&ws.bar[b], 1);
+    mbar_init(&ws.probe, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();  // the only block-wide barrier: constants and barrier initialisation
@@ -301,7 +304,10 @@ __global__ void __launch_bounds__(32 * W, 4) sw32_fused(FusedArgs A, FConst<N1> 
         es_next = load_es(ef + nwarps);
       }
     }
-    const bool ok = mbar_wait(&ws.bar[b], (uint32_t)((it / NBUF) & 1), kMaxSpin);
+    // time-out test hook (0 in normal runs): the first wait of every warp polls a barrier nothing arrives on, runs
+    // out after A.probe_polls polls and takes the time-out path below
+    const bool ok = (A.probe_polls > 0 && it == 0) ? mbar_wait(&ws.probe, 0u, A.probe_polls)
+                                                   : mbar_wait(&ws.bar[b], (uint32_t)((it / NBUF) & 1), kMaxSpin);
     if (!__all_sync(0xffffffffu, ok)) {
       if (lane == 0) atomicExch(A.err, 1);
       // drain: a second bounded wait on every buffer with copies in flight, then leave
