@@ -1,9 +1,11 @@
-"""Extract the golden vectors shipped with the reference's 1-D CGSEM example into tests/golden/.
+"""Extract the golden vectors shipped with the reference's examples into tests/golden/.
 
 Source (reference output files, read as text, run in the build container where the reference is mounted):
   examples/elliptic1d/parabola/run/residual.curve  -- CG residual history (N=5, 10 elements, tol 1e-8)
   examples/elliptic1d/parabola/run/elliptic.curve  -- solution x, u at the GLL nodes
   examples/elliptic1d/parabola/run/runtime.params  -- the namelist that produced them
+  examples/shallowwater/dipole/run/Energies.0000000000.curve -- KE and PE of the dipole run at t = 0, 500, 1000
+  examples/shallowwater/dipole/run/shallowwater.params      -- the namelist shipped beside it
 The fixtures keep the numbers verbatim (residual lines up to the first zero entry after convergence).
 
     python tests/golden/extract_reference_curves.py /path/to/reference
@@ -30,4 +32,7 @@ sol = open(os.path.join(run, "elliptic.curve")).read().split("#source")[0]
 open(os.path.join(OUT, "elliptic1d_solution.curve"), "w").write(sol)
 params = open(os.path.join(run, "runtime.params")).read()
 open(os.path.join(OUT, "elliptic1d_runtime.params"), "w").write(params)
-print("wrote", len(keep), "residual lines")
+dip = os.path.join(REF, "examples", "shallowwater", "dipole", "run")
+open(os.path.join(OUT, "dipole_energies.curve"), "w").write(open(os.path.join(dip, "Energies.0000000000.curve")).read())
+open(os.path.join(OUT, "dipole_shallowwater.params"), "w").write(open(os.path.join(dip, "shallowwater.params")).read())
+print("wrote", len(keep), "residual lines and the dipole energy curve")
