@@ -285,10 +285,11 @@ def _e2e(nat, L, ctx, sw, dof, steps, dist):
 
 
 # ------------------------------------------------------------------------------------------ elliptic legs
-def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=3000):
+def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=20000):
     """256x256 N=7 variable-coefficient Helmholtz (k = 1 + 0.5 sin 4pi x cos 4pi y, lambda = 0.1, Dirichlet 0,
-    Jacobi): plain FP64 PCG vs FP32-inner PCG under FP64 refinement, both to ||r||/||r0|| < 1e-10; GMRES(30) on the
-    advection-diffusion operator (v = (1, 0.5), kappa = 1e-3)."""
+    Jacobi): plain FP64 PCG vs FP32-inner PCG under FP64 refinement, both to ||r||/||r0|| < 1e-10; GMRES(30) and
+    Jacobi-preconditioned flexible GMRES(30) on the advection-diffusion operator (v = (1, 0.5), kappa = 1e-3) to
+    1e-10, FP64 and FP32-inner under FP64 refinement."""
     from self_gb300 import workloads as W
     from self_gb300 import _native as nat
     nod = sg.NodalStorage_2D(N, nat.GAUSS_LOBATTO, nat.CG)
@@ -332,13 +333,23 @@ def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=3000):
     out["pcg_linear_fp64"]["preconditioner_setup_seconds"] = setup
     cg.Trash()
     ad = sg.CGsemElliptic_2D(ctx, nod, mesh, np.full_like(k, 1e-3), lam=0.0, op=1, vel=(1.0, 0.5))
-    for method, key in (("gmres", "gmres30_fp64"), ("pgmres", "pgmres30_jacobi_fp64")):
+    ref = None
+    for method, prec in (("gmres", "fp64"), ("gmres", "fp32"), ("pgmres", "fp64"), ("pgmres", "fp32")):
+        key = ("gmres30_" if method == "gmres" else "pgmres30_jacobi_") + prec
+        ad.Solve(source, method=method, precision=prec, m=30, tolerance=1e-10, maxIters=60)  # warm-up
+        ctx.synchronize()
         t0 = time.perf_counter()
-        sol, rep = ad.Solve(source, method=method, m=30, tolerance=1e-10, maxIters=gmres_iters)
+        sol, rep = ad.Solve(source, method=method, precision=prec, m=30, tolerance=1e-10, maxIters=gmres_iters)
         el = time.perf_counter() - t0
-        out[key] = {"seconds": el, "arnoldi_steps": rep["iterations"], "ms_per_step": 1e3 * el / max(1, rep["iterations"]),
+        out[key] = {"seconds": el, "solves_per_s": 1.0 / el, "arnoldi_steps": rep["iterations"],
+                    "ms_per_step": 1e3 * el / max(1, rep["iterations"]), "refinement_steps": rep["outer_iterations"],
                     "rel_residual": rep["rel_residual"], "ioerr": rep["ioerr"],
                     "operator": "-kappa Lap u + v.grad u, kappa 1e-3, v (1, 0.5)"}
+        if ref is None:
+            ref = sol
+        else:
+            out[key]["max_rel_diff_vs_gmres30_fp64"] = float(np.abs(sol - ref).max() / np.abs(ref).max())
+    out["speedup_gmres_fp32_ir_vs_fp64"] = out["gmres30_fp64"]["seconds"] / out["gmres30_fp32"]["seconds"]
     ad.Trash()
     return out, (nod, mesh, k, source)
 

@@ -205,8 +205,8 @@ __global__ void __launch_bounds__(kRedThreads) reduce_partials(const double* __r
 // ---------------------------------------------------------------------------------- CG scalar logic
 // Device scalar state of one GMRES cycle.
 struct GMScalars {
-  double r0, rc, tol;
-  int i, nr, done, breakdown;
+  double r0, rc, tol;  // r0: ||r0|| of the whole solve (the stop test is relative to it)
+  int i, nr, done, breakdown;  // i: steps of the cycle so far; nr: columns in the solve
 };
 
 // Device scalar state of one (P)CG solve.
@@ -1437,16 +1437,19 @@ namespace cg {
 // the residual estimate (IterativeSolvers_Class.f90:560-600), all in FP64.
 __global__ void gmres_givens(const double* __restrict__ hcol, int i, int m, double* rho, double* c, double* s,
                              double* bhat, GMScalars* G, double* resi, int l) {
-  // hcol[0..i] = h(1..i+1, i+1) ; hcol[i+1] = ||w||
+  if (G->done) return;  // the cycle already stopped: later steps of the enqueued cycle change nothing
+  // hcol[0..i] = h(1..i+1, i+1) ; hcol[i+1] = ||w||^2
   const double hn = sqrt(hcol[i + 1]);
   double* R = rho + (size_t)i * m;  // column i of rho (rho(k, i+1) at R[k])
-  G->nr = i + 1;
+  G->i = i + 1;                     // Arnoldi steps of this cycle so far (the reference's l counts them)
   const double aeps = 2.220446049250313e-16;
-  if (fabs(hn) <= aeps) {  // AlmostEqual(h(i+1,i), 0): lucky breakdown
+  if (fabs(hn) <= aeps) {  // AlmostEqual(h(i+1,i), 0): lucky breakdown, column i stays out of the solve
+    G->nr = i;
     G->breakdown = 1;
     G->done = 1;
     return;
   }
+  G->nr = i + 1;
   R[0] = hcol[0];
   for (int k = 1; k <= i; ++k) {
     const double g = c[k - 1] * R[k - 1] + s[k - 1] * hcol[k];
@@ -1460,8 +1463,22 @@ __global__ void gmres_givens(const double* __restrict__ hcol, int i, int m, doub
   bhat[i + 1] = -s[i] * bhat[i];
   bhat[i] = c[i] * bhat[i];
   G->rc = fabs(bhat[i + 1]);
-  if (resi) resi[l] = G->rc;
+  if (resi && l > 0) resi[l] = G->rc;
+  if (!(G->rc == G->rc) || isinf(G->rc)) {  // non-finite recurrence: stop the cycle, the host reports it
+    G->done = 1;
+    return;
+  }
   if (G->rc / G->r0 <= G->tol) G->done = 1;
+}
+
+// v_{i+1} = w / sqrt(hsq), or zero once the cycle stopped on a breakdown (no division by ~0)
+template <typename R>
+__global__ void gmres_next_basis(R* __restrict__ y, const R* __restrict__ w, const double* __restrict__ hsq,
+                                 const GMScalars* __restrict__ G, size_t n) {
+  const bool zero = G->breakdown != 0;
+  const double f = zero ? 0.0 : 1.0 / sqrt(hsq[0]);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    y[k] = zero ? (R)0 : (R)(f * (double)w[k]);
 }
 
 // back substitution of the triangular system (rho y = bhat) for nr columns
@@ -2106,133 +2123,208 @@ double read1(self_cg2d* h, const double* dptr, int* rc) {
   return v;
 }
 
-// GMRES(m) (IterativeSolvers_Class.f90:493-652) on the device, FP64.  x, r are device vectors; r holds the
-// initial residual.  Returns ioerr; iters = total Arnoldi steps (the reference's l).
-// GMRES(m) of IterativeSolvers_Class.f90:493-652, or with dinv the flexible right-preconditioned GMRES of
-// Solve_PCGMRES (:656-822) with Jacobi: z_i = dinv v_i, w = A z_i, and x += Z y = dinv (V y) at the end of a
-// cycle (the preconditioner is fixed, so the basis Z is not stored).
-int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int maxIters, double tol,
-                 double* resi_host, int* iters, double* rel, double* r0_out, const double* dinv) {
+// One GMRES cycle (IterativeSolvers_Class.f90:520-640) on the device, enqueued whole: up to msteps Arnoldi steps
+// with modified Gram-Schmidt (dots accumulated in FP64) and Givens rotations in FP64, then the back substitution
+// and x += V y (or dinv (V y) for the Jacobi-preconditioned flexible form).  The stop test runs on the device (the
+// Givens kernel sets done; later steps of the enqueued cycle leave the solve unchanged), so the host synchronises
+// once per cycle.  r holds the cycle's starting residual; the basis, matrix action and update are in the
+// precision R (FP64, or FP32 for the inner solves of the refinement form).  G->r0 / G->tol set the relative stop.
+struct CycleOut {
+  int steps, nr, done, breakdown;
+  double rc;
+};
+
+template <typename R>
+int gmres_cycle(self_cg2d* h, R* x, const R* r, int m, int msteps, double r0, double tol, double rcur, R* V, R* w,
+                R* t, const R* dinv, const OpData<R>& od, double* resi_dev, int l0, int maxIters, CycleOut* out) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
   const size_t nl = h->nl;
   int rc;
-  if ((rc = ensure(ctx, h->gm_V, nl * (size_t)(m + 1)))) return rc;
+  // b = ||r|| ; v1 = r / b ; bhat(1) = b
+  if ((rc = dots<R>(h, r, r, nullptr, nullptr, h->red.p))) return rc;
+  sqrt_scalar<<<1, 1, 0, st>>>(h->red.p, h->red.p + 4);
+  SELF_LAUNCHED(ctx);
+  scale_copy<R><<<h->nblk, kRedThreads, 0, st>>>(V, r, h->red.p + 4, 1, nl);
+  SELF_LAUNCHED(ctx);
+  SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->gm_bhat.p, 0, (m + 1) * sizeof(double), st));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->gm_bhat.p, h->red.p + 4, sizeof(double), cudaMemcpyDeviceToDevice, st));
+  SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->gm_rho.p, 0, (size_t)m * m * sizeof(double), st));
+  GMScalars G{};
+  G.r0 = r0;
+  G.tol = tol;
+  G.rc = rcur;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
+  for (int i = 0; i < msteps; ++i) {
+    const R* vi = V + (size_t)i * nl;
+    if (dinv) {  // z_i = PreconditionInvert(v_i)
+      scale_by<R><<<h->nblk, kRedThreads, 0, st>>>(t, vi, dinv, nl);
+      SELF_LAUNCHED(ctx);
+      if ((rc = matrix_action<R>(h, t, w, od))) return rc;
+    } else if ((rc = matrix_action<R>(h, vi, w, od))) {
+      return rc;
+    }
+    // MGS: h(k,i) = <v_k, w>; w -= h(k,i) v_k, the axpy of step k fused with the dot of step k+1
+    if ((rc = dots<R>(h, V, w, nullptr, nullptr, h->gm_H.p))) return rc;
+    for (int k = 0; k <= i; ++k) {
+      const R* vk = V + (size_t)k * nl;
+      const R* vn = (k < i) ? V + (size_t)(k + 1) * nl : nullptr;
+      mgs_axpy_dot_fused<R><<<h->nblk, kRedThreads, 0, st>>>(w, vk, h->gm_H.p + k, vn, nl, h->partial.p, h->ticket.p,
+                                                             h->gm_H.p + k + 1);
+      SELF_LAUNCHED(ctx);
+    }
+    // gm_H[i+1] = <w,w>; Givens on the device
+    const int l = l0 + i + 1;
+    gmres_givens<<<1, 1, 0, st>>>(h->gm_H.p, i, m, h->gm_rho.p, h->gm_c.p, h->gm_s.p, h->gm_bhat.p, h->GS.p,
+                                  resi_dev, l <= maxIters ? l : 0);
+    SELF_LAUNCHED(ctx);
+    // v_{i+1} = w / h(i+1, i)
+    gmres_next_basis<R><<<h->nblk, kRedThreads, 0, st>>>(V + (size_t)(i + 1) * nl, w, h->gm_H.p + i + 1, h->GS.p,
+                                                         nl);
+    SELF_LAUNCHED(ctx);
+  }
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&G, h->GS.p, sizeof(G), cudaMemcpyDeviceToHost, st));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  out->steps = G.done ? G.i : msteps;
+  out->nr = G.nr;
+  out->done = G.done;
+  out->breakdown = G.breakdown;
+  out->rc = G.rc;
+  if (G.nr >= 1) {
+    gmres_backsolve<<<1, 1, 0, st>>>(h->gm_rho.p, h->gm_bhat.p, m, h->GS.p, h->gm_y.p);
+    SELF_LAUNCHED(ctx);
+    gmres_update<R><<<h->nblk, kRedThreads, 0, st>>>(x, V, h->gm_y.p, G.nr, nl, dinv);
+    SELF_LAUNCHED(ctx);
+  }
+  return SELF_OK;
+}
+
+int gmres_buffers(self_cg2d* h, int m, bool fp32) {
+  self_ctx* ctx = h->ctx;
+  const size_t nl = h->nl;
+  int rc;
+  if (fp32) {
+    if ((rc = ensuref(ctx, h->gm_V32, nl * (size_t)(m + 1)))) return rc;
+  } else if ((rc = ensure(ctx, h->gm_V, nl * (size_t)(m + 1)))) {
+    return rc;
+  }
   if ((rc = ensure(ctx, h->gm_H, (size_t)(m + 2)))) return rc;
   if ((rc = ensure(ctx, h->gm_rho, (size_t)m * m))) return rc;
   if ((rc = ensure(ctx, h->gm_c, m)) || (rc = ensure(ctx, h->gm_s, m)) || (rc = ensure(ctx, h->gm_bhat, m + 1)) ||
-      (rc = ensure(ctx, h->gm_y, m + 1)) || (rc = ensure(ctx, h->w, nl)))
+      (rc = ensure(ctx, h->gm_y, m + 1)) || (rc = ensure(ctx, h->w, nl)) || (rc = ensure(ctx, h->t, nl)))
     return rc;
   if (h->GS.n == 0 && h->GS.alloc(1) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "allocation failed");
-  std::vector<double> resi_dev_host;
+  return SELF_OK;
+}
+
+int resi_to_host(self_cg2d* h, DevBuf<double>& resi_dev, double* resi_host, int maxIters, int l) {
+  std::vector<double> tmp((size_t)maxIters + 1);
+  SELF_CUDA_TRY(h->ctx, cudaMemcpyAsync(tmp.data(), resi_dev.p, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        h->ctx->stream));
+  SELF_CUDA_TRY(h->ctx, cudaStreamSynchronize(h->ctx->stream));
+  for (int k = 1; k <= std::min(l, maxIters); ++k) resi_host[k] = tmp[k];
+  return SELF_OK;
+}
+
+// GMRES(m) of IterativeSolvers_Class.f90:493-652, or with dinv the flexible right-preconditioned GMRES of
+// Solve_PCGMRES (:656-822) with Jacobi: z_i = dinv v_i, w = A z_i, and x += Z y = dinv (V y) at the end of a
+// cycle (the preconditioner is fixed, so the basis Z is not stored).  FP64; x, r are device vectors, r holds the
+// initial residual and r0 its norm.  Returns ioerr (0, -1, or SELF_ERR_NONFINITE); iters = total Arnoldi steps
+// (the reference's l).
+int gmres_device(self_cg2d* h, const double* f, double* x, double* r, int m, int maxIters, double tol, double r0,
+                 double* resi_host, int* iters, double* rel, const double* dinv) {
+  self_ctx* ctx = h->ctx;
+  int rc;
+  if ((rc = gmres_buffers(h, m, false))) return rc;
   DevBuf<double> resi_dev;
-  if (resi_host && (rc = ensure(ctx, resi_dev, (size_t)maxIters + 1))) return rc;
-  if (resi_host) SELF_CUDA_TRY(ctx, cudaMemsetAsync(resi_dev.p, 0, ((size_t)maxIters + 1) * sizeof(double), st));
-  // r0
-  if ((rc = dots<double>(h, r, r, nullptr, nullptr, h->red.p))) return rc;
-  const double rr0 = read1(h, h->red.p, &rc);
-  if (rc) return rc;
-  const double r0 = std::sqrt(rr0);
-  *r0_out = r0;
-  if (resi_host) resi_host[0] = r0;
-  int l = 0;
-  int ioerr = -2;
+  if (resi_host) {
+    if ((rc = ensure(ctx, resi_dev, (size_t)maxIters + 1))) return rc;
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(resi_dev.p, 0, ((size_t)maxIters + 1) * sizeof(double), ctx->stream));
+    resi_host[0] = r0;
+  }
+  int l = 0, ioerr = -1;
   double rcur = r0;
   *iters = 0;
   if (r0 == 0.0) {
     *rel = 0.0;
     return 0;
   }
-  GMScalars G{};
-  for (int cyc = 1; cyc <= maxIters; ++cyc) {
-    // b = ||r|| ; v1 = r / b ; bhat(1) = b
-    if ((rc = dots<double>(h, r, r, nullptr, nullptr, h->red.p))) return rc;
-    sqrt_scalar<<<1, 1, 0, st>>>(h->red.p, h->red.p + 4);
-    SELF_LAUNCHED(ctx);
-    scale_copy<double><<<h->nblk, kRedThreads, 0, st>>>(h->gm_V.p, r, h->red.p + 4, 1, nl);
-    SELF_LAUNCHED(ctx);
-    SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->gm_bhat.p, 0, (m + 1) * sizeof(double), st));
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->gm_bhat.p, h->red.p + 4, sizeof(double), cudaMemcpyDeviceToDevice, st));
-    SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->gm_rho.p, 0, (size_t)m * m * sizeof(double), st));
-    G = GMScalars{};
-    G.r0 = r0;
-    G.tol = tol;
-    G.rc = rcur;
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
-    int nr = 0;
-    bool cycle_done = false;
-    for (int i = 0; i < m; ++i) {
-      l += 1;
-      nr = i + 1;
-      double* vi = h->gm_V.p + (size_t)i * nl;
-      if (dinv) {  // z_i = PreconditionInvert(v_i)
-        scale_by<double><<<h->nblk, kRedThreads, 0, st>>>(h->t.p, vi, dinv, nl);
-        SELF_LAUNCHED(ctx);
-        if ((rc = matrix_action<double>(h, h->t.p, h->w.p, h->op64))) return rc;
-      } else if ((rc = matrix_action<double>(h, vi, h->w.p, h->op64))) {
-        return rc;
-      }
-      // MGS: h(k,i) = <v_k, w>; w -= h(k,i) v_k, the axpy of step k fused with the dot of step k+1
-      if ((rc = dots<double>(h, h->gm_V.p, h->w.p, nullptr, nullptr, h->gm_H.p))) return rc;
-      for (int k = 0; k <= i; ++k) {
-        const double* vk = h->gm_V.p + (size_t)k * nl;
-        const double* vn = (k < i) ? h->gm_V.p + (size_t)(k + 1) * nl : nullptr;
-        mgs_axpy_dot_fused<double><<<h->nblk, kRedThreads, 0, st>>>(h->w.p, vk, h->gm_H.p + k, vn, nl,
-                                                                     h->partial.p, h->ticket.p, h->gm_H.p + k + 1);
-        SELF_LAUNCHED(ctx);
-      }
-      // gm_H[i+1] = <w,w>; Givens on the device
-      gmres_givens<<<1, 1, 0, st>>>(h->gm_H.p, i, m, h->gm_rho.p, h->gm_c.p, h->gm_s.p, h->gm_bhat.p, h->GS.p,
-                                    resi_host ? resi_dev.p : nullptr, l <= maxIters ? l : 0);
-      SELF_LAUNCHED(ctx);
-      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&G, h->GS.p, sizeof(G), cudaMemcpyDeviceToHost, st));
-      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      if (G.breakdown) {
-        nr = i;  // exit before this column enters the solve
-        cycle_done = true;
-        break;
-      }
-      rcur = G.rc;
-      if (!std::isfinite(rcur)) {  // NaN / Inf in the Arnoldi recurrence: stop with the non-finite status
-        *iters = l;
-        *rel = rcur;
-        return SELF_ERR_NONFINITE;
-      }
-      // v_{i+1} = w / h(i+1, i)
-      sqrt_scalar<<<1, 1, 0, st>>>(h->gm_H.p + i + 1, h->red.p + 5);
-      SELF_LAUNCHED(ctx);
-      scale_copy<double><<<h->nblk, kRedThreads, 0, st>>>(h->gm_V.p + (size_t)(i + 1) * nl, h->w.p, h->red.p + 5,
-                                                          1, nl);
-      SELF_LAUNCHED(ctx);
-      if (G.done) {
-        cycle_done = true;
-        break;
-      }
+  while (l < maxIters) {
+    CycleOut co{};
+    if ((rc = gmres_cycle<double>(h, x, r, m, std::min(m, maxIters - l), r0, tol, rcur, h->gm_V.p, h->w.p, h->t.p,
+                                  dinv, h->op64, resi_host ? resi_dev.p : nullptr, l, maxIters, &co)))
+      return rc;
+    l += co.steps;
+    rcur = co.rc;
+    if (!std::isfinite(rcur)) {
+      ioerr = SELF_ERR_NONFINITE;
+      break;
     }
-    if (!cycle_done || rcur / r0 > tol) nr = (G.breakdown && nr > 0) ? nr : (rcur / r0 > tol ? m : nr);
-    if (nr < 1) break;
-    G.nr = nr;
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
-    gmres_backsolve<<<1, 1, 0, st>>>(h->gm_rho.p, h->gm_bhat.p, m, h->GS.p, h->gm_y.p);
-    SELF_LAUNCHED(ctx);
-    gmres_update<double><<<h->nblk, kRedThreads, 0, st>>>(x, h->gm_V.p, h->gm_y.p, nr, nl, dinv);
-    SELF_LAUNCHED(ctx);
-    *iters = l;
     if (rcur / r0 <= tol) {
       ioerr = 0;
       break;
     }
-    if (l >= maxIters) break;
+    if (co.breakdown || l >= maxIters) break;
     if ((rc = residual<double>(h, f, x, r, h->op64))) return rc;
   }
-  if (rcur / r0 > tol) ioerr = -1;
-  if (resi_host) {
-    std::vector<double> tmp((size_t)maxIters + 1);
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(tmp.data(), resi_dev.p, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-    for (int k = 1; k <= std::min(l, maxIters); ++k) resi_host[k] = tmp[k];
-  }
+  *iters = l;
+  if (resi_host && (rc = resi_to_host(h, resi_dev, resi_host, maxIters, l))) return rc;
   *rel = rcur / r0;
+  return ioerr;
+}
+
+// FP32-inner GMRES under FP64 iterative refinement: every refinement step is one GMRES(m) cycle in FP32 (basis,
+// matrix action and update in FP32; Gram-Schmidt dots accumulated in FP64, Hessenberg, Givens and back
+// substitution in FP64) on A d = r from d = 0, then x += d and r = b - A x in FP64.  The restart residual of
+// GMRES(m) is thus the FP64 residual.  resi: ||r|| (FP64) per refinement step.  Returns ioerr as gmres_device.
+int gmres_ir_device(self_cg2d* h, const double* f, double* x, double* r, int m, int maxIters, double tol, double r0,
+                    double* resi_host, int* iters, int* outer_out, double* rel, const float* dinv32) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  const size_t nl = h->nl;
+  int rc;
+  if ((rc = gmres_buffers(h, m, true)) || (rc = ensuref(ctx, h->u32, nl)) || (rc = ensuref(ctx, h->r32, nl)) ||
+      (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)) || (rc = ensure(ctx, h->z, nl)))
+    return rc;
+  int total = 0, outer = 0, ioerr = -1;
+  double rn = r0;
+  if (resi_host) resi_host[0] = r0;
+  *iters = 0;
+  *outer_out = 0;
+  if (r0 == 0.0) {
+    *rel = 0.0;
+    return 0;
+  }
+  while (total < maxIters && rn / r0 >= tol) {
+    convert<float, double><<<h->nblk, kRedThreads, 0, st>>>(h->r32.p, r, nl);
+    SELF_LAUNCHED(ctx);
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->u32.p, 0, nl * sizeof(float), st));
+    CycleOut co{};
+    if ((rc = gmres_cycle<float>(h, h->u32.p, h->r32.p, m, std::min(m, maxIters - total), r0, tol, rn, h->gm_V32.p,
+                                 h->w32.p, h->z32.p, dinv32, h->op32, nullptr, 0, maxIters, &co)))
+      return rc;
+    total += co.steps;
+    outer++;
+    // x += d (FP64), r = b - A x in FP64
+    convert<double, float><<<h->nblk, kRedThreads, 0, st>>>(h->z.p, h->u32.p, nl);
+    SELF_LAUNCHED(ctx);
+    axpby<double><<<h->nblk, kRedThreads, 0, st>>>(x, h->z.p, 1.0, 1.0, nl);
+    SELF_LAUNCHED(ctx);
+    if ((rc = residual<double>(h, f, x, r, h->op64))) return rc;
+    if ((rc = dots<double>(h, r, r, nullptr, nullptr, h->red.p))) return rc;
+    rn = std::sqrt(read1(h, h->red.p, &rc));
+    if (rc) return rc;
+    if (resi_host && outer <= maxIters) resi_host[outer] = rn;
+    if (!std::isfinite(rn) || !std::isfinite(co.rc)) {
+      ioerr = SELF_ERR_NONFINITE;
+      break;
+    }
+    if (co.nr < 1) break;  // breakdown on the first column: no progress possible
+  }
+  if (ioerr != SELF_ERR_NONFINITE) ioerr = (rn / r0 < tol) ? 0 : -1;
+  *iters = total;
+  *outer_out = outer;
+  *rel = rn / r0;
   return ioerr;
 }
 
@@ -2296,8 +2388,8 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
   const bool gm = o->method == SELF_SOLVE_GMRES || o->method == SELF_SOLVE_PGMRES_JACOBI;
   if (gm && (o->m < 1 || o->m > 512))
     return set_error(ctx, SELF_ERR_INVALID, "GMRES restart length %d", o->m);
-  if (gm && o->precision != SELF_PREC_FP64)
-    return set_error(ctx, SELF_ERR_UNSUPPORTED, "GMRES runs in FP64");
+  if (gm && o->precision != SELF_PREC_FP64 && o->precision != SELF_PREC_FP32)
+    return set_error(ctx, SELF_ERR_UNSUPPORTED, "GMRES precision %d", o->precision);
   const size_t nl = h->nl;
   int rc;
   std::vector<double> x0(solution, solution + nl);
@@ -2330,10 +2422,14 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
     return set_error(ctx, SELF_ERR_NONFINITE, "non-finite initial residual (NaN or Inf in the source, initial guess "
                      "or Dirichlet data)");
   }
-  if (gm) {
-    R.ioerr = gmres_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, resi, &iters, &rel, &r0,
+  if (gm && o->precision == SELF_PREC_FP64) {
+    R.ioerr = gmres_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, r0, resi, &iters, &rel,
                            o->method == SELF_SOLVE_PGMRES_JACOBI ? h->op64.dinv.p : nullptr);
     R.outer_iterations = 1;
+  } else if (gm) {
+    R.ioerr = gmres_ir_device(h, h->f.p, h->u.p, h->r.p, o->m, o->maxIters, o->tolerance, r0, resi, &iters,
+                              &R.outer_iterations, &rel,
+                              o->method == SELF_SOLVE_PGMRES_JACOBI ? h->op32.dinv.p : nullptr);
   } else {
     const bool jac = o->method == SELF_SOLVE_PCG_JACOBI;
     if (o->precision == SELF_PREC_FP64) {

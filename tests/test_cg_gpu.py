@@ -125,6 +125,30 @@ def test_pgmres_jacobi_advection_diffusion_parity(oracle, gpu_ctx):
     assert rel_inf(sol, osol) <= 1e-8
 
 
+@pytest.mark.parametrize("method", ["gmres", "pgmres"])
+def test_fp32_inner_gmres_reaches_fp64_accuracy(oracle, gpu_ctx, method):
+    """FP32-inner GMRES(m) under FP64 refinement (one FP32 cycle per refinement step, Gram-Schmidt dots in FP64,
+    Givens in FP64, FP64 residual at every restart): ||r||/||r0|| < 1e-10 recomputed by the oracle, solution
+    within 1e-8 of the FP64 GMRES solution, Arnoldi steps within 10 % of FP64 (the refinement step is the
+    restart)."""
+    import self_gb300 as sg
+    N, nx = 5, 8
+    nod, mesh, k, source, P = _problem(oracle, N, nx, warp=0.03, lam=0.0, op=1, vel=(1.0, 0.5), kappa=1e-2)
+    cg = sg.CGsemElliptic_2D(gpu_ctx, nod, mesh, k, lam=0.0, op=1, vel=(1.0, 0.5))
+    s64, r64 = cg.Solve(source, method=method, m=30, tolerance=1e-10, maxIters=5000)
+    s32, r32 = cg.Solve(source, method=method, precision="fp32", m=30, tolerance=1e-10, maxIters=5000,
+                        return_resi=True)
+    assert r64["ioerr"] == 0 and r32["ioerr"] == 0 and r32["rel_residual"] < 1e-10
+    assert r32["outer_iterations"] >= 2
+    assert abs(r32["iterations"] - r64["iterations"]) <= 0.1 * r64["iterations"] + 30
+    res = P.residual(source, s32)
+    r0 = P.residual(source, np.zeros_like(s32))
+    assert np.sqrt(P.dot(res, res)) / np.sqrt(P.dot(r0, r0)) < 1.5e-10
+    assert rel_inf(s32, s64) < 1e-8
+    h = r32["resi"][: r32["outer_iterations"] + 1]
+    assert np.all(h[1:] > 0) and h[-1] / h[0] < 1e-10  # FP64 residual per refinement step
+
+
 def test_manufactured_solution_converges(gpu_ctx):
     """u = sin(pi x) sin(pi y), k = 1, lam = 0.1: spectral accuracy of the solved field."""
     import self_gb300 as sg

@@ -5,7 +5,8 @@ run out, and the library must report it as a status while the CUDA context stays
   first wait of every warp poll a barrier nothing arrives on, so the call returns SELF_ERR_TIMEOUT, leaves the
   state unchanged, and the next call on the same handle (and a fresh handle) steps normally.
 * Non-finite residuals: a NaN or Inf in the source or the initial guess makes self_cg2d_solve return
-  SELF_ERR_NONFINITE (ioerr -7 in the report) for PCG, FP32-refined PCG and GMRES, before any iteration.
+  SELF_ERR_NONFINITE (ioerr -7 in the report) for PCG, FP32-refined PCG, GMRES and FP32-inner GMRES, before any
+  iteration.
 * Unsupported options return SELF_ERR_UNSUPPORTED.
 The reference signals solver failure through ioerr (IterativeSolvers_Class.f90:357,402) and stops on fatal errors.
 """
@@ -64,7 +65,8 @@ def test_wait_timeout_hook_unsupported_outside_fused_stage(gpu_ctx):
     sw.Trash()
 
 
-@pytest.mark.parametrize("method,precision", [("pcg", "fp64"), ("pcg", "fp32"), ("gmres", "fp64"), ("cg", "fp64")])
+@pytest.mark.parametrize("method,precision", [("pcg", "fp64"), ("pcg", "fp32"), ("gmres", "fp64"), ("gmres", "fp32"),
+                                              ("cg", "fp64")])
 def test_nonfinite_source_is_reported(gpu_ctx, method, precision):
     import self_gb300 as sg
     from self_gb300 import _native as nat
