@@ -457,47 +457,38 @@ def batched_leg(sg, ctx, nprob=512, fp64_sample=32):
             "autotuned_elements_per_tile": {f"N{N}_b{b}": e for (N, b), e in tune.items()}}
 
 
-def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, fp64_sample=60):
-    """Poisson stream (mean 2000 req/s, seed 5): 70 % Helmholtz from the batched distribution, 30 % shallow-water
-    ensemble members (64x64, N=5, 100 steps).  Continuous batching (FP32 inner + FP64 refinement, FP32 members)
-    vs the plain FP64 path serving the same stream one request at a time (service times measured on a sample)."""
+def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, sweep_n=150, base_n=120):
+    """Poisson streams (seeded) mixing 70 % Helmholtz solves from the batched distribution and 30 % shallow-water
+    ensemble members (64x64, N=5, 100 steps), served by the library's request loop (self_serve_*): continuous
+    batching (FP32 inner + FP64 refinement, FP32 members) at the configured 2000 req/s and at 25 / 50 / 90 % of the
+    capacity it measured there; the plain FP64 path one request at a time (the same loop with max_active = 1 and
+    FP64 solves and members), run on the same 2000 req/s stream and at half its own capacity."""
     from self_gb300 import serving as S
-    reqs = S.make_requests(sg, nreq, rate=rate, seed=seed)
-    srv = S.Server(ctx)
-    srv.keep_results = False
-    srv.run(reqs)
-    srv.close()
-    st = S.latency_stats(reqs)
-    # plain FP64 path: FIFO single-request service; service time of each request measured on a sample
-    idx = np.linspace(0, nreq - 1, min(fp64_sample, nreq)).astype(int)
-    svc = {}
-    for i in idx:
-        r = reqs[i]
-        pr = r.payload
-        t0 = time.perf_counter()
-        if r.kind == "helmholtz":
-            cg = sg.CGsemElliptic_2D(ctx, pr["nodal"], pr["mesh"], pr["k"], lam=pr["lam"])
-            cg.Solve(pr["source"], method="pcg", precision="fp64", tolerance=1e-10)
-            cg.Trash()
-        else:
-            sw = sg.ShallowWater(ctx, pr["nodal"], pr["mesh"], pr["h"], pr["fcor"], pr["dt"], dhdx=pr["dhdx"],
-                                 dhdy=pr["dhdy"])
-            sw.SetSolution(pr["q"])
-            sw.ForwardStepRK3(0.0, pr["steps"])
-            sw.GetSolution()
-            sw.Trash()
-        svc[i] = time.perf_counter() - t0
-    kinds = {k: np.mean([svc[i] for i in idx if reqs[i].kind == k]) for k in ("helmholtz", "sw")
-             if any(reqs[i].kind == k for i in idx)}
-    t, lat = 0.0, []
-    for r in reqs:  # FIFO queue simulation with sampled service times (sample value where measured)
-        t = max(t, r.arrival) + svc.get(r.rid, kinds[r.kind])
-        lat.append(t - r.arrival)
-    lat = np.array(lat)
-    base = {"p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-            "throughput_req_s": nreq / (t - reqs[0].arrival), "service_sampled": int(len(idx))}
-    return {"requests": nreq, "rate_req_s": rate, "continuous_batching": st, "fp64_sequential": base,
-            "throughput_ratio": st["throughput_req_s"] / base["throughput_req_s"]}
+
+    def serve(n, r, precision, max_active=0, seed_=seed):
+        reqs = S.make_requests(sg, n, rate=r, seed=seed_)
+        srv = S.Server(ctx, precision=precision, max_active=max_active)
+        srv.keep_results = False
+        srv.run(reqs)
+        st = S.latency_stats(reqs)
+        st["offered_req_s"] = r
+        st["requests"] = n
+        return st
+
+    out = {"requests": nreq, "rate_req_s": rate, "loop": "self_serve (C++ worker thread, device-side tick decisions)"}
+    mix = serve(nreq, rate, "fp32")
+    out["continuous_batching"] = mix
+    cap = mix["throughput_req_s"]
+    out["load_sweep"] = [serve(sweep_n, f * cap, "fp32", seed_=seed + 10 + i) for i, f in enumerate((0.25, 0.5, 0.9))]
+    for row, f in zip(out["load_sweep"], (0.25, 0.5, 0.9)):
+        row["fraction_of_capacity"] = f
+    base = serve(base_n, rate, "fp64", max_active=1)
+    out["fp64_one_at_a_time"] = base
+    out["fp64_one_at_a_time_half_load"] = serve(base_n // 2, 0.5 * base["throughput_req_s"], "fp64", max_active=1,
+                                                seed_=seed + 20)
+    out["fp64_one_at_a_time_half_load"]["fraction_of_capacity"] = 0.5
+    out["throughput_ratio"] = cap / base["throughput_req_s"]
+    return out
 
 
 def run_cg_profile(args):

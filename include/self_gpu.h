@@ -256,7 +256,8 @@ int self_cgbatch_destroy(self_cgbatch* b);
 /* set the source of slot p and restart its solve from a zero initial guess */
 int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source);
 int self_cgbatch_problem_size(self_cgbatch* b, int p, long long* nlocal);
-/* solve every problem in the pool (runs self_cgbatch_step until all finished); reports in slot order */
+/* solve every problem in the pool in one launch of a graph whose conditional while node repeats the tick on the
+ * device until every problem finished; reports in slot order */
 int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* opts, self_solve_report* reports);
 int self_cgbatch_get_solution(self_cgbatch* b, int p, double* solution);
 /* continuous batching: add a problem to a free slot (its solve starts at the next step), remove a slot,
@@ -273,6 +274,67 @@ long long self_cgbatch_bytes(const self_cgbatch* b);
  * is read first and written after.  self_cgbatch_tuning returns the elements per tile in use. */
 int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path);
 int self_cgbatch_tuning(self_cgbatch* b, int N, int bucket, int* elements_per_tile);
+
+/* ---------------------------------------------------------------- continuous-batching request loop
+ * No counterpart in the reference (its drivers run one model at a time).  A worker thread inside the library owns
+ * every CUDA call of the loop; submit / poll / result / cancel / stats may be called from any thread.  Requests are
+ * admitted in arrival order while their device footprint fits hbm_budget_bytes (and while fewer than max_active
+ * run, when max_active > 0):
+ *   solve requests (Helmholtz, op 0) join one batched slot pool: each tick advances every admitted solve -- outer
+ *   FP64 residual step, outer decision and inner PCG iterations, all on the device -- with one synchronisation;
+ *   shallow-water requests run their RK3 steps on their own handle on one of sw_streams extra streams, in chunks
+ *   of sw_chunk steps enqueued asynchronously (kernels overlap the solves).
+ * A result is bit-identical to the same request served alone.  The caller keeps every array the descriptor points
+ * to, and the source / initial state, alive until poll reports the request done, failed or cancelled.  The ctx
+ * must not be used by the caller while the loop exists. */
+typedef struct self_serve self_serve;
+typedef struct {
+  double hbm_budget_bytes; /* admission limit: device bytes of the requests on the GPU */
+  int precision;           /* solves: SELF_PREC_FP32 (FP32 inner / FP64 refinement) or SELF_PREC_FP64 */
+  double tolerance;        /* solves stop at ||r||/||r0|| < tolerance (FP64 residual) */
+  double inner_tolerance;  /* FP32 inner solves: relative reduction per refinement step (default 1e-4) */
+  int max_outer;           /* refinement steps cap (default 30) */
+  int maxIters;            /* inner iterations cap per solve (default 100000) */
+  int sw_streams;          /* extra streams for shallow-water requests (default 4) */
+  int sw_chunk;            /* RK3 steps enqueued per chunk (default 10) */
+  int max_active;          /* requests on the GPU at once; 0 = no cap, 1 = one request at a time */
+} self_serve_opts;
+#define SELF_SERVE_SOLVE 0
+#define SELF_SERVE_SW 1
+#define SELF_SERVE_QUEUED 0
+#define SELF_SERVE_RUNNING 1
+#define SELF_SERVE_DONE 2
+#define SELF_SERVE_CANCELLED 3
+#define SELF_SERVE_FAILED 4
+typedef struct {
+  int state, kind, status;            /* SELF_SERVE_*, status of a failed request */
+  int steps_done;                     /* shallow-water request: RK3 steps enqueued so far */
+  double submit_s, admit_s, done_s;   /* seconds since the loop was created (-1: not yet) */
+  self_solve_report report;           /* solve request: as self_cg2d_solve reports it */
+} self_serve_info;
+typedef struct {
+  long long submitted, admitted, finished, cancelled, failed, queued, running, bytes_in_use;
+  double p50_ms, p99_ms, mean_ms;     /* latency (done - submit) of the finished requests */
+  double throughput_per_s;            /* finished / (last done - first submit) */
+  double elapsed_s;
+} self_serve_statistics;
+int self_serve_create(self_ctx* ctx, const self_serve_opts* opts, self_serve** out);
+/* stops the worker (requests still queued or running are cancelled) and frees everything */
+int self_serve_destroy(self_serve* s);
+/* Helmholtz solve (desc as self_cg2d_create, op 0; source as self_cg2d_solve; zero initial guess, homogeneous
+ * Dirichlet values): returns a ticket */
+int self_serve_submit_solve(self_serve* s, const self_cg2d_desc* desc, const double* source, long long* ticket);
+/* shallow-water ensemble member: `steps` RK3 steps from the state q0 (desc as self_dg2d_create) */
+int self_serve_submit_sw(self_serve* s, const self_dg2d_desc* desc, const double* q0, int steps, long long* ticket);
+int self_serve_poll(self_serve* s, long long ticket, self_serve_info* info);
+/* result of a done request: the solve's solution (L-vector, unmasked) or the member's final state; n values */
+int self_serve_result(self_serve* s, long long ticket, double* out, size_t n);
+/* forget a finished / cancelled / failed request (its result) */
+int self_serve_release(self_serve* s, long long ticket);
+int self_serve_cancel(self_serve* s, long long ticket);
+/* wait until nothing is queued or running (SELF_ERR_TIMEOUT after timeout_s seconds) */
+int self_serve_wait(self_serve* s, double timeout_s);
+int self_serve_stats(self_serve* s, self_serve_statistics* st);
 
 /* ---------------------------------------------------------------- dot product without allocation
  * No counterpart in the reference.  For callers that cannot allocate device memory where they need an inner

@@ -55,21 +55,28 @@ _METHODS = {"cg": SOLVE_CG, "pcg": SOLVE_PCG_JACOBI, "pcg_jacobi": SOLVE_PCG_JAC
             "pgmres": SOLVE_PGMRES_JACOBI, "pcg_linear": SOLVE_PCG_LINEAR}
 
 
+def cg2d_desc(nodal, mesh, fluxCoeff, lam=0.0, op=0, vel=(0.0, 0.0)):
+    """self_cg2d_desc over the arrays of a NodalStorage_2D (GLL, CG form) and a QuadMesh; returns (desc, keep):
+    `keep` holds the arrays the descriptor points to and must outlive every use of it."""
+    s = CG2DDesc()
+    s.N, s.nEl, s.nEdges, s.nNodes = nodal.N, mesh.nEl, mesh.nEdges, mesh.nNodes
+    s.dmat, s.qweight = nat.d(nodal.dmatS), nat.d(nodal.w)
+    s.edges, s.nodeType = nat.i(mesh.edges), nat.i(mesh.nodeType)
+    s.n2e_ptr, s.n2e_elem, s.n2e_local = nat.i(mesh.n2e_ptr), nat.i(mesh.n2e_elem), nat.i(mesh.n2e_local)
+    s.dxds, s.dxdp, s.dyds, s.dydp, s.J = (nat.d(getattr(mesh, k)) for k in ("dxds", "dxdp", "dyds", "dydp", "J"))
+    fluxCoeff = np.ascontiguousarray(fluxCoeff, dtype=np.float64)
+    s.fluxCoeff = nat.d(fluxCoeff)
+    s.lam, s.op, s.vx, s.vy = lam, op, vel[0], vel[1]
+    s.x, s.y = nat.d(mesh.x), nat.d(mesh.y)  # node positions: the linear-FEM preconditioner's mesh
+    return s, (nodal, mesh, fluxCoeff)
+
+
 class CGsemElliptic_2D:
     """op=0: weak -div(k grad u) + lam u with the reference's sign (MatrixAction = -(K + lam M) u);
     op=1: advection-diffusion -kappa Lap u + v.grad u (kappa in fluxCoeff), same sign convention."""
 
     def __init__(self, ctx, nodal, mesh, fluxCoeff, lam=0.0, op=0, vel=(0.0, 0.0)):
-        s = CG2DDesc()
-        s.N, s.nEl, s.nEdges, s.nNodes = nodal.N, mesh.nEl, mesh.nEdges, mesh.nNodes
-        s.dmat, s.qweight = nat.d(nodal.dmatS), nat.d(nodal.w)
-        s.edges, s.nodeType = nat.i(mesh.edges), nat.i(mesh.nodeType)
-        s.n2e_ptr, s.n2e_elem, s.n2e_local = nat.i(mesh.n2e_ptr), nat.i(mesh.n2e_elem), nat.i(mesh.n2e_local)
-        s.dxds, s.dxdp, s.dyds, s.dydp, s.J = (nat.d(getattr(mesh, k)) for k in ("dxds", "dxdp", "dyds", "dydp", "J"))
-        fluxCoeff = np.ascontiguousarray(fluxCoeff, dtype=np.float64)
-        s.fluxCoeff = nat.d(fluxCoeff)
-        s.lam, s.op, s.vx, s.vy = lam, op, vel[0], vel[1]
-        s.x, s.y = nat.d(mesh.x), nat.d(mesh.y)  # node positions: the linear-FEM preconditioner's mesh
+        s, self._keep = cg2d_desc(nodal, mesh, fluxCoeff, lam, op, vel)
         self.ctx, self.nodal, self.mesh = ctx, nodal, mesh
         self.nl = nodal.n * nodal.n * mesh.nEl
         p = C.c_void_p()

@@ -2,11 +2,14 @@
 //
 // Each problem keeps its own device arrays (operator factors, topology, vectors).  Work is described by tile
 // tables: ETile (problem, N, first element, count) for the element operator, GTile (problem, first group, count)
-// for the direct-stiffness sum, VTile (problem, first node, last node) for vector phases.  Two compacted table
-// sets live on the device -- "inner" (problems running inner iterations) and "outer" (problems waiting for their
-// FP64 residual) -- with their tile counts in device memory; every kernel is a fixed-size grid that strides over
-// the tiles, so a change of the active set only re-uploads table contents and the captured iteration graph stays
-// valid.  One inner PCG iteration is three launches over all active problems (a switch on N selects the
+// for the direct-stiffness sum, VTile (problem, first node, last node) for vector phases.  The host uploads the
+// tables of every problem in the pool ("all") when the pool changes; at every tick two compacted sets -- "outer"
+// (problems waiting for their FP64 residual) and "inner" (problems running inner iterations) -- are rebuilt from
+// them on the device (bk_compact_offsets / bk_compact_copy), and the outer decision (converged, next inner solve)
+// is made on the device too (bk_decide).  A tick is therefore one captured graph with no host round trip, and a
+// whole batched solve is one launch of a graph whose conditional while node repeats the tick until bk_decide finds
+// no problem running.  Every kernel is a fixed-size grid over the table capacity (blocks past the current count
+// exit at once).  One inner PCG iteration is three launches over all active problems (a switch on N selects the
 // compile-time element body):
 //   bk_apply : v_new = w + beta v_old (per-problem parity picks the buffers), z = L(v_new) per element, tile
 //              partial <v_new, z>;
@@ -77,6 +80,14 @@ struct Scal {
   float alpha32, beta32;
   int iter, phase, total, fresh;  // fresh: no outer update yet (initial residual pending)
   int max_total, max_inner;       // iteration limits of the current solve
+  int outer, pad;                 // refinement steps taken (the outer decision runs on the device)
+};
+
+// Parameters of the outer decision (bk_decide), fixed per captured graph.
+struct DecideArgs {
+  double tol, inner_tol;
+  int fp32, max_outer, max_total;
+  unsigned int max_bodies;  // bound of the persistent loop (bodies run before its condition is cleared)
 };
 
 // gate 0 runs problems in phase 0, gate 1 those in phase 1, gate 2 those in phase 1 that are not fresh,
@@ -786,6 +797,147 @@ __global__ void __launch_bounds__(kThreads) bk_rr(TileView V, const Prob* __rest
   }
 }
 
+// Outer decision of every problem in phase 1 once its FP64 residual norm squared is in red[p] -- the per-tick
+// decision of the host loop, moved onto the device so that ticks need no host round trip: the first residual
+// becomes r0; converged (||r||/||r0|| < tol, or r0 = 0, or a NaN), out of iterations or out of refinement steps ->
+// phase 2; otherwise the next inner solve (phase 0, inner stop relative to this residual).  counters[0] = problems
+// still running (phase 0 or 1); counters[1] counts loop bodies.  With use_cond, clears the persistent loop's
+// condition when no problem is running or the body budget is spent.  One block.
+__global__ void __launch_bounds__(kThreads) bk_decide(Scal* __restrict__ S, const double* __restrict__ red, int cap,
+                                                      DecideArgs a, unsigned int* __restrict__ counters,
+                                                      cudaGraphConditionalHandle cond, int use_cond) {
+  int active = 0;
+  for (int p = threadIdx.x; p < cap; p += kThreads) {
+    Scal& s = S[p];
+    if (s.phase == 1) {
+      const double rn = sqrt(red[p]);
+      s.rr = rn;
+      if (s.fresh) {
+        s.r0 = rn;
+        s.fresh = 0;
+      }
+      const bool conv = s.r0 == 0.0 || rn / s.r0 < a.tol || !(rn == rn);
+      if (conv || s.total >= a.max_total || s.outer >= a.max_outer) {
+        s.phase = 2;
+      } else {
+        s.outer += 1;
+        s.phase = 0;
+        s.iter = 0;
+        s.num = s.den = s.vz = 0;
+        s.rin0 = rn;
+        s.tol = a.fp32 ? a.inner_tol : a.tol * s.r0 / rn;
+      }
+    }
+    if (s.phase == 0 || s.phase == 1) {
+      s.max_total = a.max_total;
+      s.max_inner = a.max_total;
+      ++active;
+    }
+  }
+  const double tot = block_sum_r<double>((double)active);
+  if (threadIdx.x == 0) {
+    counters[0] = (unsigned int)tot;
+    const unsigned int bodies = ++counters[1];
+    if (use_cond) cudaGraphSetConditional(cond, (tot > 0.0 && bodies < a.max_bodies) ? 1u : 0u);
+  }
+}
+
+// Device compaction of a tile-table set: the tiles of the problems in phase ph, copied in order from the view of
+// every problem in the pool (problem p's tiles are A.et[a_e[p] .. a_e[p+1]), A.gt[a_g[p] ..], A.vt[a_v[p] ..]).
+// Part 1 (one block of 1024 threads): per-problem first tile in the compacted tables (prefix sums over the
+// problems) and the tile counts.
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) bk_compact_offsets(const int* __restrict__ a_e, const int* __restrict__ a_g,
+                                                                   const int* __restrict__ a_v,
+                                                                   const Scal* __restrict__ S, int cap, int ph,
+                                                                   int* __restrict__ d_e, int* __restrict__ d_g,
+                                                                   int* __restrict__ d_v, int* __restrict__ d_cnt) {
+  __shared__ int wsum[3][kScanThreads / 32];
+  __shared__ int carry[3];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x < 3) carry[threadIdx.x] = 0;
+  __syncthreads();
+  for (int base = 0; base < cap; base += kScanThreads) {
+    const int p = base + threadIdx.x;
+    int c[3] = {0, 0, 0};
+    if (p < cap && S[p].phase == ph) {
+      c[0] = a_e[p + 1] - a_e[p];
+      c[1] = a_g[p + 1] - a_g[p];
+      c[2] = a_v[p + 1] - a_v[p];
+    }
+    int inc[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      int v = c[k];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+      }
+      inc[k] = v;
+      if (lane == 31) wsum[k][wid] = v;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        int v = wsum[k][lane];
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += t;
+        }
+        wsum[k][lane] = v;  // inclusive prefix over the warps
+      }
+    }
+    __syncthreads();
+    int excl[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) excl[k] = carry[k] + (wid > 0 ? wsum[k][wid - 1] : 0) + inc[k] - c[k];
+    if (p < cap) {
+      d_e[p] = excl[0];
+      d_g[p] = excl[1];
+      d_v[p] = excl[2];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) carry[k] += wsum[k][kScanThreads / 32 - 1];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    d_e[cap] = carry[0];
+    d_g[cap] = carry[1];
+    d_v[cap] = carry[2];
+    d_cnt[0] = carry[0];
+    d_cnt[1] = carry[1];
+    d_cnt[2] = carry[2];
+  }
+}
+
+// Part 2: copy the selected problems' tiles (grid-stride over every tile of the full view).
+__global__ void __launch_bounds__(kThreads) bk_compact_copy(TileView A, const int* __restrict__ a_g,
+                                                            const Scal* __restrict__ S, int ph, ETile* __restrict__ det,
+                                                            GTile* __restrict__ dgt, VTile* __restrict__ dvt,
+                                                            const int* __restrict__ d_e, const int* __restrict__ d_g,
+                                                            const int* __restrict__ d_v) {
+  const int ne = A.cnt[0], ng = A.cnt[1], nv = A.cnt[2];
+  const int total = ne + ng + nv;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    if (i < ne) {
+      const ETile t = A.et[i];
+      if (S[t.prob].phase == ph) det[d_e[t.prob] + (i - A.eptr[t.prob])] = t;
+    } else if (i < ne + ng) {
+      const int j = i - ne;
+      const GTile t = A.gt[j];
+      if (S[t.prob].phase == ph) dgt[d_g[t.prob] + (j - a_g[t.prob])] = t;
+    } else {
+      const int j = i - ne - ng;
+      const VTile t = A.vt[j];
+      if (S[t.prob].phase == ph) dvt[d_v[t.prob] + (j - A.vptr[t.prob])] = t;
+    }
+  }
+}
+
 }  // namespace cgb
 }  // namespace selfgpu
 
@@ -805,14 +957,13 @@ struct self_cgbatch {
     std::vector<double> Jww;
     std::vector<int> src, dirnodes;
     long long bytes = 0;
-    int outer = 0;
   };
   // one compacted tile-table set on the device (fixed capacity; contents re-uploaded when the set changes)
   struct View {
     DevBuf<selfgpu::cgb::ETile> et;
     DevBuf<selfgpu::cgb::GTile> gt;
     DevBuf<selfgpu::cgb::VTile> vt;
-    DevBuf<int> cnt, eptr, vptr;
+    DevBuf<int> cnt, eptr, vptr, gptr;  // gptr[p]: first group tile of problem p
     std::vector<int> members;  // problems of the set at the last upload
     bool valid = false;
     size_t cap_e = 0, cap_g = 0, cap_v = 0;  // table capacities
@@ -830,7 +981,17 @@ struct self_cgbatch {
   DevBuf<selfgpu::cgb::DTable> DT;
   selfgpu::cgb::DTable hDT;
   bool haveD[10] = {};
-  View inner, outer, tune;
+  // all: every problem in the pool (uploaded by the host when the pool changes); inner / outer: the problems in
+  // phase 0 / 1, compacted from `all` on the device at every tick; tune: autotuning tables
+  View all, inner, outer, tune;
+  DevBuf<unsigned int> counters;  // bk_decide: problems running, loop bodies
+  // tick graphs (one tick = outer step + decision + inner iterations) per precision and grid level, and the
+  // persistent solve graphs (the tick inside a conditional while node), captured for one set of DecideArgs
+  cudaGraphExec_t tick_graphs[2][4] = {};
+  cudaGraphExec_t loop_graphs[2][4] = {};
+  long long tick_launches[2][4] = {};
+  selfgpu::cgb::DecideArgs graph_args{};
+  bool graph_args_set = false;
   size_t cap_et = 0, cap_gt = 0, cap_vt = 0;  // table capacities (tiles of every problem in the pool)
   bool dirty = true;
   int epb[10][4];
@@ -843,9 +1004,10 @@ struct self_cgbatch {
   int graph_k = 8;
   long long bytes_in_use = 0;
   ~self_cgbatch() {
-    for (auto& row : graphs)
-      for (auto& g : row)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto* set : {&graphs, &tick_graphs, &loop_graphs})
+      for (auto& row : *set)
+        for (auto& g : row)
+          if (g) cudaGraphExecDestroy(g);
   }
 };
 
@@ -873,11 +1035,12 @@ int zeros(self_ctx* ctx, DevBuf<T>& b, size_t n) {
 }
 
 void drop_graphs(self_cgbatch* b) {
-  for (auto& row : b->graphs)
-    for (auto& g : row) {
-      if (g) cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto* set : {&b->graphs, &b->tick_graphs, &b->loop_graphs})
+    for (auto& row : *set)
+      for (auto& g : row) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
 }
 
 // grow the slot arrays (host and device) to hold at least `want` problems
@@ -924,11 +1087,12 @@ int upload_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& 
   std::vector<ETile> et;
   std::vector<GTile> gt;
   std::vector<VTile> vt;
-  std::vector<int> eptr(b->cap + 1, 0), vptr(b->cap + 1, 0);
+  std::vector<int> eptr(b->cap + 1, 0), vptr(b->cap + 1, 0), gptr(b->cap + 1, 0);
   size_t m = 0;
   for (int p = 0; p < b->cap; ++p) {
     eptr[p] = (int)et.size();
     vptr[p] = (int)vt.size();
+    gptr[p] = (int)gt.size();
     if (m >= members.size() || members[m] != p) continue;
     ++m;
     const Prob& P = b->hp[p];
@@ -942,6 +1106,7 @@ int upload_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& 
   }
   eptr[b->cap] = (int)et.size();
   vptr[b->cap] = (int)vt.size();
+  gptr[b->cap] = (int)gt.size();
   if (et.size() > v.cap_e || gt.size() > v.cap_g || vt.size() > v.cap_v)
     return set_error(b->ctx, SELF_ERR_INVALID, "batch: tile tables exceed their capacity");
   const int cnt[3] = {(int)et.size(), (int)gt.size(), (int)vt.size()};
@@ -954,6 +1119,7 @@ int upload_view(self_cgbatch* b, self_cgbatch::View& v, const std::vector<int>& 
   SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.cnt.p, cnt, sizeof(cnt), cudaMemcpyHostToDevice, st));
   SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.eptr.p, eptr.data(), eptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.vptr.p, vptr.data(), vptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(v.gptr.p, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(st));  // host vectors go out of scope
   v.members = members;
   v.valid = onlyN < 0;
@@ -970,7 +1136,7 @@ int alloc_view(self_cgbatch* b, self_cgbatch::View& v, size_t ce, size_t cg, siz
   v.cap_v = std::max<size_t>(1, cv);
   if ((rc = zeros(b->ctx, v.et, v.cap_e)) || (rc = zeros(b->ctx, v.gt, v.cap_g)) || (rc = zeros(b->ctx, v.vt, v.cap_v)) ||
       (rc = zeros(b->ctx, v.cnt, 3)) || (rc = zeros(b->ctx, v.eptr, (size_t)b->cap + 1)) ||
-      (rc = zeros(b->ctx, v.vptr, (size_t)b->cap + 1)))
+      (rc = zeros(b->ctx, v.vptr, (size_t)b->cap + 1)) || (rc = zeros(b->ctx, v.gptr, (size_t)b->cap + 1)))
     return rc;
   v.members.clear();
   v.valid = false;
@@ -1006,12 +1172,14 @@ int refresh(self_cgbatch* b) {
     b->cap_gt = std::max(ng, b->cap_gt + b->cap_gt / 4);
     b->cap_vt = std::max(nv, b->cap_vt + b->cap_vt / 4);
     if ((rc = alloc_view(b, b->inner, b->cap_et, b->cap_gt, b->cap_vt)) ||
-        (rc = alloc_view(b, b->outer, b->cap_et, b->cap_gt, b->cap_vt)))
+        (rc = alloc_view(b, b->outer, b->cap_et, b->cap_gt, b->cap_vt)) ||
+        (rc = alloc_view(b, b->all, b->cap_et, b->cap_gt, b->cap_vt)))
       return rc;
     drop_graphs(b);
   } else {
-    b->inner.valid = b->outer.valid = false;  // same buffers, new contents on the next use
+    b->inner.valid = b->outer.valid = b->all.valid = false;  // same buffers, new contents on the next use
   }
+  if (!b->counters.p && (rc = zeros(b->ctx, b->counters, 2))) return rc;
   if (ne1 > b->tune.cap_e || !b->tune.et.p)
     if ((rc = alloc_view(b, b->tune, ne1, ng, nv))) return rc;
   const size_t np = std::max({b->cap_et, 2 * b->cap_vt, b->tune.cap_e});
@@ -1070,92 +1238,185 @@ int enqueue_inner(self_cgbatch* b, int L) {
   return SELF_OK;
 }
 
-int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
-  self_ctx* ctx = b->ctx;
+// Compaction of view D (problems in phase ph) from the pool view, at grid level L
+int enqueue_compact(self_cgbatch* b, self_cgbatch::View& D, int ph, int L) {
+  cudaStream_t st = b->ctx->stream;
+  const self_cgbatch::View& A = b->all;
+  bk_compact_offsets<<<1, kScanThreads, 0, st>>>(A.eptr.p, A.gptr.p, A.vptr.p, b->S.p, b->cap, ph, D.eptr.p, D.gptr.p,
+                                                 D.vptr.p, D.cnt.p);
+  SELF_LAUNCHED(b->ctx);
+  const size_t tiles = A.cap_e + A.cap_g + A.cap_v;
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>((tiles + kThreads - 1) / kThreads >> (2 * L), 4096));
+  bk_compact_copy<<<grid, kThreads, 0, st>>>(A.dev(), A.gptr.p, b->S.p, ph, D.et.p, D.gt.p, D.vt.p, D.eptr.p,
+                                             D.gptr.p, D.vptr.p);
+  SELF_LAUNCHED(b->ctx);
+  return SELF_OK;
+}
+
+// One tick on the device, enqueued (and captured into a graph by the callers): the outer step of the problems in
+// phase 1 (FP32 form: x += the inner correction; FP64 residual r = b - A x and <r, r>), the outer decision
+// (bk_decide), then the start of new inner solves and graph_k inner PCG iterations of the problems in phase 0.
+// Both sets are compacted on the device, so the tick needs nothing from the host.
+template <typename R>
+int enqueue_tick(self_cgbatch* b, int L, const DecideArgs& da, cudaGraphConditionalHandle cond, int use_cond) {
+  cudaStream_t st = b->ctx->stream;
+  int rc;
+  const auto& O = b->outer;
+  const TileView VO = O.dev();
+  if ((rc = enqueue_compact(b, b->outer, 1, L))) return rc;
+  const int ge = level_grid(O.cap_e, L), gg = level_grid(O.cap_g, L), gv = level_grid(O.cap_v, L);
+  if (sizeof(R) == 4) {  // x += u32 for problems whose inner solve ended
+    bk_correct<<<gv, kThreads, 0, st>>>(VO, b->probs.p, b->S.p);
+    SELF_LAUNCHED(b->ctx);
+  }
+  bk_apply_plain<double><<<ge, kThreads, 0, st>>>(VO, b->probs.p, b->S.p, b->DT.p, V_X, V_R, 1, 1);
+  SELF_LAUNCHED(b->ctx);
+  bk_dss<double><<<gg, kThreads, 0, st>>>(VO, b->probs.p, b->S.p, V_R, 1);
+  SELF_LAUNCHED(b->ctx);
+  bk_rr<<<gv, kThreads, 0, st>>>(VO, b->probs.p, b->S.p, b->partial.p, b->ticket.p, b->red.p);
+  SELF_LAUNCHED(b->ctx);
+  bk_decide<<<1, kThreads, 0, st>>>(b->S.p, b->red.p, b->cap, da, b->counters.p, cond, use_cond);
+  SELF_LAUNCHED(b->ctx);
+  if ((rc = enqueue_compact(b, b->inner, 0, L))) return rc;
+  return enqueue_inner<R>(b, L);
+}
+
+DecideArgs decide_args(const self_solve_opts* o) {
   const bool fp32 = o->precision == SELF_PREC_FP32;
-  const double inner_tol = fp32 ? (o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4) : o->tolerance;
-  const int max_outer = fp32 ? (o->max_outer > 0 ? o->max_outer : 30) : 2;
+  DecideArgs a{};
+  a.tol = o->tolerance;
+  a.inner_tol = fp32 ? (o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4) : o->tolerance;
+  a.fp32 = fp32 ? 1 : 0;
+  a.max_outer = fp32 ? (o->max_outer > 0 ? o->max_outer : 30) : 2;
+  a.max_total = o->maxIters;
+  // every loop body moves each running problem by at least one inner iteration or one refinement decision
+  a.max_bodies = (unsigned int)std::min<long long>(2000000000LL, (long long)o->maxIters + 2LL * a.max_outer + 16);
+  return a;
+}
+
+// Pool view upload (when the pool changed) and the smallest grid level covering its tiles.
+int prepare(self_cgbatch* b, const self_solve_opts* o, int* level) {
   int rc;
   if ((rc = refresh(b))) return rc;
-  for (int p = 0; p < b->cap; ++p) {
-    b->hs[p].max_total = o->maxIters;
-    b->hs[p].max_inner = o->maxIters;
-  }
-  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
-  std::vector<int> outer_set;
+  std::vector<int> used;
   for (int p = 0; p < b->cap; ++p)
-    if (b->slots[p].used && b->hs[p].phase == 1) outer_set.push_back(p);
-  if (!outer_set.empty()) {
-    if ((rc = ensure_view(b, b->outer, outer_set))) return rc;
-    const TileView V = b->outer.dev();
-    const int gv = std::max(1, b->outer.n_v);
-    if (fp32) {  // x += u32 for problems whose inner solve ended
-      bk_correct<<<gv, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p);
-      SELF_LAUNCHED(ctx);
-    }
-    if ((rc = k_apply_plain<double>(b, b->outer, V_X, V_R, 1, 1)) || (rc = k_dss<double>(b, b->outer, V_R, 1, false)))
-      return rc;
-    bk_rr<<<gv, kThreads, 0, ctx->stream>>>(V, b->probs.p, b->S.p, b->partial.p, b->ticket.p, b->red.p);
-    SELF_LAUNCHED(ctx);
-    std::vector<double> rr(b->cap);
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(rr.data(), b->red.p, b->cap * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int p : outer_set) {
-      Scal& s = b->hs[p];
-      const double rn = std::sqrt(rr[p]);
-      s.rr = rn;
-      if (s.fresh) {
-        s.r0 = rn;
-        s.fresh = 0;
-      }
-      const bool conv = s.r0 == 0.0 || rn / s.r0 < o->tolerance || !(rn == rn);
-      if (conv || s.total >= o->maxIters || b->slots[p].outer >= max_outer) {
-        s.phase = 2;
-        continue;
-      }
-      b->slots[p].outer++;
-      s.phase = 0;
-      s.iter = 0;
-      s.num = s.den = s.vz = 0;
-      s.rin0 = rn;
-      s.tol = fp32 ? inner_tol : o->tolerance * s.r0 / rn;
-    }
-    SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
+    if (b->slots[p].used) used.push_back(p);
+  if ((rc = ensure_view(b, b->all, used))) return rc;
+  int L = self_cgbatch::kLevels - 1;
+  while (L > 0 && ((size_t)b->all.n_e > (size_t)level_grid(b->all.cap_e, L) ||
+                   (size_t)b->all.n_g > (size_t)level_grid(b->all.cap_g, L) ||
+                   (size_t)b->all.n_v > (size_t)level_grid(b->all.cap_v, L)))
+    --L;
+  *level = L;
+  const DecideArgs a = decide_args(o);
+  if (b->graph_args_set && std::memcmp(&a, &b->graph_args, sizeof(a)) != 0) drop_graphs(b);
+  b->graph_args = a;
+  b->graph_args_set = true;
+  return SELF_OK;
+}
+
+// Tick graph of the given precision and level (captured once).
+int tick_graph(self_cgbatch* b, bool fp32, int L, cudaGraphExec_t* out) {
+  self_ctx* ctx = b->ctx;
+  cudaGraphExec_t& G = b->tick_graphs[fp32 ? 1 : 0][L];
+  if (!G) {
+    cudaGraph_t g;
+    const long long l0 = ctx->launches.load();
+    SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = fp32 ? enqueue_tick<float>(b, L, b->graph_args, 0, 0) : enqueue_tick<double>(b, L, b->graph_args, 0, 0);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&G, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
+    b->tick_launches[fp32 ? 1 : 0][L] = ctx->launches.load() - l0;
+    ctx->launches.fetch_sub(b->tick_launches[fp32 ? 1 : 0][L]);
   }
-  std::vector<int> inner_set;
-  for (int p = 0; p < b->cap; ++p)
-    if (b->slots[p].used && b->hs[p].phase == 0) inner_set.push_back(p);
-  if (!inner_set.empty()) {
-    if ((rc = ensure_view(b, b->inner, inner_set))) return rc;
-    int L = self_cgbatch::kLevels - 1;  // smallest grid level covering the current tiles
-    while (L > 0 && ((size_t)b->inner.n_e > (size_t)level_grid(b->inner.cap_e, L) ||
-                     (size_t)b->inner.n_g > (size_t)level_grid(b->inner.cap_g, L) ||
-                     (size_t)b->inner.n_v > (size_t)level_grid(b->inner.cap_v, L)))
-      --L;
-    cudaGraphExec_t& G = b->graphs[fp32 ? 1 : 0][L];
-    long long& nk = b->graph_launches[fp32 ? 1 : 0][L];
-    if (!G) {
-      cudaGraph_t g;
-      const long long l0 = ctx->launches.load();
-      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      rc = fp32 ? enqueue_inner<float>(b, L) : enqueue_inner<double>(b, L);
-      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
-      if (rc) return rc;
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&G, g, 0);
+  *out = G;
+  return SELF_OK;
+}
+
+// Persistent solve graph: the tick as the body of a conditional while node whose condition bk_decide clears when
+// no problem is running (or the body budget is spent), so a whole batched solve is one graph launch.
+int loop_graph(self_cgbatch* b, bool fp32, int L, cudaGraphExec_t* out) {
+  self_ctx* ctx = b->ctx;
+  cudaGraphExec_t& G = b->loop_graphs[fp32 ? 1 : 0][L];
+  if (!G) {
+    cudaGraph_t g = nullptr;
+    SELF_CUDA_TRY(ctx, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond;
+    cudaError_t ce = cudaGraphConditionalHandleCreate(&cond, g, 1u, cudaGraphCondAssignDefault);
+    if (ce != cudaSuccess) {
       cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
-      nk = ctx->launches.load() - l0;
-      ctx->launches.fetch_sub(nk);
+      return set_error(ctx, SELF_ERR_CUDA, "conditional handle: %s", cudaGetErrorString(ce));
     }
-    SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
-    ctx->launches.fetch_add(nk);
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    ce = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (ce != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return set_error(ctx, SELF_ERR_CUDA, "conditional node: %s", cudaGetErrorString(ce));
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    const long long l0 = ctx->launches.load();
+    ce = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return set_error(ctx, SELF_ERR_CUDA, "capture into the loop body: %s", cudaGetErrorString(ce));
+    }
+    int rc = fp32 ? enqueue_tick<float>(b, L, b->graph_args, cond, 1) : enqueue_tick<double>(b, L, b->graph_args, cond, 1);
+    ce = cudaStreamEndCapture(ctx->stream, &body);
+    ctx->launches.fetch_sub(ctx->launches.load() - l0);
+    if (rc || ce != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return rc ? rc : set_error(ctx, SELF_ERR_CUDA, "loop body capture: %s", cudaGetErrorString(ce));
+    }
+    ce = cudaGraphInstantiate(&G, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "loop graph instantiate: %s", cudaGetErrorString(ce));
   }
+  *out = G;
+  return SELF_OK;
+}
+
+// Enqueue one tick (no host synchronisation); the slot states are copied into hs by the next sync_states.
+int tick_async(self_cgbatch* b, const self_solve_opts* o) {
+  self_ctx* ctx = b->ctx;
+  int rc, L;
+  if ((rc = prepare(b, o, &L))) return rc;
+  const bool fp32 = o->precision == SELF_PREC_FP32;
+  cudaGraphExec_t G;
+  if ((rc = tick_graph(b, fp32, L, &G))) return rc;
+  SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
+  ctx->launches.fetch_add(b->tick_launches[fp32 ? 1 : 0][L]);
+  return SELF_OK;
+}
+
+// Device slot states into hs (waits for the stream).
+int sync_states(self_cgbatch* b) {
+  self_ctx* ctx = b->ctx;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->hs.data(), b->S.p, b->cap * sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return SELF_OK;
+}
+
+int tick(self_cgbatch* b, const self_solve_opts* o, int* nfinished) {
+  int rc;
+  if ((rc = tick_async(b, o)) || (rc = sync_states(b))) return rc;
   int fin = 0;
   for (int p = 0; p < b->cap; ++p) fin += b->slots[p].used && b->hs[p].phase == 2;
   if (nfinished) *nfinished = fin;
+  return SELF_OK;
+}
+
+// Device copy of slot p's state (stream-ordered before the next tick)
+int put_state(self_cgbatch* b, int p) {
+  SELF_CUDA_TRY(b->ctx, cudaMemcpyAsync(b->S.p + p, &b->hs[p], sizeof(Scal), cudaMemcpyHostToDevice, b->ctx->stream));
   return SELF_OK;
 }
 
@@ -1230,7 +1491,6 @@ int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, 
   }
   self_cgbatch::Slot& S = b->slots[slot];
   S.used = true;
-  S.outer = 0;
   S.bytes = (long long)(m->fac32.bytes() + m->dinv32.bytes() + 6 * nl * 4 + m->fac64.bytes() + m->dinv64.bytes() +
                         7 * nl * 8 + m->src.bytes() + m->gptr.bytes() + m->gidx.bytes() + m->gdir.bytes());
   b->bytes_in_use += S.bytes;
@@ -1248,7 +1508,7 @@ int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, 
   sc.fresh = 1;
   b->dirty = true;
   *slot_out = slot;
-  return SELF_OK;
+  return put_state(b, slot);
 }
 
 }  // namespace
@@ -1297,7 +1557,7 @@ int self_cgbatch_remove(self_cgbatch* b, int p) {
   std::memset(&b->hs[p], 0, sizeof(Scal));
   b->hs[p].phase = 3;
   b->dirty = true;
-  return SELF_OK;
+  return put_state(b, p);
 }
 
 int self_cgbatch_footprint(const self_cg2d_desc* d, long long* bytes) {
@@ -1319,8 +1579,10 @@ int self_cgbatch_set_source(self_cgbatch* b, int p, const double* source) {
   std::memset(&s, 0, sizeof(s));
   s.phase = 1;
   s.fresh = 1;
-  b->slots[p].outer = 0;
   SELF_CUDA_TRY(b->ctx, cudaMemset(b->hp[p].x, 0, b->hp[p].nl * sizeof(double)));
+  int rc = put_state(b, p);
+  if (rc) return rc;
+  SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(b->ctx->stream));
   return SELF_OK;
 }
 
@@ -1348,7 +1610,7 @@ int self_cgbatch_report(self_cgbatch* b, int p, self_solve_report* rep, int* fin
   const double rel = s.r0 > 0 ? s.rr / s.r0 : 0.0;
   rep->ioerr = (s.phase == 2 && rel < 1e300 && (s.r0 == 0 || rel == rel)) ? 0 : -2;
   rep->iterations = s.total;
-  rep->outer_iterations = b->slots[p].outer;
+  rep->outer_iterations = s.outer;
   rep->r0 = s.r0;
   rep->rel_residual = rel;
   if (finished) *finished = s.phase == 2;
@@ -1363,7 +1625,8 @@ int self_cgbatch_step(self_cgbatch* b, const self_solve_opts* o, int* nfinished)
 
 long long self_cgbatch_bytes(const self_cgbatch* b) { return b ? b->bytes_in_use : 0; }
 
-// Solve every problem in the batch from a zero initial guess (ticks until all finished).
+// Solve every problem in the batch from a zero initial guess: one launch of the persistent loop graph (ticks run
+// on the device until every problem finished), then the slot states are read back once.
 int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* o, self_solve_report* reports) {
   if (!b || !o || !(o->tolerance > 0) || o->maxIters < 1) return SELF_ERR_INVALID;
   self_ctx* ctx = b->ctx;
@@ -1376,13 +1639,19 @@ int self_cgbatch_solve(self_cgbatch* b, const self_solve_opts* o, self_solve_rep
     std::memset(&s, 0, sizeof(s));
     s.phase = 1;
     s.fresh = 1;
-    b->slots[p].outer = 0;
     SELF_CUDA_TRY(ctx, cudaMemsetAsync(b->hp[p].x, 0, b->hp[p].nl * sizeof(double), ctx->stream));
   }
-  int rc, fin = 0;
-  const long long max_ticks = (long long)o->maxIters / std::max(1, b->graph_k) + 1000;
-  for (long long t = 0; t < max_ticks && fin < nused; ++t)
-    if ((rc = tick(b, o, &fin))) return rc;
+  int rc, L;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(b->S.p, b->hs.data(), b->cap * sizeof(Scal), cudaMemcpyHostToDevice, ctx->stream));
+  if (nused > 0) {
+    if ((rc = prepare(b, o, &L))) return rc;
+    const bool fp32 = o->precision == SELF_PREC_FP32;
+    cudaGraphExec_t G;
+    if ((rc = loop_graph(b, fp32, L, &G))) return rc;
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(b->counters.p, 0, 2 * sizeof(unsigned int), ctx->stream));
+    SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, ctx->stream));
+  }
+  if ((rc = sync_states(b))) return rc;
   int k = 0;
   for (int p = 0; p < b->cap; ++p) {
     if (!b->slots[p].used) continue;
@@ -1423,6 +1692,7 @@ int self_cgbatch_autotune(self_cgbatch* b, const char* cache_path) {
   std::vector<int> used;
   for (int p = 0; p < b->cap; ++p)
     if (b->slots[p].used) used.push_back(p);
+  if ((rc = sync_states(b))) return rc;  // the device states are the live ones; restored below
   std::vector<Scal> hs(b->cap);
   for (auto& s : hs) {
     std::memset(&s, 0, sizeof(s));

@@ -131,20 +131,28 @@ def bathymetry_gradient(nodal, mesh, h):
     return dhdx, dhdy
 
 
+def dg2d_desc(nodal, mesh, model, nEq, dt, precision, g=9.81, linear_drag=0.0, h=None, dhdx=None, dhdy=None,
+              fcor=None, u=None, v=None, relax=None, rfac=None, kappa=0.0):
+    """self_dg2d_desc over the arrays of a NodalStorage_2D and a QuadMesh; returns (desc, keep): `keep` holds the
+    arrays the descriptor points to and must outlive every use of it."""
+    s = nat.DG2DDesc()
+    s.N, s.nEl, s.nEdges, s.nEq, s.model, s.precision = nodal.N, mesh.nEl, mesh.nEdges, nEq, model, precision
+    s.dmatS, s.dmatP, s.qweight = nat.d(nodal.dmatS), nat.d(nodal.dmatP), nat.d(nodal.w)
+    s.lagW, s.lagE, s.lagS, s.lagN = nat.d(nodal.lW), nat.d(nodal.lE), nat.d(nodal.lS), nat.d(nodal.lN)
+    s.edges = nat.i(mesh.edges)
+    s.dxds, s.dxdp, s.dyds, s.dydp, s.J = (nat.d(getattr(mesh, k)) for k in ("dxds", "dxdp", "dyds", "dydp", "J"))
+    s.nhx, s.nhy, s.nlen = nat.d(mesh.nhx), nat.d(mesh.nhy), nat.d(mesh.nlen)
+    s.h, s.dhdx, s.dhdy, s.fcor = nat.d(h), nat.d(dhdx), nat.d(dhdy), nat.d(fcor)
+    s.relax, s.rfac, s.u, s.v = nat.d(relax), nat.d(rfac), nat.d(u), nat.d(v)
+    s.g, s.linear_drag, s.dt, s.kappa = g, linear_drag, dt, kappa
+    return s, (nodal, mesh, h, dhdx, dhdy, fcor, u, v, relax, rfac)
+
+
 class _DG2D:
     def __init__(self, ctx, nodal, mesh, model, nEq, dt, precision, g=9.81, linear_drag=0.0, h=None, dhdx=None,
                  dhdy=None, fcor=None, u=None, v=None, relax=None, rfac=None, kappa=0.0):
-        s = nat.DG2DDesc()
-        s.N, s.nEl, s.nEdges, s.nEq, s.model, s.precision = nodal.N, mesh.nEl, mesh.nEdges, nEq, model, precision
-        s.dmatS, s.dmatP, s.qweight = nat.d(nodal.dmatS), nat.d(nodal.dmatP), nat.d(nodal.w)
-        s.lagW, s.lagE, s.lagS, s.lagN = nat.d(nodal.lW), nat.d(nodal.lE), nat.d(nodal.lS), nat.d(nodal.lN)
-        s.edges = nat.i(mesh.edges)
-        s.dxds, s.dxdp, s.dyds, s.dydp, s.J = (nat.d(getattr(mesh, k)) for k in ("dxds", "dxdp", "dyds", "dydp", "J"))
-        s.nhx, s.nhy, s.nlen = nat.d(mesh.nhx), nat.d(mesh.nhy), nat.d(mesh.nlen)
-        s.h, s.dhdx, s.dhdy, s.fcor = nat.d(h), nat.d(dhdx), nat.d(dhdy), nat.d(fcor)
-        s.relax, s.rfac, s.u, s.v = nat.d(relax), nat.d(rfac), nat.d(u), nat.d(v)
-        s.g, s.linear_drag, s.dt, s.kappa = g, linear_drag, dt, kappa
-        self._keep = (nodal, mesh, h, dhdx, dhdy, fcor, u, v, relax, rfac)
+        s, self._keep = dg2d_desc(nodal, mesh, model, nEq, dt, precision, g, linear_drag, h, dhdx, dhdy, fcor, u, v,
+                                  relax, rfac, kappa)
         self.ctx = ctx
         self.nodal, self.mesh, self.nEq, self.dt, self.precision = nodal, mesh, nEq, dt, precision
         self.nq = nodal.n * nodal.n * nEq * mesh.nEl

@@ -1,18 +1,14 @@
-"""Continuous-batching serving loop for elliptic solves and short shallow-water ensemble runs on one GPU.
+"""Continuous-batching serving of elliptic solves and short shallow-water ensemble runs on one GPU.
 
-Requests arrive over time (seeded Poisson stream).  The loop admits a request as soon as its device footprint
-fits the HBM budget, then keeps it on the GPU until it finishes:
+The request loop is the library's (self_serve_*, a worker thread in C++ that owns every CUDA call): requests are
+admitted in arrival order while their device footprint fits the HBM budget and stay on the GPU until they finish.
+Helmholtz solves share one batched slot pool whose ticks (outer FP64 residual step, outer decision and inner PCG
+iterations) run on the device with one synchronisation per tick; shallow-water members run on their own handles on
+a few extra streams, in chunks of RK3 steps enqueued asynchronously, so their kernels overlap the solves.  A result
+depends only on its own request, so it is bit-identical alone and in the mix (tests/test_serving_gpu.py).
 
-* Helmholtz solves join a single CGBatch slot pool (self_cgbatch_add): every loop tick advances all active
-  solves together -- FP64 outer residual updates for those whose inner solve ended, then one CUDA graph of
-  FP32 inner PCG iterations covering every active problem (one launch per phase for all of them, whatever their
-  mesh size and degree).  Finished solves leave their slot (self_cgbatch_remove) and free their memory.
-* Shallow-water ensemble members (FP32 form) each get their own handle on one of a few extra streams and advance
-  in chunks of RK3 steps enqueued asynchronously, so their kernels overlap with the batched solves on the device.
-
-Every result depends only on its own request: the batched solver's per-problem arithmetic and reduction order do
-not depend on which other problems share the pool, and each ensemble member runs on its own handle, so a result
-computed in the mix is bit-identical to the same request served alone (tests/test_serving_gpu.py checks this).
+This module is the Python driver: it builds the requests' descriptors, submits each request at its arrival time
+and reads back the outcome.
 """
 import ctypes as C
 import time
@@ -20,9 +16,32 @@ import time
 import numpy as np
 
 from . import _native as nat
-from .batch import CGBatch
-from .cgsem import CG2DDesc, SolveOpts, SolveReport
-from .dgsem import Context, ShallowWater
+from .cgsem import CG2DDesc, SolveReport, cg2d_desc
+from .dgsem import dg2d_desc
+
+QUEUED, RUNNING, DONE, CANCELLED, FAILED = 0, 1, 2, 3, 4
+
+
+class ServeOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("precision", C.c_int), ("tolerance", C.c_double),
+                ("inner_tolerance", C.c_double), ("max_outer", C.c_int), ("maxIters", C.c_int),
+                ("sw_streams", C.c_int), ("sw_chunk", C.c_int), ("max_active", C.c_int)]
+
+
+class ServeInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("kind", C.c_int), ("status", C.c_int), ("steps_done", C.c_int),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double), ("report", SolveReport)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("finished", C.c_longlong),
+                ("cancelled", C.c_longlong), ("failed", C.c_longlong), ("queued", C.c_longlong),
+                ("running", C.c_longlong), ("bytes_in_use", C.c_longlong), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("throughput_per_s", C.c_double),
+                ("elapsed_s", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def poisson_arrivals(n, rate, seed):
@@ -36,133 +55,94 @@ class Request:
         self.admitted = self.finished = None
         self.result = None
         self.report = None
+        self.state = None
 
 
 class Server:
+    """Drives one self_serve loop per run().  precision "fp32": FP32-inner solves under FP64 refinement and FP32
+    shallow-water members; "fp64": the plain FP64 path for both.  max_active = 1 serves one request at a time."""
+
     def __init__(self, ctx, hbm_budget=150e9, sw_streams=4, sw_chunk=10, tolerance=1e-10, inner_tolerance=1e-4,
-                 precision="fp32", graph_chunk=None):
+                 precision="fp32", max_active=0):
         self.ctx = ctx
         self.budget = hbm_budget
-        self.sw_chunk = sw_chunk
-        self.pool = CGBatch(ctx, [])
-        self.opts = SolveOpts()
-        self.opts.method, self.opts.precision = 1, nat.PREC_FP32 if precision == "fp32" else nat.PREC_FP64
-        self.opts.maxIters, self.opts.m, self.opts.tolerance = 100000, 0, tolerance
-        self.opts.inner_tolerance, self.opts.max_outer = inner_tolerance, 30
-        self.sw_ctx = [Context(0) for _ in range(sw_streams)]
-        self.active_cg = {}  # slot -> request
-        self.active_sw = []  # (request, handle, ctx, steps_done)
-        self.used = 0
+        self.sw_streams, self.sw_chunk = sw_streams, sw_chunk
+        self.tolerance, self.inner_tolerance = tolerance, inner_tolerance
+        self.precision = nat.PREC_FP32 if precision == "fp32" else nat.PREC_FP64
+        self.max_active = max_active
         self.keep_results = True
-
-    # -------------------------------------------------------------------------------- admission
-    def _cg_footprint(self, pr):
-        d = CG2DDesc()
-        d.N, d.nEl = pr["nodal"].N, pr["mesh"].nEl
-        b = C.c_longlong()
-        nat.check(nat.lib().self_cgbatch_footprint(C.byref(d), C.byref(b)))
-        return b.value
-
-    def _sw_footprint(self, pr):
-        n2 = (pr["nodal"].N + 1) ** 2
-        return pr["mesh"].nEl * n2 * 4 * 40  # FP32 state, register, metrics, aux, traces and staging
+        self.stats = None
 
     def footprint(self, req):
-        return self._cg_footprint(req.payload) if req.kind == "helmholtz" else self._sw_footprint(req.payload)
-
-    def _admit(self, req, now):
+        """Device bytes the loop charges a request at admission (the same estimate as the library's)."""
         pr = req.payload
         if req.kind == "helmholtz":
-            nod, mesh = pr["nodal"], pr["mesh"]
             d = CG2DDesc()
-            k = np.ascontiguousarray(pr["k"], dtype=np.float64)
-            d.N, d.nEl, d.nEdges, d.nNodes = nod.N, mesh.nEl, mesh.nEdges, mesh.nNodes
-            d.dmat, d.qweight = nat.d(nod.dmatS), nat.d(nod.w)
-            d.edges, d.nodeType = nat.i(mesh.edges), nat.i(mesh.nodeType)
-            d.n2e_ptr, d.n2e_elem, d.n2e_local = nat.i(mesh.n2e_ptr), nat.i(mesh.n2e_elem), nat.i(mesh.n2e_local)
-            d.dxds, d.dxdp, d.dyds, d.dydp, d.J = (nat.d(getattr(mesh, f)) for f in ("dxds", "dxdp", "dyds", "dydp", "J"))
-            d.fluxCoeff = nat.d(k)
-            d.lam, d.op = pr.get("lam", 0.1), 0
-            slot = C.c_int()
-            src = np.ascontiguousarray(pr["source"], dtype=np.float64)
-            nat.check(nat.lib().self_cgbatch_add(self.pool.ptr, C.byref(d), nat.d(src), C.byref(slot)), self.ctx.ptr)
-            self.pool.sizes_by_slot = getattr(self.pool, "sizes_by_slot", {})
-            nl = C.c_longlong()
-            nat.check(nat.lib().self_cgbatch_problem_size(self.pool.ptr, slot.value, C.byref(nl)))
-            self.pool.sizes_by_slot[slot.value] = nl.value
-            self.active_cg[slot.value] = req
-        else:
-            cx = self.sw_ctx[len(self.active_sw) % len(self.sw_ctx)]
-            sw = ShallowWater(cx, pr["nodal"], pr["mesh"], pr["h"], pr["fcor"], pr["dt"], dhdx=pr["dhdx"],
-                              dhdy=pr["dhdy"], precision=nat.PREC_FP32)
-            sw.SetSolution(pr["q"])
-            self.active_sw.append([req, sw, cx, 0])
-        req.admitted = now
-        self.used += self.footprint(req)
+            d.N, d.nEl = pr["nodal"].N, pr["mesh"].nEl
+            b = C.c_longlong()
+            nat.check(nat.lib().self_cgbatch_footprint(C.byref(d), C.byref(b)))
+            return b.value
+        nn = (pr["nodal"].N + 1) ** 2
+        return pr["mesh"].nEl * (nn * 3 * 4 * 40 // 3) * (1 if self.precision == nat.PREC_FP32 else 2) + 4096
 
-    # -------------------------------------------------------------------------------- loop
-    def run(self, requests, t_offset=None):
-        """Serve `requests` (sorted by arrival time, seconds from the start).  Returns the list of requests with
-        admitted/finished times filled in."""
-        pending = list(requests)
-        queue = []
-        t0 = time.perf_counter() if t_offset is None else t_offset
-        lib = nat.lib()
-        done = 0
-        total = len(pending)
-        while done < total:
-            now = time.perf_counter() - t0
-            while pending and pending[0].arrival <= now:
-                queue.append(pending.pop(0))
-            while queue and self.used + self.footprint(queue[0]) <= self.budget:
-                self._admit(queue.pop(0), now)
-            # shallow-water members: enqueue the next chunk on idle streams
-            for ent in self.active_sw:
-                req, sw, cx, steps = ent
-                if steps < req.payload["steps"] and lib.self_ctx_query(cx.ptr) == 1:
-                    k = min(self.sw_chunk, req.payload["steps"] - steps)
-                    sw.ForwardStepRK3_async(0.0, k)
-                    ent[3] = steps + k
-            # batched solves: one tick for every active problem
-            if self.active_cg:
-                nfin = C.c_int()
-                nat.check(lib.self_cgbatch_step(self.pool.ptr, C.byref(self.opts), C.byref(nfin)), self.ctx.ptr)
-                for slot in list(self.active_cg):
-                    rep, fin = SolveReport(), C.c_int()
-                    nat.check(lib.self_cgbatch_report(self.pool.ptr, slot, C.byref(rep), C.byref(fin)))
-                    if fin.value:
-                        req = self.active_cg.pop(slot)
-                        req.report = rep.as_dict()
-                        if self.keep_results:
-                            out = np.zeros(self.pool.sizes_by_slot[slot])
-                            nat.check(lib.self_cgbatch_get_solution(self.pool.ptr, slot, nat.d(out)))
-                            req.result = out
-                        nat.check(lib.self_cgbatch_remove(self.pool.ptr, slot))
-                        req.finished = time.perf_counter() - t0
-                        self.used -= self.footprint(req)
-                        done += 1
-            # finished shallow-water members
-            still = []
-            for ent in self.active_sw:
-                req, sw, cx, steps = ent
-                if steps >= req.payload["steps"] and lib.self_ctx_query(cx.ptr) == 1:
-                    if self.keep_results:
-                        req.result = sw.GetSolution()
-                    sw.Trash()
-                    req.finished = time.perf_counter() - t0
-                    self.used -= self.footprint(req)
-                    done += 1
+    def _desc(self, req):
+        pr = req.payload
+        if req.kind == "helmholtz":
+            d, keep = cg2d_desc(pr["nodal"], pr["mesh"], pr["k"], pr.get("lam", 0.1))
+            src = np.ascontiguousarray(pr["source"], dtype=np.float64)
+            return d, (keep, src), src
+        d, keep = dg2d_desc(pr["nodal"], pr["mesh"], nat.MODEL_SW_CONSERVATIVE, 3, pr["dt"], self.precision,
+                            h=pr["h"], dhdx=pr["dhdx"], dhdy=pr["dhdy"], fcor=pr["fcor"])
+        q = np.ascontiguousarray(pr["q"], dtype=np.float64)
+        return d, (keep, q), q
+
+    def run(self, requests):
+        """Serve `requests` (sorted by arrival time, seconds from the start): each is submitted at its arrival time
+        and the call returns when all are finished.  admitted / finished are on the arrival clock."""
+        L = nat.lib()
+        o = ServeOpts(self.budget, self.precision, self.tolerance, self.inner_tolerance, 30, 100000, self.sw_streams,
+                      self.sw_chunk, self.max_active)
+        sp = C.c_void_p()
+        nat.check(L.self_serve_create(self.ctx.ptr, C.byref(o), C.byref(sp)), self.ctx.ptr)
+        tickets = []
+        try:
+            descs = [self._desc(r) for r in requests]  # kept alive until the loop is destroyed
+            t0 = time.perf_counter()
+            for r, (d, k, data) in zip(requests, descs):
+                wait = r.arrival - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
+                t = C.c_longlong()
+                if r.kind == "helmholtz":
+                    nat.check(L.self_serve_submit_solve(sp, C.byref(d), nat.d(data), C.byref(t)))
                 else:
-                    still.append(ent)
-            self.active_sw = still
-            if not self.active_cg and not self.active_sw and not queue and pending:
-                time.sleep(max(0.0, min(1e-3, pending[0].arrival - (time.perf_counter() - t0))))
+                    nat.check(L.self_serve_submit_sw(sp, C.byref(d), nat.d(data), int(r.payload["steps"]), C.byref(t)))
+                tickets.append(t.value)
+            nat.check(L.self_serve_wait(sp, C.c_double(3600.0)))
+            for r, t, (d, k, data) in zip(requests, tickets, descs):
+                info = ServeInfo()
+                nat.check(L.self_serve_poll(sp, C.c_longlong(t), C.byref(info)))
+                r.state = info.state
+                if info.state != DONE:
+                    raise nat.SelfError(info.status, f"request {r.rid} ended in state {info.state}")
+                shift = r.arrival - info.submit_s
+                r.admitted, r.finished = info.admit_s + shift, info.done_s + shift
+                if r.kind == "helmholtz":
+                    r.report = {k2: getattr(info.report, k2) for k2, _ in SolveReport._fields_}
+                if self.keep_results:
+                    n = data.size if r.kind == "sw" else r.payload["mesh"].nEl * (r.payload["nodal"].N + 1) ** 2
+                    out = np.zeros(n)
+                    nat.check(L.self_serve_result(sp, C.c_longlong(t), nat.d(out), C.c_size_t(n)))
+                    r.result = out
+            st = ServeStats()
+            nat.check(L.self_serve_stats(sp, C.byref(st)))
+            self.stats = st.as_dict()
+        finally:
+            L.self_serve_destroy(sp)
         return requests
 
     def close(self):
-        self.pool.Trash()
-        for c in self.sw_ctx:
-            c.close()
+        pass
 
 
 def latency_stats(reqs):

@@ -1,4 +1,5 @@
-"""Continuous-batching serving loop: every result computed in the mix equals the same request served alone."""
+"""Continuous-batching request loop (self_serve_*): every result computed in the mix equals the same request served
+alone; admission respects the HBM budget; cancellation and statistics through the C ABI."""
 import numpy as np
 import pytest
 
@@ -46,3 +47,42 @@ def test_admission_respects_the_budget(gpu_ctx):
     order = sorted(reqs, key=lambda r: r.admitted)
     for a, b in zip(order, order[1:]):
         assert b.admitted >= a.finished - 1e-9 or srv.footprint(a) + srv.footprint(b) <= srv.budget
+
+
+def test_cancel_and_stats_through_the_c_abi(gpu_ctx):
+    """Queued requests behind a one-at-a-time cap can be cancelled; statistics count them; poll reports states."""
+    import ctypes as C
+
+    import self_gb300 as sg
+    from self_gb300 import _native as nat
+    from self_gb300 import serving as S
+    L = nat.lib()
+    reqs = [r for r in _reqs(sg, seed=9) if r.kind == "helmholtz"][:3]
+    srv = S.Server(gpu_ctx, max_active=1)
+    o = S.ServeOpts(srv.budget, srv.precision, 1e-10, 1e-4, 30, 100000, 1, 5, 1)
+    sp = C.c_void_p()
+    nat.check(L.self_serve_create(gpu_ctx.ptr, C.byref(o), C.byref(sp)))
+    try:
+        tickets, keep = [], []
+        for r in reqs:
+            d, k, src = srv._desc(r)
+            keep.append((d, k, src))
+            t = C.c_longlong()
+            nat.check(L.self_serve_submit_solve(sp, C.byref(d), nat.d(src), C.byref(t)))
+            tickets.append(t.value)
+        nat.check(L.self_serve_cancel(sp, C.c_longlong(tickets[-1])))
+        nat.check(L.self_serve_wait(sp, C.c_double(600.0)))
+        states = []
+        for t in tickets:
+            info = S.ServeInfo()
+            nat.check(L.self_serve_poll(sp, C.c_longlong(t), C.byref(info)))
+            states.append(info.state)
+        assert states[0] == S.DONE and states[-1] in (S.CANCELLED, S.DONE)
+        st = S.ServeStats()
+        nat.check(L.self_serve_stats(sp, C.byref(st)))
+        assert st.submitted == 3 and st.finished + st.cancelled == 3 and st.queued == 0 and st.running == 0
+        assert st.p99_ms >= st.p50_ms > 0 and st.bytes_in_use == 0
+        assert L.self_serve_poll(sp, C.c_longlong(12345), C.byref(S.ServeInfo())) != 0  # unknown ticket
+    finally:
+        L.self_serve_destroy(sp)
+
