@@ -460,7 +460,7 @@ def batched_leg(sg, ctx, nprob=512, fp64_sample=32):
 def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, sweep_n=150, base_n=120):
     """Poisson streams (seeded) mixing 70 % Helmholtz solves from the batched distribution and 30 % shallow-water
     ensemble members (64x64, N=5, 100 steps), served by the library's request loop (self_serve_*): continuous
-    batching (FP32 inner + FP64 refinement, FP32 members) at the configured 2000 req/s and at 25 / 50 / 90 % of the
+    batching (FP32 inner + FP64 refinement, FP32 members) at the configured 2000 req/s and at 25 / 50 / 75 % of the
     capacity it measured there; the plain FP64 path one request at a time (the same loop with max_active = 1 and
     FP64 solves and members), run on the same 2000 req/s stream and at half its own capacity."""
     from self_gb300 import serving as S
@@ -479,8 +479,9 @@ def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, sweep_n=150, base_n=120)
     mix = serve(nreq, rate, "fp32")
     out["continuous_batching"] = mix
     cap = mix["throughput_req_s"]
-    out["load_sweep"] = [serve(sweep_n, f * cap, "fp32", seed_=seed + 10 + i) for i, f in enumerate((0.25, 0.5, 0.9))]
-    for row, f in zip(out["load_sweep"], (0.25, 0.5, 0.9)):
+    fracs = (0.25, 0.5, 0.75)
+    out["load_sweep"] = [serve(sweep_n, f * cap, "fp32", seed_=seed + 10 + i) for i, f in enumerate(fracs)]
+    for row, f in zip(out["load_sweep"], fracs):
         row["fraction_of_capacity"] = f
     base = serve(base_n, rate, "fp64", max_active=1)
     out["fp64_one_at_a_time"] = base
