@@ -211,6 +211,9 @@ typedef struct {
   int pc_iterations;      /* SELF_SOLVE_PCG_LINEAR: inner CG steps per application (CGsemParams pcIterates, 50) */
   double pc_tolerance;    /* SELF_SOLVE_PCG_LINEAR: inner stop ||r||/||r0|| < pc_tolerance (pcTolerance, 1e-4) */
   int pc_nodes;           /* SELF_SOLVE_PCG_LINEAR: SELF_PC_NODES_POSITION or SELF_PC_NODES_CONNECTIVITY */
+  /* FP32 inner CG at N = 7: nonzero runs the element operator's derivative contractions on the tensor cores
+   * (tcgen05 GEMMs of 32-element tiles, compensated TF32 products); 0 uses the CUDA-core line form */
+  int tensor_cores;
 } self_solve_opts;
 /* How the preconditioner mesh identifies shared GLL nodes.  POSITION is the reference (AlmostEqual positions,
  * ~1 ulp): where positions of one node computed in different elements differ by more (transfinite elements, e.g.
@@ -231,6 +234,10 @@ typedef struct self_cg2d self_cg2d;
 int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* desc, self_cg2d** out);
 int self_cg2d_destroy(self_cg2d* h);
 int self_cg2d_matrix_action(self_cg2d* h, const double* u, double* Au);
+/* The FP32 form of MatrixAction that the FP32 inner solves use (u and Au in FP64 on the host, the operator in
+ * FP32); tensor_cores != 0 (N = 7 only) runs the derivative contractions on the tensor cores with compensated TF32
+ * products, as self_solve_opts.tensor_cores does in the solves. */
+int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int tensor_cores);
 int self_cg2d_residual(self_cg2d* h, const double* source, const double* solution, double* r);
 int self_cg2d_dot(self_cg2d* h, const double* u, const double* v, double* out);
 int self_cg2d_mask(self_cg2d* h, double* u);

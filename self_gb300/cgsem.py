@@ -35,7 +35,8 @@ class CG2DDesc(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("maxIters", C.c_int), ("m", C.c_int),
                 ("tolerance", C.c_double), ("inner_tolerance", C.c_double), ("max_outer", C.c_int),
-                ("pc_iterations", C.c_int), ("pc_tolerance", C.c_double), ("pc_nodes", C.c_int)]
+                ("pc_iterations", C.c_int), ("pc_tolerance", C.c_double), ("pc_nodes", C.c_int),
+                ("tensor_cores", C.c_int)]
 
     def __init__(self, *a, **kw):
         super().__init__(*a, **kw)
@@ -97,6 +98,14 @@ class CGsemElliptic_2D:
         self._chk(nat.lib().self_cg2d_matrix_action(self.ptr, nat.d(u), nat.d(out)))
         return out
 
+    def MatrixAction32(self, u, tensor_cores=False):
+        """MatrixAction with the FP32 operator of the inner solves (contractions on the tensor cores with
+        tensor_cores=True, N = 7)."""
+        u = self._vec(u)
+        out = np.zeros(self.nl)
+        self._chk(nat.lib().self_cg2d_matrix_action_f32(self.ptr, nat.d(u), nat.d(out), 1 if tensor_cores else 0))
+        return out
+
     def Residual(self, source, solution):
         out = np.zeros(self.nl)
         self._chk(nat.lib().self_cg2d_residual(self.ptr, nat.d(self._vec(source)), nat.d(self._vec(solution)),
@@ -120,8 +129,9 @@ class CGsemElliptic_2D:
 
     def Solve(self, source, solution=None, method="pcg", precision="fp64", maxIters=20000, tolerance=1e-10, m=30,
               inner_tolerance=1e-4, max_outer=30, dirichlet=None, return_resi=False, pc_iterations=50,
-              pc_tolerance=1e-4, pc_nodes="position"):
+              pc_tolerance=1e-4, pc_nodes="position", tensor_cores=False):
         o = SolveOpts()
+        o.tensor_cores = 1 if tensor_cores else 0
         o.method = _METHODS[method]
         o.precision = nat.PREC_FP32 if precision == "fp32" else nat.PREC_FP64
         o.maxIters, o.m, o.tolerance = maxIters, m, tolerance

@@ -871,6 +871,7 @@ __global__ void __launch_bounds__(kRedThreads) pcg_start_fused(const R* __restri
 }
 
 #include "pc_linear.cuh"
+#include "tc_apply.cuh"
 
 // ---------------------------------------------------------------------------------- generic vector ops
 template <typename R>
@@ -965,8 +966,10 @@ namespace cg {
 // Buffers a captured PCG iteration graph was built on.
 struct PcgGraphKey {
   const void *u, *r, *v, *v2, *w, *z, *dinv, *fac;
+  int tc;  // tensor-core form of the FP32 apply
   bool operator==(const PcgGraphKey& o) const {
-    return u == o.u && r == o.r && v == o.v && v2 == o.v2 && w == o.w && z == o.z && dinv == o.dinv && fac == o.fac;
+    return u == o.u && r == o.r && v == o.v && v2 == o.v2 && w == o.w && z == o.z && dinv == o.dinv &&
+           fac == o.fac && tc == o.tc;
   }
 };
 
@@ -1020,6 +1023,7 @@ struct self_cg2d {
   selfgpu::cg::PcgGraphKey pcg_key[2][2] = {};
   long long pcg_graph_launches = 0;  // kernels in a captured PCG graph
   int apply_grid = 0;                // blocks of the fused apply (grid-stride over element groups)
+  int tc = 0;                        // FP32 apply at N = 7 on the tensor cores (set per solve from the options)
   // linear-FEM preconditioner (SELF_SOLVE_PCG_LINEAR): node positions kept from create; the linear mesh's topology,
   // sub-quad factors and work vectors are built on first use
   struct PcLinear {
@@ -1150,6 +1154,21 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
   const int epb = (sizeof(R) == 4 || eo) ? line_epb<N1>() : cg_epb<N1>();
   const int groups = (h->nEl + epb - 1) / epb;
   const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
+  if constexpr (sizeof(R) == 4 && N1 == 8) {
+    if (h->tc) {  // tensor-core contractions (tcgen05, compensated TF32), 32 elements per tile
+      static int tc_resident[2] = {0, 0};
+      int& q = tc_resident[NF == 6];
+      const int smem = (int)sizeof(tc::Smem);
+      if (q == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_tc<NF>, kRedThreads, smem) != cudaSuccess)
+        q = 2;
+      q = std::max(1, std::min(q, 4));  // 128 TMEM columns per block: at most 4 blocks per SM hold them at once
+      const int tgroups = (h->nEl + tc::kTileElems - 1) / tc::kTileElems;
+      const int tgrid = std::max(1, std::min({h->apply_grid, q * std::max(1, h->ctx->num_sms), tgroups}));
+      pcg_apply_tc<NF><<<tgrid, kRedThreads, smem, h->ctx->stream>>>(w, vold, vnew, h->src.p, fac, z, h->nEl, C,
+                                                                      h->S.p, h->partial.p, h->ticket.p);
+      return;
+    }
+  }
   if constexpr (sizeof(R) == 4) {
     pcg_apply_fused_f32<N1, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
         w, vold, vnew, h->src.p, fac, z, h->nEl, C, h->S.p, h->partial.p, h->ticket.p);
@@ -1350,8 +1369,8 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
       SELF_LAUNCHED(ctx);
     }
     const int prec = sizeof(R) == 4 ? 1 : 0;
-    PcgGraphKey key{u, r, v, v2, w, z, dinv, od.fac.p};
-    if (pc) key = PcgGraphKey{u, r, v, v2, w, z, pc->ul, pc->fac};
+    PcgGraphKey key{u, r, v, v2, w, z, dinv, od.fac.p, h->tc};
+    if (pc) key = PcgGraphKey{u, r, v, v2, w, z, pc->ul, pc->fac, h->tc};
     cudaGraphExec_t& G = pc ? h->pcl.graph[prec] : h->pcg_graph[prec][dinv ? 1 : 0];
     PcgGraphKey& gk = pc ? h->pcl.key[prec] : h->pcg_key[prec][dinv ? 1 : 0];
     long long& glaunches = pc ? h->pcl.graph_launches : h->pcg_graph_launches;
@@ -1750,6 +1769,37 @@ int self_cg2d_destroy(self_cg2d* h) {
 }
 
 // MatrixAction: Au = Mask(GlobalSum(L(UnMask(u)))).  u is read only (the reference leaves u masked).
+int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int tensor_cores) {
+  if (!h || !u || !Au) return SELF_ERR_INVALID;
+  self_ctx* ctx = h->ctx;
+  SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  if (tensor_cores && h->N != 7)
+    return set_error(ctx, SELF_ERR_UNSUPPORTED, "tensor-core FP32 operator: N = 7 only (N = %d)", h->N);
+  const size_t nl = h->nl;
+  int rc;
+  if ((rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->z, nl)) || (rc = ensuref(ctx, h->w32, nl)) ||
+      (rc = ensuref(ctx, h->v32, nl)) || (rc = ensuref(ctx, h->v2_32, nl)) || (rc = ensuref(ctx, h->z32, nl)))
+    return rc;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->r.p, u, nl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->w32.p, h->r.p, nl);
+  SELF_LAUNCHED(ctx);
+  CGScalars hs{};  // first iteration of the fused apply: v = w, z = L(unmask(w)), alpha from num = 1
+  hs.num = 1.0;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
+  h->tc = tensor_cores ? 1 : 0;
+  rc = launch_apply_fused<float>(h, h->w32.p, h->v2_32.p, h->v32.p, h->z32.p, h->op32);
+  h->tc = 0;
+  if (rc || (rc = launch_dss<float>(h, h->z32.p))) return rc;
+  convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->z32.p, nl);
+  SELF_LAUNCHED(ctx);
+  CGScalars out{};
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&out, h->S.p, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(Au, h->z.p, nl * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (out.ioerr == SELF_ERR_TIMEOUT) return set_error(ctx, SELF_ERR_TIMEOUT, "tensor-core barrier wait ran out");
+  return SELF_OK;
+}
+
 int self_cg2d_matrix_action(self_cg2d* h, const double* u, double* Au) {
   if (!h || !u || !Au) return SELF_ERR_INVALID;
   self_ctx* ctx = h->ctx;
@@ -2454,6 +2504,7 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
       if ((rc = ensuref(ctx, h->u32, nl)) || (rc = ensuref(ctx, h->r32, nl)) || (rc = ensuref(ctx, h->v32, nl)) ||
           (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)) || (rc = ensuref(ctx, h->v2_32, nl)))
         return rc;
+      h->tc = (o->tensor_cores && h->N == 7) ? 1 : 0;
       const double inner_tol = o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4;
       const int max_outer = o->max_outer > 0 ? o->max_outer : 30;
       double rn = r0;
@@ -2468,10 +2519,14 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         int it_in = 0;
         double rel_in = 0;
         const PcRun<float> pc = use_pcl ? pcl_run<float>(h, o->pc_iterations) : PcRun<float>{};
-        pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p, jac ? h->op32.dinv.p : nullptr,
-                          o->maxIters - total, inner_tol, rn, nullptr, &it_in, &rel_in, h->op32, false,
-                          use_pcl ? &pc : nullptr);
+        const int inner_err = pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p,
+                                                jac ? h->op32.dinv.p : nullptr, o->maxIters - total, inner_tol, rn,
+                                                nullptr, &it_in, &rel_in, h->op32, false, use_pcl ? &pc : nullptr);
         total += it_in;
+        if (inner_err == SELF_ERR_TIMEOUT) {  // a bounded tensor-core wait ran out in the inner solve
+          h->tc = 0;
+          return set_error(ctx, SELF_ERR_TIMEOUT, "FP32 inner solve: a tensor-core barrier wait ran out");
+        }
         // x += d (FP64), r = b - A x in FP64
         convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->u32.p, nl);
         SELF_LAUNCHED(ctx);
@@ -2488,6 +2543,7 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         }
         if (it_in == 0) break;
       }
+      h->tc = 0;
       iters = total;
       rel = rn / r0;
       R.outer_iterations = outer;
