@@ -1156,12 +1156,14 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
   const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
   if constexpr (sizeof(R) == 4 && N1 == 8) {
     if (h->tc) {  // tensor-core contractions (tcgen05, compensated TF32), 32 elements per tile
-      static int tc_resident[2] = {0, 0};
-      int& q = tc_resident[NF == 6];
+      static bool attr_set[2] = {false, false};
       const int smem = (int)sizeof(tc::Smem);
-      if (q == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_tc<NF>, kRedThreads, smem) != cudaSuccess)
-        q = 2;
-      q = std::max(1, std::min(q, 4));  // 128 TMEM columns per block: at most 4 blocks per SM hold them at once
+      if (!attr_set[NF == 6]) {
+        cudaFuncSetAttribute(pcg_apply_tc<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set[NF == 6] = true;
+      }
+      // 4 blocks per SM: the shared-memory and register limits, and 4 x 128 TMEM columns fill the SM's 512
+      const int q = 4;
       const int tgroups = (h->nEl + tc::kTileElems - 1) / tc::kTileElems;
       const int tgrid = std::max(1, std::min({h->apply_grid, q * std::max(1, h->ctx->num_sms), tgroups}));
       pcg_apply_tc<NF><<<tgrid, kRedThreads, smem, h->ctx->stream>>>(w, vold, vnew, h->src.p, fac, z, h->nEl, C,

@@ -12,7 +12,8 @@
 // MMAs A_hi B and A_lo B give all four products A_x D_y in FP32 accumulators and the epilogue adds the two column
 // halves: the products' relative error is about 2^-21 (FP32 is 2^-24), against 2^-11 for one TF32 product.
 // Operand layout (no swizzle, K-major): 8-row groups of two 128-byte core matrices (k 0-3, k 4-7); the leading
-// byte offset (next core matrix along K) is 128, the stride byte offset (next 8-row group) 256.  Accumulators:
+// byte offset (next core matrix along K) is 144 and the stride byte offset (next 8-row group) 288, padded so that
+// the transposed operand writes of a warp (8 rows of 4 groups x 8 columns) fall in 32 distinct banks.  Accumulators:
 // TMEM columns 0-63 of a 128-column allocation per CTA (rows 0-127 in columns 0-31, rows 128-255 in columns 32-63;
 // s in the first 16 of each, p in the next 16); warp w reads TMEM lanes 32 (w % 4) .. + 31 of column block w / 4.
 // Every mbarrier wait is bounded; on time-out (a block-uniform decision) the kernel flags the solve (ioerr
@@ -23,15 +24,16 @@ namespace tc {
 
 constexpr int kTileElems = 32;
 constexpr int kTileRows = kTileElems * 8;  // 256 lines = blockDim
-constexpr int kOpBytes = kTileRows * 8 * 4;  // one A operand (256 x 8 TF32)
-constexpr int kBBytes = 16 * 8 * 4;          // one B operand (16 x 8 TF32)
+constexpr int kLBO = 144, kSBO = 288;         // operand strides (bytes): next core matrix along K, next 8 rows
+constexpr int kOpFloats = kTileRows / 8 * kSBO / 4;  // one A operand (256 x 8 TF32, padded)
+constexpr int kBFloats = 2 * kSBO / 4;               // one B operand (16 x 8 TF32, padded)
 constexpr uint32_t kTmemCols = 128;  // 64 used; the allocation keeps a margin (at most 4 blocks per SM)
 constexpr long long kMaxPolls = 1LL << 22;
 
 struct alignas(128) Smem {
-  float As_hi[kTileRows * 8], As_lo[kTileRows * 8];  // s-direction operand (rows (e, j))
-  float Ap_hi[kTileRows * 8], Ap_lo[kTileRows * 8];  // p-direction operand (rows (e, i))
-  float B1[16 * 8], B2[16 * 8];                       // [D_hi | D_lo] for stage 1, [D^T_hi | D^T_lo] for stage 2
+  float As_hi[kOpFloats], As_lo[kOpFloats];  // s-direction operand (rows (e, j))
+  float Ap_hi[kOpFloats], Ap_lo[kOpFloats];  // p-direction operand (rows (e, i))
+  float B1[kBFloats], B2[kBFloats];          // [D_hi | D_lo] for stage 1, [D^T_hi | D^T_lo] for stage 2
   float T[kTileRows * 9];                             // transposes of the p-direction outputs (padded rows)
   uint64_t mbar;
   uint32_t tmem_base;
@@ -40,12 +42,12 @@ struct alignas(128) Smem {
 __device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // byte offset of element (row r, k) in a K-major operand
-__device__ __forceinline__ int opoff(int r, int k) { return (r >> 3) * 256 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4; }
+__device__ __forceinline__ int opoff(int r, int k) { return (r >> 3) * kSBO + (k >> 2) * kLBO + (r & 7) * 16 + (k & 3) * 4; }
 
-// shared-memory matrix descriptor: start address, LBO 128, SBO 256, descriptor version 1 (bits 46-48 = 0b001),
-// base offset 0, no swizzle
+// shared-memory matrix descriptor: start address, LBO, SBO, descriptor version 1 (bits 46-48 = 0b001), base offset
+// 0, no swizzle
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(kLBO >> 4) << 16) | ((uint64_t)(kSBO >> 4) << 32) |
          ((uint64_t)1 << 46);
 }
 
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(tc::kTileRows) pcg_apply_tc(const float* __res
   auto issue = [&](uint64_t dB) {  // one thread: s and p MMAs of both halves (hi then lo with accumulation)
     tc::fence_after();
     for (int h = 0; h < 2; ++h) {
-      const uint32_t off = (uint32_t)(h * 128 / 8 * 256);  // 16 row groups of 256 bytes per half
+      const uint32_t off = (uint32_t)(h * 128 / 8 * tc::kSBO);  // 16 row groups per half
       const uint32_t dcol = tmem + (uint32_t)(32 * h);
       tc::mma(dcol, tc::sdesc(tc::sa(sm.As_hi) + off), dB, 0);
       tc::mma(dcol, tc::sdesc(tc::sa(sm.As_lo) + off), dB, 1);
