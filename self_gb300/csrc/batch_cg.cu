@@ -1055,10 +1055,21 @@ int ensure_cap(self_cgbatch* b, int want) {
   std::memset(&e, 0, sizeof(e));
   e.phase = 3;
   b->hs.resize(nc, e);
+  const int old_cap = b->cap;
   b->cap = nc;
   int rc;
-  if ((rc = zeros(b->ctx, b->probs, nc)) || (rc = zeros(b->ctx, b->S, nc)) || (rc = zeros(b->ctx, b->red, nc)) ||
-      (rc = zeros(b->ctx, b->ticket, nc)))
+  // the device slot states are the live ones (the outer decisions run on the device): the grown array keeps them,
+  // and the new slots start empty (phase 3)
+  DevBuf<Scal> S2;
+  if (S2.alloc(nc) != cudaSuccess) return set_error(b->ctx, SELF_ERR_ALLOC, "batch: device allocation failed");
+  SELF_CUDA_TRY(b->ctx, cudaStreamSynchronize(b->ctx->stream));
+  if (old_cap > 0 && b->S.p)
+    SELF_CUDA_TRY(b->ctx, cudaMemcpy(S2.p, b->S.p, (size_t)old_cap * sizeof(Scal), cudaMemcpyDeviceToDevice));
+  SELF_CUDA_TRY(b->ctx, cudaMemcpy(S2.p + old_cap, b->hs.data() + old_cap, (size_t)(nc - old_cap) * sizeof(Scal),
+                                   cudaMemcpyHostToDevice));
+  std::swap(b->S.p, S2.p);
+  std::swap(b->S.n, S2.n);
+  if ((rc = zeros(b->ctx, b->probs, nc)) || (rc = zeros(b->ctx, b->red, nc)) || (rc = zeros(b->ctx, b->ticket, nc)))
     return rc;
   drop_graphs(b);  // the captured graphs hold the old arrays
   b->cap_et = b->cap_gt = b->cap_vt = 0;  // per-problem pointer tables are sized by the slot count
