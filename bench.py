@@ -144,7 +144,7 @@ FLOPS_PER_EL_STAGE_N7 = FLOPS_VOLUME_PER_EL_N7 + FLOPS_EDGE_PER_EL_N7
 # aux + 3 2n edge geometry + 2 4 nEq n traces write + read)
 BYTES_FP64_PER_EL_STAGE_N7 = 8 * (4 * 3 * 64 + 5 * 64 + 3 * 64 + 3 * 2 * 8 + 2 * 4 * 3 * 8)
 # DRAM bytes (read + write) per launch measured by ncu --set full on this workload (one launch each)
-NCU_TRAFFIC_BYTES = {"sw32_fused": 84.90e6, "dg_volume": 129.5e6}
+NCU_TRAFFIC_BYTES = {"sw32_fused": 80.76e6 + 3.96e6, "dg_volume": 130.06e6 + 24.99e6}
 
 
 def cpu_baseline(oracle, nod, mesh, q, h, fcor, dhdx, dhdy, dt, budget_s=12.0, max_steps=5000):
