@@ -312,19 +312,26 @@ def elliptic_leg(sg, ctx, nx=256, N=7, gmres_iters=20000):
         else:
             out["pcg_fp32"]["max_rel_diff_vs_fp64"] = float(np.abs(sol - s64).max() / np.abs(s64).max())
     out["speedup_fp32_ir_vs_fp64"] = out["pcg_fp64"]["seconds"] / out["pcg_fp32"]["seconds"]
-    # the same FP32-inner solve with the operator's derivative contractions on the tensor cores (tcgen05, compensated
-    # TF32)
-    cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-10, maxIters=200, tensor_cores=True)
-    ctx.synchronize()
-    t0 = time.perf_counter()
-    sol, rep = cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-10, maxIters=50000, tensor_cores=True)
-    el = time.perf_counter() - t0
-    out["pcg_fp32_tensor_cores"] = {"seconds": el, "solves_per_s": 1.0 / el, "iterations": rep["iterations"],
-                                    "ms_per_iteration": 1e3 * el / max(1, rep["iterations"]),
-                                    "outer": rep["outer_iterations"], "rel_residual": rep["rel_residual"],
-                                    "ioerr": rep["ioerr"],
-                                    "max_rel_diff_vs_fp64": float(np.abs(sol - s64).max() / np.abs(s64).max()),
-                                    "kernel": "pcg_apply_tc (tcgen05.mma kind::tf32, 3 products per contraction)"}
+    out["pcg_fp32"]["layout"] = "compact (one value per unknown; pcg_apply_compact_f32 + pcg_update_compact)"
+
+    def fp32_variant(**kw):
+        cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-10, maxIters=200, **kw)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        sol, rep = cg.Solve(source, method="pcg", precision="fp32", tolerance=1e-10, maxIters=50000, **kw)
+        el = time.perf_counter() - t0
+        return {"seconds": el, "solves_per_s": 1.0 / el, "iterations": rep["iterations"],
+                "ms_per_iteration": 1e3 * el / max(1, rep["iterations"]), "outer": rep["outer_iterations"],
+                "rel_residual": rep["rel_residual"], "ioerr": rep["ioerr"],
+                "max_rel_diff_vs_fp64": float(np.abs(sol - s64).max() / np.abs(s64).max())}
+
+    # the same FP32-inner solve on the element-local masked L-vectors (3 launches per iteration: apply, direct-
+    # stiffness sum, update), and with the operator's derivative contractions on the tensor cores (tcgen05,
+    # compensated TF32; element-local layout)
+    out["pcg_fp32_element_local"] = fp32_variant(inner_layout="local")
+    out["pcg_fp32_element_local"]["kernel"] = "pcg_apply_fused_f32 + cg_dss_mask_pairs + pcg_update_fused_vec"
+    out["pcg_fp32_tensor_cores"] = fp32_variant(tensor_cores=True)
+    out["pcg_fp32_tensor_cores"]["kernel"] = "pcg_apply_tc (tcgen05.mma kind::tf32, 3 products per contraction)"
     # the reference's own %Solve: PCG with the linear-FEM preconditioner (pcIterates = 20, pcTolerance = 1e-4 as in
     # its paraboloid example); the first call builds the preconditioner mesh (host) and captures the graphs
     t0 = time.perf_counter()
@@ -533,11 +540,12 @@ def run_cg_profile(args):
     cg = sg.CGsemElliptic_2D(ctx, nod, mesh, k, lam=0.1)
     warm = 32 if method == "pcg" else 4
     cg.Solve(source, method=method, precision=prec, tolerance=1e-10, maxIters=warm, pc_iterations=20,
-             tensor_cores=args.profile_tc)
+             tensor_cores=args.profile_tc, inner_layout=args.profile_layout)
     ctx.synchronize()
     t0 = time.perf_counter()
     _, rep = cg.Solve(source, method=method, precision=prec, tolerance=1e-30, maxIters=args.profile_cg, max_outer=1,
-                      pc_iterations=20, pc_tolerance=0.0, tensor_cores=args.profile_tc)
+                      pc_iterations=20, pc_tolerance=0.0, tensor_cores=args.profile_tc,
+                      inner_layout=args.profile_layout)
     el = time.perf_counter() - t0
     print(f"profile-cg: {rep['iterations']} {prec.upper()} {method} iterations in {el:.4f} s", flush=True)
     cg.Trash()
@@ -732,6 +740,8 @@ def main():
     ap.add_argument("--profile-method", default="pcg", choices=["pcg", "pcg_linear", "gmres"])
     ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--profile-tc", action="store_true", help="FP32 profile run with the tensor-core operator")
+    ap.add_argument("--profile-layout", default="compact", choices=["compact", "local"],
+                    help="FP32 inner vectors of the profile run: compact (one value per unknown) or element-local")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_cg > 0:

@@ -214,7 +214,14 @@ typedef struct {
   /* FP32 inner CG at N = 7: nonzero runs the element operator's derivative contractions on the tensor cores
    * (tcgen05 GEMMs of 32-element tiles, compensated TF32 products); 0 uses the CUDA-core line form */
   int tensor_cores;
+  /* storage of the FP32 inner (P)CG vectors: SELF_LAYOUT_COMPACT (default) one value per unknown, grouped by
+   * mesh entity (element interiors, edges, corners), when the mesh is conforming (else the element-local form);
+   * SELF_LAYOUT_LOCAL the masked element-local L-vectors.  The linear-FEM preconditioner and the tensor-core apply
+   * run on the element-local form. */
+  int inner_layout;
 } self_solve_opts;
+#define SELF_LAYOUT_COMPACT 0
+#define SELF_LAYOUT_LOCAL 1
 /* How the preconditioner mesh identifies shared GLL nodes.  POSITION is the reference (AlmostEqual positions,
  * ~1 ulp): where positions of one node computed in different elements differ by more (transfinite elements, e.g.
  * SpecMesh files), the node stays split, the split sub-quad sides become Dirichlet and the PCG can stall, as the
@@ -234,10 +241,15 @@ typedef struct self_cg2d self_cg2d;
 int self_cg2d_create(self_ctx* ctx, const self_cg2d_desc* desc, self_cg2d** out);
 int self_cg2d_destroy(self_cg2d* h);
 int self_cg2d_matrix_action(self_cg2d* h, const double* u, double* Au);
-/* The FP32 form of MatrixAction that the FP32 inner solves use (u and Au in FP64 on the host, the operator in
- * FP32); tensor_cores != 0 (N = 7 only) runs the derivative contractions on the tensor cores with compensated TF32
- * products, as self_solve_opts.tensor_cores does in the solves. */
-int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int tensor_cores);
+/* The FP32 form of MatrixAction that the FP32 inner solves use (u and Au masked L-vectors in FP64 on the host, the
+ * operator in FP32), in one of the inner solves' forms: SELF_F32_LOCAL (element-local L-vectors, CUDA-core line
+ * contractions), SELF_F32_TENSOR_CORES (N = 7 only: the derivative contractions on the tensor cores with compensated
+ * TF32 products, as self_solve_opts.tensor_cores), SELF_F32_COMPACT (the compact node layout of
+ * self_solve_opts.inner_layout; SELF_ERR_UNSUPPORTED on a mesh it does not cover). */
+#define SELF_F32_LOCAL 0
+#define SELF_F32_TENSOR_CORES 1
+#define SELF_F32_COMPACT 2
+int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int form);
 int self_cg2d_residual(self_cg2d* h, const double* source, const double* solution, double* r);
 int self_cg2d_dot(self_cg2d* h, const double* u, const double* v, double* out);
 int self_cg2d_mask(self_cg2d* h, double* u);

@@ -36,7 +36,7 @@ class SolveOpts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("maxIters", C.c_int), ("m", C.c_int),
                 ("tolerance", C.c_double), ("inner_tolerance", C.c_double), ("max_outer", C.c_int),
                 ("pc_iterations", C.c_int), ("pc_tolerance", C.c_double), ("pc_nodes", C.c_int),
-                ("tensor_cores", C.c_int)]
+                ("tensor_cores", C.c_int), ("inner_layout", C.c_int)]
 
     def __init__(self, *a, **kw):
         super().__init__(*a, **kw)
@@ -52,6 +52,8 @@ class SolveReport(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+INNER_LAYOUTS = {"compact": 0, "local": 1}  # SELF_LAYOUT_COMPACT, SELF_LAYOUT_LOCAL
+F32_FORMS = {"local": 0, "tensor_cores": 1, "compact": 2}  # SELF_F32_LOCAL, _TENSOR_CORES, _COMPACT
 _METHODS = {"cg": SOLVE_CG, "pcg": SOLVE_PCG_JACOBI, "pcg_jacobi": SOLVE_PCG_JACOBI, "gmres": SOLVE_GMRES,
             "pgmres": SOLVE_PGMRES_JACOBI, "pcg_linear": SOLVE_PCG_LINEAR}
 
@@ -98,12 +100,14 @@ class CGsemElliptic_2D:
         self._chk(nat.lib().self_cg2d_matrix_action(self.ptr, nat.d(u), nat.d(out)))
         return out
 
-    def MatrixAction32(self, u, tensor_cores=False):
-        """MatrixAction with the FP32 operator of the inner solves (contractions on the tensor cores with
-        tensor_cores=True, N = 7)."""
+    def MatrixAction32(self, u, tensor_cores=False, form=None):
+        """MatrixAction with the FP32 operator of the inner solves, on masked L-vectors: form "local" (element-local
+        vectors, CUDA-core contractions), "tensor_cores" (N = 7; also tensor_cores=True) or "compact" (the compact
+        node layout)."""
+        form = form or ("tensor_cores" if tensor_cores else "local")
         u = self._vec(u)
         out = np.zeros(self.nl)
-        self._chk(nat.lib().self_cg2d_matrix_action_f32(self.ptr, nat.d(u), nat.d(out), 1 if tensor_cores else 0))
+        self._chk(nat.lib().self_cg2d_matrix_action_f32(self.ptr, nat.d(u), nat.d(out), F32_FORMS[form]))
         return out
 
     def Residual(self, source, solution):
@@ -129,9 +133,10 @@ class CGsemElliptic_2D:
 
     def Solve(self, source, solution=None, method="pcg", precision="fp64", maxIters=20000, tolerance=1e-10, m=30,
               inner_tolerance=1e-4, max_outer=30, dirichlet=None, return_resi=False, pc_iterations=50,
-              pc_tolerance=1e-4, pc_nodes="position", tensor_cores=False):
+              pc_tolerance=1e-4, pc_nodes="position", tensor_cores=False, inner_layout="compact"):
         o = SolveOpts()
         o.tensor_cores = 1 if tensor_cores else 0
+        o.inner_layout = INNER_LAYOUTS[inner_layout]
         o.method = _METHODS[method]
         o.precision = nat.PREC_FP32 if precision == "fp32" else nat.PREC_FP64
         o.maxIters, o.m, o.tolerance = maxIters, m, tolerance

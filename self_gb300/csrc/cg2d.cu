@@ -702,6 +702,28 @@ __global__ void __launch_bounds__(kRedThreads, 2) cg_apply_local_eo(const double
   }
 }
 
+// End-of-iteration scalar step (one thread): den = num, num = <r, w>, beta, ||r|| and the stop tests.
+__device__ __forceinline__ void pcg_end_iteration(CGScalars* S, double rw, double rr) {
+  const double rn = sqrt(rr);
+  S->den = S->num;
+  S->num = rw;
+  S->beta = S->num / S->den;
+  S->beta32 = (float)S->beta;
+  S->iter += 1;
+  if (S->resi) S->resi[S->iter] = rn;
+  S->rr = rn;
+  if (!(rn == rn) || isinf(rn)) {  // non-finite residual
+    S->done = 1;
+    S->ioerr = -7;
+  } else if (rn / S->r0 < S->tol) {
+    S->done = 1;
+    S->ioerr = 0;
+  } else if (S->iter >= S->maxIters) {
+    S->done = 1;
+    S->ioerr = -1;
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ u, R* __restrict__ r,
                                                                 R* __restrict__ w, const R* __restrict__ v,
@@ -748,25 +770,7 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused(R* __restrict__ 
   }
   const R acc[2] = {prw, prr};
   double tot[2];
-  if (!grid_sums_last<2, R>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
-  const double rn = sqrt(tot[1]);
-  S->den = S->num;
-  S->num = tot[0];
-  S->beta = S->num / S->den;
-  S->beta32 = (float)S->beta;
-  S->iter += 1;
-  if (S->resi) S->resi[S->iter] = rn;
-  S->rr = rn;
-  if (!(rn == rn) || isinf(rn)) {  // non-finite residual
-    S->done = 1;
-    S->ioerr = -7;
-  } else if (rn / S->r0 < S->tol) {
-    S->done = 1;
-    S->ioerr = 0;
-  } else if (S->iter >= S->maxIters) {
-    S->done = 1;
-    S->ioerr = -1;
-  }
+  if (grid_sums_last<2, R>(acc, partial, ticket, tot) && threadIdx.x == 0) pcg_end_iteration(S, tot[0], tot[1]);
 }
 
 // pcg_update_fused over 16-byte groups of consecutive nodes (float4: 4 FP32 nodes, double2: 2 FP64 nodes; the
@@ -831,25 +835,7 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_fused_vec(V* __restric
   }
   const R acc[2] = {prw, prr};
   double tot[2];
-  if (!grid_sums_last<2, R>(acc, partial, ticket, tot) || threadIdx.x != 0) return;
-  const double rn = sqrt(tot[1]);
-  S->den = S->num;
-  S->num = tot[0];
-  S->beta = S->num / S->den;
-  S->beta32 = (float)S->beta;
-  S->iter += 1;
-  if (S->resi) S->resi[S->iter] = rn;
-  S->rr = rn;
-  if (!(rn == rn) || isinf(rn)) {  // non-finite residual
-    S->done = 1;
-    S->ioerr = -7;
-  } else if (rn / S->r0 < S->tol) {
-    S->done = 1;
-    S->ioerr = 0;
-  } else if (S->iter >= S->maxIters) {
-    S->done = 1;
-    S->ioerr = -1;
-  }
+  if (grid_sums_last<2, R>(acc, partial, ticket, tot) && threadIdx.x == 0) pcg_end_iteration(S, tot[0], tot[1]);
 }
 
 // w = dinv r and num = <r, w> before the first iteration
@@ -872,6 +858,7 @@ __global__ void __launch_bounds__(kRedThreads) pcg_start_fused(const R* __restri
 
 #include "pc_linear.cuh"
 #include "tc_apply.cuh"
+#include "compact.cuh"
 
 // ---------------------------------------------------------------------------------- generic vector ops
 template <typename R>
@@ -1012,6 +999,8 @@ struct self_cg2d {
   DevBuf<selfgpu::cg::GMScalars> GS;
   std::vector<double> h_J, h_w;
   std::vector<double> h_fac, h_dinv;
+  bool affine = false;               // every element affine (see build_factors)
+  std::vector<double> h_kw, h_ec;    // then: k w_i w_j per node, (c11, c12, c22, lambda J) per element
   bool upload_dev = true;  // false: compile the host arrays only (used by the batched solver)
   int nblk = 0;
   // fused (P)CG: second direction buffer, block ticket of the grid-wide sums, one captured iteration graph per
@@ -1024,6 +1013,22 @@ struct self_cg2d {
   long long pcg_graph_launches = 0;  // kernels in a captured PCG graph
   int apply_grid = 0;                // blocks of the fused apply (grid-stride over element groups)
   int tc = 0;                        // FP32 apply at N = 7 on the tensor cores (set per solve from the options)
+  // FP32 inner PCG on the compact node layout (one value per unknown; built on first use, when the shared-node
+  // groups are those of a conforming mesh: see compact_build)
+  struct Compact {
+    bool tried = false, ok = false;
+    int M = 0, nInt = 0, nE2 = 0, nE1 = 0, nC = 0, ng = 0, ngp = 0, nz = 0;
+    DevBuf<int4> desc;
+    DevBuf<int> coff, cl;
+    DevBuf<float> dinv, u, r, v, v2, w, zc;
+    DevBuf<float> fac;  // the FP32 element factors line-interleaved by pass group (compact.cuh factor_index)
+    bool affine = false;  // affine elements: kw (k w_i w_j per node, line-interleaved) and ec per element instead
+    DevBuf<float> kw;
+    DevBuf<float4> ec;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    selfgpu::cg::PcgGraphKey key[2] = {};
+    long long graph_launches = 0;
+  } cpt;
   // linear-FEM preconditioner (SELF_SOLVE_PCG_LINEAR): node positions kept from create; the linear mesh's topology,
   // sub-quad factors and work vectors are built on first use
   struct PcLinear {
@@ -1051,6 +1056,8 @@ struct self_cg2d {
       for (auto& g : row)
         if (g) cudaGraphExecDestroy(g);
     for (auto& g : pcl.graph)
+      if (g) cudaGraphExecDestroy(g);
+    for (auto& g : cpt.graph)
       if (g) cudaGraphExecDestroy(g);
   }
 };
@@ -1365,6 +1372,8 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
   hs.ioerr = hs.done ? 0 : -2;
   hs.resi = resi_dev;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+  // a solve that stopped on a device time-out may have left blocks outside the grid sum: start from a clean ticket
+  SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->ticket.p, 0, sizeof(unsigned int), st));
   if (!hs.done) {
     if (!pc) {
       pcg_start_fused<R><<<h->nblk, kRedThreads, 0, st>>>(r, dinv, w, h->nl, h->S.p, h->partial.p, h->ticket.p);
@@ -1432,6 +1441,164 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
     for (long long gl = 0; gl < max_launches; ++gl) {
       SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
       ctx->launches.fetch_add(glaunches);
+      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (hs.done) break;
+    }
+  }
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  *iters = hs.iter;
+  *rel = hs.iter > 0 ? hs.rr / r0 : 0.0;
+  if (!hs.done) hs.ioerr = -1;
+  return hs.ioerr;
+}
+
+// FP32 PCG on the compact layout (cpt vectors; r holds the right-hand side, u the zero initial guess): two launches
+// per iteration (pcg_apply_compact_f32, pcg_update_compact), captured kGraphIters iterations to a graph.
+template <int N1>
+CompactView compact_view(self_cg2d* h) {
+  auto& Cp = h->cpt;
+  return CompactView{Cp.desc.p, Cp.coff.p, Cp.nInt, Cp.nE2, Cp.nE1, Cp.nC, Cp.ngp, h->nEl};
+}
+
+template <int N1, int NF>
+int launch_compact_apply_t(self_cg2d* h, const float* w, const float* vold, float* vnew) {
+  CGConst<N1, float> Cg;
+  for (int k = 0; k < N1 * N1; ++k) Cg.D[k] = h->op32.D[k];
+  const bool aff = NF == 4 && h->cpt.affine;
+  static int resident[11][3] = {};
+  int& nb = resident[N1][aff ? 2 : (NF == 6)];
+  if (nb == 0) {
+    int q = 0;
+    const cudaError_t ce = aff ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                     &q, pcg_apply_compact_f32<N1, NF, NF == 4>, kRedThreads, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                     &q, pcg_apply_compact_f32<N1, NF, false>, kRedThreads, 0);
+    nb = std::max(1, ce == cudaSuccess ? q : 3);
+  }
+  const int groups = (h->nEl + line_epb<N1>() - 1) / line_epb<N1>();
+  const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
+  AffineOp<N1> A{h->cpt.kw.p, h->cpt.ec.p, {}};
+  for (int j = 0; j < N1; ++j)
+    for (int i = 0; i < N1; ++i) A.ww[i + N1 * j] = (float)(h->h_w[i] * h->h_w[j]);
+  if (aff)
+    pcg_apply_compact_f32<N1, NF, NF == 4><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+        w, vold, vnew, compact_view<N1>(h), h->cpt.fac.p, A, h->cpt.zc.p, Cg, h->S.p, h->partial.p, h->ticket.p);
+  else
+    pcg_apply_compact_f32<N1, NF, false><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+        w, vold, vnew, compact_view<N1>(h), h->cpt.fac.p, A, h->cpt.zc.p, Cg, h->S.p, h->partial.p, h->ticket.p);
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+template <int N1>
+int launch_compact_update_t(self_cg2d* h, const float* vnew, bool jac) {
+  auto& Cp = h->cpt;
+  static int nbu[11] = {};  // resident blocks per SM: one full wave, grid-stride over the node groups
+  if (nbu[N1] == 0) {
+    int q = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_update_compact<N1>, kRedThreads, 0) != cudaSuccess) q = 4;
+    nbu[N1] = std::max(1, q);
+  }
+  const int grid = std::max(1, std::min({h->nblk, nbu[N1] * std::max(1, h->ctx->num_sms), (Cp.ngp / 4 + kRedThreads - 1) / kRedThreads}));
+  pcg_update_compact<N1><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+      reinterpret_cast<float4*>(Cp.u.p), reinterpret_cast<float4*>(Cp.r.p), reinterpret_cast<float4*>(Cp.w.p),
+      reinterpret_cast<const float4*>(vnew), Cp.zc.p, jac ? reinterpret_cast<const float4*>(Cp.dinv.p) : nullptr,
+      compact_view<N1>(h), h->S.p, h->partial.p, h->ticket.p);
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+template <int N1>
+int launch_compact_assemble_t(self_cg2d* h, double* out) {
+  auto& Cp = h->cpt;
+  compact_assemble<N1><<<h->nblk, kRedThreads, 0, h->ctx->stream>>>(out, Cp.zc.p, Cp.cl.p, Cp.ng,
+                                                                   compact_view<N1>(h));
+  SELF_LAUNCHED(h->ctx);
+  return SELF_OK;
+}
+
+// the compact kernels by degree: apply (op = 0), update (1), assemble into a masked FP64 L-vector (2)
+int compact_dispatch(self_cg2d* h, int op, const float* w, const float* vold, float* vnew, bool jac, double* out) {
+  const bool adv = h->nf == 6;
+#define SELF_CG_CASE(NV)                                                                             \
+  case NV:                                                                                           \
+    if (op == 0)                                                                                     \
+      return adv ? launch_compact_apply_t<NV, 6>(h, w, vold, vnew) : launch_compact_apply_t<NV, 4>(h, w, vold, vnew); \
+    if (op == 1) return launch_compact_update_t<NV>(h, vnew, jac);                                  \
+    return launch_compact_assemble_t<NV>(h, out);
+  switch (h->n) {
+    SELF_CG_CASE(3)
+    SELF_CG_CASE(4)
+    SELF_CG_CASE(5)
+    SELF_CG_CASE(6)
+    SELF_CG_CASE(7)
+    SELF_CG_CASE(8)
+    SELF_CG_CASE(9)
+    SELF_CG_CASE(10)
+    default:
+      return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "CG degree %d", h->N);
+  }
+#undef SELF_CG_CASE
+}
+
+int launch_compact_apply(self_cg2d* h, const float* w, const float* vold, float* vnew) {
+  return compact_dispatch(h, 0, w, vold, vnew, false, nullptr);
+}
+int launch_compact_assemble(self_cg2d* h, double* out) {
+  return compact_dispatch(h, 2, nullptr, nullptr, nullptr, false, out);
+}
+// one PCG iteration on the compact layout: apply, then update
+int launch_compact(self_cg2d* h, const float* w, const float* vold, float* vnew, bool jac) {
+  int rc = compact_dispatch(h, 0, w, vold, vnew, jac, nullptr);
+  return rc ? rc : compact_dispatch(h, 1, w, vold, vnew, jac, nullptr);
+}
+
+int pcg_device_compact(self_cg2d* h, bool jac, int maxIters, double tol, double r0, int* iters, double* rel) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  auto& Cp = h->cpt;
+  CGScalars hs{};
+  hs.r0 = r0;
+  hs.tol = tol;
+  hs.maxIters = maxIters;
+  hs.done = maxIters <= 0 || r0 == 0.0;
+  hs.ioerr = hs.done ? 0 : -2;
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+  SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->ticket.p, 0, sizeof(unsigned int), st));
+  if (!hs.done) {
+    const float* dinv = jac ? Cp.dinv.p : nullptr;
+    pcg_start_fused<float><<<h->nblk, kRedThreads, 0, st>>>(Cp.r.p, dinv, Cp.w.p, Cp.ngp, h->S.p, h->partial.p,
+                                                            h->ticket.p);
+    SELF_LAUNCHED(ctx);
+    cudaGraphExec_t& G = Cp.graph[jac ? 1 : 0];
+    const PcgGraphKey key{Cp.u.p, Cp.r.p, Cp.v.p, Cp.v2.p, Cp.w.p, Cp.zc.p, dinv, h->op32.fac.p, 0};
+    if (G && !(Cp.key[jac ? 1 : 0] == key)) {
+      cudaGraphExecDestroy(G);
+      G = nullptr;
+    }
+    if (!G) {
+      cudaGraph_t g;
+      int rc = SELF_OK;
+      const long long l0 = ctx->launches.load();
+      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < kGraphIters && !rc; ++k)
+        rc = launch_compact(h, Cp.w.p, k % 2 == 0 ? Cp.v.p : Cp.v2.p, k % 2 == 0 ? Cp.v2.p : Cp.v.p, jac);
+      cudaError_t ce = cudaStreamEndCapture(st, &g);
+      if (rc) return rc;
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&G, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
+      Cp.key[jac ? 1 : 0] = key;
+      Cp.graph_launches = ctx->launches.load() - l0;
+      ctx->launches.fetch_sub(Cp.graph_launches);
+    }
+    const long long max_launches = (long long)maxIters / kGraphIters + 2;
+    for (long long gl = 0; gl < max_launches; ++gl) {
+      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
+      ctx->launches.fetch_add(Cp.graph_launches);
       SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
       SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (hs.done) break;
@@ -1692,6 +1859,40 @@ int build_factors(self_cg2d* h, const self_cg2d_desc* d, std::vector<double>& Jw
   h->h_fac = fac;
   h->h_dinv = dinv;
   if (!h->upload_dev) return SELF_OK;
+  // affine elements (metric terms and J the same at every node of the element to 1e-9 relative, far below the
+  // FP32 rounding of the factors; the metric terms of a straight-sided element differ from node to node only by
+  // the rounding of the derivative sums): the Helmholtz factors split into k w_i w_j per node and four numbers per
+  // element, which the compact FP32 apply streams instead
+  h->affine = nf == 4;
+  for (int e = 0; e < h->nEl && h->affine; ++e) {
+    const size_t b = (size_t)e * NN;
+    auto geo = [&](size_t id, double* c) {
+      const double xs = d->dxds[id], xp = d->dxdp[id], ys = d->dyds[id], yp = d->dydp[id], J = d->J[id];
+      c[0] = (yp * yp + xp * xp) / J;
+      c[1] = -(ys * yp + xs * xp) / J;
+      c[2] = (xs * xs + ys * ys) / J;
+      c[3] = J;
+    };
+    double c0[4];
+    geo(b, c0);
+    const double sc = std::max(std::fabs(c0[0]), std::fabs(c0[2]));
+    for (size_t t = 0; t < NN && h->affine; ++t) {
+      double c[4];
+      geo(b + t, c);
+      for (int q = 0; q < 3; ++q)
+        if (std::fabs(c[q] - c0[q]) > 1e-9 * sc) h->affine = false;
+      if (std::fabs(c[3] - c0[3]) > 1e-9 * std::fabs(c0[3])) h->affine = false;
+    }
+    if (h->affine) {
+      h->h_ec.insert(h->h_ec.end(), {c0[0], c0[1], c0[2], h->lambda * c0[3]});
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) h->h_kw.push_back(d->fluxCoeff[b + i + (size_t)n * j] * w[i] * w[j]);
+    }
+  }
+  if (!h->affine) {
+    std::vector<double>().swap(h->h_ec);
+    std::vector<double>().swap(h->h_kw);
+  }
   int rc;
   if ((rc = upload(h->ctx, h->op64.fac, fac))) return rc;
   if ((rc = upload(h->ctx, h->op64.dinv, dinv))) return rc;
@@ -1701,6 +1902,214 @@ int build_factors(self_cg2d* h, const self_cg2d_desc* d, std::vector<double>& Jw
   if ((rc = upload(h->ctx, h->op32.dinv, di32))) return rc;
   h->op32.D.assign(D, D + NN);
   h->have32 = true;
+  return SELF_OK;
+}
+
+// compact.cuh's layout functions for a run-time degree (host side of the compact build)
+int compact_interior_index(int n, int e, int ii, int jj, int nEl) {
+  switch (n) {
+    case 3: return interior_index<3>(e, ii, jj, nEl);
+    case 4: return interior_index<4>(e, ii, jj, nEl);
+    case 5: return interior_index<5>(e, ii, jj, nEl);
+    case 6: return interior_index<6>(e, ii, jj, nEl);
+    case 7: return interior_index<7>(e, ii, jj, nEl);
+    case 8: return interior_index<8>(e, ii, jj, nEl);
+    case 9: return interior_index<9>(e, ii, jj, nEl);
+    default: return interior_index<10>(e, ii, jj, nEl);
+  }
+}
+size_t compact_factor_index(int n, int nf, int g, int f, int i, int line) {
+  switch (n) {
+    case 3: return factor_index<3>(nf, g, f, i, line);
+    case 4: return factor_index<4>(nf, g, f, i, line);
+    case 5: return factor_index<5>(nf, g, f, i, line);
+    case 6: return factor_index<6>(nf, g, f, i, line);
+    case 7: return factor_index<7>(nf, g, f, i, line);
+    case 8: return factor_index<8>(nf, g, f, i, line);
+    case 9: return factor_index<9>(nf, g, f, i, line);
+    default: return factor_index<10>(nf, g, f, i, line);
+  }
+}
+
+// Compact node layout of the FP32 inner PCG (compact.cuh): entity numbering, element descriptors, the compact ->
+// element-local map and the Jacobi diagonal, from the shared-node groups.  Leaves cpt.ok false (the element-local
+// form is used) when the groups are not those of a conforming mesh: an interior node shared or masked, a side whose
+// nodes are partly Dirichlet or shared with several sides in different orders, an edge shared by more than two
+// sides, or sizes beyond 32-bit indexing.
+int compact_build(self_cg2d* h) {
+  auto& C = h->cpt;
+  C.tried = true;
+  C.ok = false;
+  const int n = h->n, N = h->N, M = n - 2, nEl = h->nEl;
+  const size_t NN = (size_t)n * n, nl = h->nl;
+  if (M < 1 || nl >= ((size_t)1 << 28) || !h->have32) return SELF_OK;
+  const std::vector<int>& src = h->h_src;
+  std::vector<unsigned char> mask(nl, 0);
+  std::vector<int> gof(nl, -1), gpos(nl, -1);
+  for (int g = 0; g < h->ngroups; ++g)
+    for (int k = h->h_gptr[g]; k < h->h_gptr[g + 1]; ++k) {
+      const int l = h->h_gidx[k];
+      gof[l] = g;
+      gpos[l] = k - h->h_gptr[g];
+      if (h->h_gdir[g]) mask[l] = 1;
+    }
+  auto lid = [&](int e, int i, int j) { return (int)((size_t)e * NN + i + (size_t)n * j); };
+  auto side_lid = [&](int e, int s, int m) {  // side s: 0 south (j = 0), 1 east (i = N), 2 north (j = N), 3 west
+    switch (s) {
+      case 0: return lid(e, m, 0);
+      case 1: return lid(e, N, m);
+      case 2: return lid(e, m, N);
+      default: return lid(e, 0, m);
+    }
+  };
+  auto side_of = [&](int l, int& e, int& s, int& m) {  // side and position of a node inside a side (not a corner)
+    e = (int)(l / NN);
+    const int t = (int)(l - (size_t)e * NN), i = t % n, j = t / n;
+    const bool ib = i == 0 || i == N, jb = j == 0 || j == N;
+    if (ib == jb) return false;
+    if (j == 0) { s = 0; m = i; }
+    else if (i == N) { s = 1; m = j; }
+    else if (j == N) { s = 2; m = i; }
+    else { s = 3; m = j; }
+    return true;
+  };
+  for (int e = 0; e < nEl; ++e)
+    for (int j = 1; j < N; ++j)
+      for (int i = 1; i < N; ++i) {
+        const int l = lid(e, i, j);
+        if (mask[l] || src[l] != l || gof[l] >= 0) return SELF_OK;
+      }
+  // sides: the primary side (its nodes are their own primary copies) and the orientation of the others
+  std::vector<int> skey(4 * (size_t)nEl, -1), nsec(4 * (size_t)nEl, 0);
+  std::vector<unsigned char> sflip(4 * (size_t)nEl, 0), sslot(4 * (size_t)nEl, 0);
+  for (int e = 0; e < nEl; ++e)
+    for (int s = 0; s < 4; ++s) {
+      int nm = 0;
+      for (int m = 1; m < N; ++m) nm += mask[side_lid(e, s, m)];
+      if (nm == N - 1) continue;  // Dirichlet side
+      if (nm) return SELF_OK;
+      int pe = -1, ps = -1, flip = 0;
+      for (int m = 1; m < N; ++m) {
+        int qe, qs, qm;
+        if (!side_of(src[side_lid(e, s, m)], qe, qs, qm)) return SELF_OK;
+        if (m == 1) {
+          pe = qe;
+          ps = qs;
+          if (qm == 1) flip = 0;
+          else if (qm == N - 1) flip = 1;
+          else return SELF_OK;
+        } else if (qe != pe || qs != ps || qm != (flip ? N - m : m)) {
+          return SELF_OK;
+        }
+      }
+      const int key = pe * 4 + ps, me = e * 4 + s;
+      if (key == me) {
+        if (flip) return SELF_OK;
+      } else {
+        sslot[me] = 1;
+        if (++nsec[key] > 1) return SELF_OK;
+      }
+      skey[me] = key;
+      sflip[me] = (unsigned char)flip;
+    }
+  for (int me = 0; me < 4 * nEl; ++me)
+    if (skey[me] >= 0 && skey[skey[me]] != skey[me]) return SELF_OK;  // a secondary side's primary is not a side
+  std::vector<int> eid(4 * (size_t)nEl, -1);
+  int nE2 = 0, nE1 = 0;
+  for (int k = 0; k < 4 * nEl; ++k)
+    if (skey[k] == k && nsec[k] == 1) eid[k] = nE2++;
+  for (int k = 0; k < 4 * nEl; ++k)
+    if (skey[k] == k && nsec[k] == 0) eid[k] = nE2 + nE1++;
+  // corners, numbered in order of first appearance; slots in the order of the copies in the shared-node group
+  static const int ci[4] = {0, 1, 1, 0}, cj[4] = {0, 0, 1, 1};  // SW, SE, NE, NW
+  std::vector<int> corner_of(nl, -1), cprim, coff(1, 0);
+  std::vector<int4> desc(3 * (size_t)nEl);
+  for (int e = 0; e < nEl; ++e) {
+    int code[4], cc[4], fs[4];
+    for (int s = 0; s < 4; ++s) {
+      const int me = e * 4 + s;
+      code[s] = skey[me] < 0 ? -1 : (eid[skey[me]] << 2) | (sslot[me] << 1) | sflip[me];
+    }
+    for (int c = 0; c < 4; ++c) {
+      const int l = lid(e, ci[c] * N, cj[c] * N);
+      cc[c] = -1;
+      fs[c] = 0;
+      if (mask[l]) continue;
+      const int p = src[l];
+      const int pt = (int)(p % NN), pi = pt % n, pj = pt / n;
+      if (!((pi == 0 || pi == N) && (pj == 0 || pj == N))) return SELF_OK;
+      if (gof[l] != gof[p] || (gof[p] >= 0 && gpos[p] != 0)) return SELF_OK;
+      if (corner_of[p] < 0) {
+        corner_of[p] = (int)cprim.size();
+        cprim.push_back(p);
+        const int g = gof[p];
+        coff.push_back(coff.back() + (g >= 0 ? h->h_gptr[g + 1] - h->h_gptr[g] : 1));
+      }
+      const int id = corner_of[p];
+      cc[c] = (id << 1) | (l == p ? 1 : 0);
+      fs[c] = coff[id] + (gof[l] >= 0 ? gpos[l] : 0);
+    }
+    desc[3 * (size_t)e] = make_int4(code[0], code[1], code[2], code[3]);
+    desc[3 * (size_t)e + 1] = make_int4(cc[0], cc[1], cc[2], cc[3]);
+    desc[3 * (size_t)e + 2] = make_int4(fs[0], fs[1], fs[2], fs[3]);
+  }
+  const int nC = (int)cprim.size();
+  const size_t nInt = (size_t)nEl * M * M, nEM = (size_t)(nE2 + nE1) * M;
+  const size_t ng = nInt + nEM + nC, ngp = (ng + 3) / 4 * 4, nz = nInt + 2 * nEM + (size_t)coff.back();
+  if (nz >= ((size_t)1 << 30) || ((size_t)(nE2 + nE1) << 2) >= ((size_t)1 << 30)) return SELF_OK;
+  std::vector<int> cl(ng);
+  for (int e = 0; e < nEl; ++e)
+    for (int j = 1; j < N; ++j)
+      for (int i = 1; i < N; ++i) cl[compact_interior_index(n, e, i - 1, j - 1, nEl)] = lid(e, i, j);
+  // the FP32 factors line-interleaved by pass group (factor_index), the last group padded with zeros
+  const int nf = h->nf, epl = kRedThreads / n, ngrp = (nEl + epl - 1) / epl;
+  std::vector<float> facT(h->affine ? 0 : (size_t)ngrp * nf * n * epl * n, 0.f);
+  for (int e = 0; e < nEl && !h->affine; ++e)
+    for (int f = 0; f < nf; ++f)
+      for (int t = 0; t < n; ++t)
+        for (int i = 0; i < n; ++i)
+          facT[compact_factor_index(n, nf, e / epl, f, i, (e % epl) * n + t)] =
+              (float)h->h_fac[(size_t)e * nf * NN + (size_t)f * NN + (size_t)t * n + i];
+  for (int k = 0; k < 4 * nEl; ++k)
+    if (eid[k] >= 0)
+      for (int m = 1; m < N; ++m) cl[nInt + (size_t)eid[k] * M + (m - 1)] = side_lid(k / 4, k % 4, m);
+  for (int c = 0; c < nC; ++c) cl[nInt + nEM + c] = cprim[c];
+  std::vector<float> dinv(ngp, 0.f);
+  for (size_t k = 0; k < ng; ++k) dinv[k] = (float)h->h_dinv[cl[k]];
+  self_ctx* ctx = h->ctx;
+  int rc;
+  if ((rc = upload(ctx, C.desc, desc)) || (rc = upload(ctx, C.coff, coff)) || (rc = upload(ctx, C.cl, cl)) ||
+      (rc = upload(ctx, C.dinv, dinv)))
+    return rc;
+  C.affine = h->affine;
+  if (C.affine) {  // one streamed value per node (k w_i w_j, line-interleaved) and four per element
+    std::vector<float> kwT((size_t)ngrp * n * epl * n, 0.f);
+    std::vector<float4> ec(nEl);
+    for (int e = 0; e < nEl; ++e) {
+      for (int t = 0; t < n; ++t)
+        for (int i = 0; i < n; ++i)
+          kwT[compact_factor_index(n, 1, e / epl, 0, i, (e % epl) * n + t)] = (float)h->h_kw[(size_t)e * NN + (size_t)t * n + i];
+      ec[e] = make_float4((float)h->h_ec[4 * (size_t)e], (float)h->h_ec[4 * (size_t)e + 1],
+                          (float)h->h_ec[4 * (size_t)e + 2], (float)h->h_ec[4 * (size_t)e + 3]);
+    }
+    if ((rc = upload(ctx, C.kw, kwT)) || (rc = upload(ctx, C.ec, ec))) return rc;
+  } else if ((rc = upload(ctx, C.fac, facT))) {
+    return rc;
+  }
+  for (DevBuf<float>* b : {&C.u, &C.r, &C.v, &C.v2, &C.w}) {
+    if (b->alloc(ngp) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu floats", ngp);
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(b->p, 0, ngp * sizeof(float), ctx->stream));
+  }
+  if (C.zc.alloc(nz) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu floats", nz);
+  C.M = M;
+  C.nInt = (int)nInt;
+  C.nE2 = nE2;
+  C.nE1 = nE1;
+  C.nC = nC;
+  C.ng = (int)ng;
+  C.ngp = (int)ngp;
+  C.nz = (int)nz;
+  C.ok = true;
   return SELF_OK;
 }
 
@@ -1771,29 +2180,42 @@ int self_cg2d_destroy(self_cg2d* h) {
 }
 
 // MatrixAction: Au = Mask(GlobalSum(L(UnMask(u)))).  u is read only (the reference leaves u masked).
-int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int tensor_cores) {
+int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int form) {
   if (!h || !u || !Au) return SELF_ERR_INVALID;
   self_ctx* ctx = h->ctx;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-  if (tensor_cores && h->N != 7)
+  if (form < SELF_F32_LOCAL || form > SELF_F32_COMPACT) return set_error(ctx, SELF_ERR_INVALID, "FP32 form %d", form);
+  if (form == SELF_F32_TENSOR_CORES && h->N != 7)
     return set_error(ctx, SELF_ERR_UNSUPPORTED, "tensor-core FP32 operator: N = 7 only (N = %d)", h->N);
   const size_t nl = h->nl;
   int rc;
-  if ((rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->z, nl)) || (rc = ensuref(ctx, h->w32, nl)) ||
-      (rc = ensuref(ctx, h->v32, nl)) || (rc = ensuref(ctx, h->v2_32, nl)) || (rc = ensuref(ctx, h->z32, nl)))
-    return rc;
+  if ((rc = ensure(ctx, h->r, nl)) || (rc = ensure(ctx, h->z, nl))) return rc;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->r.p, u, nl * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->w32.p, h->r.p, nl);
-  SELF_LAUNCHED(ctx);
   CGScalars hs{};  // first iteration of the fused apply: v = w, z = L(unmask(w)), alpha from num = 1
   hs.num = 1.0;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
-  h->tc = tensor_cores ? 1 : 0;
-  rc = launch_apply_fused<float>(h, h->w32.p, h->v2_32.p, h->v32.p, h->z32.p, h->op32);
-  h->tc = 0;
-  if (rc || (rc = launch_dss<float>(h, h->z32.p))) return rc;
-  convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->z32.p, nl);
-  SELF_LAUNCHED(ctx);
+  if (form == SELF_F32_COMPACT) {
+    if (!h->cpt.tried && (rc = compact_build(h))) return rc;
+    auto& Cp = h->cpt;
+    if (!Cp.ok) return set_error(ctx, SELF_ERR_UNSUPPORTED, "compact layout: mesh not covered");
+    compact_gather_f32<<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.w.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
+    SELF_LAUNCHED(ctx);
+    if ((rc = launch_compact_apply(h, Cp.w.p, Cp.v2.p, Cp.v.p))) return rc;
+    SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->z.p, 0, nl * sizeof(double), ctx->stream));
+    if ((rc = launch_compact_assemble(h, h->z.p))) return rc;
+  } else {
+    if ((rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->v32, nl)) || (rc = ensuref(ctx, h->v2_32, nl)) ||
+        (rc = ensuref(ctx, h->z32, nl)))
+      return rc;
+    convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->w32.p, h->r.p, nl);
+    SELF_LAUNCHED(ctx);
+    h->tc = form == SELF_F32_TENSOR_CORES ? 1 : 0;
+    rc = launch_apply_fused<float>(h, h->w32.p, h->v2_32.p, h->v32.p, h->z32.p, h->op32);
+    h->tc = 0;
+    if (rc || (rc = launch_dss<float>(h, h->z32.p))) return rc;
+    convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->z32.p, nl);
+    SELF_LAUNCHED(ctx);
+  }
   CGScalars out{};
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&out, h->S.p, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream));
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(Au, h->z.p, nl * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2503,10 +2925,14 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
       R.outer_iterations = 1;
     } else {
       // FP32 inner (P)CG under FP64 iterative refinement: x += A32^-1 r64, r64 = b - A64 x
-      if ((rc = ensuref(ctx, h->u32, nl)) || (rc = ensuref(ctx, h->r32, nl)) || (rc = ensuref(ctx, h->v32, nl)) ||
-          (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)) || (rc = ensuref(ctx, h->v2_32, nl)))
-        return rc;
       h->tc = (o->tensor_cores && h->N == 7) ? 1 : 0;
+      const bool want_cpt = !use_pcl && !h->tc && o->inner_layout != SELF_LAYOUT_LOCAL;
+      if (want_cpt && !h->cpt.tried && (rc = compact_build(h))) return rc;
+      const bool use_cpt = want_cpt && h->cpt.ok;
+      if (!use_cpt &&
+          ((rc = ensuref(ctx, h->u32, nl)) || (rc = ensuref(ctx, h->r32, nl)) || (rc = ensuref(ctx, h->v32, nl)) ||
+           (rc = ensuref(ctx, h->w32, nl)) || (rc = ensuref(ctx, h->z32, nl)) || (rc = ensuref(ctx, h->v2_32, nl))))
+        return rc;
       const double inner_tol = o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4;
       const int max_outer = o->max_outer > 0 ? o->max_outer : 30;
       double rn = r0;
@@ -2515,25 +2941,39 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
       if (resi) resi[0] = r0;
       while (outer < max_outer && rn / r0 >= o->tolerance && total < o->maxIters) {
         outer++;
-        convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->r32.p, h->r.p, nl);
-        SELF_LAUNCHED(ctx);
-        SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->u32.p, 0, nl * sizeof(float), ctx->stream));
         int it_in = 0;
         double rel_in = 0;
-        const PcRun<float> pc = use_pcl ? pcl_run<float>(h, o->pc_iterations) : PcRun<float>{};
-        const int inner_err = pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p,
-                                                jac ? h->op32.dinv.p : nullptr, o->maxIters - total, inner_tol, rn,
-                                                nullptr, &it_in, &rel_in, h->op32, false, use_pcl ? &pc : nullptr);
-        total += it_in;
-        if (inner_err == SELF_ERR_TIMEOUT) {  // a bounded tensor-core wait ran out in the inner solve
-          h->tc = 0;
-          return set_error(ctx, SELF_ERR_TIMEOUT, "FP32 inner solve: a tensor-core barrier wait ran out");
+        if (use_cpt) {  // compact layout: r32 = the unknowns of r64, x += d at the primary copies
+          auto& Cp = h->cpt;
+          compact_gather_f32<<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.r.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
+          SELF_LAUNCHED(ctx);
+          SELF_CUDA_TRY(ctx, cudaMemsetAsync(Cp.u.p, 0, (size_t)Cp.ngp * sizeof(float), ctx->stream));
+          const int inner_err = pcg_device_compact(h, jac, o->maxIters - total, inner_tol, rn, &it_in, &rel_in);
+          total += it_in;
+          if (inner_err == SELF_ERR_TIMEOUT)
+            return set_error(ctx, SELF_ERR_TIMEOUT, "FP32 inner solve: a staged-copy barrier wait ran out");
+          compact_scatter_add<<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, Cp.u.p, Cp.cl.p, Cp.ng);
+          SELF_LAUNCHED(ctx);
+        } else {
+          convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->r32.p, h->r.p, nl);
+          SELF_LAUNCHED(ctx);
+          SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->u32.p, 0, nl * sizeof(float), ctx->stream));
+          const PcRun<float> pc = use_pcl ? pcl_run<float>(h, o->pc_iterations) : PcRun<float>{};
+          const int inner_err = pcg_device<float>(h, h->u32.p, h->r32.p, h->v32.p, h->w32.p, h->z32.p,
+                                                  jac ? h->op32.dinv.p : nullptr, o->maxIters - total, inner_tol, rn,
+                                                  nullptr, &it_in, &rel_in, h->op32, false, use_pcl ? &pc : nullptr);
+          total += it_in;
+          if (inner_err == SELF_ERR_TIMEOUT) {  // a bounded tensor-core wait ran out in the inner solve
+            h->tc = 0;
+            return set_error(ctx, SELF_ERR_TIMEOUT, "FP32 inner solve: a tensor-core barrier wait ran out");
+          }
+          // x += d (FP64)
+          convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->u32.p, nl);
+          SELF_LAUNCHED(ctx);
+          axpby<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, h->z.p, 1.0, 1.0, nl);
+          SELF_LAUNCHED(ctx);
         }
-        // x += d (FP64), r = b - A x in FP64
-        convert<double, float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->z.p, h->u32.p, nl);
-        SELF_LAUNCHED(ctx);
-        axpby<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, h->z.p, 1.0, 1.0, nl);
-        SELF_LAUNCHED(ctx);
+        // r = b - A x in FP64
         if ((rc = residual<double>(h, h->f.p, h->u.p, h->r.p, h->op64))) return rc;
         if ((rc = dots<double>(h, h->r.p, h->r.p, nullptr, nullptr, h->red.p))) return rc;
         rn = std::sqrt(read1(h, h->red.p, &rc));

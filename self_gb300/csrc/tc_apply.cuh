@@ -175,7 +175,6 @@ __global__ void __launch_bounds__(tc::kTileRows) pcg_apply_tc(const float* __res
   const uint32_t tmem = sm.tmem_base;
   const int r = tid;                    // this thread's line: element le, row j
   const int le = r >> 3, j = r & 7;
-  const int half = r >> 7;              // M = 128 half of the tile
   // TMEM address of this warp's lanes and column block: lane field 32 (warp % 4), columns 32 * (warp / 4)
   const uint32_t tw = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
   const uint64_t dB1 = tc::sdesc(tc::sa(sm.B1)), dB2 = tc::sdesc(tc::sa(sm.B2));
