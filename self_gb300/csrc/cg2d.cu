@@ -387,14 +387,14 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused(const R* __restri
 }
 
 // FP32 form of pcg_apply_fused, one thread per grid line: thread (e, t) of a block pass holds line t of element e
-// (the N1 nodes u(., t)) in registers and forms
-//   us(., t) = D u(., t)                       row pass, D read by warp-uniform (broadcast) float4 loads;
+// (the N1 nodes u(., t)) in registers and forms (line_op_f32)
+//   us(., t) = D u(., t)                       row pass, D entries as constant-bank FMA operands;
 //   up(c, .) = D u(c, .)                       column pass: the same thread as column c, u(c, .) read back from a
 //                                              per-line padded buffer (row stride N1 + 1: bank-conflict free for
 //                                              the row-major write and the column read);
 //   F1, F2 at its row nodes, (D^T F1)(., t) in registers, (D^T F2)(c, .) in the column pass, both summed into Lu.
-// Shared memory per node is a handful of accesses instead of reading the four contraction rows node by node; the
-// arithmetic is that of pcg_apply_fused in another summation order.
+// A warp holds whole elements when 32 % N1 == 0, and the transposes then need warp barriers only.  The arithmetic
+// is that of pcg_apply_fused in another summation order.
 template <int N1>
 constexpr int line_epb() {
   return kRedThreads / N1;  // elements per block pass
@@ -411,36 +411,23 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused_f32(const float* 
   if (S->done) return;
   constexpr int NN = N1 * N1;
   constexpr int EPL = line_epb<N1>();
-  constexpr int DS = 4 * ((N1 + 3) / 4);  // padded row of D
-  constexpr int LS = N1 + 1;              // padded line in the transpose buffers
-  __shared__ __align__(16) float Dr[N1][DS];  // Dr[i][m] = D(i, m)
-  __shared__ __align__(16) float Dc[N1][DS];  // Dc[i][m] = D(m, i)
+  constexpr int LS = N1 + 1;  // padded line in the transpose buffers
   __shared__ float X[EPL * N1 * LS];
   __shared__ float Y[EPL * N1 * LS];
-  for (int t = threadIdx.x; t < N1 * DS; t += kRedThreads) {
-    const int r = t / DS, m = t - r * DS;
-    Dr[r][m] = m < N1 ? Cg.D[r + N1 * m] : 0.f;
-    Dc[r][m] = m < N1 ? Cg.D[m + N1 * r] : 0.f;
-  }
   const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;  // element in the pass, line index
   const bool first = S->iter == 0;
   const float beta = first ? 0.f : S->beta32;
   const int ngroups = (nEl + EPL - 1) / EPL;
-  const int line = le < EPL ? le * N1 + t : 0;  // this thread's line in the buffers (idle threads: unused)
-  float* Xl = X + (size_t)line * LS;
-  float* Yl = Y + (size_t)line * LS;
   float pa = 0.f;
   for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
     const int e = g * EPL + le;
     const bool active = le < EPL && e < nEl;
-    float u[N1], us[N1], up[N1];
     const size_t l0 = (size_t)e * NN + (size_t)N1 * t;  // row t: nodes (i, t), i = 0..N1-1
+    const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
+    float u[N1], Lu[N1];
     if (active) {
-      {  // the factor lines are read two barriers later: request them into L2 with the first loads
-        const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) prefetch_l2(fe + f * NN);
-      }
+      for (int f = 0; f < 4; ++f) prefetch_l2(fe + f * NN);  // the factor lines are read two barriers later
       int sl[N1];
       float wl[N1], vl[N1], vn[N1];
       load_line<N1>(src + l0, sl);
@@ -457,65 +444,15 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_fused_f32(const float* 
         u[i] = sl[i] == (int)(l0 + i) ? vn[i] : (first ? w[sl[i]] : w[sl[i]] + beta * vold[sl[i]]);
       }
       store_line<N1>(vnew + l0, vn);
-#pragma unroll
-      for (int i = 0; i < N1; ++i) {
-        us[i] = row_dot<N1>(Dr[i], u);
-        Xl[i] = u[i];  // u(i, t)
-      }
     }
-    __syncthreads();  // (first pass: D is in place as well)
+    auto fl = [&](int f, float (&G)[N1]) { load_line<N1>(fe + f * NN, G); };
+    line_op_f32<N1, NF>(Cg.D, fl, active, le < EPL ? le : 0, t, X, Y, u, Lu);
     if (active) {
-      // column pass: this thread is column c = t of element le: u(c, m) = line m, entry c
-      float uc[N1];
-#pragma unroll
-      for (int m = 0; m < N1; ++m) uc[m] = X[(size_t)(le * N1 + m) * LS + t];
-#pragma unroll
-      for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = row_dot<N1>(Dr[j], uc);  // up(c, j)
-    }
-    __syncthreads();
-    float a[N1];
-    if (active) {
-      const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
-      float F1[N1], G11[N1], G12[N1], G22[N1];
-      load_line<N1>(fe, G11);
-      load_line<N1>(fe + NN, G12);
-      load_line<N1>(fe + 2 * NN, G22);
-#pragma unroll
-      for (int i = 0; i < N1; ++i) {
-        up[i] = Yl[i];
-        F1[i] = G11[i] * us[i] + G12[i] * up[i];
-        Xl[i] = G12[i] * us[i] + G22[i] * up[i];  // F2(i, t); X is free: the column pass has read u
-      }
-#pragma unroll
-      for (int i = 0; i < N1; ++i) a[i] = row_dot<N1>(Dc[i], F1);  // (D^T F1)(i, t)
-    }
-    __syncthreads();
-    if (active) {
-      float fc[N1];
-#pragma unroll
-      for (int m = 0; m < N1; ++m) fc[m] = X[(size_t)(le * N1 + m) * LS + t];  // F2(c, m)
-#pragma unroll
-      for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = row_dot<N1>(Dc[j], fc);  // (D^T F2)(c, j)
-    }
-    __syncthreads();
-    if (active) {
-      const float* fe = fac + (size_t)e * NF * NN + (size_t)N1 * t;
-      float Mv[N1], Lu[N1];
-      load_line<N1>(fe + 3 * NN, Mv);
-#pragma unroll
-      for (int i = 0; i < N1; ++i) Lu[i] = -(a[i] + Yl[i]) - Mv[i] * u[i];
-      if (NF == 6) {
-        float B1[N1], B2[N1];
-        load_line<N1>(fe + 4 * NN, B1);
-        load_line<N1>(fe + 5 * NN, B2);
-#pragma unroll
-        for (int i = 0; i < N1; ++i) Lu[i] -= B1[i] * us[i] + B2[i] * up[i];
-      }
       store_line<N1>(z + l0, Lu);
 #pragma unroll
       for (int i = 0; i < N1; ++i) pa += u[i] * Lu[i];
     }
-    __syncthreads();  // the next pass reuses X and Y
+    line_sync<N1>();  // the next pass reuses X and Y
   }
   const float acc[1] = {pa};
   double tot[1];

@@ -150,4 +150,91 @@ __device__ __forceinline__ void eo_matvec(const EOTable<N1>& T, const double (&x
   }
 }
 
+// Warp-synchronous when a warp holds whole elements (32 % N1 == 0: the transposes stay inside the warp), else block
+// barriers.
+template <int N1>
+__device__ __forceinline__ void line_sync() {
+  if constexpr (32 % N1 == 0)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+// sum_m D(i, m) x[m] (T = false) or sum_m D(m, i) x[m] (T = true), m in order (D column-major): with i and m
+// known at compile time and D a kernel parameter every D entry is a constant-bank operand of its FMA, no load
+template <int N1, bool T>
+__device__ __forceinline__ float drow(const float (&D)[N1 * N1], int i, const float (&x)[N1]) {
+  float s = 0.f;
+#pragma unroll
+  for (int m = 0; m < N1; ++m) s = fmaf(T ? D[m + N1 * i] : D[i + N1 * m], x[m], s);
+  return s;
+}
+
+// The FP32 CGSEM element operator on line t (nodes (i, t)) of element le of a block pass, one thread per grid line
+// (every thread of the block calls it, threads without a line pass active = false and only join the barriers):
+//   Lu = -( D_s^T (G11 us + G12 up) + D_p^T (G12 us + G22 up) ) - M u  [ - (B1 us + B2 up) for NF = 6 ],
+// us = D_s u from the line in registers, up = D_p u and the second transposed contraction through the padded
+// transpose buffers X, Y (row stride N1 + 1); fl(f, G) loads the line's values of factor f (G11, G12, G22, M, B1,
+// B2).  Four barriers (line_sync); on return X and Y are free.
+template <int N1, int NF, class FL>
+__device__ __forceinline__ void line_op_f32(const float (&D)[N1 * N1], const FL& fl, bool active, int le, int t,
+                                            float* X, float* Y, const float (&u)[N1], float (&Lu)[N1]) {
+  constexpr int LS = N1 + 1;
+  float* Xl = X + (size_t)(le * N1 + t) * LS;
+  float* Yl = Y + (size_t)(le * N1 + t) * LS;
+  float us[N1], up[N1], a[N1];
+  if (active) {
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      us[i] = drow<N1, false>(D, i, u);
+      Xl[i] = u[i];
+    }
+  }
+  line_sync<N1>();
+  if (active) {  // column pass: column c = t, up(c, .) = D u(c, .)
+    float uc[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) uc[m] = X[(size_t)(le * N1 + m) * LS + t];
+#pragma unroll
+    for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = drow<N1, false>(D, j, uc);
+  }
+  line_sync<N1>();
+  if (active) {
+    float F1[N1], G11[N1], G12[N1], G22[N1];
+    fl(0, G11);
+    fl(1, G12);
+    fl(2, G22);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      up[i] = Yl[i];
+      F1[i] = G11[i] * us[i] + G12[i] * up[i];
+      Xl[i] = G12[i] * us[i] + G22[i] * up[i];  // F2(i, t)
+    }
+#pragma unroll
+    for (int i = 0; i < N1; ++i) a[i] = drow<N1, true>(D, i, F1);  // (D^T F1)(i, t)
+  }
+  line_sync<N1>();
+  if (active) {  // column pass: (D^T F2)(c, .)
+    float fc[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) fc[m] = X[(size_t)(le * N1 + m) * LS + t];
+#pragma unroll
+    for (int j = 0; j < N1; ++j) Y[(size_t)(le * N1 + j) * LS + t] = drow<N1, true>(D, j, fc);
+  }
+  line_sync<N1>();
+  if (active) {
+    float Mv[N1];
+    fl(3, Mv);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) Lu[i] = -(a[i] + Yl[i]) - Mv[i] * u[i];
+    if constexpr (NF == 6) {
+      float B1[N1], B2[N1];
+      fl(4, B1);
+      fl(5, B2);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) Lu[i] -= B1[i] * us[i] + B2[i] * up[i];
+    }
+  }
+}
+
 }  // namespace selfgpu
