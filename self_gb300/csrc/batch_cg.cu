@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -252,12 +253,16 @@ __device__ __forceinline__ bool tile_last(const double (&bv)[NS], double* __rest
 }
 
 // ------------------------------------------------------------------ FP32 element operator, one thread per line
-// The FP32 inner iterations run the element operator as one thread per grid line (the form of the single-problem
-// FP32 PCG apply): a round covers up to 256 / N1 elements, thread (le, t) holding line t (nodes (i, t)) of element
-// e0 + le in registers; the two column passes go through padded transpose buffers (row stride N1 + 1) and the
-// derivative rows are read as 16-byte broadcasts from a zero-padded table.
+// The FP32 inner iterations run the element operator as one thread per grid line (line_op_f32, the operator of the
+// single-problem FP32 PCG apply): a round covers up to 256 / N1 elements, thread (le, t) holding line t (nodes
+// (i, t)) of element e0 + le in registers; the two column passes go through padded transpose buffers (row stride
+// N1 + 1), warp-synchronous when a warp holds whole elements; the derivative matrix is read as constant-bank FMA
+// operands from c_dline.
 constexpr int kLineBuf = 256 * 11;  // transpose buffer floats: (256 / N1) * N1 * (N1 + 1) <= 256 * 11 for N1 <= 10
-constexpr int kDRow = 12;           // padded derivative row (floats) for N1 <= 12
+
+// D (column-major) of degrees N = 2..9 (N1 = 3..10) in constant memory, one table per device shared by every batch
+// (set by the first problem of a degree; add() refuses a problem whose D differs from the table)
+__constant__ float c_dline[8][100];
 
 template <int N1>
 constexpr int line_round_elems() {
@@ -265,40 +270,24 @@ constexpr int line_round_elems() {
 }
 int line_round_elems_rt(int N) { return 256 / (N + 1); }
 
-// Dr(i, m) = D(i, m), Dc(i, m) = D(m, i), rows of 4 ceil(N1 / 4) floats (zero padded), for degree N = N1 - 1
-template <int N1>
-__device__ __forceinline__ void load_line_tables(const DTable* __restrict__ DT, float* Dr, float* Dc) {
-  constexpr int DS = 4 * ((N1 + 3) / 4);
-  for (int k = threadIdx.x; k < N1 * DS; k += blockDim.x) {
-    const int r = k / DS, m = k - r * DS;
-    Dr[k] = m < N1 ? DT->d32[N1 - 1][r + N1 * m] : 0.f;
-    Dc[k] = m < N1 ? DT->d32[N1 - 1][m + N1 * r] : 0.f;
-  }
-}
-
 // One round of ne <= 256 / N1 elements from e0.  FUSED: v_new = w + beta v_old (written), u = v_new gathered through
 // src, z = L(u), returns the thread's sum of u * Lu; otherwise out = L(w gathered through src), or with rhs
 // out = rhs - L in FP64, rounded (the plain apply's result).
 template <int N1, bool FUSED>
-__device__ __noinline__ float line_round(const Prob& p, const float* __restrict__ Dr, const float* __restrict__ Dc,
-                                         int e0, int ne, const float* __restrict__ w, const float* __restrict__ vold,
-                                         float* __restrict__ vnew, float beta, bool first, float* __restrict__ z,
-                                         const double* __restrict__ rhs, float* X, float* Y) {
-  constexpr int NN = N1 * N1, DS = 4 * ((N1 + 3) / 4), LS = N1 + 1, EPL = line_round_elems<N1>();
+__device__ __noinline__ float line_round(const Prob& p, int e0, int ne, const float* __restrict__ w,
+                                         const float* __restrict__ vold, float* __restrict__ vnew, float beta,
+                                         bool first, float* __restrict__ z, const double* __restrict__ rhs, float* X,
+                                         float* Y) {
+  constexpr int NN = N1 * N1, EPL = line_round_elems<N1>();
   const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;
   const bool active = le < EPL && le < ne;
   const int e = e0 + le;
   const size_t l0 = (size_t)e * NN + (size_t)N1 * t;
-  const int line = le < EPL ? le * N1 + t : 0;
-  float* Xl = X + line * LS;
-  float* Yl = Y + line * LS;
-  float u[N1], us[N1], up[N1], a[N1];
+  const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
+  float u[N1], Lu[N1];
   if (active) {
-    {  // the factor lines are read two barriers later: request them into L2 with the first loads
-      const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
 #pragma unroll
-      for (int f = 0; f < 4; ++f) prefetch_l2(fe + f * NN);
-    }
+    for (int f = 0; f < 4; ++f) prefetch_l2(fe + f * NN);  // the factor lines are read two barriers later
     int sl[N1];
     load_line<N1>(p.src + l0, sl);
     if (FUSED) {
@@ -321,52 +310,12 @@ __device__ __noinline__ float line_round(const Prob& p, const float* __restrict_
 #pragma unroll
       for (int i = 0; i < N1; ++i) u[i] = w[sl[i]];
     }
-#pragma unroll
-    for (int i = 0; i < N1; ++i) {
-      us[i] = row_dot<N1>(Dr + i * DS, u);
-      Xl[i] = u[i];
-    }
   }
-  __syncthreads();
-  if (active) {  // column pass: up(c, .) = D u(c, .), c = t
-    float uc[N1];
-#pragma unroll
-    for (int m = 0; m < N1; ++m) uc[m] = X[(le * N1 + m) * LS + t];
-#pragma unroll
-    for (int j = 0; j < N1; ++j) Y[(le * N1 + j) * LS + t] = row_dot<N1>(Dr + j * DS, uc);
-  }
-  __syncthreads();
-  if (active) {
-    const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
-    float G11[N1], G12[N1], G22[N1], F1[N1];
-    load_line<N1>(fe, G11);
-    load_line<N1>(fe + NN, G12);
-    load_line<N1>(fe + 2 * NN, G22);
-#pragma unroll
-    for (int i = 0; i < N1; ++i) {
-      up[i] = Yl[i];
-      F1[i] = G11[i] * us[i] + G12[i] * up[i];
-      Xl[i] = G12[i] * us[i] + G22[i] * up[i];  // F2(i, t)
-    }
-#pragma unroll
-    for (int i = 0; i < N1; ++i) a[i] = row_dot<N1>(Dc + i * DS, F1);  // (D^T F1)(i, t)
-  }
-  __syncthreads();
-  if (active) {  // column pass: (D^T F2)(c, .)
-    float fc[N1];
-#pragma unroll
-    for (int m = 0; m < N1; ++m) fc[m] = X[(le * N1 + m) * LS + t];
-#pragma unroll
-    for (int j = 0; j < N1; ++j) Y[(le * N1 + j) * LS + t] = row_dot<N1>(Dc + j * DS, fc);
-  }
-  __syncthreads();
+  auto fl = [&](int f, float (&G)[N1]) { load_line<N1>(fe + f * NN, G); };
+  line_op_f32<N1, 4>(reinterpret_cast<const float(&)[N1 * N1]>(c_dline[N1 - 3][0]), fl, active,
+                     le < EPL ? le : 0, t, X, Y, u, Lu);
   float prod = 0.f;
   if (active) {
-    const float* fe = p.fac32 + (size_t)e * 4 * NN + (size_t)N1 * t;
-    float M[N1], Lu[N1];
-    load_line<N1>(fe + 3 * NN, M);
-#pragma unroll
-    for (int i = 0; i < N1; ++i) Lu[i] = -(a[i] + Yl[i]) - M[i] * u[i];
     if (FUSED) {
       store_line<N1>(z + l0, Lu);
 #pragma unroll
@@ -382,18 +331,16 @@ __device__ __noinline__ float line_round(const Prob& p, const float* __restrict_
   return prod;
 }
 
-// all rounds of element tile t in the line form (the tile's table entry and D are loaded by the caller's switch)
+// all rounds of element tile t in the line form (the tile's table entry is loaded by the caller's switch)
 template <int N1, bool FUSED>
-__device__ __forceinline__ float line_tile(const Prob& p, const DTable* __restrict__ DT, float* Dr, float* Dc,
-                                           const ETile& t, const float* w, const float* vold, float* vnew,
-                                           float beta, bool first, float* z, const double* rhs, float* X, float* Y) {
+__device__ __forceinline__ float line_tile(const Prob& p, const ETile& t, const float* w, const float* vold,
+                                           float* vnew, float beta, bool first, float* z, const double* rhs, float* X,
+                                           float* Y) {
   constexpr int EPL = line_round_elems<N1>();
-  load_line_tables<N1>(DT, Dr, Dc);
-  __syncthreads();
   float prod = 0.f;
   for (int r0 = 0; r0 < t.ne; r0 += EPL) {
-    if (r0 > 0) __syncthreads();
-    prod += line_round<N1, FUSED>(p, Dr, Dc, t.e0 + r0, min(EPL, t.ne - r0), w, vold, vnew, beta, first, z, rhs, X, Y);
+    __syncthreads();  // the transpose buffers of the previous round (or tile) are free
+    prod += line_round<N1, FUSED>(p, t.e0 + r0, min(EPL, t.ne - r0), w, vold, vnew, beta, first, z, rhs, X, Y);
   }
   return prod;
 }
@@ -417,11 +364,9 @@ __global__ void __launch_bounds__(kThreads) bk_apply_plain(TileView V, const Pro
     if constexpr (sizeof(R) == 4) {  // FP32: the line form of the inner iterations (what the autotuner times)
       __shared__ __align__(16) float X[kLineBuf];
       __shared__ __align__(16) float Y[kLineBuf];
-      __shared__ __align__(16) float Dr[10 * kDRow];
-      __shared__ __align__(16) float Dc[10 * kDRow];
 #define SELF_BK_LINE(NV)                                                                                         \
   case NV:                                                                                                       \
-    line_tile<NV, false>(p, DT, Dr, Dc, t, x, nullptr, nullptr, 0.f, true, out, rhs, X, Y);                       \
+    line_tile<NV, false>(p, t, x, nullptr, nullptr, 0.f, true, out, rhs, X, Y);                                  \
     break;
       switch (n) {
         SELF_BK_LINE(3)
@@ -567,11 +512,9 @@ __global__ void __launch_bounds__(kThreads) bk_apply(TileView V, const Prob* __r
     if constexpr (sizeof(R) == 4) {  // FP32: one thread per grid line
       __shared__ __align__(16) float X[kLineBuf];
       __shared__ __align__(16) float Y[kLineBuf];
-      __shared__ __align__(16) float Dr[10 * kDRow];
-      __shared__ __align__(16) float Dc[10 * kDRow];
 #define SELF_BK_LINE(NV)                                                                                         \
   case NV:                                                                                                       \
-    prod = line_tile<NV, true>(p, DT, Dr, Dc, t, w, vold, vnew, beta, first, z, nullptr, X, Y);                  \
+    prod = line_tile<NV, true>(p, t, w, vold, vnew, beta, first, z, nullptr, X, Y);                              \
     break;
       switch (n) {
         SELF_BK_LINE(3)
@@ -1155,6 +1098,27 @@ int alloc_view(self_cgbatch* b, self_cgbatch::View& v, size_t ce, size_t cg, siz
   return SELF_OK;
 }
 
+// c_dline of this device for N1 = n: set from D (column-major FP64, rounded to FP32) by the first problem of the
+// degree, compared with it for every later one (the batched FP32 operator reads the table, not the problem's D)
+int set_dline(self_ctx* ctx, int n, const std::vector<double>& D) {
+  static std::mutex mu;
+  static std::vector<std::vector<float>> tables;  // [device * 8 + n - 3]
+  std::lock_guard<std::mutex> lock(mu);
+  const size_t slot = (size_t)ctx->device * 8 + (size_t)(n - 3);
+  if (tables.size() <= slot) tables.resize(slot + 1);
+  std::vector<float> d32(D.begin(), D.begin() + (size_t)n * n);
+  std::vector<float>& T = tables[slot];
+  if (T.empty()) {
+    SELF_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_dline, d32.data(), d32.size() * sizeof(float),
+                                          (size_t)(n - 3) * 100 * sizeof(float), cudaMemcpyHostToDevice));
+    T = d32;
+  } else if (T != d32) {
+    return set_error(ctx, SELF_ERR_UNSUPPORTED,
+                     "batched solver: derivative matrix of degree %d differs from the one in use on this device", n - 1);
+  }
+  return SELF_OK;
+}
+
 // After the pool changed: upload the problem descriptors, size the tables for every problem (at the largest
 // tile count any element-per-tile choice gives) and drop the captured graphs if the table buffers moved.
 int refresh(self_cgbatch* b) {
@@ -1447,6 +1411,8 @@ int add_problem(self_cgbatch* b, const self_cg2d_desc* d, const double* source, 
     if ((rc = ensure_cap(b, b->cap + 1))) return rc;
   }
   const int n = hc.n;
+  if (n < 3 || n > 10) return set_error(b->ctx, SELF_ERR_UNSUPPORTED, "batched solver: degree %d outside 2..9", hc.N);
+  if ((rc = set_dline(b->ctx, n, hc.D))) return rc;
   if (!b->haveD[hc.N]) {
     for (int k = 0; k < n * n; ++k) {
       b->hDT.d64[hc.N][k] = hc.D[k];
