@@ -213,6 +213,7 @@ struct GMScalars {
 struct CGScalars {
   double num, den, vz, rr, r0, tol;
   int iter, done, ioerr, maxIters;
+  int bodies, pad;  // loop-graph bodies run in this solve (the device-side loop's bound and launch count)
   double* resi;         // residual history (resi[iter] = ||r||), or null
   double alpha, beta;   // step lengths of the current iteration, formed once by the last block of the kernel
   float alpha32, beta32;  // before (no per-thread FP64 division); FP32 copies for the FP32 kernels
@@ -1283,14 +1284,84 @@ namespace cg {
 // (P)CG iterations on the device from the current residual; returns ioerr and fills iters/resi.
 // abs_stop: the reference's early return when ||r0|| < TOL (CGsemElliptic_2D_Class.f90:1160-1162); the inner
 // solves of the iterative refinement use a purely relative stop.
-// The iterations run as a captured graph of kGraphIters fused iterations (three launches each, the two direction
-// buffers alternating); the host reads the scalar block after each graph launch.
-constexpr int kGraphIters = 16;  // even: the current direction is back in `v` after every graph launch
+// The whole solve is one launch of a graph whose conditional while node repeats a body of kGraphIters fused
+// iterations (three launches each, two on the compact layout; the direction buffers alternate) until the device
+// scalars report the stop; the host reads the scalar block once, after the solve.
+constexpr int kGraphIters = 16;  // even: the current direction is back in `v` after every body
 
 
 // With pc (linear-FEM preconditioner) every outer iteration starts with the inner solve u_l = M^-1 r and
 // w, num = <r, w> (pc_num); the graph then holds kGraphItersPC outer iterations of 3 * pc->iters + 5 launches.
 constexpr int kGraphItersPC = 2;
+
+// Last kernel of a loop-graph body: repeat the body while the solve runs, at most maxIters / per_graph + 2 bodies.
+__global__ void pcg_loop_cond(CGScalars* S, cudaGraphConditionalHandle cond, int per_graph) {
+  const int b = ++S->bodies;
+  cudaGraphSetConditional(cond, (!S->done && b < S->maxIters / per_graph + 2) ? 1u : 0u);
+}
+
+// The whole (P)CG solve as one graph: a conditional while node whose body is per_graph iterations, enqueued by
+// body(k), and pcg_loop_cond; the device decides when to stop (no host round trip between iterations).
+// glaunches = the kernels of one body (taken back out of the context's launch counter: replay_until_done counts
+// them per body run).
+template <class Body>
+int capture_iterations(self_cg2d* h, cudaGraphExec_t& G, long long& glaunches, int per_graph, Body body) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  cudaGraph_t g = nullptr;
+  SELF_CUDA_TRY(ctx, cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle cond;
+  cudaError_t ce = cudaGraphConditionalHandleCreate(&cond, g, 1u, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (ce == cudaSuccess) ce = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return set_error(ctx, SELF_ERR_CUDA, "PCG loop graph: %s", cudaGetErrorString(ce));
+  }
+  cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+  const long long l0 = ctx->launches.load();
+  ce = cudaStreamBeginCaptureToGraph(st, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return set_error(ctx, SELF_ERR_CUDA, "PCG loop body capture: %s", cudaGetErrorString(ce));
+  }
+  int rc = SELF_OK;
+  for (int k = 0; k < per_graph && !rc; ++k) rc = body(k);
+  if (!rc) {
+    pcg_loop_cond<<<1, 1, 0, st>>>(h->S.p, cond, per_graph);
+    ctx->launches.fetch_add(1);
+  }
+  const cudaError_t le = rc ? cudaSuccess : cudaGetLastError();
+  ce = cudaStreamEndCapture(st, &bodyg);
+  glaunches = ctx->launches.load() - l0;
+  ctx->launches.fetch_sub(glaunches);
+  if (rc || le != cudaSuccess || ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    if (rc) return rc;
+    return set_error(ctx, SELF_ERR_CUDA, "PCG loop body capture: %s",
+                     cudaGetErrorString(le != cudaSuccess ? le : ce));
+  }
+  ce = cudaGraphInstantiate(&G, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
+  return SELF_OK;
+}
+
+// One launch of the loop graph G runs the solve to its stop; hs holds the scalars afterwards.
+int replay_until_done(self_cg2d* h, cudaGraphExec_t G, long long glaunches, CGScalars& hs) {
+  self_ctx* ctx = h->ctx;
+  cudaStream_t st = ctx->stream;
+  SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
+  SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  ctx->launches.fetch_add((long long)hs.bodies * glaunches);
+  return SELF_OK;
+}
 
 template <typename R>
 int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int maxIters, double tol, double r0,
@@ -1328,11 +1399,8 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
       G = nullptr;
     }
     if (!G) {
-      cudaGraph_t g;
-      int rc = SELF_OK;
-      const long long l0 = ctx->launches.load();
-      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < per_graph && !rc; ++k) {
+      const int rc = capture_iterations(h, G, glaunches, per_graph, [&](int k) -> int {
+        int rc = SELF_OK;
         R* vold = (k % 2 == 0) ? v : v2;
         R* vnew = (k % 2 == 0) ? v2 : v;
         if (pc) {
@@ -1362,26 +1430,13 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
           }
           SELF_LAUNCHED(ctx);
         }
-      }
-      cudaError_t ce = cudaStreamEndCapture(st, &g);
+        return rc;
+      });
       if (rc) return rc;
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&G, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
       gk = key;
       if (pc) h->pcl.key_iters[prec] = pc->iters;
-      glaunches = ctx->launches.load() - l0;
-      ctx->launches.fetch_sub(glaunches);
     }
-    const long long max_launches = (long long)maxIters / per_graph + 2;
-    for (long long gl = 0; gl < max_launches; ++gl) {
-      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
-      ctx->launches.fetch_add(glaunches);
-      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
-      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      if (hs.done) break;
-    }
+    if (const int rc = replay_until_done(h, G, glaunches, hs)) return rc;
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -1435,10 +1490,12 @@ int launch_compact_update_t(self_cg2d* h, const float* vnew, bool jac) {
   static int nbu[11] = {};  // resident blocks per SM: one full wave, grid-stride over the node groups
   if (nbu[N1] == 0) {
     int q = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_update_compact<N1>, kRedThreads, 0) != cudaSuccess) q = 4;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_update_compact<N1>, kRedThreads, 0) != cudaSuccess)
+      q = 4;
     nbu[N1] = std::max(1, q);
   }
-  const int grid = std::max(1, std::min({h->nblk, nbu[N1] * std::max(1, h->ctx->num_sms), (Cp.ngp / 4 + kRedThreads - 1) / kRedThreads}));
+  const int groups = (Cp.ngp / 4 + kRedThreads - 1) / kRedThreads;
+  const int grid = std::max(1, std::min({h->nblk, nbu[N1] * std::max(1, h->ctx->num_sms), groups}));
   pcg_update_compact<N1><<<grid, kRedThreads, 0, h->ctx->stream>>>(
       reinterpret_cast<float4*>(Cp.u.p), reinterpret_cast<float4*>(Cp.r.p), reinterpret_cast<float4*>(Cp.w.p),
       reinterpret_cast<const float4*>(vnew), Cp.zc.p, jac ? reinterpret_cast<const float4*>(Cp.dinv.p) : nullptr,
@@ -1516,30 +1573,13 @@ int pcg_device_compact(self_cg2d* h, bool jac, int maxIters, double tol, double 
       G = nullptr;
     }
     if (!G) {
-      cudaGraph_t g;
-      int rc = SELF_OK;
-      const long long l0 = ctx->launches.load();
-      SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < kGraphIters && !rc; ++k)
-        rc = launch_compact(h, Cp.w.p, k % 2 == 0 ? Cp.v.p : Cp.v2.p, k % 2 == 0 ? Cp.v2.p : Cp.v.p, jac);
-      cudaError_t ce = cudaStreamEndCapture(st, &g);
+      const int rc = capture_iterations(h, G, Cp.graph_launches, kGraphIters, [&](int k) {
+        return launch_compact(h, Cp.w.p, k % 2 == 0 ? Cp.v.p : Cp.v2.p, k % 2 == 0 ? Cp.v2.p : Cp.v.p, jac);
+      });
       if (rc) return rc;
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&G, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
       Cp.key[jac ? 1 : 0] = key;
-      Cp.graph_launches = ctx->launches.load() - l0;
-      ctx->launches.fetch_sub(Cp.graph_launches);
     }
-    const long long max_launches = (long long)maxIters / kGraphIters + 2;
-    for (long long gl = 0; gl < max_launches; ++gl) {
-      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
-      ctx->launches.fetch_add(Cp.graph_launches);
-      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
-      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      if (hs.done) break;
-    }
+    if (const int rc = replay_until_done(h, G, Cp.graph_launches, hs)) return rc;
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -2025,11 +2065,14 @@ int compact_build(self_cg2d* h) {
     for (int e = 0; e < nEl; ++e) {
       for (int t = 0; t < n; ++t)
         for (int i = 0; i < n; ++i)
-          kwT[compact_factor_index(n, 1, e / epl, 0, i, (e % epl) * n + t)] = (float)h->h_kw[(size_t)e * NN + (size_t)t * n + i];
+          kwT[compact_factor_index(n, 1, e / epl, 0, i, (e % epl) * n + t)] =
+              (float)h->h_kw[(size_t)e * NN + (size_t)t * n + i];
       ec[e] = make_float4((float)h->h_ec[4 * (size_t)e], (float)h->h_ec[4 * (size_t)e + 1],
                           (float)h->h_ec[4 * (size_t)e + 2], (float)h->h_ec[4 * (size_t)e + 3]);
     }
     if ((rc = upload(ctx, C.kw, kwT)) || (rc = upload(ctx, C.ec, ec))) return rc;
+    std::vector<double>().swap(h->h_kw);  // on the device now; the compact build runs once per handle
+    std::vector<double>().swap(h->h_ec);
   } else if ((rc = upload(ctx, C.fac, facT))) {
     return rc;
   }
