@@ -835,6 +835,163 @@ __global__ void __launch_bounds__(kRedThreads) mgs_axpy_dot_fused(R* __restrict_
 }
 
 // x += sum_k V_k y_k
+// ---------------------------------------------------------------------------------- on-chip modified Gram-Schmidt
+// One cooperative launch per Arnoldi step (one block per SM, all resident): each block keeps its chunk of w in
+// shared memory for the whole step, so the i + 1 projections stream only the basis vectors (each read twice: the
+// dot of projection k and the axpy of projection k, fused with the next dot) instead of w, v_k and v_{k+1} and a
+// write of w per projection; the step ends by writing v_{i+1} = w / ||w|| (gmres_next_basis) from shared memory.
+// The MGS order is the reference's: h(k) = <v_k, w> with w already reduced by v_0 .. v_{k-1}.  Grid-wide sums are
+// deterministic (every block adds the block partials in block order) and every barrier wait is bounded.
+constexpr int kMgsThreads = 1024;
+constexpr long long kMgsMaxPolls = 1LL << 22;  // polls of the barrier generation word; a round ends within µs
+
+__device__ __forceinline__ double block_sum_mgs(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = ln < (int)(blockDim.x >> 5) ? sh[ln] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+// Sum of v over the grid into *tot (every thread); false after a barrier time-out (err set, the caller returns).
+// part: 2 x gridDim.x partials (alternating rounds), bar: {arrivals, generation}.
+__device__ __forceinline__ bool mgs_allreduce(double v, double* __restrict__ part, int round, unsigned int* bar,
+                                              int* err, double* sh, double* tot) {
+  __shared__ int s_ok;
+  const double b = block_sum_mgs(v, sh);
+  const unsigned int nb = gridDim.x;
+  double* P = part + (size_t)(round & 1) * nb;
+  if (threadIdx.x == 0) {
+    P[blockIdx.x] = b;
+    __threadfence();
+    volatile unsigned int* gen = bar + 1;
+    const unsigned int g = *gen;  // this round's generation: it moves only after every block arrived
+    bool ok = true;
+    if (atomicAdd(bar, 1u) == nb - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long polls = 0;
+      while (*gen == g && ++polls < kMgsMaxPolls) {
+      }
+      ok = *gen != g;
+    }
+    __threadfence();
+    if (!ok) atomicExch(err, 1);
+    s_ok = ok && *((volatile int*)err) == 0;
+  }
+  __syncthreads();
+  if (!s_ok) return false;
+  double a = 0.0;
+  for (unsigned int k = threadIdx.x; k < nb; k += blockDim.x) a += __ldcg(&P[k]);
+  const double t = block_sum_mgs(a, sh);
+  if (threadIdx.x == 0) sh[32] = t;
+  __syncthreads();
+  *tot = sh[32];
+  __syncthreads();  // sh is reused by the next sum
+  return true;
+}
+
+// the stream element of mgs_onchip: 16-byte vectors of FP32 values; FP64 values one by one (measured: double2 made
+// the FP64 step 15 % slower, float4 the FP32 step 32 % faster than single values)
+template <typename R>
+struct MgsVec;
+template <>
+struct MgsVec<float> {
+  using T = float4;
+  static constexpr int N = 4;
+};
+template <>
+struct MgsVec<double> {
+  using T = double;
+  static constexpr int N = 1;
+};
+
+// MGS of w against V[0..i] and v_{i+1} = w / ||w||: H[k] = h(k, i) for k <= i, H[i + 1] = ||w||^2.  Block b owns
+// nodes [b chunk, (b + 1) chunk) of the L-vectors.
+template <typename R>
+__global__ void __launch_bounds__(kMgsThreads, 1) mgs_onchip(const R* __restrict__ w, R* __restrict__ V, size_t nl,
+                                                            int i, int chunk, double* __restrict__ H,
+                                                            double* __restrict__ part, unsigned int* bar, int* err) {
+  using VT = typename MgsVec<R>::T;
+  constexpr int EV = MgsVec<R>::N;
+  extern __shared__ __align__(16) unsigned char mgs_smem[];
+  R* ws = reinterpret_cast<R*>(mgs_smem);
+  VT* wv = reinterpret_cast<VT*>(mgs_smem);
+  __shared__ double sh[33];
+  const size_t c0 = (size_t)blockIdx.x * chunk;  // chunk is a multiple of 4: c0 starts a 16-byte vector
+  const int n = c0 < nl ? (int)(nl - c0 < (size_t)chunk ? nl - c0 : (size_t)chunk) : 0;
+  const int nv = n / EV;  // whole vectors; the tail (the last block only) goes node by node
+  // a thread's products are summed in R (FP32 vectors: no per-node FP64 conversions on GB300's narrow FP64 pipe),
+  // the block and grid sums in FP64, as in mgs_axpy_dot_fused
+  R acc = 0;
+  double h = 0.0;
+  {
+    const VT* wg = reinterpret_cast<const VT*>(w + c0);
+    const VT* v0 = reinterpret_cast<const VT*>(V + c0);
+#pragma unroll 2
+    for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+      const VT x = wg[q], a = v0[q];
+      wv[q] = x;
+      const R* xs = reinterpret_cast<const R*>(&x);
+      const R* as = reinterpret_cast<const R*>(&a);
+#pragma unroll
+      for (int c = 0; c < EV; ++c) acc += as[c] * xs[c];
+    }
+    for (int q = nv * EV + threadIdx.x; q < n; q += blockDim.x) {
+      const R x = w[c0 + q];
+      ws[q] = x;
+      acc += V[c0 + q] * x;
+    }
+  }
+  if (!mgs_allreduce((double)acc, part, 0, bar, err, sh, &h)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) H[0] = h;
+  for (int k = 0; k <= i; ++k) {
+    const R* vk = V + (size_t)k * nl + c0;
+    const R* vn = V + (size_t)(k + 1) * nl + c0;
+    const VT* vkv = reinterpret_cast<const VT*>(vk);
+    const VT* vnv = reinterpret_cast<const VT*>(vn);
+    const R hk = (R)h;
+    const bool last = k == i;
+    acc = 0;
+#pragma unroll 2
+    for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+      VT y = wv[q];
+      const VT a = vkv[q];
+      VT b = a;
+      if (!last) b = vnv[q];
+      R* ys = reinterpret_cast<R*>(&y);
+      const R* as = reinterpret_cast<const R*>(&a);
+      const R* bs = reinterpret_cast<const R*>(&b);
+#pragma unroll
+      for (int c = 0; c < EV; ++c) {
+        ys[c] = ys[c] - hk * as[c];
+        acc += last ? ys[c] * ys[c] : bs[c] * ys[c];
+      }
+      wv[q] = y;
+    }
+    for (int q = nv * EV + threadIdx.x; q < n; q += blockDim.x) {
+      const R y = ws[q] - hk * vk[q];
+      ws[q] = y;
+      acc += last ? y * y : vn[q] * y;
+    }
+    if (!mgs_allreduce((double)acc, part, k + 1, bar, err, sh, &h)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) H[k + 1] = h;
+  }
+  // v_{i+1} = w / ||w||, zero on a lucky breakdown (the rule of gmres_givens / gmres_next_basis)
+  const bool zero = fabs(sqrt(h)) <= 2.220446049250313e-16;
+  const double f = zero ? 0.0 : 1.0 / sqrt(h);
+  R* vo = V + (size_t)(i + 1) * nl + c0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) vo[q] = zero ? (R)0 : (R)(f * (double)ws[q]);
+}
+
 template <typename R>
 __global__ void gmres_update(R* __restrict__ x, const R* __restrict__ V, const double* __restrict__ y, int nr,
                              size_t n, const R* __restrict__ dinv) {
@@ -934,6 +1091,9 @@ struct self_cg2d {
   DevBuf<double> gm_V, gm_y;  // GMRES basis (m+1) * nl, y
   DevBuf<float> gm_V32;
   DevBuf<double> gm_H, gm_rho, gm_c, gm_s, gm_bhat;
+  DevBuf<double> mgs_part;          // on-chip MGS: 2 x SMs block partials
+  DevBuf<unsigned int> mgs_bar;     // {arrivals, generation}
+  DevBuf<int> mgs_err;              // barrier time-out flag
   DevBuf<selfgpu::cg::GMScalars> GS;
   std::vector<double> h_J, h_w;
   std::vector<double> h_fac, h_dinv;
@@ -2588,6 +2748,40 @@ struct CycleOut {
   double rc;
 };
 
+// Launch shape of mgs_onchip: one block per SM, chunk = the L-vector share of a block (a multiple of 4 nodes);
+// false (streaming MGS) when the L-vector length is not a multiple of 4 (16-byte vector access), the share does not
+// fit the opt-in shared memory of a block, the device has no cooperative launch, or a buffer cannot be allocated.
+template <typename R>
+bool mgs_onchip_plan(self_cg2d* h, int* nb, int* chunk, size_t* smem) {
+  self_ctx* ctx = h->ctx;
+  int coop = 0, optin = 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop) return false;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess)
+    return false;
+  if (h->nl % 4 != 0) return false;  // every basis vector and block chunk must start on a 16-byte boundary
+  const int sms = std::max(1, ctx->num_sms);
+  const size_t c = ((h->nl + sms - 1) / sms + 3) / 4 * 4;
+  const size_t bytes = c * sizeof(R);
+  if (bytes + 2048 > (size_t)optin) return false;
+  static size_t attr_set[2] = {0, 0};
+  size_t& as = attr_set[sizeof(R) == 4];
+  if (as < bytes) {
+    if (cudaFuncSetAttribute(mgs_onchip<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+      return false;
+    as = bytes;
+  }
+  int q = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, mgs_onchip<R>, kMgsThreads, bytes) != cudaSuccess || q < 1)
+    return false;
+  if (h->mgs_part.n < 2 * (size_t)sms && h->mgs_part.alloc(2 * (size_t)sms) != cudaSuccess) return false;
+  if (!h->mgs_bar.p && h->mgs_bar.alloc(2) != cudaSuccess) return false;
+  if (!h->mgs_err.p && h->mgs_err.alloc(1) != cudaSuccess) return false;
+  *nb = sms;
+  *chunk = (int)c;
+  *smem = bytes;
+  return true;
+}
+
 template <typename R>
 int gmres_cycle(self_cg2d* h, R* x, const R* r, int m, int msteps, double r0, double tol, double rcur, R* V, R* w,
                 R* t, const R* dinv, const OpData<R>& od, double* resi_dev, int l0, int maxIters, CycleOut* out) {
@@ -2609,6 +2803,11 @@ int gmres_cycle(self_cg2d* h, R* x, const R* r, int m, int msteps, double r0, do
   G.tol = tol;
   G.rc = rcur;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->GS.p, &G, sizeof(G), cudaMemcpyHostToDevice, st));
+  // on-chip MGS when every SM's share of w fits its shared memory and all blocks can be resident together
+  int nbm = 0, chunk = 0;
+  size_t smem = 0;
+  const bool onchip = mgs_onchip_plan<R>(h, &nbm, &chunk, &smem);
+  if (onchip) SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->mgs_err.p, 0, sizeof(int), st));
   for (int i = 0; i < msteps; ++i) {
     const R* vi = V + (size_t)i * nl;
     if (dinv) {  // z_i = PreconditionInvert(v_i)
@@ -2617,6 +2816,25 @@ int gmres_cycle(self_cg2d* h, R* x, const R* r, int m, int msteps, double r0, do
       if ((rc = matrix_action<R>(h, t, w, od))) return rc;
     } else if ((rc = matrix_action<R>(h, vi, w, od))) {
       return rc;
+    }
+    const int l = l0 + i + 1;
+    if (onchip) {  // MGS with w in shared memory, v_{i+1} written by the same launch; then Givens
+      SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->mgs_bar.p, 0, 2 * sizeof(unsigned int), st));
+      const R* wc = w;
+      size_t nlc = nl;
+      int ic = i, ch = chunk;
+      double *Hc = h->gm_H.p, *pc = h->mgs_part.p;
+      unsigned int* bc = h->mgs_bar.p;
+      int* ec = h->mgs_err.p;
+      void* args[] = {(void*)&wc, (void*)&V, (void*)&nlc, (void*)&ic, (void*)&ch, (void*)&Hc, (void*)&pc, (void*)&bc,
+                      (void*)&ec};
+      SELF_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((const void*)mgs_onchip<R>, dim3(nbm), dim3(kMgsThreads), args,
+                                                     smem, st));
+      SELF_LAUNCHED(ctx);
+      gmres_givens<<<1, 1, 0, st>>>(h->gm_H.p, i, m, h->gm_rho.p, h->gm_c.p, h->gm_s.p, h->gm_bhat.p, h->GS.p,
+                                    resi_dev, l <= maxIters ? l : 0);
+      SELF_LAUNCHED(ctx);
+      continue;
     }
     // MGS: h(k,i) = <v_k, w>; w -= h(k,i) v_k, the axpy of step k fused with the dot of step k+1
     if ((rc = dots<R>(h, V, w, nullptr, nullptr, h->gm_H.p))) return rc;
@@ -2628,7 +2846,6 @@ int gmres_cycle(self_cg2d* h, R* x, const R* r, int m, int msteps, double r0, do
       SELF_LAUNCHED(ctx);
     }
     // gm_H[i+1] = <w,w>; Givens on the device
-    const int l = l0 + i + 1;
     gmres_givens<<<1, 1, 0, st>>>(h->gm_H.p, i, m, h->gm_rho.p, h->gm_c.p, h->gm_s.p, h->gm_bhat.p, h->GS.p,
                                   resi_dev, l <= maxIters ? l : 0);
     SELF_LAUNCHED(ctx);
@@ -2639,6 +2856,11 @@ int gmres_cycle(self_cg2d* h, R* x, const R* r, int m, int msteps, double r0, do
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&G, h->GS.p, sizeof(G), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if (onchip) {
+    int err = 0;
+    SELF_CUDA_TRY(ctx, cudaMemcpy(&err, h->mgs_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return set_error(ctx, SELF_ERR_TIMEOUT, "GMRES: a grid barrier wait of the on-chip MGS ran out");
+  }
   out->steps = G.done ? G.i : msteps;
   out->nr = G.nr;
   out->done = G.done;
