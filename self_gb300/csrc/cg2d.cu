@@ -1261,12 +1261,9 @@ void launch_apply_fused_t(self_cg2d* h, const R* w, const R* vold, R* vnew, cons
   const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
   if constexpr (sizeof(R) == 4 && N1 == 8) {
     if (h->tc) {  // tensor-core contractions (tcgen05, compensated TF32), 32 elements per tile
-      static bool attr_set[2] = {false, false};
       const int smem = (int)sizeof(tc::Smem);
-      if (!attr_set[NF == 6]) {
-        cudaFuncSetAttribute(pcg_apply_tc<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr_set[NF == 6] = true;
-      }
+      // set for the current device on every launch (a process may drive several devices; the call is cheap)
+      cudaFuncSetAttribute(pcg_apply_tc<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
       // 4 blocks per SM: the shared-memory and register limits, and 4 x 128 TMEM columns fill the SM's 512
       const int q = 4;
       const int tgroups = (h->nEl + tc::kTileElems - 1) / tc::kTileElems;
@@ -2763,13 +2760,9 @@ bool mgs_onchip_plan(self_cg2d* h, int* nb, int* chunk, size_t* smem) {
   const size_t c = ((h->nl + sms - 1) / sms + 3) / 4 * 4;
   const size_t bytes = c * sizeof(R);
   if (bytes + 2048 > (size_t)optin) return false;
-  static size_t attr_set[2] = {0, 0};
-  size_t& as = attr_set[sizeof(R) == 4];
-  if (as < bytes) {
-    if (cudaFuncSetAttribute(mgs_onchip<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
-      return false;
-    as = bytes;
-  }
+  // for the current device, once per cycle (a process may drive several devices; the call is cheap)
+  if (cudaFuncSetAttribute(mgs_onchip<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return false;
   int q = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, mgs_onchip<R>, kMgsThreads, bytes) != cudaSuccess || q < 1)
     return false;

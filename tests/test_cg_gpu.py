@@ -97,9 +97,11 @@ def test_fp32_refinement_reaches_fp64_accuracy(oracle, gpu_ctx):
     assert rel_inf(s32, s64) < 1e-8
 
 
-def test_gmres_advection_diffusion_parity(oracle, gpu_ctx):
+@pytest.mark.parametrize("N,nx", [(4, 6), (4, 5)])
+def test_gmres_advection_diffusion_parity(oracle, gpu_ctx, N, nx):
+    """GMRES(30) against the oracle's: 6x6 N=4 (900 local nodes) runs the on-chip Gram-Schmidt, 5x5 N=4 (625, not a
+    multiple of 4) the streaming one."""
     import self_gb300 as sg
-    N, nx = 4, 6
     nod, mesh, k, source, P = _problem(oracle, N, nx, lam=0.0, op=1, vel=(1.0, 0.5), kappa=1e-2)
     cg = sg.CGsemElliptic_2D(gpu_ctx, nod, mesh, k, lam=0.0, op=1, vel=(1.0, 0.5))
     sol, rep = cg.Solve(source, method="gmres", m=30, tolerance=1e-10, maxIters=2000, return_resi=True)
