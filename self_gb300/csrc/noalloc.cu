@@ -19,7 +19,7 @@
 //    streams, or different host threads) race on it, so the caller serialises them;
 //  * every GPU that loads the library holds the array until the process exits;
 //  * the first call in a CUDA context looks up the array's device address (cudaGetSymbolAddress) with that
-//    context's device current; the address is kept per context (keyed by the driver's context ID), so a new
+//    context's device current; the address is kept per context (keyed by the CUDA context ID), so a new
 //    context on the same device -- after cudaDeviceReset, say -- looks it up again on its first call.
 #include <cuda.h>
 #include <cuda_runtime.h>
