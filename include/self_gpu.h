@@ -214,10 +214,11 @@ typedef struct {
   /* FP32 inner CG at N = 7: nonzero runs the element operator's derivative contractions on the tensor cores
    * (tcgen05 GEMMs of 32-element tiles, compensated TF32 products); 0 uses the CUDA-core line form */
   int tensor_cores;
-  /* storage of the FP32 inner (P)CG vectors: SELF_LAYOUT_COMPACT (default) one value per unknown, grouped by
-   * mesh entity (element interiors, edges, corners), when the mesh is conforming (else the element-local form);
-   * SELF_LAYOUT_LOCAL the masked element-local L-vectors.  The linear-FEM preconditioner and the tensor-core apply
-   * run on the element-local form. */
+  /* storage of the (P)CG vectors (the FP32 inner iterations and the FP64 solve): SELF_LAYOUT_COMPACT (default)
+   * one value per unknown, grouped by mesh entity (element interiors, edges, corners), when the mesh is conforming
+   * (FP64: and N >= 5, the even-odd operator; else the element-local form); SELF_LAYOUT_LOCAL the masked
+   * element-local L-vectors.  The linear-FEM preconditioner and the tensor-core apply run on the element-local form;
+   * GMRES always does. */
   int inner_layout;
 } self_solve_opts;
 #define SELF_LAYOUT_COMPACT 0

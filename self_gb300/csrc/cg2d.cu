@@ -1116,16 +1116,22 @@ struct self_cg2d {
   struct Compact {
     bool tried = false, ok = false;
     int M = 0, nInt = 0, nE2 = 0, nE1 = 0, nC = 0, ng = 0, ngp = 0, nz = 0;
+    int fp64 = -1;  // FP64 solves on the layout: 1 when the even-odd FP64 line operator applies (N1 >= 6)
     DevBuf<int4> desc;
     DevBuf<int> coff, cl;
-    DevBuf<float> dinv, u, r, v, v2, w, zc;
     DevBuf<float> fac;  // the FP32 element factors line-interleaved by pass group (compact.cuh factor_index)
     bool affine = false;  // affine elements: kw (k w_i w_j per node, line-interleaved) and ec per element instead
     DevBuf<float> kw;
     DevBuf<float4> ec;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    selfgpu::cg::PcgGraphKey key[2] = {};
-    long long graph_launches = 0;
+    template <typename R>
+    struct Vecs {  // Krylov vectors, contribution space and captured solve graphs of one precision
+      DevBuf<R> dinv, u, r, v, v2, w, zc;
+      cudaGraphExec_t graph[2] = {nullptr, nullptr};
+      selfgpu::cg::PcgGraphKey key[2] = {};
+      long long graph_launches = 0;
+    };
+    Vecs<float> f32;
+    Vecs<double> f64;  // allocated on the first FP64 solve
   } cpt;
   // linear-FEM preconditioner (SELF_SOLVE_PCG_LINEAR): node positions kept from create; the linear mesh's topology,
   // sub-quad factors and work vectors are built on first use
@@ -1155,7 +1161,9 @@ struct self_cg2d {
         if (g) cudaGraphExecDestroy(g);
     for (auto& g : pcl.graph)
       if (g) cudaGraphExecDestroy(g);
-    for (auto& g : cpt.graph)
+    for (auto& g : cpt.f32.graph)
+      if (g) cudaGraphExecDestroy(g);
+    for (auto& g : cpt.f64.graph)
       if (g) cudaGraphExecDestroy(g);
   }
 };
@@ -1603,13 +1611,16 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
   return hs.ioerr;
 }
 
-// FP32 PCG on the compact layout (cpt vectors; r holds the right-hand side, u the zero initial guess): two launches
-// per iteration (pcg_apply_compact_f32, pcg_update_compact), captured kGraphIters iterations to a graph.
+// (P)CG on the compact layout (r holds the right-hand side, u the zero initial guess): two launches per iteration
+// (pcg_apply_compact_f32 / _f64, pcg_update_compact), the solve one launch of a loop graph.
 template <int N1>
 CompactView compact_view(self_cg2d* h) {
   auto& Cp = h->cpt;
   return CompactView{Cp.desc.p, Cp.coff.p, Cp.nInt, Cp.nE2, Cp.nE1, Cp.nC, Cp.ngp, h->nEl};
 }
+
+inline self_cg2d::Compact::Vecs<float>& cvecs(self_cg2d* h, const float*) { return h->cpt.f32; }
+inline self_cg2d::Compact::Vecs<double>& cvecs(self_cg2d* h, const double*) { return h->cpt.f64; }
 
 template <int N1, int NF>
 int launch_compact_apply_t(self_cg2d* h, const float* w, const float* vold, float* vnew) {
@@ -1631,32 +1642,58 @@ int launch_compact_apply_t(self_cg2d* h, const float* w, const float* vold, floa
   AffineOp<N1> A{h->cpt.kw.p, h->cpt.ec.p, {}};
   for (int j = 0; j < N1; ++j)
     for (int i = 0; i < N1; ++i) A.ww[i + N1 * j] = (float)(h->h_w[i] * h->h_w[j]);
+  float* zc = h->cpt.f32.zc.p;
   if (aff)
     pcg_apply_compact_f32<N1, NF, NF == 4><<<grid, kRedThreads, 0, h->ctx->stream>>>(
-        w, vold, vnew, compact_view<N1>(h), h->cpt.fac.p, A, h->cpt.zc.p, Cg, h->S.p, h->partial.p, h->ticket.p);
+        w, vold, vnew, compact_view<N1>(h), h->cpt.fac.p, A, zc, Cg, h->S.p, h->partial.p, h->ticket.p);
   else
     pcg_apply_compact_f32<N1, NF, false><<<grid, kRedThreads, 0, h->ctx->stream>>>(
-        w, vold, vnew, compact_view<N1>(h), h->cpt.fac.p, A, h->cpt.zc.p, Cg, h->S.p, h->partial.p, h->ticket.p);
+        w, vold, vnew, compact_view<N1>(h), h->cpt.fac.p, A, zc, Cg, h->S.p, h->partial.p, h->ticket.p);
   SELF_LAUNCHED(h->ctx);
   return SELF_OK;
 }
 
-template <int N1>
-int launch_compact_update_t(self_cg2d* h, const float* vnew, bool jac) {
+template <int N1, int NF>
+int launch_compact_apply_t(self_cg2d* h, const double* w, const double* vold, double* vnew) {
+  if constexpr (N1 >= 6) {
+    EOPair<N1> T;
+    if (!eo_pair<N1>(h->op64.D, T)) return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "FP64 compact apply: no even-odd D");
+    static int resident[11][2] = {};
+    int& nb = resident[N1][NF == 6];
+    if (nb == 0) {
+      int q = 0;
+      const cudaError_t ce =
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_apply_compact_f64<N1, NF>, kRedThreads, 0);
+      nb = std::max(1, ce == cudaSuccess ? q : 2);
+    }
+    const int groups = (h->nEl + line_epb<N1>() - 1) / line_epb<N1>();
+    const int grid = std::max(1, std::min({h->apply_grid, nb * std::max(1, h->ctx->num_sms), groups}));
+    pcg_apply_compact_f64<N1, NF><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+        w, vold, vnew, compact_view<N1>(h), h->op64.fac.p, h->cpt.f64.zc.p, T, h->S.p, h->partial.p, h->ticket.p);
+    SELF_LAUNCHED(h->ctx);
+    return SELF_OK;
+  } else {
+    return set_error(h->ctx, SELF_ERR_UNSUPPORTED, "FP64 compact apply: degree %d", N1 - 1);
+  }
+}
+
+template <int N1, typename R>
+int launch_compact_update_t(self_cg2d* h, const R* vnew, bool jac) {
   auto& Cp = h->cpt;
+  auto& Vc = cvecs(h, vnew);
   static int nbu[11] = {};  // resident blocks per SM: one full wave, grid-stride over the node groups
   if (nbu[N1] == 0) {
     int q = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_update_compact<N1>, kRedThreads, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, pcg_update_compact<N1, R>, kRedThreads, 0) !=
+        cudaSuccess)
       q = 4;
     nbu[N1] = std::max(1, q);
   }
   const int groups = (Cp.ngp / 4 + kRedThreads - 1) / kRedThreads;
   const int grid = std::max(1, std::min({h->nblk, nbu[N1] * std::max(1, h->ctx->num_sms), groups}));
-  pcg_update_compact<N1><<<grid, kRedThreads, 0, h->ctx->stream>>>(
-      reinterpret_cast<float4*>(Cp.u.p), reinterpret_cast<float4*>(Cp.r.p), reinterpret_cast<float4*>(Cp.w.p),
-      reinterpret_cast<const float4*>(vnew), Cp.zc.p, jac ? reinterpret_cast<const float4*>(Cp.dinv.p) : nullptr,
-      compact_view<N1>(h), h->S.p, h->partial.p, h->ticket.p);
+  pcg_update_compact<N1, R><<<grid, kRedThreads, 0, h->ctx->stream>>>(
+      Vc.u.p, Vc.r.p, Vc.w.p, vnew, Vc.zc.p, jac ? Vc.dinv.p : nullptr, compact_view<N1>(h), h->S.p, h->partial.p,
+      h->ticket.p);
   SELF_LAUNCHED(h->ctx);
   return SELF_OK;
 }
@@ -1664,20 +1701,21 @@ int launch_compact_update_t(self_cg2d* h, const float* vnew, bool jac) {
 template <int N1>
 int launch_compact_assemble_t(self_cg2d* h, double* out) {
   auto& Cp = h->cpt;
-  compact_assemble<N1><<<h->nblk, kRedThreads, 0, h->ctx->stream>>>(out, Cp.zc.p, Cp.cl.p, Cp.ng,
-                                                                   compact_view<N1>(h));
+  compact_assemble<N1, float><<<h->nblk, kRedThreads, 0, h->ctx->stream>>>(out, Cp.f32.zc.p, Cp.cl.p, Cp.ng,
+                                                                          compact_view<N1>(h));
   SELF_LAUNCHED(h->ctx);
   return SELF_OK;
 }
 
-// the compact kernels by degree: apply (op = 0), update (1), assemble into a masked FP64 L-vector (2)
-int compact_dispatch(self_cg2d* h, int op, const float* w, const float* vold, float* vnew, bool jac, double* out) {
+// the compact kernels by degree: apply (op = 0), update (1), assemble the FP32 output into a masked FP64 L-vector (2)
+template <typename R>
+int compact_dispatch(self_cg2d* h, int op, const R* w, const R* vold, R* vnew, bool jac, double* out) {
   const bool adv = h->nf == 6;
-#define SELF_CG_CASE(NV)                                                                             \
-  case NV:                                                                                           \
-    if (op == 0)                                                                                     \
+#define SELF_CG_CASE(NV)                                                                                 \
+  case NV:                                                                                               \
+    if (op == 0)                                                                                         \
       return adv ? launch_compact_apply_t<NV, 6>(h, w, vold, vnew) : launch_compact_apply_t<NV, 4>(h, w, vold, vnew); \
-    if (op == 1) return launch_compact_update_t<NV>(h, vnew, jac);                                  \
+    if (op == 1) return launch_compact_update_t<NV, R>(h, vnew, jac);                                   \
     return launch_compact_assemble_t<NV>(h, out);
   switch (h->n) {
     SELF_CG_CASE(3)
@@ -1695,48 +1733,89 @@ int compact_dispatch(self_cg2d* h, int op, const float* w, const float* vold, fl
 }
 
 int launch_compact_apply(self_cg2d* h, const float* w, const float* vold, float* vnew) {
-  return compact_dispatch(h, 0, w, vold, vnew, false, nullptr);
+  return compact_dispatch<float>(h, 0, w, vold, vnew, false, nullptr);
 }
 int launch_compact_assemble(self_cg2d* h, double* out) {
-  return compact_dispatch(h, 2, nullptr, nullptr, nullptr, false, out);
+  return compact_dispatch<float>(h, 2, nullptr, nullptr, nullptr, false, out);
 }
 // one PCG iteration on the compact layout: apply, then update
-int launch_compact(self_cg2d* h, const float* w, const float* vold, float* vnew, bool jac) {
-  int rc = compact_dispatch(h, 0, w, vold, vnew, jac, nullptr);
-  return rc ? rc : compact_dispatch(h, 1, w, vold, vnew, jac, nullptr);
+template <typename R>
+int launch_compact(self_cg2d* h, const R* w, const R* vold, R* vnew, bool jac) {
+  int rc = compact_dispatch<R>(h, 0, w, vold, vnew, jac, nullptr);
+  return rc ? rc : compact_dispatch<R>(h, 1, w, vold, vnew, jac, nullptr);
 }
 
-int pcg_device_compact(self_cg2d* h, bool jac, int maxIters, double tol, double r0, int* iters, double* rel) {
+// The FP64 vectors of the compact layout (first FP64 solve), with the Jacobi diagonal gathered from the FP64
+// element-local one.  False when the FP64 compact apply does not apply (no even-odd line operator: N < 5).
+int compact_fp64_ready(self_cg2d* h, bool* ready) {
+  auto& Cp = h->cpt;
+  *ready = false;
+  if (!Cp.ok) return SELF_OK;
+  if (Cp.fp64 < 0) {
+    bool eo = false;
+    switch (h->n) {
+      case 6: { EOPair<6> T; eo = eo_pair<6>(h->op64.D, T); break; }
+      case 7: { EOPair<7> T; eo = eo_pair<7>(h->op64.D, T); break; }
+      case 8: { EOPair<8> T; eo = eo_pair<8>(h->op64.D, T); break; }
+      case 9: { EOPair<9> T; eo = eo_pair<9>(h->op64.D, T); break; }
+      case 10: { EOPair<10> T; eo = eo_pair<10>(h->op64.D, T); break; }
+      default: break;
+    }
+    Cp.fp64 = eo ? 1 : 0;
+  }
+  if (!Cp.fp64) return SELF_OK;
+  auto& V = Cp.f64;
+  self_ctx* ctx = h->ctx;
+  if (!V.u.p) {
+    const size_t ngp = Cp.ngp;
+    for (DevBuf<double>* b : {&V.dinv, &V.u, &V.r, &V.v, &V.v2, &V.w}) {
+      if (b->alloc(ngp) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu doubles", ngp);
+      SELF_CUDA_TRY(ctx, cudaMemsetAsync(b->p, 0, ngp * sizeof(double), ctx->stream));
+    }
+    if (V.zc.alloc(Cp.nz) != cudaSuccess)
+      return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %d doubles", Cp.nz);
+    compact_gather<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(V.dinv.p, h->op64.dinv.p, Cp.cl.p, Cp.ng, Cp.ngp);
+    SELF_LAUNCHED(ctx);
+  }
+  *ready = true;
+  return SELF_OK;
+}
+
+template <typename R>
+int pcg_device_compact(self_cg2d* h, bool jac, int maxIters, double tol, double r0, double* resi_dev, bool abs_stop,
+                       int* iters, double* rel) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
   auto& Cp = h->cpt;
+  auto& Vc = cvecs(h, (const R*)nullptr);
   CGScalars hs{};
   hs.r0 = r0;
   hs.tol = tol;
   hs.maxIters = maxIters;
-  hs.done = maxIters <= 0 || r0 == 0.0;
+  hs.done = (abs_stop && r0 < tol) || maxIters <= 0 || r0 == 0.0;
   hs.ioerr = hs.done ? 0 : -2;
+  hs.resi = resi_dev;
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(h->S.p, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
   SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->ticket.p, 0, sizeof(unsigned int), st));
   if (!hs.done) {
-    const float* dinv = jac ? Cp.dinv.p : nullptr;
-    pcg_start_fused<float><<<h->nblk, kRedThreads, 0, st>>>(Cp.r.p, dinv, Cp.w.p, Cp.ngp, h->S.p, h->partial.p,
-                                                            h->ticket.p);
+    const R* dinv = jac ? Vc.dinv.p : nullptr;
+    pcg_start_fused<R><<<h->nblk, kRedThreads, 0, st>>>(Vc.r.p, dinv, Vc.w.p, Cp.ngp, h->S.p, h->partial.p,
+                                                        h->ticket.p);
     SELF_LAUNCHED(ctx);
-    cudaGraphExec_t& G = Cp.graph[jac ? 1 : 0];
-    const PcgGraphKey key{Cp.u.p, Cp.r.p, Cp.v.p, Cp.v2.p, Cp.w.p, Cp.zc.p, dinv, h->op32.fac.p, 0};
-    if (G && !(Cp.key[jac ? 1 : 0] == key)) {
+    cudaGraphExec_t& G = Vc.graph[jac ? 1 : 0];
+    const PcgGraphKey key{Vc.u.p, Vc.r.p, Vc.v.p, Vc.v2.p, Vc.w.p, Vc.zc.p, dinv, nullptr, 0};
+    if (G && !(Vc.key[jac ? 1 : 0] == key)) {
       cudaGraphExecDestroy(G);
       G = nullptr;
     }
     if (!G) {
-      const int rc = capture_iterations(h, G, Cp.graph_launches, kGraphIters, [&](int k) {
-        return launch_compact(h, Cp.w.p, k % 2 == 0 ? Cp.v.p : Cp.v2.p, k % 2 == 0 ? Cp.v2.p : Cp.v.p, jac);
+      const int rc = capture_iterations(h, G, Vc.graph_launches, kGraphIters, [&](int k) {
+        return launch_compact<R>(h, Vc.w.p, k % 2 == 0 ? Vc.v.p : Vc.v2.p, k % 2 == 0 ? Vc.v2.p : Vc.v.p, jac);
       });
       if (rc) return rc;
-      Cp.key[jac ? 1 : 0] = key;
+      Vc.key[jac ? 1 : 0] = key;
     }
-    if (const int rc = replay_until_done(h, G, Cp.graph_launches, hs)) return rc;
+    if (const int rc = replay_until_done(h, G, Vc.graph_launches, hs)) return rc;
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -2213,7 +2292,7 @@ int compact_build(self_cg2d* h) {
   self_ctx* ctx = h->ctx;
   int rc;
   if ((rc = upload(ctx, C.desc, desc)) || (rc = upload(ctx, C.coff, coff)) || (rc = upload(ctx, C.cl, cl)) ||
-      (rc = upload(ctx, C.dinv, dinv)))
+      (rc = upload(ctx, C.f32.dinv, dinv)))
     return rc;
   C.affine = h->affine;
   if (C.affine) {  // one streamed value per node (k w_i w_j, line-interleaved) and four per element
@@ -2233,11 +2312,12 @@ int compact_build(self_cg2d* h) {
   } else if ((rc = upload(ctx, C.fac, facT))) {
     return rc;
   }
-  for (DevBuf<float>* b : {&C.u, &C.r, &C.v, &C.v2, &C.w}) {
+  for (DevBuf<float>* b : {&C.f32.u, &C.f32.r, &C.f32.v, &C.f32.v2, &C.f32.w}) {
     if (b->alloc(ngp) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu floats", ngp);
     SELF_CUDA_TRY(ctx, cudaMemsetAsync(b->p, 0, ngp * sizeof(float), ctx->stream));
   }
-  if (C.zc.alloc(nz) != cudaSuccess) return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu floats", nz);
+  if (C.f32.zc.alloc(nz) != cudaSuccess)
+    return set_error(ctx, SELF_ERR_ALLOC, "device allocation of %zu floats", nz);
   C.M = M;
   C.nInt = (int)nInt;
   C.nE2 = nE2;
@@ -2335,9 +2415,9 @@ int self_cg2d_matrix_action_f32(self_cg2d* h, const double* u, double* Au, int f
     if (!h->cpt.tried && (rc = compact_build(h))) return rc;
     auto& Cp = h->cpt;
     if (!Cp.ok) return set_error(ctx, SELF_ERR_UNSUPPORTED, "compact layout: mesh not covered");
-    compact_gather_f32<<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.w.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
+    compact_gather<float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.f32.w.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
     SELF_LAUNCHED(ctx);
-    if ((rc = launch_compact_apply(h, Cp.w.p, Cp.v2.p, Cp.v.p))) return rc;
+    if ((rc = launch_compact_apply(h, Cp.f32.w.p, Cp.f32.v2.p, Cp.f32.v.p))) return rc;
     SELF_CUDA_TRY(ctx, cudaMemsetAsync(h->z.p, 0, nl * sizeof(double), ctx->stream));
     if ((rc = launch_compact_assemble(h, h->z.p))) return rc;
   } else {
@@ -3107,10 +3187,28 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         if ((rc = ensure(ctx, resi_dev, (size_t)o->maxIters + 1))) return rc;
         SELF_CUDA_TRY(ctx, cudaMemsetAsync(resi_dev.p, 0, ((size_t)o->maxIters + 1) * sizeof(double), ctx->stream));
       }
-      const PcRun<double> pc = use_pcl ? pcl_run<double>(h, o->pc_iterations) : PcRun<double>{};
-      R.ioerr = pcg_device<double>(h, h->u.p, h->r.p, h->v.p, h->w.p, h->z.p, jac ? h->op64.dinv.p : nullptr,
-                                   o->maxIters, o->tolerance, r0, resi ? resi_dev.p : nullptr, &iters, &rel, h->op64,
-                                   true, use_pcl ? &pc : nullptr);
+      // the compact layout (default) when the FP64 compact operator applies: CG on the correction d (d0 = 0,
+      // the residual of the initial guess as right-hand side), x += d at the primary copies
+      bool cpt64 = false;
+      if (!use_pcl && o->inner_layout != SELF_LAYOUT_LOCAL) {
+        if (!h->cpt.tried && (rc = compact_build(h))) return rc;
+        if ((rc = compact_fp64_ready(h, &cpt64))) return rc;
+      }
+      if (cpt64) {
+        auto& Cp = h->cpt;
+        compact_gather<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.f64.r.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
+        SELF_LAUNCHED(ctx);
+        SELF_CUDA_TRY(ctx, cudaMemsetAsync(Cp.f64.u.p, 0, (size_t)Cp.ngp * sizeof(double), ctx->stream));
+        R.ioerr = pcg_device_compact<double>(h, jac, o->maxIters, o->tolerance, r0, resi ? resi_dev.p : nullptr, true,
+                                             &iters, &rel);
+        compact_scatter_add<double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, Cp.f64.u.p, Cp.cl.p, Cp.ng);
+        SELF_LAUNCHED(ctx);
+      } else {
+        const PcRun<double> pc = use_pcl ? pcl_run<double>(h, o->pc_iterations) : PcRun<double>{};
+        R.ioerr = pcg_device<double>(h, h->u.p, h->r.p, h->v.p, h->w.p, h->z.p, jac ? h->op64.dinv.p : nullptr,
+                                     o->maxIters, o->tolerance, r0, resi ? resi_dev.p : nullptr, &iters, &rel,
+                                     h->op64, true, use_pcl ? &pc : nullptr);
+      }
       if (resi) {
         SELF_CUDA_TRY(ctx, cudaMemcpyAsync(resi, resi_dev.p, ((size_t)o->maxIters + 1) * sizeof(double),
                                            cudaMemcpyDeviceToHost, ctx->stream));
@@ -3140,14 +3238,15 @@ int self_cg2d_solve(self_cg2d* h, const self_solve_opts* o, const double* source
         double rel_in = 0;
         if (use_cpt) {  // compact layout: r32 = the unknowns of r64, x += d at the primary copies
           auto& Cp = h->cpt;
-          compact_gather_f32<<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.r.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
+          compact_gather<float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(Cp.f32.r.p, h->r.p, Cp.cl.p, Cp.ng, Cp.ngp);
           SELF_LAUNCHED(ctx);
-          SELF_CUDA_TRY(ctx, cudaMemsetAsync(Cp.u.p, 0, (size_t)Cp.ngp * sizeof(float), ctx->stream));
-          const int inner_err = pcg_device_compact(h, jac, o->maxIters - total, inner_tol, rn, &it_in, &rel_in);
+          SELF_CUDA_TRY(ctx, cudaMemsetAsync(Cp.f32.u.p, 0, (size_t)Cp.ngp * sizeof(float), ctx->stream));
+          const int inner_err = pcg_device_compact<float>(h, jac, o->maxIters - total, inner_tol, rn, nullptr, false,
+                                                          &it_in, &rel_in);
           total += it_in;
           if (inner_err == SELF_ERR_TIMEOUT)
             return set_error(ctx, SELF_ERR_TIMEOUT, "FP32 inner solve: a staged-copy barrier wait ran out");
-          compact_scatter_add<<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, Cp.u.p, Cp.cl.p, Cp.ng);
+          compact_scatter_add<float><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->u.p, Cp.f32.u.p, Cp.cl.p, Cp.ng);
           SELF_LAUNCHED(ctx);
         } else {
           convert<float, double><<<h->nblk, kRedThreads, 0, ctx->stream>>>(h->r32.p, h->r.p, nl);

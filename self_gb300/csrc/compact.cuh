@@ -74,6 +74,23 @@ __device__ __forceinline__ void ld_chunk(const float* __restrict__ p, float* x) 
 }
 
 template <int CH>
+__device__ __forceinline__ void ld_chunk(const double* __restrict__ p, double* x) {
+#pragma unroll
+  for (int c = 0; c + 1 < CH; c += 2) {
+    const double2 v = *reinterpret_cast<const double2*>(p + c);
+    x[c] = v.x, x[c + 1] = v.y;
+  }
+  if constexpr (CH == 1) x[0] = p[0];
+}
+
+template <int CH>
+__device__ __forceinline__ void st_chunk(double* __restrict__ p, const double* x) {
+#pragma unroll
+  for (int c = 0; c + 1 < CH; c += 2) *reinterpret_cast<double2*>(p + c) = make_double2(x[c], x[c + 1]);
+  if constexpr (CH == 1) p[0] = x[0];
+}
+
+template <int CH>
 __device__ __forceinline__ void st_chunk(float* __restrict__ p, const float* x) {
   if constexpr (CH == 4)
     *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
@@ -276,9 +293,115 @@ __global__ void __launch_bounds__(kRedThreads) pcg_apply_compact_f32(const float
   }
 }
 
+// FP64 form: the even-odd FP64 line operator of pcg_apply_fused_eo (line_op_f64, factors in the element-local
+// layout) with the compact gathers and slot stores of pcg_apply_compact_f32.
+template <int N1, int NF>
+__global__ void __launch_bounds__(kRedThreads, 2) pcg_apply_compact_f64(const double* __restrict__ w,
+                                                                        const double* __restrict__ vold,
+                                                                        double* __restrict__ vnew, CompactView V,
+                                                                        const double* __restrict__ fac,
+                                                                        double* __restrict__ zc, EOPair<N1> Tg,
+                                                                        CGScalars* S, double* __restrict__ partial,
+                                                                        unsigned int* __restrict__ ticket) {
+  if (S->done) return;
+  constexpr int M = N1 - 2, NN = N1 * N1;
+  constexpr int EPL = line_epb<N1>();
+  constexpr int LS = N1 + 1;
+  constexpr int CI = chunk_of<M>();
+  __shared__ EOPair<N1> T;
+  __shared__ double X[EPL * N1 * LS];
+  __shared__ double Y[EPL * N1 * LS];
+  eo_copy_tables<N1>(Tg, T);
+  __syncthreads();
+  const int nEl = V.nEl;
+  const int le = threadIdx.x / N1, t = threadIdx.x - le * N1;
+  const bool first = S->iter == 0;
+  const double beta = first ? 0.0 : S->beta;
+  const int ngroups = (nEl + EPL - 1) / EPL;
+  const bool irow = t > 0 && t < N1 - 1;
+  double pa = 0.0;
+  for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int e = g * EPL + le;
+    const bool active = le < EPL && e < nEl;
+    double u[N1], Lu[N1];
+    int ib = 0, cstride = 0;
+    if (active) {
+      int gi[N1], zi[N1];
+      unsigned own;
+      compact_line<N1>(V, e, t, V.desc[3 * e], V.desc[3 * e + 1], V.desc[3 * e + 2], gi, zi, own);
+      double wl[N1], vl[N1];
+      if (irow) {
+        const int ne = min(EPL, nEl - g * EPL);
+        ib = interior_index<N1>(e, 0, t - 1, nEl);
+        cstride = ne * M * CI;
+#pragma unroll
+        for (int c = 0; c < M / CI; ++c) {
+          ld_chunk<CI>(w + ib + c * cstride, wl + 1 + c * CI);
+          if (first) {
+#pragma unroll
+            for (int r = 0; r < CI; ++r) vl[1 + c * CI + r] = 0.0;
+          } else {
+            ld_chunk<CI>(vold + ib + c * cstride, vl + 1 + c * CI);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int i = q ? N1 - 1 : 0;
+          wl[i] = gi[i] >= 0 ? w[gi[i]] : 0.0;
+          vl[i] = (gi[i] >= 0 && !first) ? vold[gi[i]] : 0.0;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < N1; ++i) {
+          wl[i] = gi[i] >= 0 ? w[gi[i]] : 0.0;
+          vl[i] = (gi[i] >= 0 && !first) ? vold[gi[i]] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < N1; ++i) u[i] = first ? wl[i] : wl[i] + beta * vl[i];
+      if (irow) {
+#pragma unroll
+        for (int c = 0; c < M / CI; ++c) st_chunk<CI>(vnew + ib + c * cstride, u + 1 + c * CI);
+        if (own & 1u) vnew[gi[0]] = u[0];
+        if ((own >> (N1 - 1)) & 1u) vnew[gi[N1 - 1]] = u[N1 - 1];
+      } else {
+#pragma unroll
+        for (int i = 0; i < N1; ++i)
+          if ((own >> i) & 1u) vnew[gi[i]] = u[i];
+      }
+    }
+    line_op_f64<N1, NF>(T, fac + (size_t)(active ? e : 0) * NF * NN + (size_t)N1 * t, active, le < EPL ? le : 0, t, X,
+                        Y, u, Lu);
+    if (active) {
+      int gi[N1], zi[N1];
+      unsigned own;
+      compact_line<N1>(V, e, t, V.desc[3 * e], V.desc[3 * e + 1], V.desc[3 * e + 2], gi, zi, own);
+      if (irow) {
+#pragma unroll
+        for (int c = 0; c < M / CI; ++c) st_chunk<CI>(zc + ib + c * cstride, Lu + 1 + c * CI);
+        if (zi[0] >= 0) zc[zi[0]] = Lu[0];
+        if (zi[N1 - 1] >= 0) zc[zi[N1 - 1]] = Lu[N1 - 1];
+      } else {
+#pragma unroll
+        for (int i = 0; i < N1; ++i)
+          if (zi[i] >= 0) zc[zi[i]] = Lu[i];
+      }
+#pragma unroll
+      for (int i = 0; i < N1; ++i) pa += u[i] * Lu[i];
+    }
+  }
+  const double acc[1] = {pa};
+  double tot[1];
+  if (grid_sums_last<1, double>(acc, partial, ticket, tot) && threadIdx.x == 0) {
+    S->vz = tot[0];
+    S->alpha = S->num / tot[0];
+    S->alpha32 = (float)S->alpha;
+  }
+}
+
 // Assembled z at compact node m from the contribution space (see the file header for the sums).
-template <int N1>
-__device__ __forceinline__ float compact_z(const CompactView& V, const float* __restrict__ zc, int m) {
+template <int N1, typename R>
+__device__ __forceinline__ R compact_z(const CompactView& V, const R* __restrict__ zc, int m) {
   constexpr int M = N1 - 2;
   if (m < V.nInt) return zc[m];
   int q = m - V.nInt;
@@ -289,30 +412,51 @@ __device__ __forceinline__ float compact_z(const CompactView& V, const float* __
     return id < V.nE2 ? zc[b] + zc[b + M] : zc[b];
   }
   q -= nEM;
-  if (q >= V.nC) return 0.f;  // padding
-  const float* c = zc + V.nInt + 2 * nEM;
-  float s = 0.f;
+  if (q >= V.nC) return R(0);  // padding
+  const R* c = zc + V.nInt + 2 * nEM;
+  R s = 0;
   for (int k = V.coff[q], k1 = V.coff[q + 1]; k < k1; ++k) s += c[k];
   return s;
 }
 
-// a = num/<v,z>; u += a v, r -= a z, w = dinv r over 16-byte groups of the compact vectors (z assembled on the fly
-// from the contribution space), partial sums of <r,w> and <r,r>, then the end-of-iteration scalar step.
-template <int N1>
-__global__ void __launch_bounds__(kRedThreads) pcg_update_compact(float4* __restrict__ u, float4* __restrict__ r,
-                                                                  float4* __restrict__ w,
-                                                                  const float4* __restrict__ v,
-                                                                  const float* __restrict__ zc,
-                                                                  const float4* __restrict__ dinv, CompactView V,
+// four consecutive nodes (16-byte aligned for FP32, two 16-byte halves for FP64)
+template <typename R>
+struct Q4 {
+  R x, y, z, w;
+};
+__device__ __forceinline__ Q4<float> ld4(const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Q4<double> ld4(const double* p) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st4(float* p, const Q4<float>& q) {
+  *reinterpret_cast<float4*>(p) = make_float4(q.x, q.y, q.z, q.w);
+}
+__device__ __forceinline__ void st4(double* p, const Q4<double>& q) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(q.x, q.y);
+  reinterpret_cast<double2*>(p)[1] = make_double2(q.z, q.w);
+}
+
+// a = num/<v,z>; u += a v, r -= a z, w = dinv r over groups of 4 nodes of the compact vectors (z assembled on the
+// fly from the contribution space), partial sums of <r,w> and <r,r>, then the end-of-iteration scalar step.
+template <int N1, typename R>
+__global__ void __launch_bounds__(kRedThreads) pcg_update_compact(R* __restrict__ u, R* __restrict__ r,
+                                                                  R* __restrict__ w, const R* __restrict__ v,
+                                                                  const R* __restrict__ zc,
+                                                                  const R* __restrict__ dinv, CompactView V,
                                                                   CGScalars* S, double* __restrict__ partial,
                                                                   unsigned int* __restrict__ ticket) {
   if (S->done) return;
-  const float a = S->alpha32;
-  float prw = 0.f, prr = 0.f;
+  const R a = sizeof(R) == 4 ? (R)S->alpha32 : (R)S->alpha;
+  R prw = 0, prr = 0;
   const int nq = V.ngp / 4, nqi = V.nInt / 4, stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  auto update = [&](int q, const float4& uu, const float4& vv, const float4& rr, const float4& dd, const float4& zz) {
-    float4 uo, ro, wo;
+  const Q4<R> one{1, 1, 1, 1};
+  auto update = [&](int q, const Q4<R>& uu, const Q4<R>& vv, const Q4<R>& rr, const Q4<R>& dd, const Q4<R>& zz) {
+    Q4<R> uo, ro, wo;
     uo.x = uu.x + a * vv.x;
     uo.y = uu.y + a * vv.y;
     uo.z = uu.z + a * vv.z;
@@ -327,23 +471,24 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_compact(float4* __rest
     wo.w = dinv ? ro.w * dd.w : ro.w;
     prw += ro.x * wo.x + ro.y * wo.y + ro.z * wo.z + ro.w * wo.w;
     prr += ro.x * ro.x + ro.y * ro.y + ro.z * ro.z + ro.w * ro.w;
-    u[q] = uo;
-    r[q] = ro;
-    w[q] = wo;
+    st4(u + 4 * q, uo);
+    st4(r + 4 * q, ro);
+    st4(w + 4 * q, wo);
   };
-  // interior groups: plain streams, U groups per thread with every load issued before any use
-  constexpr int U = 2;
+  // interior groups: plain streams, U groups per thread with every load issued before any use (FP64: one, the
+  // registers of two would cost occupancy)
+  constexpr int U = sizeof(R) == 4 ? 2 : 1;
   for (int q0 = tid; q0 < nqi; q0 += U * stride) {
-    float4 uu[U], vv[U], rr[U], dd[U], zz[U];
+    Q4<R> uu[U], vv[U], rr[U], dd[U], zz[U];
 #pragma unroll
     for (int k = 0; k < U; ++k) {
       const int q = q0 + k * stride;
       if (q >= nqi) continue;
-      uu[k] = u[q];
-      vv[k] = v[q];
-      rr[k] = r[q];
-      dd[k] = dinv ? dinv[q] : make_float4(1.f, 1.f, 1.f, 1.f);
-      zz[k] = reinterpret_cast<const float4*>(zc)[q];
+      uu[k] = ld4(u + 4 * q);
+      vv[k] = ld4(v + 4 * q);
+      rr[k] = ld4(r + 4 * q);
+      dd[k] = dinv ? ld4(dinv + 4 * q) : one;
+      zz[k] = ld4(zc + 4 * q);
     }
 #pragma unroll
     for (int k = 0; k < U; ++k)
@@ -351,37 +496,39 @@ __global__ void __launch_bounds__(kRedThreads) pcg_update_compact(float4* __rest
   }
   // shared-node groups (and the group straddling the interior's end): z assembled from the contribution slots
   for (int q = nqi + tid; q < nq; q += stride) {
-    const float4 uu = u[q], vv = v[q], rr = r[q];
-    const float4 dd = dinv ? dinv[q] : make_float4(1.f, 1.f, 1.f, 1.f);
-    float4 zz;
+    const Q4<R> uu = ld4(u + 4 * q), vv = ld4(v + 4 * q), rr = ld4(r + 4 * q);
+    const Q4<R> dd = dinv ? ld4(dinv + 4 * q) : one;
+    Q4<R> zz;
     zz.x = compact_z<N1>(V, zc, 4 * q);
     zz.y = compact_z<N1>(V, zc, 4 * q + 1);
     zz.z = compact_z<N1>(V, zc, 4 * q + 2);
     zz.w = compact_z<N1>(V, zc, 4 * q + 3);
     update(q, uu, vv, rr, dd, zz);
   }
-  const float acc[2] = {prw, prr};
+  const R acc[2] = {prw, prr};
   double tot[2];
-  if (grid_sums_last<2, float>(acc, partial, ticket, tot) && threadIdx.x == 0) pcg_end_iteration(S, tot[0], tot[1]);
+  if (grid_sums_last<2, R>(acc, partial, ticket, tot) && threadIdx.x == 0) pcg_end_iteration(S, tot[0], tot[1]);
 }
 
 // out[cl[n]] = assembled z at unknown n (out zero elsewhere: the masked L-vector of Mask(GlobalSum(L v)))
-template <int N1>
-__global__ void compact_assemble(double* __restrict__ out, const float* __restrict__ zc, const int* __restrict__ cl,
+template <int N1, typename R>
+__global__ void compact_assemble(double* __restrict__ out, const R* __restrict__ zc, const int* __restrict__ cl,
                                  int ng, CompactView V) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < ng; n += gridDim.x * blockDim.x)
     out[cl[n]] = (double)compact_z<N1>(V, zc, n);
 }
 
-// r32[n] = (float) r64[cl[n]] (the unknown's primary copy in the masked L-vector); padding zero
-__global__ void compact_gather_f32(float* __restrict__ y, const double* __restrict__ x, const int* __restrict__ cl,
-                                   int ng, int ngp) {
+// y[n] = (R) x[cl[n]] (the unknown's primary copy in the masked FP64 L-vector); padding zero
+template <typename R>
+__global__ void compact_gather(R* __restrict__ y, const double* __restrict__ x, const int* __restrict__ cl, int ng,
+                               int ngp) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < ngp; n += gridDim.x * blockDim.x)
-    y[n] = n < ng ? (float)x[cl[n]] : 0.f;
+    y[n] = n < ng ? (R)x[cl[n]] : R(0);
 }
 
-// x64[cl[n]] += (double) y32[n]: the inner correction added to the masked FP64 iterate at the primary copies
-__global__ void compact_scatter_add(double* __restrict__ x, const float* __restrict__ y, const int* __restrict__ cl,
+// x[cl[n]] += y[n]: a correction on the compact layout added to the masked FP64 iterate at the primary copies
+template <typename R>
+__global__ void compact_scatter_add(double* __restrict__ x, const R* __restrict__ y, const int* __restrict__ cl,
                                     int ng) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < ng; n += gridDim.x * blockDim.x) x[cl[n]] += (double)y[n];
 }

@@ -69,3 +69,32 @@ def test_compact_matches_local_no_dirichlet(gpu_ctx):
 def test_compact_plain_cg(gpu_ctx):
     """Unpreconditioned: the FP32 iteration count moves with the rounding of the dot sums (10 % bar)."""
     _check(_solve_both(gpu_ctx, 7, 6, 0.03, method="cg", its=0.10))
+
+
+@pytest.mark.parametrize("N,nx,warp", [(7, 12, 0.05), (5, 9, 0.03), (3, 6, 0.0)])
+def test_compact_fp64_pcg_matches_local(gpu_ctx, N, nx, warp):
+    """FP64 Jacobi PCG on the compact layout (CG on the correction from the residual of the initial guess; N >= 5:
+    the even-odd FP64 operator; N = 3 runs the element-local form under the same option) against the element-local
+    solve: residual histories within 1e-9 over the first 20 iterations, iterations within 2 % (+2), solutions within
+    1e-10; the compact solve launches two kernels per iteration."""
+    import self_gb300 as sg
+    from self_gb300 import workloads as W
+    nod = sg.NodalStorage_2D(N, sg._native.GAUSS_LOBATTO, sg._native.CG)
+    mesh = sg.QuadMesh(nx, nx, N, sg._native.GAUSS_LOBATTO, warp=warp, boundary_flag=sg._native.DIRICHLET)
+    k, f, source = W.helmholtz(mesh, N)
+    cg = sg.CGsemElliptic_2D(gpu_ctx, nod, mesh, k, lam=0.1)
+    x0 = np.random.default_rng(N).normal(size=cg.nl) * 1e-3  # a nonzero initial guess
+    out = {}
+    for layout in ("local", "compact"):
+        l0 = gpu_ctx.kernel_launches()
+        sol, rep = cg.Solve(source, solution=x0, method="pcg", tolerance=1e-10, return_resi=True,
+                            inner_layout=layout)
+        out[layout] = (sol, rep, gpu_ctx.kernel_launches() - l0)
+    (sl, rl, ll), (sc, rc, lc) = out["local"], out["compact"]
+    for rep in (rl, rc):
+        assert rep["ioerr"] == 0 and rep["rel_residual"] < 1e-10, rep
+    assert abs(rc["iterations"] - rl["iterations"]) <= 0.02 * rl["iterations"] + 2
+    assert rel_inf(rc["resi"][:20], rl["resi"][:20]) <= 1e-9
+    assert rel_inf(sc, sl) < 1e-10
+    if N >= 5:
+        assert lc < ll, (ll, lc)
