@@ -513,14 +513,15 @@ def serving_leg(sg, ctx, nreq=300, rate=2000.0, seed=5, sweep_n=150, base_n=120)
 
 
 def run_cg_profile(args):
-    """Bounded CGSEM workload for profilers (no JSON line): the 256x256 N=7 Helmholtz problem of the elliptic
-    leg, `--profile-cg K` PCG iterations (`--profile-method`: pcg = Jacobi, pcg_linear = the linear-FEM
+    """Bounded CGSEM workload for profilers (no JSON line; the solves looped from the host so that every kernel
+    launch is listed): the 256x256 N=7 Helmholtz problem of the elliptic leg, `--profile-cg K` PCG iterations (`--profile-method`: pcg = Jacobi, pcg_linear = the linear-FEM
     preconditioner with 20 inner iterations; `--profile-precision`) after a short warm-up solve; gmres = K FP64
     GMRES(30) Arnoldi steps on the advection-diffusion operator of the leg."""
     import self_gb300 as sg
     from self_gb300 import _native as nat
     from self_gb300 import workloads as W
     ctx = sg.Context(0)
+    ctx.host_loop()  # every PCG launch visible to kernel profilers (no conditional graph nodes)
     N, nx = 7, 256
     nod = sg.NodalStorage_2D(N, nat.GAUSS_LOBATTO, nat.CG)
     mesh = sg.QuadMesh(nx, nx, N, nat.GAUSS_LOBATTO, boundary_flag=nat.DIRICHLET)

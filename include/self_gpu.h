@@ -381,6 +381,11 @@ int self_ctx_timer_start(self_ctx* ctx);
 int self_ctx_timer_stop(self_ctx* ctx, double* ms);
 /* Overwrite a scratch buffer of `bytes` on the context's stream (evicts L2 between timed steps). */
 int self_ctx_flush_l2(self_ctx* ctx, size_t bytes);
+/* host_loop != 0: the context's single-problem (P)CG solves repeat their captured 16-iteration graph from the host
+ * (one synchronisation per graph) instead of one launch of a conditional-while graph, so that kernel profilers,
+ * which do not list kernels inside conditional graph nodes, see every launch.  The same kernels and iterations;
+ * 0 (the default) restores the device-side loop. */
+int self_ctx_host_loop(self_ctx* ctx, int host_loop);
 /* Measured fused-multiply-add rate of the device (TFLOP/s, FP64 when fp64 != 0 else FP32): the compute
  * roofline used for kernels bound by the FP64 pipe. */
 int self_probe_fma_peak(self_ctx* ctx, int fp64, double* tflops);

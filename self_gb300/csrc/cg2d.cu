@@ -1048,10 +1048,11 @@ namespace cg {
 // Buffers a captured PCG iteration graph was built on.
 struct PcgGraphKey {
   const void *u, *r, *v, *v2, *w, *z, *dinv, *fac;
-  int tc;  // tensor-core form of the FP32 apply
+  int tc;         // tensor-core form of the FP32 apply
+  int host_loop;  // captured as a plain graph repeated from the host (else a conditional-while loop)
   bool operator==(const PcgGraphKey& o) const {
     return u == o.u && r == o.r && v == o.v && v2 == o.v2 && w == o.w && z == o.z && dinv == o.dinv &&
-           fac == o.fac && tc == o.tc;
+           fac == o.fac && tc == o.tc && host_loop == o.host_loop;
   }
 };
 
@@ -1473,6 +1474,23 @@ template <class Body>
 int capture_iterations(self_cg2d* h, cudaGraphExec_t& G, long long& glaunches, int per_graph, Body body) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
+  if (ctx->host_loop) {  // a plain graph of per_graph iterations, repeated from the host by replay_until_done
+    cudaGraph_t g;
+    int rc = SELF_OK;
+    const long long l0 = ctx->launches.load();
+    SELF_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < per_graph && !rc; ++k) rc = body(k);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    glaunches = ctx->launches.load() - l0;
+    ctx->launches.fetch_sub(glaunches);
+    if (ce == cudaSuccess && rc) cudaGraphDestroy(g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&G, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return set_error(ctx, SELF_ERR_CUDA, "PCG graph instantiate: %s", cudaGetErrorString(ce));
+    return SELF_OK;
+  }
   cudaGraph_t g = nullptr;
   SELF_CUDA_TRY(ctx, cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle cond;
@@ -1517,10 +1535,22 @@ int capture_iterations(self_cg2d* h, cudaGraphExec_t& G, long long& glaunches, i
   return SELF_OK;
 }
 
-// One launch of the loop graph G runs the solve to its stop; hs holds the scalars afterwards.
-int replay_until_done(self_cg2d* h, cudaGraphExec_t G, long long glaunches, CGScalars& hs) {
+// One launch of the loop graph G runs the solve to its stop; hs holds the scalars afterwards.  Host-looped form
+// (self_ctx_host_loop): G repeated, one synchronisation per launch, at most maxIters / per_graph + 2 launches.
+int replay_until_done(self_cg2d* h, cudaGraphExec_t G, long long glaunches, CGScalars& hs, int per_graph = 1) {
   self_ctx* ctx = h->ctx;
   cudaStream_t st = ctx->stream;
+  if (ctx->host_loop) {
+    const long long max_launches = (long long)hs.maxIters / per_graph + 2;
+    for (long long gl = 0; gl < max_launches; ++gl) {
+      SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
+      ctx->launches.fetch_add(glaunches);
+      SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+      SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (hs.done) break;
+    }
+    return SELF_OK;
+  }
   SELF_CUDA_TRY(ctx, cudaGraphLaunch(G, st));
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -1553,8 +1583,8 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
       SELF_LAUNCHED(ctx);
     }
     const int prec = sizeof(R) == 4 ? 1 : 0;
-    PcgGraphKey key{u, r, v, v2, w, z, dinv, od.fac.p, h->tc};
-    if (pc) key = PcgGraphKey{u, r, v, v2, w, z, pc->ul, pc->fac, h->tc};
+    PcgGraphKey key{u, r, v, v2, w, z, dinv, od.fac.p, h->tc, ctx->host_loop};
+    if (pc) key = PcgGraphKey{u, r, v, v2, w, z, pc->ul, pc->fac, h->tc, ctx->host_loop};
     cudaGraphExec_t& G = pc ? h->pcl.graph[prec] : h->pcg_graph[prec][dinv ? 1 : 0];
     PcgGraphKey& gk = pc ? h->pcl.key[prec] : h->pcg_key[prec][dinv ? 1 : 0];
     long long& glaunches = pc ? h->pcl.graph_launches : h->pcg_graph_launches;
@@ -1601,7 +1631,7 @@ int pcg_device(self_cg2d* h, R* u, R* r, R* v, R* w, R* z, const R* dinv, int ma
       gk = key;
       if (pc) h->pcl.key_iters[prec] = pc->iters;
     }
-    if (const int rc = replay_until_done(h, G, glaunches, hs)) return rc;
+    if (const int rc = replay_until_done(h, G, glaunches, hs, per_graph)) return rc;
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -1803,7 +1833,7 @@ int pcg_device_compact(self_cg2d* h, bool jac, int maxIters, double tol, double 
                                                         h->ticket.p);
     SELF_LAUNCHED(ctx);
     cudaGraphExec_t& G = Vc.graph[jac ? 1 : 0];
-    const PcgGraphKey key{Vc.u.p, Vc.r.p, Vc.v.p, Vc.v2.p, Vc.w.p, Vc.zc.p, dinv, nullptr, 0};
+    const PcgGraphKey key{Vc.u.p, Vc.r.p, Vc.v.p, Vc.v2.p, Vc.w.p, Vc.zc.p, dinv, nullptr, 0, ctx->host_loop};
     if (G && !(Vc.key[jac ? 1 : 0] == key)) {
       cudaGraphExecDestroy(G);
       G = nullptr;
@@ -1815,7 +1845,7 @@ int pcg_device_compact(self_cg2d* h, bool jac, int maxIters, double tol, double 
       if (rc) return rc;
       Vc.key[jac ? 1 : 0] = key;
     }
-    if (const int rc = replay_until_done(h, G, Vc.graph_launches, hs)) return rc;
+    if (const int rc = replay_until_done(h, G, Vc.graph_launches, hs, kGraphIters)) return rc;
   }
   SELF_CUDA_TRY(ctx, cudaMemcpyAsync(&hs, h->S.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
   SELF_CUDA_TRY(ctx, cudaStreamSynchronize(st));

@@ -20,6 +20,7 @@ struct self_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
+  int host_loop = 0;  // (P)CG solves looped from the host (profilers), see self_ctx_host_loop
 };
 
 namespace selfgpu {

@@ -323,6 +323,12 @@ int self_ctx_query(self_ctx* ctx) {
   return set_error(ctx, SELF_ERR_CUDA, "stream query: %s", cudaGetErrorString(e));
 }
 
+int self_ctx_host_loop(self_ctx* ctx, int host_loop) {
+  if (!ctx) return SELF_ERR_INVALID;
+  ctx->host_loop = host_loop ? 1 : 0;
+  return SELF_OK;
+}
+
 int self_ctx_flush_l2(self_ctx* ctx, size_t bytes) {
   if (!ctx) return SELF_ERR_INVALID;
   SELF_CUDA_TRY(ctx, cudaSetDevice(ctx->device));

@@ -39,6 +39,11 @@ class Context:
     def kernel_launches(self):
         return int(nat.lib().self_ctx_kernel_launches(self.ptr))
 
+    def host_loop(self, on=True):
+        """(P)CG solves repeat their 16-iteration graph from the host (for kernel profilers) instead of one
+        conditional-while graph launch (self_ctx_host_loop)."""
+        nat.check(nat.lib().self_ctx_host_loop(self.ptr, 1 if on else 0), self.ptr)
+
     def close(self):
         if self.ptr:
             for h in list(getattr(self, "_handles", ())):
