@@ -12,21 +12,6 @@ namespace selfgpu {
 // request the 128-byte line holding p into L2 (no register result; the load that follows later hits L2)
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-template <int N1>
-__device__ __forceinline__ float row_dot(const float* __restrict__ drow, const float (&x)[N1]) {
-  // drow: N1 floats padded to a multiple of 4 (zeros), 16-byte aligned; x: registers
-  float s = 0.f;
-#pragma unroll
-  for (int k = 0; k < (N1 + 3) / 4; ++k) {
-    const float4 d = *reinterpret_cast<const float4*>(drow + 4 * k);
-    if (4 * k + 0 < N1) s = fmaf(d.x, x[4 * k + 0], s);
-    if (4 * k + 1 < N1) s = fmaf(d.y, x[4 * k + 1], s);
-    if (4 * k + 2 < N1) s = fmaf(d.z, x[4 * k + 2], s);
-    if (4 * k + 3 < N1) s = fmaf(d.w, x[4 * k + 3], s);
-  }
-  return s;
-}
-
 // a line of N1 consecutive 4- or 8-byte values: 16-byte loads when a line is a whole number of 16-byte chunks (the
 // line then starts on a 16-byte boundary: the element base is a multiple of NN values and every vector's length a
 // multiple of a line), 8-byte loads for a whole number of 8-byte chunks, single values otherwise
