@@ -73,6 +73,7 @@ struct EdgeArgs {
   double kappa;
   int nEdges;
   double g, t;
+  double sg;  // sqrt(g) (correctly rounded on the host, as on the device)
 };
 
 // ------------------------------------------------------------------------------------ arithmetic
@@ -90,7 +91,7 @@ struct Ar {
 struct SWFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double un_adv, double fin, double fout, double g, double* f) {
+                                                 double un_adv, double fin, double fout, double g, double sg, double* f) {
     (void)fin;
     (void)fout;
     (void)un_adv;
@@ -114,7 +115,7 @@ struct SWFlux {
       f[2] = A::mul(0.5, A::sub(a2, A::mul(fac, A::sub(pR, pL))));
     } else {
       // depths are positive: one reciprocal square root per side gives 1/H and sqrt(g H) = sqrt(g) H / sqrt(H)
-      const double rR = rsqrt(pR), rL = rsqrt(pL), sg = sqrt(g);
+      const double rR = rsqrt(pR), rL = rsqrt(pL);  // sg = sqrt(g), formed once on the host
       const double ipR = rR * rR, ipL = rL * rL;
       const double cR = sg * (pR * rR), cL = sg * (pL * rL);
       const double wR = uOut * ipR, wL = uIn * ipL;
@@ -148,7 +149,7 @@ struct SWFlux {
 struct SWLinFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double depth, double fin, double fout, double g, double* f) {
+                                                 double depth, double fin, double fout, double g, double sg, double* f) {
     (void)fin;
     (void)fout;
     // RiemannSolver, LINEAR branch (ShallowWaterClass.f90:2106-2113)
@@ -174,7 +175,7 @@ struct SWLinFlux {
 struct SWSkewFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double depth, double fin, double fout, double g, double* f) {
+                                                 double depth, double fin, double fout, double g, double sg, double* f) {
     // RiemannSolver, SKEW_SYMMETRIC branch (ShallowWaterClass.f90:2114-2133)
     using A = Ar<EX>;
     const double uL = in[0], vL = in[1], pL = in[2], uR = ex[0], vR = ex[1], pR = ex[2];
@@ -209,7 +210,7 @@ struct SWSkewFlux {
 struct AdvFlux {
   template <int NEQ, bool EX>
   static __device__ __forceinline__ void riemann(const double* in, const double* ex, double nx, double ny,
-                                                 double un, double fin, double fout, double g, double* f) {
+                                                 double un, double fin, double fout, double g, double sg, double* f) {
     (void)fin;
     (void)fout;
     (void)nx;
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
     const double* b2 = A.bs + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
-    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, f);
+    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, A.sg, f);
     if (A.gtx) {  // BR1: - kappa dc/dn with the averaged gradient (AdvectionClass.f90 EdgeFlux :1413-1420)
       using X = Ar<EX>;
       const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i, o2i = (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2) + kk;
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
     }
   } else {
     Phys::template external<NEQ, EX>(e2f, nx, ny, A.t, in, ex);
-    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, f);
+    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, A.sg, f);
     if (A.gtx) {  // BR1: the inner gradient on the boundary
       using X = Ar<EX>;
       const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i;
@@ -833,6 +834,7 @@ int launch_edge_t(self_dg2d* h, double t) {
   EA.kappa = h->kappa;
   EA.nEdges = h->nEdges;
   EA.g = h->g;
+  EA.sg = std::sqrt(h->g);
   EA.t = t;
   const int nthr = h->nEdges * N1;
   if (PH == 1)
