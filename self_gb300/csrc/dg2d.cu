@@ -302,25 +302,27 @@ constexpr int elems_per_block() {
 template <int N1, int NEQ, bool EX>
 __device__ __forceinline__ void write_traces(const NodalConst<N1>& C, const double* sq /*[EPB][NEQ][N1*N1]*/,
                                              double* bs, int e, int tid) {
-  // 4 sides x NEQ x N1 values per element; side 0..3 = S,E,N,W (CalculateSolutionAtBoundaries)
+  // 4 sides x NEQ x N1 values per element; side 0..3 = S,E,N,W (CalculateSolutionAtBoundaries).  A thread takes a
+  // pair: one column trace (S or N: along j at column k) and one row trace (E or W: along i at row k) of the same
+  // variable, so a warp never splits between the two access patterns and N1 = 8 needs one round of 48 threads
   using A = Ar<EX>;
-  constexpr int NV = 4 * NEQ * N1;
-  for (int t = tid; t < NV; t += N1 * N1) {
+  constexpr int NP = 2 * NEQ * N1;
+  for (int t = tid; t < NP; t += N1 * N1) {
     const int k = t % N1;
     const int v = (t / N1) % NEQ;
-    const int side = t / (N1 * NEQ);
+    const int hsel = t / (N1 * NEQ);  // 0: S and E, 1: N and W
     const double* Q = sq + v * N1 * N1;
-    double acc = 0.0;
-    if (side == 0 || side == 2) {
-      const double* L = (side == 0) ? C.lS : C.lN;
+    const double* Lc = hsel ? C.lN : C.lS;
+    const double* Lr = hsel ? C.lW : C.lE;
+    double ac = 0.0, ar = 0.0;
 #pragma unroll
-      for (int m = 0; m < N1; ++m) acc = A::add(acc, A::mul(L[m], Q[k + N1 * m]));
-    } else {
-      const double* L = (side == 1) ? C.lE : C.lW;
-#pragma unroll
-      for (int m = 0; m < N1; ++m) acc = A::add(acc, A::mul(L[m], Q[m + N1 * k]));
+    for (int m = 0; m < N1; ++m) {
+      ac = A::add(ac, A::mul(Lc[m], Q[k + N1 * m]));
+      ar = A::add(ar, A::mul(Lr[m], Q[m + N1 * k]));
     }
-    bs[(size_t)N1 * NEQ * (side + 4 * (size_t)e) + k + N1 * v] = acc;
+    const int sc = hsel ? 2 : 0, sr = hsel ? 3 : 1;
+    bs[(size_t)N1 * NEQ * (sc + 4 * (size_t)e) + k + N1 * v] = ac;
+    bs[(size_t)N1 * NEQ * (sr + 4 * (size_t)e) + k + N1 * v] = ar;
   }
 }
 
