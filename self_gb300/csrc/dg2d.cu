@@ -252,16 +252,27 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
   const double* b1 = A.bs + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
 #pragma unroll
   for (int v = 0; v < NEQ; ++v) in[v] = b1[i + N1 * v];
-  if (e2f > 0) {
-    const int e2 = e2f - 1, s2 = abs(E[3]) - 1, start = E[4], inc = E[5];
-    const int kk = start - inc + i * inc;
+  // the exterior state (neighbour's trace or boundary condition), then one Riemann solve for both kinds of edge:
+  // a warp holding interior and boundary edges does not run the solver twice
+  const bool interior = e2f > 0;
+  int e2 = 0, s2 = 0, kk = 0;
+  if (interior) {
+    const int start = E[4], inc = E[5];
+    e2 = e2f - 1;
+    s2 = abs(E[3]) - 1;
+    kk = start - inc + i * inc;
     const double* b2 = A.bs + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) ex[v] = b2[kk + N1 * v];
-    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, A.sg, f);
+  } else {
+    Phys::template external<NEQ, EX>(e2f, nx, ny, A.t, in, ex);
+  }
+  Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, A.sg, f);
+  using X = Ar<EX>;
+  const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i;
+  if (interior) {
     if (A.gtx) {  // BR1: - kappa dc/dn with the averaged gradient (AdvectionClass.f90 EdgeFlux :1413-1420)
-      using X = Ar<EX>;
-      const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i, o2i = (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2) + kk;
+      const size_t o2i = (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2) + kk;
 #pragma unroll
       for (int v = 0; v < NEQ; ++v) {
         const double gx = X::mul(X::add(A.gtx[o1i + N1 * v], A.gtx[o2i + N1 * v]), 0.5);
@@ -273,23 +284,19 @@ __global__ void __launch_bounds__(256) dg_edge_flux(EdgeArgs A) {
     double* o2 = A.bf + (size_t)N1 * NEQ * (s2 + 4 * (size_t)e2);
 #pragma unroll
     for (int v = 0; v < NEQ; ++v) {
-      const double fl = Ar<EX>::mul(f[v], len);
+      const double fl = X::mul(f[v], len);
       o1[i + N1 * v] = fl;
       o2[kk + N1 * v] = -fl;
     }
   } else {
-    Phys::template external<NEQ, EX>(e2f, nx, ny, A.t, in, ex);
-    Phys::template riemann<NEQ, EX>(in, ex, nx, ny, un, fin, fout, A.g, A.sg, f);
     if (A.gtx) {  // BR1: the inner gradient on the boundary
-      using X = Ar<EX>;
-      const size_t o1i = (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1) + i;
 #pragma unroll
       for (int v = 0; v < NEQ; ++v)
         f[v] = X::sub(f[v], X::mul(A.kappa, X::add(X::mul(A.gtx[o1i + N1 * v], nx), X::mul(A.gty[o1i + N1 * v], ny))));
     }
     double* o1 = A.bf + (size_t)N1 * NEQ * (s1 + 4 * (size_t)e1);
 #pragma unroll
-    for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = Ar<EX>::mul(f[v], len);
+    for (int v = 0; v < NEQ; ++v) o1[i + N1 * v] = X::mul(f[v], len);
   }
 }
 
